@@ -1,0 +1,183 @@
+/*
+ * wedge_cuda.h -- C ABI of the GB300 (sm_103a) edge-pull engine.
+ *
+ * This is the drop-in boundary for Wedge's pull-only edge-pull path.  A C host
+ * that today runs
+ *     application_select -> graph_data_read_from_file ->
+ *     graph_data_initialize_data_structures -> execution_impl_* ->
+ *     execution_get_vertex_prop_string_*
+ * calls, in the same order,
+ *     wedge_cuda_load_graph -> wedge_cuda_run -> wedge_cuda_read_results.
+ *
+ * Conventions
+ *  - Plain C types only; no CUDA or framework types cross this boundary.
+ *  - Every function returns WEDGE_OK (0) or a negative WEDGE_ERR_* status.
+ *  - One host thread per graph handle.  The device owns all graph and
+ *    property memory; the host receives copies.
+ *  - Vertex ids are < 2^32 - 1 on the device (the reference allows 48 bits,
+ *    graphdata.c:212-243); larger graphs are rejected with WEDGE_ERR_FORMAT.
+ *  - Properties come back in the reference's own representation, one 64-bit
+ *    word per vertex as in graph_vertex_props (include/graphdata.h:54):
+ *      BFS  uint64 parent, UINT64_MAX = unreached   (execution_bfs.c:69-73)
+ *      CC   double label                             (execution_cc.c:47-51)
+ *      PR   double rank / outdegree'                 (execution_pr.c:31-35)
+ *      SSSP uint64 distance, UINT64_MAX = unreached  (execution_sssp.c:48-52)
+ *           or double distance for FP64 weights (no reference counterpart).
+ */
+#ifndef WEDGE_CUDA_H
+#define WEDGE_CUDA_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define WEDGE_CUDA_ABI_VERSION 1
+
+/* application ids; names and aliases as in source/application.c:49-68 */
+enum wedge_app {
+    WEDGE_APP_BFS = 0,
+    WEDGE_APP_CC = 1,
+    WEDGE_APP_PR = 2,
+    WEDGE_APP_SSSP = 3
+};
+
+enum wedge_status {
+    WEDGE_OK = 0,
+    WEDGE_ERR_IO = -1,             /* file missing, short read (graphdata.c:960-965) */
+    WEDGE_ERR_FORMAT = -2,         /* size mismatch, unsorted dst, id out of range (graphdata.c:968-979) */
+    WEDGE_ERR_OOM = -3,
+    WEDGE_ERR_CUDA = -4,
+    WEDGE_ERR_NOT_CONVERGED = -5,  /* iteration cap reached before the frontier emptied */
+    WEDGE_ERR_ARG = -6,
+    WEDGE_ERR_UNSUPPORTED = -7
+};
+
+/* how the third word of a weighted edge record is read */
+enum wedge_weights {
+    WEDGE_WEIGHTS_NONE = 0,
+    WEDGE_WEIGHTS_U64 = 1, /* reference behaviour (phase_edge_pull_sssp.c:93,137) */
+    WEDGE_WEIGHTS_F64 = 2  /* IEEE double weights, double min-plus */
+};
+
+enum wedge_precision {
+    WEDGE_PREC_FP64 = 0,  /* reference arithmetic (PageRank) */
+    WEDGE_PREC_FP32C = 1  /* FP32 ranks, per-destination two-sum compensated sums, FP64 global terms */
+};
+
+/* how each iteration chooses between the dense pull and the Wedge pull */
+enum wedge_sched {
+    WEDGE_SCHED_PLAIN = 0,   /* fixed threshold: dense iff active out-edge mass > t% of |E| (execution_bfs.c:132,141) */
+    WEDGE_SCHED_DENSE = 1,   /* always dense */
+    WEDGE_SCHED_WEDGE = 2    /* Wedge whenever the frontier allows it */
+};
+
+/* single phases, for hosts that keep the reference's own driver loop (include/phases.h:58-88, wedge.h:24-27) */
+enum wedge_phase {
+    WEDGE_PHASE_INIT = 0,          /* execution_initialize_* */
+    WEDGE_PHASE_PULL_DENSE = 1,    /* perform_edge_pull_phase_{bfs,cc,pr,sssp} */
+    WEDGE_PHASE_PULL_WEDGE = 2,    /* perform_edge_pull_phase_*_with_wedge_frontier */
+    WEDGE_PHASE_VERTEX_PR = 3,     /* edge_pull_op_merge_with_merge_buffer + perform_vertex_phase_pr */
+    WEDGE_PHASE_WEDGE_BUILD = 4,   /* wedge_generate_frontier */
+    WEDGE_PHASE_ADVANCE = 5        /* frontier swap / clear between iterations (execution_bfs.c:320-338) */
+};
+
+#define WEDGE_FLAG_GRAPH 1u   /* run the traversal as one CUDA graph looping on a device convergence flag */
+#define WEDGE_FLAG_TIMING 2u  /* record per-phase CUDA events (Pull/Wedge times of the statistics block) */
+
+typedef struct wedge_params {
+    uint64_t root;            /* -r, default 0 (include/cmdline.h:29) */
+    uint32_t threshold_pct;   /* -t, default 20 (include/cmdline.h:30) */
+    uint32_t num_iterations;  /* -N, PageRank iterations, default 1 (include/cmdline.h:28) */
+    double damping;           /* PageRank damping; 0 selects the reference's 0.875 (include/constants.h:39) */
+    int32_t precision;        /* enum wedge_precision (PageRank only) */
+    int32_t sched;            /* enum wedge_sched */
+    uint32_t max_iterations;  /* cap for BFS/CC/SSSP; 0 = |V| + 1 */
+    uint32_t flags;           /* WEDGE_FLAG_* */
+} wedge_params_t;
+
+/* EXECUTION STATISTICS block of source/main.c:153-182, plus device counters */
+typedef struct wedge_stats {
+    uint64_t iterations;          /* Total Iterations */
+    uint64_t wedge_iterations;    /* Iterations with Wedge */
+    double running_ms;            /* Running Time: whole traversal on the device */
+    double pull_ms_dense;         /* No Frontier Pull Time (needs WEDGE_FLAG_TIMING) */
+    double pull_ms_wedge;         /* Frontier Pull Time (needs WEDGE_FLAG_TIMING) */
+    double wedge_ms;              /* Wedge Time (needs WEDGE_FLAG_TIMING) */
+    double vertex_ms;             /* PageRank vertex phase (needs WEDGE_FLAG_TIMING) */
+    uint64_t edges_scanned;       /* in-edges read by the pulls, summed over iterations */
+    uint64_t tiles_scanned;       /* 128-edge tiles visited by the pulls */
+    uint64_t pull_launches;       /* edge-pull kernel launches */
+    uint64_t kernel_launches;     /* all kernel launches of the run */
+    double pr_sum;                /* PageRank Sum (execution_pr.c:63-71); 0 for other apps */
+} wedge_stats_t;
+
+typedef struct wedge_graph wedge_graph_t;
+
+/* ---------------------------------------------------------------- loading */
+
+/* graph_data_read_from_file (graphdata.c:946-1133) + graph_data_initialize_data_structures
+ * (graphdata.c:648-942).  The file is header {uint64 V, uint64 E} followed by E records
+ * {uint64 src, uint64 dst} -- or {src, dst, weight} when app == WEDGE_APP_SSSP
+ * (application.c:171) -- grouped by ascending dst.  The size is checked exactly. */
+int wedge_cuda_load_graph(const char* path, int app, wedge_graph_t** out);
+
+/* as wedge_cuda_load_graph, choosing how SSSP weights are read (enum wedge_weights) */
+int wedge_cuda_load_graph_ex(const char* path, int app, int weight_kind, wedge_graph_t** out);
+
+/* the same file format, already in host memory (bytes = whole file image) */
+int wedge_cuda_load_graph_image(const void* image, uint64_t bytes, int app, int weight_kind, wedge_graph_t** out);
+
+/* host edge arrays grouped by ascending dst (the file's records without the header);
+ * weights may be NULL (weight_kind NONE) or hold raw 64-bit words */
+int wedge_cuda_load_edges(uint64_t num_vertices, uint64_t num_edges, const uint32_t* src, const uint32_t* dst,
+                          const uint64_t* weights, int weight_kind, wedge_graph_t** out);
+
+/* the reference's in-memory edge-vector list (graphdata.c:212-243; one vector = 4 words
+ * valid|dst-slice|src48, followed by 4 weight words when weighted), as a host would pass it
+ * to perform_edge_pull_phase_* (include/phases.h:58-60) */
+int wedge_cuda_load_edge_vectors(uint64_t num_vertices, const uint64_t* vectors, uint64_t num_vectors,
+                                 int weighted, int weight_kind, wedge_graph_t** out);
+
+/* synthetic inputs generated on the device (bit-identical to the CPU generators):
+ * R-MAT with quadrant probabilities a,b,c; symmetrise adds every reverse edge */
+int wedge_cuda_generate_rmat(uint32_t scale, uint32_t edge_factor, double a, double b, double c, uint64_t seed,
+                             int symmetrise, int weight_kind, wedge_graph_t** out);
+/* side x side 4-neighbour grid, both directions, plus floor(frac * 4*side*(side-1)) random directed pairs */
+int wedge_cuda_generate_grid(uint32_t side, double long_range_frac, uint64_t seed, int weight_kind,
+                             wedge_graph_t** out);
+
+/* ---------------------------------------------------------------- running */
+
+/* execution_initialize_* + execution_impl_{bfs,cc,pr,sssp} (execution.h:107-129): the whole
+ * traversal on the device; stats may be NULL.  Properties stay on the device. */
+int wedge_cuda_run(wedge_graph_t* g, int app, const wedge_params_t* params, wedge_stats_t* stats);
+
+/* one phase (enum wedge_phase) of the reference's driver loop, for hosts that sequence phases
+ * themselves.  *active_mass receives the reduced changed-edge mass after a pull
+ * (phase_op_combine_global_var_from_buf, phases.c:26-35) and may be NULL. */
+int wedge_cuda_run_phase(wedge_graph_t* g, int app, int phase, const wedge_params_t* params,
+                         uint64_t* active_mass);
+
+/* ---------------------------------------------------------------- results */
+
+/* graph_vertex_props, one 64-bit word per vertex (see the header comment); bytes >= 8*V */
+int wedge_cuda_read_results(wedge_graph_t* g, void* host_props, uint64_t bytes);
+/* graph_vertex_outdegrees as uint64 counts; bytes >= 8*V */
+int wedge_cuda_read_outdegrees(wedge_graph_t* g, uint64_t* host_outdeg, uint64_t bytes);
+
+uint64_t wedge_cuda_num_vertices(const wedge_graph_t* g);
+uint64_t wedge_cuda_num_edges(const wedge_graph_t* g);
+/* the CUDA stream (cudaStream_t) the graph's kernels run on, as an opaque pointer */
+void* wedge_cuda_stream(const wedge_graph_t* g);
+/* graph_data_* teardown (the reference never frees); safe on NULL */
+void wedge_cuda_free(wedge_graph_t* g);
+const char* wedge_cuda_status_string(int status);
+int wedge_cuda_abi_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

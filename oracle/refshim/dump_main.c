@@ -45,10 +45,14 @@ int main(int argc, char** argv)
     }
     if (!graph_data_read_from_file(path, 1, nodes))
         return 4;
-    graph_data_initialize_data_structures(threads, 1, nodes);
+    /* The reference's main sets these after graph_data_initialize_data_structures
+     * (main.c:75-79), whose execution_initialize_* already seeds the root from
+     * graph_param_root_vertex -- still 0 then, so `-r` does not move the BFS/SSSP
+     * root there.  Setting them first gives `-r` its documented meaning. */
     graph_param_num_static_iterations = iters;
     graph_param_root_vertex = root < graph_num_vertices ? root : 0;
     graph_param_frontier_threshold_pct = thr;
+    graph_data_initialize_data_structures(threads, 1, nodes);
 
     SSpindleTaskSpec spec;
     spec.func = &application_execute;

@@ -882,6 +882,15 @@ static inline uint64_t min_step(const orc_graph_t* g, int kind, const uint64_t* 
     return lane_min_sssp_f64(g, w, w + 4, acc);
 }
 
+/* folds one vector's reduced candidates into the destination accumulator
+ * (phase_edge_pull_cc.c:135, phase_edge_pull_sssp.c:142) */
+static inline uint64_t min_combine(int kind, uint64_t acc, uint64_t cand)
+{
+    if (kind == MIN_SSSP)
+        return min_epu32(cand, acc);
+    return as_d(cand) < as_d(acc) ? cand : acc;
+}
+
 /* "proposed value differs" test at a destination change: CC compares the bit
  * patterns of min(current, acc) (phase_edge_pull_cc.c:107-113); SSSP writes
  * only when acc < current (phase_edge_pull_sssp.c:112-116). */
@@ -935,13 +944,17 @@ static void pull_min_dense(run_t* r, int kind)
         uint64_t acc = min_init(kind), prev = UINT64_MAX;
         for (uint64_t i = base; i < max; ++i) {
             const uint64_t* w = &g->vec[i * words];
+            /* the gather precedes the flush of the previous destination
+             * (phase_edge_pull_cc.c:99 before :105-128), so a destination does
+             * not yet see its predecessor's update of this pass */
+            const uint64_t cand = min_step(g, kind, w, min_init(kind));
             const uint64_t d = dst_of(w);
             if (prev < d) {
                 min_flush(r, kind, prev, acc, &changed);
                 acc = min_init(kind);
             }
             prev = d;
-            acc = min_step(g, kind, w, acc);
+            acc = min_combine(kind, acc, cand);
         }
         min_unit_end(r, kind, u, prev, acc, &changed);
     }
@@ -976,13 +989,14 @@ static void pull_min_wedge(run_t* r, int kind)
                                         ((uint64_t)__builtin_ctzll(bits) << LOG2_PRECISION);
                     for (uint64_t k = 0; k < (1ull << LOG2_PRECISION); ++k) {
                         const uint64_t* w = &g->vec[(vi + k) * words];
+                        const uint64_t cand = min_step(g, kind, w, min_init(kind)); /* gather first */
                         const uint64_t d = dst_of(w);
                         if (prev < d) {
                             min_flush(r, kind, prev, acc, &changed);
                             acc = min_init(kind);
                         }
                         prev = d;
-                        acc = min_step(g, kind, w, acc);
+                        acc = min_combine(kind, acc, cand);
                     }
                 }
             }

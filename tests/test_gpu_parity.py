@@ -1,0 +1,328 @@
+"""Parity of the CUDA engine (through the C ABI) with the oracle and the
+reference's golden outputs.  Bars: CC labels and SSSP distances bit-exact;
+BFS reached set and levels exact, every parent an in-neighbour one level up;
+PageRank FP64 within 1e-12 relative L1; compensated FP32 PageRank within 1e-6
+relative L1 of FP64."""
+import os
+
+import numpy as np
+import pytest
+
+from helpers import UNREACHED, bfs_levels, check_bfs, golden, rel_l1
+
+pytestmark = pytest.mark.gpu
+
+META, DATA = golden()
+PR_TOL = 1e-12
+PR32_TOL = 1e-6
+
+
+@pytest.fixture(scope="module")
+def W(engine_lib):
+    return engine_lib
+
+
+@pytest.fixture(scope="module")
+def O(oracle_lib):
+    return oracle_lib
+
+
+def graph_edges(O, kind, p, symmetric=False):
+    if kind == "rmat":
+        V, s, d = O.rmat(p["scale"], p["edge_factor"], p["seed"])
+    else:
+        V, s, d = O.grid(p["side"], p["frac"], p["seed"])
+    if symmetric:
+        s, d = O.symmetrise(s, d)
+    s, d = O.sort_edges(V, s, d)
+    return V, s, d
+
+
+def run_engine(W, V, s, d, app, w=None, weight_kind=None, **params):
+    wk = weight_kind if weight_kind is not None else W.WEIGHTS_U64
+    with W.Graph.from_edges(V, s, d, w, wk if w is not None else W.WEIGHTS_NONE) as g:
+        st = g.run(app, W.Params(**params))
+        props = g.read_results()
+        od = g.read_outdegrees()
+    assert st["pull_launches"] > 0 or len(s) == 0
+    return props, od, st
+
+
+@pytest.mark.parametrize("case", META, ids=[c["key"] for c in META])
+def test_engine_matches_reference_golden(W, O, case):
+    V, s, d = graph_edges(O, case["kind"], case["params"], case["variant"] == "symmetric")
+    app = {"bfs": W.APP_BFS, "cc": W.APP_CC, "pr": W.APP_PR, "sssp": W.APP_SSSP}[case["app"]]
+    ra = case["run"]
+    w = O.weights(s, d) if case["app"] == "sssp" else None
+    props, od, st = run_engine(W, V, s, d, app, w, root=ra.get("root", 0), threshold_pct=ra.get("threshold_pct", 20),
+                               num_iterations=ra.get("iterations", 1))
+    ref = DATA[case["key"] + ".props"]
+    if case["app"] in ("cc", "sssp"):
+        assert np.array_equal(props, ref)
+    elif case["app"] == "bfs":
+        root = ra.get("root", 0)
+        lv = check_bfs(props, V, s, d, root)
+        reached = ref != UNREACHED
+        reached[root] = True
+        assert np.array_equal(lv >= 0, reached)
+    else:
+        assert rel_l1(props.view(np.float64), ref.view(np.float64)) < PR_TOL
+        assert np.array_equal(od.astype(np.float64), DATA[case["key"] + ".outdeg"].view(np.float64))
+        assert abs(st["pr_sum"] - 1.0) < 1e-9
+
+
+SIZES = [(8, 4, 11), (11, 16, 12), (13, 8, 13), (14, 32, 14)]
+SCHEDS = ["plain", "dense", "wedge"]
+
+
+def sched_id(W, name):
+    return {"plain": W.SCHED_PLAIN, "dense": W.SCHED_DENSE, "wedge": W.SCHED_WEDGE}[name]
+
+
+@pytest.mark.parametrize("scale,ef,seed", SIZES)
+@pytest.mark.parametrize("sched", SCHEDS)
+def test_cc_bit_exact(W, O, scale, ef, seed, sched):
+    for symmetric in (True, False):
+        V, s, d = graph_edges(O, "rmat", dict(scale=scale, edge_factor=ef, seed=seed), symmetric)
+        ref, _, _ = O.Graph.from_edges(V, s, d, O.CC).run(threads=4)
+        got, _, st = run_engine(W, V, s, d, W.APP_CC, sched=sched_id(W, sched))
+        assert np.array_equal(got, ref)
+        if sched == "wedge":
+            assert st["wedge_iterations"] >= 1 or st["iterations"] <= 2
+
+
+@pytest.mark.parametrize("scale,ef,seed", SIZES)
+@pytest.mark.parametrize("sched", SCHEDS)
+def test_sssp_bit_exact(W, O, scale, ef, seed, sched):
+    V, s, d = graph_edges(O, "rmat", dict(scale=scale, edge_factor=ef, seed=seed))
+    w = O.weights(s, d)
+    for root in (0, 3):
+        ref, _, _ = O.Graph.from_edges(V, s, d, O.SSSP, w).run(root=root, threads=4)
+        got, _, _ = run_engine(W, V, s, d, W.APP_SSSP, w, root=root, sched=sched_id(W, sched))
+        assert np.array_equal(got, ref)
+
+
+@pytest.mark.parametrize("scale,ef,seed", SIZES)
+def test_sssp_fp64_weights_bit_exact(W, O, scale, ef, seed):
+    V, s, d = graph_edges(O, "rmat", dict(scale=scale, edge_factor=ef, seed=seed))
+    w = O.weights(s, d, O.WEIGHTS_F64)
+    ref, _, _ = O.Graph.from_edges(V, s, d, O.SSSP, w).run(root=0, threads=2, weight_kind=O.WEIGHTS_F64)
+    got, _, _ = run_engine(W, V, s, d, W.APP_SSSP, w, weight_kind=W.WEIGHTS_F64, root=0)
+    assert np.array_equal(got, ref)  # 0 ULP
+
+
+@pytest.mark.parametrize("scale,ef,seed", SIZES)
+@pytest.mark.parametrize("sched", SCHEDS)
+def test_bfs_levels_exact_parents_valid(W, O, scale, ef, seed, sched):
+    V, s, d = graph_edges(O, "rmat", dict(scale=scale, edge_factor=ef, seed=seed))
+    for root in (0, 1, V - 1):
+        lv = bfs_levels(V, s, d, root)
+        got, _, _ = run_engine(W, V, s, d, W.APP_BFS, root=root, sched=sched_id(W, sched))
+        check_bfs(got, V, s, d, root, lv)
+        ref, _, _ = O.Graph.from_edges(V, s, d, O.BFS).run(root=root, threads=4)
+        check_bfs(ref, V, s, d, root, lv)
+
+
+@pytest.mark.parametrize("scale,ef,seed", SIZES)
+@pytest.mark.parametrize("damping", [0.875, 0.85])
+def test_pagerank_fp64(W, O, scale, ef, seed, damping):
+    V, s, d = graph_edges(O, "rmat", dict(scale=scale, edge_factor=ef, seed=seed))
+    ref, _, _ = O.Graph.from_edges(V, s, d, O.PR).run(iterations=16, damping=damping, threads=4)
+    got, _, st = run_engine(W, V, s, d, W.APP_PR, num_iterations=16, damping=damping)
+    assert rel_l1(got.view(np.float64), ref.view(np.float64)) < PR_TOL
+    assert abs(st["pr_sum"] - 1.0) < 1e-9
+
+
+@pytest.mark.parametrize("scale,ef,seed", SIZES)
+def test_pagerank_fp32_compensated(W, O, scale, ef, seed):
+    V, s, d = graph_edges(O, "rmat", dict(scale=scale, edge_factor=ef, seed=seed))
+    ref, _, _ = O.Graph.from_edges(V, s, d, O.PR).run(iterations=30, threads=4)
+    got, _, _ = run_engine(W, V, s, d, W.APP_PR, num_iterations=30, precision=W.PREC_FP32C)
+    a, b = got.view(np.float64), ref.view(np.float64)
+    err = rel_l1(a, b)
+    assert err < PR32_TOL, err
+
+
+def test_grid_sssp_and_bfs(W, O):
+    V, s, d = graph_edges(O, "grid", dict(side=64, frac=0.01, seed=3))
+    w = O.weights(s, d)
+    ref, _, _ = O.Graph.from_edges(V, s, d, O.SSSP, w).run(root=0, threads=4)
+    got, _, st = run_engine(W, V, s, d, W.APP_SSSP, w, root=0)
+    assert np.array_equal(got, ref)
+    got, _, _ = run_engine(W, V, s, d, W.APP_BFS, root=17)
+    check_bfs(got, V, s, d, 17)
+
+
+# ---------------------------------------------------------------- edge cases
+def test_hub_spanning_many_tiles(W, O):
+    """one destination with 5000 in-edges (40 tiles), others tiny"""
+    V = 6000
+    src = np.concatenate([np.arange(5000, dtype=np.uint32), np.array([1, 2, 3], np.uint32)])
+    dst = np.concatenate([np.full(5000, 5001, np.uint32), np.array([5002, 5002, 5003], np.uint32)])
+    order = np.lexsort((src, dst))
+    s, d = src[order], dst[order]
+    ref, _, _ = O.Graph.from_edges(V, s, d, O.PR).run(iterations=5, threads=2)
+    got, _, _ = run_engine(W, V, s, d, W.APP_PR, num_iterations=5)
+    assert rel_l1(got.view(np.float64), ref.view(np.float64)) < PR_TOL
+    # CC: the hub takes the minimum source label
+    got, _, _ = run_engine(W, V, s, d, W.APP_CC)
+    assert got.view(np.float64)[5001] == 0.0
+    got, _, _ = run_engine(W, V, s, d, W.APP_BFS, root=4999)
+    assert got[5001] == 4999
+
+
+def test_empty_and_tiny_graphs(W, O):
+    s = np.zeros(0, np.uint32)
+    d = np.zeros(0, np.uint32)
+    got, _, _ = run_engine(W, 5, s, d, W.APP_BFS, root=2)
+    assert np.all(got == UNREACHED)
+    got, _, _ = run_engine(W, 5, s, d, W.APP_CC)
+    assert got.view(np.float64).tolist() == [0.0, 1.0, 2.0, 3.0, 4.0]
+    got, _, _ = run_engine(W, 1, np.array([0], np.uint32), np.array([0], np.uint32), W.APP_PR, num_iterations=3)
+    assert abs(got.view(np.float64)[0] - 1.0) < 1e-15
+
+
+@pytest.mark.parametrize("name", ["path", "star", "fanin"])
+def test_known_answers(W, O, name):
+    from test_oracle import KATS, _kat
+
+    V, edges, levels = KATS[name]
+    s, d = _kat(O, V, edges)
+    got, _, _ = run_engine(W, V, s, d, W.APP_BFS, root=0)
+    assert check_bfs(got, V, s, d, 0).tolist() == levels
+    dist, _, _ = run_engine(W, V, s, d, W.APP_SSSP, np.ones(len(s), np.uint64), root=0)
+    assert [(-1 if x == UNREACHED else int(x)) for x in dist] == levels
+
+
+def test_root_out_of_range_uses_vertex_zero(W, O):
+    V, s, d = graph_edges(O, "rmat", dict(scale=9, edge_factor=8, seed=1))
+    a, _, _ = run_engine(W, V, s, d, W.APP_BFS, root=10**9)
+    b, _, _ = run_engine(W, V, s, d, W.APP_BFS, root=0)
+    check_bfs(a, V, s, d, 0)
+    assert np.array_equal(a != UNREACHED, b != UNREACHED)
+
+
+# ---------------------------------------------------------------- load paths
+def test_load_paths_agree(W, O, tmp_path):
+    V, s, d = graph_edges(O, "rmat", dict(scale=12, edge_factor=8, seed=21))
+    w = O.weights(s, d)
+    p2 = str(tmp_path / "g2.bin")
+    p3 = str(tmp_path / "g3.bin")
+    O.write_file(p2, V, s, d)
+    O.write_file(p3, V, s, d, w)
+    ref_pr, _, _ = run_engine(W, V, s, d, W.APP_PR, num_iterations=4)
+    with W.Graph.load(p2, W.APP_PR) as g:
+        g.run(W.APP_PR, W.Params(num_iterations=4))
+        assert np.array_equal(g.read_results(), ref_pr)  # same CSC -> same summation order
+    with W.Graph.load_image(open(p2, "rb").read(), W.APP_PR) as g:
+        g.run(W.APP_PR, W.Params(num_iterations=4))
+        assert np.array_equal(g.read_results(), ref_pr)
+    vec = O.Graph.from_edges(V, s, d, O.PR).edge_vectors()
+    with W.Graph.from_edge_vectors(V, vec, weighted=False) as g:
+        g.run(W.APP_PR, W.Params(num_iterations=4))
+        assert np.array_equal(g.read_results(), ref_pr)
+    ref_ss, _, _ = O.Graph.from_edges(V, s, d, O.SSSP, w).run(root=0, threads=2)
+    with W.Graph.load(p3, W.APP_SSSP) as g:
+        g.run(W.APP_SSSP, W.Params(root=0))
+        assert np.array_equal(g.read_results(), ref_ss)
+    vecw = O.Graph.from_edges(V, s, d, O.SSSP, w).edge_vectors()
+    with W.Graph.from_edge_vectors(V, vecw, weighted=True) as g:
+        g.run(W.APP_SSSP, W.Params(root=0))
+        assert np.array_equal(g.read_results(), ref_ss)
+
+
+@pytest.mark.parametrize("symmetrise", [False, True])
+def test_device_generator_matches_cpu_generator(W, O, symmetrise):
+    V, s, d = graph_edges(O, "rmat", dict(scale=13, edge_factor=8, seed=4), symmetrise)
+    a, od_a, _ = run_engine(W, V, s, d, W.APP_PR, num_iterations=3)
+    with W.Graph.rmat(13, 8, 4, symmetrise=symmetrise) as g:
+        assert g.V == V and g.E == len(s)
+        g.run(W.APP_PR, W.Params(num_iterations=3))
+        assert np.array_equal(g.read_results(), a)
+        assert np.array_equal(g.read_outdegrees(), od_a)
+
+
+def test_device_grid_generator_matches_cpu(W, O):
+    V, s, d = graph_edges(O, "grid", dict(side=48, frac=0.01, seed=3))
+    w = O.weights(s, d)
+    ref, _, _ = run_engine(W, V, s, d, W.APP_SSSP, w, root=5)
+    with W.Graph.grid(48, 0.01, 3, W.WEIGHTS_U64) as g:
+        assert g.V == V and g.E == len(s)
+        g.run(W.APP_SSSP, W.Params(root=5))
+        assert np.array_equal(g.read_results(), ref)
+
+
+def test_bad_inputs(W, O, tmp_path):
+    V, s, d = graph_edges(O, "rmat", dict(scale=8, edge_factor=4, seed=1))
+    p = str(tmp_path / "g.bin")
+    O.write_file(p, V, s, d)
+    with pytest.raises(W.WedgeError) as e:
+        W.Graph.load(p, W.APP_SSSP)  # 2-tuples where SSSP expects 3-tuples
+    assert e.value.status == -2
+    raw = open(p, "rb").read()
+    with pytest.raises(W.WedgeError) as e:
+        W.Graph.load_image(raw[:-8], W.APP_BFS)
+    assert e.value.status == -2
+    with pytest.raises(W.WedgeError) as e:
+        W.Graph.from_edges(V, d[::-1].copy(), d[::-1].copy())  # descending destinations
+    assert e.value.status == -2
+    with pytest.raises(W.WedgeError) as e:
+        W.Graph.from_edges(4, np.array([9], np.uint32), np.array([0], np.uint32))  # id out of range
+    assert e.value.status == -2
+    with W.Graph.from_edges(V, s, d) as g:
+        with pytest.raises(W.WedgeError) as e:
+            g.run(W.APP_SSSP)  # no weights loaded
+        assert e.value.status == -6
+        with pytest.raises(W.WedgeError) as e:
+            g.run(W.APP_BFS, W.Params(threshold_pct=101))
+        assert e.value.status == -6
+
+
+# ---------------------------------------------------------------- execution modes
+@pytest.mark.parametrize("app", ["bfs", "cc", "sssp"])
+def test_cuda_graph_loop_matches_host_loop(W, O, app):
+    V, s, d = graph_edges(O, "rmat", dict(scale=13, edge_factor=16, seed=5), app == "cc")
+    w = O.weights(s, d) if app == "sssp" else None
+    a = {"bfs": W.APP_BFS, "cc": W.APP_CC, "sssp": W.APP_SSSP}[app]
+    host, _, st1 = run_engine(W, V, s, d, a, w, root=0)
+    graph, _, st2 = run_engine(W, V, s, d, a, w, root=0, flags=W.FLAG_GRAPH)
+    timed, _, st3 = run_engine(W, V, s, d, a, w, root=0, flags=W.FLAG_TIMING)
+    if app == "bfs":
+        check_bfs(graph, V, s, d, 0)
+        check_bfs(timed, V, s, d, 0)
+    else:
+        assert np.array_equal(host, graph) and np.array_equal(host, timed)
+    assert st3["pull_ms_dense"] + st3["pull_ms_wedge"] > 0
+
+
+def test_phase_api_drives_the_reference_loop(W, O):
+    """execution_impl_bfs's own loop (execution_bfs.c:139-353) over wedge_cuda_run_phase"""
+    V, s, d = graph_edges(O, "rmat", dict(scale=12, edge_factor=16, seed=6))
+    E = len(s)
+    p = W.Params(root=0)
+    with W.Graph.from_edges(V, s, d) as g:
+        g.run_phase(W.APP_BFS, 0, p)
+        od = g.read_outdegrees()
+        active = int(od[0])
+        threshold = E * 20 // 100
+        iters = 0
+        while True:
+            iters += 1
+            phase = 1 if active > threshold else 2
+            active = g.run_phase(W.APP_BFS, phase, p)
+            if active == 0:
+                break
+            g.run_phase(W.APP_BFS, 4, p)  # wedge build (no-op when the next pull is dense)
+            g.run_phase(W.APP_BFS, 5, p)  # advance
+            assert iters < 100
+        check_bfs(g.read_results(), V, s, d, 0)
+
+
+def test_iteration_cap_reports_not_converged(W, O):
+    V, s, d = graph_edges(O, "grid", dict(side=32, frac=0.0, seed=3))
+    with W.Graph.from_edges(V, s, d) as g:
+        with pytest.raises(W.WedgeError) as e:
+            g.run(W.APP_BFS, W.Params(root=0, max_iterations=3))
+        assert e.value.status == -5
+        st = g.run(W.APP_BFS, W.Params(root=0, max_iterations=3), allow_not_converged=True)
+        assert st["iterations"] == 3

@@ -1,0 +1,1457 @@
+// sm_103a edge-pull engine: graph build, traversal kernels, drivers, C ABI.
+//
+// Reference correspondence (stanford-mast/Wedge):
+//   build_from_device_edges   graphdata.c:402-585 (vertex index, out-degrees, CSRI)
+//   pull_kernel<BFS>          phase_edge_pull_bfs.c:109-332
+//   pull_kernel<CC>           phase_edge_pull_cc.c:53-297
+//   pull_kernel<SSSP>         phase_edge_pull_sssp.c:57-306
+//   pull_kernel<PR>           phase_edge_pull_pr.c:28-116
+//   pr_finish_kernel          phases.c:71-114 (ordered merge) + phases.c:37-46 (total rank)
+//   pr_vertex_kernel          phase_vertex_pr.c:26-77
+//   collect_kernel            wedge.c:63-155 (walk of the active-vertex bitmap)
+//   wedge_build_kernel        wedge.c:37-46 (CSRI walk setting frontier bits)
+//   decide_kernel             execution_*.c driver loop: mass reduce, dense/Wedge choice, convergence
+//   run_traversal / run_pr    execution_{bfs,cc,sssp}.c:122-365 / execution_pr.c:396-486
+#include <cub/device/device_scan.cuh>
+
+#include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
+
+#include "engine.cuh"
+#include "pull.cuh"
+
+namespace wedge {
+
+constexpr int PULL_THREADS = 256;
+constexpr int AUX_THREADS = 256;
+
+int compute_grids(wedge_graph* h);
+
+int cuda_status(cudaError_t e)
+{
+    if (e == cudaErrorMemoryAllocation)
+        return WEDGE_ERR_OOM;
+    return WEDGE_ERR_CUDA;
+}
+
+int new_handle(wedge_graph** out)
+{
+    wedge_graph* h = (wedge_graph*)calloc(1, sizeof(wedge_graph));
+    if (!h)
+        return WEDGE_ERR_OOM;
+    h->built_app = -1;
+    h->last_app = -1;
+    h->graph_app = -1;
+    WEDGE_CHECK(cudaGetDevice(&h->device));
+    WEDGE_CHECK(cudaDeviceGetAttribute(&h->num_sms, cudaDevAttrMultiProcessorCount, h->device));
+    WEDGE_CHECK(cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking));
+    for (int i = 0; i < 8; ++i)
+        WEDGE_CHECK(cudaEventCreate(&h->ev[i]));
+    WEDGE_CHECK(cudaMallocHost((void**)&h->h_ctrl, sizeof(Ctrl)));
+    *out = h;
+    return WEDGE_OK;
+}
+
+int track(wedge_graph* h, void* p)
+{
+    if (h->nallocs >= (int)(sizeof(h->allocs) / sizeof(h->allocs[0])))
+        return WEDGE_ERR_OOM;
+    h->allocs[h->nallocs++] = p;
+    return WEDGE_OK;
+}
+
+static int track_state(wedge_graph* h, void* p)
+{
+    if (h->nstate >= (int)(sizeof(h->state_allocs) / sizeof(h->state_allocs[0])))
+        return WEDGE_ERR_OOM;
+    h->state_allocs[h->nstate++] = p;
+    return WEDGE_OK;
+}
+
+static void free_state(wedge_graph* h)
+{
+    for (int i = 0; i < h->nstate; ++i)
+        cudaFree(h->state_allocs[i]);
+    h->nstate = 0;
+    memset(&h->s, 0, sizeof(h->s));
+    h->built_app = -1;
+    if (h->graph_exec) {
+        cudaGraphExecDestroy(h->graph_exec);
+        h->graph_exec = nullptr;
+        h->graph_app = -1;
+    }
+}
+
+void free_handle(wedge_graph* h)
+{
+    if (!h)
+        return;
+    if (h->stream)
+        cudaStreamSynchronize(h->stream);
+    free_state(h);
+    for (int i = 0; i < h->nallocs; ++i)
+        cudaFree(h->allocs[i]);
+    for (int i = 0; i < 8; ++i)
+        if (h->ev[i])
+            cudaEventDestroy(h->ev[i]);
+    if (h->h_ctrl)
+        cudaFreeHost(h->h_ctrl);
+    if (h->stream)
+        cudaStreamDestroy(h->stream);
+    free(h);
+}
+
+template <class T>
+static int dalloc(wedge_graph* h, T** p, uint64_t count, bool state = false)
+{
+    *p = nullptr;
+    const size_t bytes = (size_t)(count ? count : 1) * sizeof(T);
+    cudaError_t e = cudaMalloc((void**)p, bytes);
+    if (e != cudaSuccess)
+        return cuda_status(e);
+    return state ? track_state(h, *p) : track(h, *p);
+}
+
+static uint32_t grid_for(uint64_t work, uint32_t threads, uint32_t cap)
+{
+    uint64_t b = (work + threads - 1) / threads;
+    if (b < 1)
+        b = 1;
+    return (uint32_t)(b < cap ? b : cap);
+}
+
+/* ================================================================= build */
+
+__global__ void validate_kernel(const uint32_t* src, const uint32_t* dst, uint64_t E, uint64_t V, int* err)
+{
+    for (uint64_t e = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; e < E; e += (uint64_t)gridDim.x * blockDim.x) {
+        const uint32_t d = dst[e];
+        if (src[e] >= V || d >= V)
+            atomicOr(err, 1);
+        if (e > 0 && dst[e - 1] > d)
+            atomicOr(err, 2);
+    }
+}
+
+// head flag of edge e: first in-edge of its destination (graphdata.c:402-427)
+__global__ void head_flag_kernel(const uint32_t* dst, uint64_t E, uint32_t* flag)
+{
+    for (uint64_t e = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; e < E; e += (uint64_t)gridDim.x * blockDim.x)
+        flag[e] = (e == 0 || dst[e] != dst[e - 1]) ? 1u : 0u;
+}
+
+// kidx = inclusive scan of head flags: compressed destination = kidx - 1
+__global__ void compress_kernel(const uint32_t* dst, const uint32_t* kidx, uint64_t E, uint32_t* dst_id,
+                                unsigned long long* dst_off)
+{
+    for (uint64_t e = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; e < E; e += (uint64_t)gridDim.x * blockDim.x) {
+        if (e == 0 || dst[e] != dst[e - 1]) {
+            const uint32_t k = kidx[e] - 1u;
+            dst_id[k] = dst[e];
+            dst_off[k] = e;
+        }
+    }
+}
+
+__global__ void tile_index_kernel(const uint32_t* kidx, uint64_t E, uint32_t T, uint32_t Vne, uint32_t* tile_dst0,
+                                  unsigned long long* dst_off)
+{
+    for (uint64_t t = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; t <= T; t += (uint64_t)gridDim.x * blockDim.x) {
+        tile_dst0[t] = (t < T) ? kidx[t * TILE] - 1u : Vne;
+        if (t == 0)
+            dst_off[Vne] = E;
+    }
+}
+
+__global__ void outdeg_kernel(const uint32_t* src, uint64_t E, uint32_t* outdeg)
+{
+    for (uint64_t e = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; e < E; e += (uint64_t)gridDim.x * blockDim.x)
+        atomicAdd(&outdeg[src[e]], 1u);
+}
+
+__global__ void widen_kernel(const uint32_t* in, unsigned long long* out, uint64_t n)
+{
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x)
+        out[i] = in[i];
+}
+
+// CSRI fill (graphdata.c:535-569): chunk id of every out-edge, grouped by source
+__global__ void csri_fill_kernel(const uint32_t* src, uint64_t E, unsigned long long* cursor, uint32_t* csri)
+{
+    for (uint64_t e = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; e < E; e += (uint64_t)gridDim.x * blockDim.x) {
+        const unsigned long long pos = atomicAdd(&cursor[src[e]], 1ull);
+        csri[pos] = (uint32_t)(e / CHUNK);
+    }
+}
+
+__global__ void split_kernel(const unsigned long long* dst_off, uint32_t Vne, uint32_t* split_k, uint32_t* split_t0,
+                             uint32_t* split_t1, unsigned int* count)
+{
+    for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < Vne; k += gridDim.x * blockDim.x) {
+        const uint32_t t0 = (uint32_t)(dst_off[k] / TILE);
+        const uint32_t t1 = (uint32_t)((dst_off[k + 1] - 1) / TILE);
+        if (t0 != t1) {
+            const unsigned int i = atomicAdd(count, 1u);
+            split_k[i] = k;
+            split_t0[i] = t0;
+            split_t1[i] = t1;
+        }
+    }
+}
+
+__global__ void pad_kernel(uint32_t* src, unsigned long long* w, uint64_t E, uint64_t Epad)
+{
+    for (uint64_t e = E + blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; e < Epad; e += (uint64_t)gridDim.x * blockDim.x) {
+        src[e] = NONE32;
+        if (w)
+            w[e] = 0ull;
+    }
+}
+
+template <class InT, class OutT>
+static int device_scan(wedge_graph* h, const InT* in, OutT* out, uint64_t n, bool inclusive)
+{
+    size_t bytes = 0;
+    if (inclusive)
+        WEDGE_CHECK(cub::DeviceScan::InclusiveSum(nullptr, bytes, in, out, (long long)n, h->stream));
+    else
+        WEDGE_CHECK(cub::DeviceScan::ExclusiveSum(nullptr, bytes, in, out, (long long)n, h->stream));
+    void* tmp = nullptr;
+    WEDGE_CHECK(cudaMallocAsync(&tmp, bytes, h->stream));
+    cudaError_t e = inclusive ? cub::DeviceScan::InclusiveSum(tmp, bytes, in, out, (long long)n, h->stream)
+                              : cub::DeviceScan::ExclusiveSum(tmp, bytes, in, out, (long long)n, h->stream);
+    cudaFreeAsync(tmp, h->stream);
+    WEDGE_CHECK(e);
+    return WEDGE_OK;
+}
+
+// Builds the device CSC from destination-sorted device edge arrays.  d_src and
+// d_w (if any) must hold roundup(E, TILE) entries and become owned by the
+// handle; d_dst is consumed and freed.
+int build_from_device_edges(wedge_graph* h, uint64_t V, uint64_t E, uint32_t* d_src, uint32_t* d_dst,
+                            unsigned long long* d_w, int weight_kind)
+{
+    cudaStream_t st = h->stream;
+    DevGraph& g = h->g;
+    g.V = V;
+    g.E = E;
+    g.Epad = (E + TILE - 1) / TILE * TILE;
+    g.T = (uint32_t)(g.Epad / TILE);
+    g.weight_kind = (uint32_t)weight_kind;
+    h->weight_kind = weight_kind;
+    g.src = d_src;
+    g.w = d_w;
+    const uint32_t cap = (uint32_t)h->num_sms * 16u;
+
+    int* d_err = nullptr;
+    WEDGE_CHECK(cudaMallocAsync((void**)&d_err, sizeof(int), st));
+    WEDGE_CHECK(cudaMemsetAsync(d_err, 0, sizeof(int), st));
+    if (E)
+        validate_kernel<<<grid_for(E, AUX_THREADS, cap), AUX_THREADS, 0, st>>>(d_src, d_dst, E, V, d_err);
+    int herr = 0;
+    WEDGE_CHECK(cudaMemcpyAsync(&herr, d_err, sizeof(int), cudaMemcpyDeviceToHost, st));
+    WEDGE_CHECK(cudaStreamSynchronize(st));
+    cudaFreeAsync(d_err, st);
+    if (herr) {
+        cudaFreeAsync(d_dst, st);
+        return WEDGE_ERR_FORMAT;
+    }
+
+    // compressed destinations
+    uint32_t* kidx = nullptr;
+    WEDGE_CHECK(cudaMallocAsync((void**)&kidx, (E ? E : 1) * sizeof(uint32_t), st));
+    uint32_t Vne = 0;
+    if (E) {
+        head_flag_kernel<<<grid_for(E, AUX_THREADS, cap), AUX_THREADS, 0, st>>>(d_dst, E, kidx);
+        int rc = device_scan(h, kidx, kidx, E, true);
+        if (rc)
+            return rc;
+        WEDGE_CHECK(cudaMemcpyAsync(&Vne, kidx + (E - 1), sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
+        WEDGE_CHECK(cudaStreamSynchronize(st));
+    }
+    g.Vne = Vne;
+    uint32_t *dst_id, *tile_dst0, *outdeg, *csri;
+    unsigned long long *dst_off, *csri_off;
+    int rc;
+    if ((rc = dalloc(h, &dst_id, Vne)) || (rc = dalloc(h, &dst_off, (uint64_t)Vne + 1)) ||
+        (rc = dalloc(h, &tile_dst0, (uint64_t)g.T + 1)) || (rc = dalloc(h, &outdeg, V)) ||
+        (rc = dalloc(h, &csri_off, V + 1)) || (rc = dalloc(h, &csri, E)))
+        return rc;
+    if (E) {
+        compress_kernel<<<grid_for(E, AUX_THREADS, cap), AUX_THREADS, 0, st>>>(d_dst, kidx, E, dst_id, dst_off);
+    }
+    tile_index_kernel<<<grid_for((uint64_t)g.T + 1, AUX_THREADS, cap), AUX_THREADS, 0, st>>>(kidx, E, g.T, Vne,
+                                                                                               tile_dst0, dst_off);
+    cudaFreeAsync(kidx, st);
+    cudaFreeAsync(d_dst, st);
+
+    // out-degrees and CSRI
+    WEDGE_CHECK(cudaMemsetAsync(outdeg, 0, V * sizeof(uint32_t), st));
+    if (E)
+        outdeg_kernel<<<grid_for(E, AUX_THREADS, cap), AUX_THREADS, 0, st>>>(d_src, E, outdeg);
+    unsigned long long* wide = nullptr;
+    WEDGE_CHECK(cudaMallocAsync((void**)&wide, (V + 1) * sizeof(unsigned long long), st));
+    widen_kernel<<<grid_for(V, AUX_THREADS, cap), AUX_THREADS, 0, st>>>(outdeg, wide, V);
+    WEDGE_CHECK(cudaMemsetAsync(wide + V, 0, sizeof(unsigned long long), st));
+    if ((rc = device_scan(h, wide, csri_off, V + 1, false)))
+        return rc;
+    WEDGE_CHECK(cudaMemcpyAsync(wide, csri_off, (V + 1) * sizeof(unsigned long long), cudaMemcpyDeviceToDevice, st));
+    if (E)
+        csri_fill_kernel<<<grid_for(E, AUX_THREADS, cap), AUX_THREADS, 0, st>>>(d_src, E, wide, csri);
+    cudaFreeAsync(wide, st);
+
+    // destinations whose in-edges span tiles (PageRank fixup list)
+    uint32_t *split_k, *split_t0, *split_t1;
+    if ((rc = dalloc(h, &split_k, g.T)) || (rc = dalloc(h, &split_t0, g.T)) || (rc = dalloc(h, &split_t1, g.T)))
+        return rc;
+    unsigned int* d_cnt = nullptr;
+    WEDGE_CHECK(cudaMallocAsync((void**)&d_cnt, sizeof(unsigned int), st));
+    WEDGE_CHECK(cudaMemsetAsync(d_cnt, 0, sizeof(unsigned int), st));
+    if (Vne)
+        split_kernel<<<grid_for(Vne, AUX_THREADS, cap), AUX_THREADS, 0, st>>>(dst_off, Vne, split_k, split_t0, split_t1,
+                                                                             d_cnt);
+    unsigned int nsplit = 0;
+    WEDGE_CHECK(cudaMemcpyAsync(&nsplit, d_cnt, sizeof(unsigned int), cudaMemcpyDeviceToHost, st));
+    if (g.Epad > E)
+        pad_kernel<<<1, 128, 0, st>>>(d_src, d_w, E, g.Epad);
+    WEDGE_CHECK(cudaStreamSynchronize(st));
+    cudaFreeAsync(d_cnt, st);
+    WEDGE_CHECK(cudaGetLastError());
+    g.nsplit = nsplit;
+    g.dst_id = dst_id;
+    g.dst_off = dst_off;
+    g.tile_dst0 = tile_dst0;
+    g.outdeg = outdeg;
+    g.csri_off = csri_off;
+    g.csri = csri;
+    g.split_k = split_k;
+    g.split_t0 = split_t0;
+    g.split_t1 = split_t1;
+
+    return compute_grids(h);
+}
+
+/* ============================================================ traversal */
+
+__device__ __forceinline__ unsigned long long warp_sum_u64(unsigned long long x)
+{
+#pragma unroll
+    for (int d = 16; d > 0; d >>= 1)
+        x += __shfl_xor_sync(FULL, x, d);
+    return x;
+}
+
+__device__ __forceinline__ double warp_sum_f64(double x)
+{
+#pragma unroll
+    for (int d = 16; d > 0; d >>= 1)
+        x = __dadd_rn(x, __shfl_xor_sync(FULL, x, d));
+    return x;
+}
+
+__device__ __forceinline__ const uint32_t* cur_front(const DevState& s, uint32_t parity)
+{
+    return parity ? s.front1 : s.front0;
+}
+
+// pull output bitmap: BFS writes the other half of its double buffer
+__device__ __forceinline__ uint32_t* next_front(const DevState& s, uint32_t app, uint32_t parity)
+{
+    return (app == WEDGE_APP_BFS) ? (parity ? s.front0 : s.front1) : s.front0;
+}
+
+// Edge pull over all tiles (dense) or over the tiles of the Wedge frontier.
+// block_cnt[4*b + {0,1,2}] = changed mass, in-edges read, tiles visited.
+template <int APP>
+__global__ void __launch_bounds__(PULL_THREADS) pull_kernel(DevGraph g, DevState s, unsigned long long* block_cnt)
+{
+    __shared__ unsigned long long sh_cnt[PULL_THREADS / 32][3];
+    __shared__ double sh_sum[PULL_THREADS / 32];
+    Ctrl* c = s.ctrl;
+    if (c->done)
+        return;
+    const int lane = threadIdx.x & 31;
+    const int wib = threadIdx.x >> 5;
+    const uint32_t gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const uint32_t nw = (gridDim.x * blockDim.x) >> 5;
+    const uint32_t mode = c->mode;
+    const uint32_t ntiles = (mode == MODE_DENSE) ? g.T : c->tiles;
+    const uint32_t parity = c->parity;
+    const uint32_t* cur = cur_front(s, parity);
+    uint32_t* nxt = next_front(s, APP, parity);
+    unsigned long long mass = 0, edges = 0, tiles = 0;
+    double psum = 0.0;
+
+    for (uint32_t i = gw; i < ntiles; i += nw) {
+        uint32_t t = i, cmask = 0xFu;
+        if (mode != MODE_DENSE) {
+            t = s.tile_list[i];
+            if (lane == 0) {
+                const uint32_t sh = (t & 7u) * 4u;
+                cmask = (s.chunk_bits[t >> 3] >> sh) & 0xFu;
+                atomicAnd(&s.chunk_bits[t >> 3], ~(0xFu << sh)); /* consume (phase_edge_pull_bfs.c:256) */
+            }
+            cmask = __shfl_sync(FULL, cmask, 0);
+        }
+        ++tiles;
+        const uint32_t k0 = g.tile_dst0[t];
+        const uint32_t kend = g.tile_dst0[t + 1];
+        if (APP == WEDGE_APP_BFS) {
+            // skip a tile whose destinations are all visited (the reference's jump over
+            // converged vertices, phase_edge_pull_bfs.c:189-204)
+            const uint32_t klim = min(kend, g.Vne - 1u);
+            const uint32_t w0 = k0 >> 5, w1 = klim >> 5;
+            bool open = false;
+            if ((uint32_t)lane <= w1 - w0) {
+                const uint32_t wi = w0 + lane;
+                const uint32_t lo = (wi == w0) ? (k0 & 31u) : 0u;
+                const uint32_t hi = (wi == w1) ? (klim & 31u) : 31u;
+                const uint32_t range = (hi == 31u ? FULL : ((2u << hi) - 1u)) & ~((1u << lo) - 1u);
+                open = (~s.vis_c[wi] & range) != 0u;
+            }
+            if (!__any_sync(FULL, open))
+                continue;
+        }
+        TileGeo tg;
+        tile_geometry(g, t, k0, kend, lane, tg);
+        const bool on = (cmask >> (lane >> 3)) & 1u;
+        uint4 sv = make_uint4(NONE32, NONE32, NONE32, NONE32);
+        if (on)
+            sv = ld_stream_v4(g.src + tg.base + 4u * (uint32_t)lane);
+        const uint32_t sa[4] = {sv.x, sv.y, sv.z, sv.w};
+
+        if (APP == WEDGE_APP_BFS) {
+            uint32_t v[4];
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+                v[q] = NONE32;
+                if (sa[q] != NONE32) {
+                    ++edges;
+                    const uint32_t k = pos_dst(tg, q);
+                    if (!test_bit32(s.vis_c, k) && test_bit32(cur, sa[q]))
+                        v[q] = sa[q];
+                }
+            }
+            seg_reduce(v, tg, lane, MinU32(), [&](uint32_t k, uint32_t val, int) {
+                if (val == NONE32)
+                    return;
+                const uint32_t vtx = g.dst_id[k];
+                const uint32_t old = atomicMin(&s.prop32[vtx], val);
+                if (old == NONE32) {
+                    atomicOr(&s.vis_c[k >> 5], 1u << (k & 31u));
+                    atomicOr(&nxt[vtx >> 5], 1u << (vtx & 31u));
+                    mass += g.outdeg[vtx];
+                }
+            });
+        } else if (APP == WEDGE_APP_CC) {
+            uint32_t v[4];
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+                v[q] = NONE32;
+                if (sa[q] != NONE32) {
+                    ++edges;
+                    v[q] = s.prop32[sa[q]];
+                }
+            }
+            seg_reduce(v, tg, lane, MinU32(), [&](uint32_t k, uint32_t val, int) {
+                const uint32_t vtx = g.dst_id[k];
+                if (val < s.prop32[vtx]) {
+                    const uint32_t old = atomicMin(&s.prop32[vtx], val);
+                    if (val < old) {
+                        const uint32_t b = 1u << (vtx & 31u);
+                        if (!(atomicOr(&nxt[vtx >> 5], b) & b))
+                            mass += g.outdeg[vtx];
+                    }
+                }
+            });
+        } else if (APP == WEDGE_APP_SSSP) {
+            unsigned long long wv[4] = {0, 0, 0, 0};
+            if (on) {
+                const ulonglong2 a = ld_stream_v2u64(g.w + tg.base + 4u * (uint32_t)lane);
+                const ulonglong2 b = ld_stream_v2u64(g.w + tg.base + 4u * (uint32_t)lane + 2u);
+                wv[0] = a.x;
+                wv[1] = a.y;
+                wv[2] = b.x;
+                wv[3] = b.y;
+            }
+            unsigned long long v[4];
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+                v[q] = NONE64;
+                if (sa[q] != NONE32) {
+                    ++edges;
+                    const unsigned long long d = s.prop64[sa[q]];
+                    if (g.weight_kind == WEDGE_WEIGHTS_F64)
+                        v[q] = (unsigned long long)__double_as_longlong(
+                            __dadd_rn(__longlong_as_double((long long)d), __longlong_as_double((long long)wv[q])));
+                    else
+                        v[q] = (d == NONE64) ? NONE64 : d + wv[q]; /* phase_edge_pull_sssp.c:136-137 */
+                }
+            }
+            seg_reduce(v, tg, lane, MinU64(), [&](uint32_t k, unsigned long long val, int) {
+                const uint32_t vtx = g.dst_id[k];
+                if (val < s.prop64[vtx]) {
+                    const unsigned long long old = atomicMin(&s.prop64[vtx], val);
+                    if (val < old) {
+                        const uint32_t b = 1u << (vtx & 31u);
+                        if (!(atomicOr(&nxt[vtx >> 5], b) & b))
+                            mass += g.outdeg[vtx];
+                    }
+                }
+            });
+        } else if (APP == WEDGE_APP_PR) {
+            if (s.precision == WEDGE_PREC_FP32C) {
+                F2 v[4];
+#pragma unroll
+                for (int q = 0; q < 4; ++q) {
+                    v[q] = F2{0.0f, 0.0f};
+                    if (sa[q] != NONE32) {
+                        ++edges;
+                        v[q].s = s.rank32[sa[q]];
+                    }
+                }
+                const AddF2 add;
+                const F2 ls = add(add(v[0], v[1]), add(v[2], v[3]));
+                psum = __dadd_rn(psum, warp_sum_f64(__dadd_rn((double)ls.s, (double)ls.c)));
+                seg_reduce(v, tg, lane, add, [&](uint32_t k, F2 val, int kind) {
+                    if (kind == EMIT_COMPLETE) {
+                        s.acc[g.dst_id[k]] = __dadd_rn((double)val.s, (double)val.c);
+                    } else {
+                        float* p = (kind == EMIT_HEAD) ? s.head_part32 : s.tail_part32;
+                        p[2u * t] = val.s;
+                        p[2u * t + 1u] = val.c;
+                    }
+                });
+            } else {
+                double v[4];
+#pragma unroll
+                for (int q = 0; q < 4; ++q) {
+                    v[q] = 0.0;
+                    if (sa[q] != NONE32) {
+                        ++edges;
+                        v[q] = s.rank[sa[q]];
+                    }
+                }
+                psum = __dadd_rn(psum, warp_sum_f64(__dadd_rn(__dadd_rn(v[0], v[1]), __dadd_rn(v[2], v[3]))));
+                seg_reduce(v, tg, lane, AddF64(), [&](uint32_t k, double val, int kind) {
+                    if (kind == EMIT_COMPLETE)
+                        s.acc[g.dst_id[k]] = val;
+                    else if (kind == EMIT_HEAD)
+                        s.head_part[t] = val;
+                    else
+                        s.tail_part[t] = val;
+                });
+            }
+        }
+    }
+    // per-block counters (no same-address atomics): reduced by decide_kernel
+    mass = warp_sum_u64(mass);
+    edges = warp_sum_u64(edges);
+    if (lane == 0) {
+        sh_cnt[wib][0] = mass;
+        sh_cnt[wib][1] = edges;
+        sh_cnt[wib][2] = tiles;
+        sh_sum[wib] = psum;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        unsigned long long a = 0, b = 0, t2 = 0;
+        double ps = 0.0;
+        for (int w = 0; w < PULL_THREADS / 32; ++w) {
+            a += sh_cnt[w][0];
+            b += sh_cnt[w][1];
+            t2 += sh_cnt[w][2];
+            ps = __dadd_rn(ps, sh_sum[w]);
+        }
+        block_cnt[4u * blockIdx.x + 0u] = a;
+        block_cnt[4u * blockIdx.x + 1u] = b;
+        block_cnt[4u * blockIdx.x + 2u] = t2;
+        if (APP == WEDGE_APP_PR)
+            s.block_part[blockIdx.x] = ps;
+    }
+}
+
+__device__ __forceinline__ uint32_t choose_mode(uint32_t sched, unsigned long long mass, unsigned long long thr)
+{
+    if (sched == WEDGE_SCHED_DENSE)
+        return MODE_DENSE;
+    if (sched == WEDGE_SCHED_WEDGE)
+        return MODE_WEDGE;
+    return mass > thr ? MODE_DENSE : MODE_WEDGE; /* execution_bfs.c:141 */
+}
+
+// After a pull: reduce the block counters, count the iteration, stop when no
+// edge was activated (execution_bfs.c:239-251) or at the cap, choose the next
+// pull (execution_bfs.c:141, execution_cc.c:103).
+__global__ void decide_kernel(DevState s, const unsigned long long* block_cnt, uint32_t nblocks, uint32_t app)
+{
+    __shared__ unsigned long long sh[3][AUX_THREADS / 32];
+    Ctrl* c = s.ctrl;
+    if (c->done)
+        return;
+    unsigned long long m = 0, e = 0, t = 0;
+    for (uint32_t i = threadIdx.x; i < nblocks; i += blockDim.x) {
+        m += block_cnt[4u * i];
+        e += block_cnt[4u * i + 1u];
+        t += block_cnt[4u * i + 2u];
+    }
+    m = warp_sum_u64(m);
+    e = warp_sum_u64(e);
+    t = warp_sum_u64(t);
+    if ((threadIdx.x & 31) == 0) {
+        sh[0][threadIdx.x >> 5] = m;
+        sh[1][threadIdx.x >> 5] = e;
+        sh[2][threadIdx.x >> 5] = t;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        m = e = t = 0;
+        for (int w = 0; w < AUX_THREADS / 32; ++w) {
+            m += sh[0][w];
+            e += sh[1][w];
+            t += sh[2][w];
+        }
+        c->edges_scanned += e;
+        c->tiles_scanned += t;
+        c->pull_launches += 1u;
+        if (c->mode == MODE_WEDGE)
+            c->wedge_iters += 1u;
+        c->iter += 1u;
+        c->last_mass = m;
+        c->mass = m;
+        if (app == WEDGE_APP_BFS)
+            c->parity ^= 1u;
+        c->tiles = 0u;
+        c->items = 0u;
+        if (m == 0ull) {
+            c->done = 1u;
+            c->loop = 0u;
+        } else if (c->iter >= c->max_iter) {
+            c->done = 1u;
+            c->not_converged = 1u;
+            c->loop = 0u;
+        } else {
+            c->mode = choose_mode(c->sched, m, c->threshold);
+        }
+    }
+}
+
+// Walk the vertices activated by the last pull (the reference walks
+// graph_frontier_active_vertices, wedge.c:86-153) and emit one work item per
+// PIECE of each vertex's CSRI list; warp-aggregated with a shuffle scan.
+__global__ void collect_kernel(DevGraph g, DevState s, uint32_t app)
+{
+    Ctrl* c = s.ctrl;
+    if (c->done || c->mode != MODE_WEDGE)
+        return;
+    const uint32_t* fb = (app == WEDGE_APP_BFS) ? cur_front(s, c->parity) : s.front0;
+    const uint64_t nwords = (g.V + 31) / 32;
+    const int lane = threadIdx.x & 31;
+    const uint64_t gw = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) >> 5;
+    const uint64_t nw = ((uint64_t)gridDim.x * blockDim.x) >> 5;
+    for (uint64_t base = gw * 32; base < nwords; base += nw * 32) {
+        const uint64_t wi = base + lane;
+        const uint32_t bits = wi < nwords ? fb[wi] : 0u;
+        uint32_t cnt = 0;
+        for (uint32_t b = bits; b; b &= b - 1u) {
+            const uint64_t v = wi * 32 + (uint32_t)(__ffs(b) - 1);
+            const unsigned long long len = g.csri_off[v + 1] - g.csri_off[v];
+            cnt += (uint32_t)((len + PIECE - 1) / PIECE);
+        }
+        uint32_t incl = cnt;
+#pragma unroll
+        for (int d = 1; d < 32; d <<= 1) {
+            const uint32_t y = __shfl_up_sync(FULL, incl, d);
+            if (lane >= d)
+                incl += y;
+        }
+        const uint32_t total = __shfl_sync(FULL, incl, 31);
+        if (total == 0)
+            continue;
+        uint32_t pos = 0;
+        if (lane == 31)
+            pos = atomicAdd(&c->items, total);
+        pos = __shfl_sync(FULL, pos, 31) + incl - cnt;
+        for (uint32_t b = bits; b; b &= b - 1u) {
+            const uint64_t v = wi * 32 + (uint32_t)(__ffs(b) - 1);
+            const unsigned long long len = g.csri_off[v + 1] - g.csri_off[v];
+            const uint32_t np = (uint32_t)((len + PIECE - 1) / PIECE);
+            for (uint32_t p = 0; p < np; ++p)
+                s.items[pos++] = make_uint2((uint32_t)v, p);
+        }
+    }
+}
+
+// Set the Wedge frontier bit of every chunk holding an out-edge of an active
+// vertex (wedge.c:37-46); the first bit set in a tile appends the tile to the
+// tile list (ballot + popc aggregated).
+__global__ void wedge_build_kernel(DevGraph g, DevState s)
+{
+    Ctrl* c = s.ctrl;
+    if (c->done || c->mode != MODE_WEDGE)
+        return;
+    const int lane = threadIdx.x & 31;
+    const uint32_t gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const uint32_t nw = (gridDim.x * blockDim.x) >> 5;
+    const uint32_t n = c->items;
+    const uint32_t lt = (1u << lane) - 1u;
+    for (uint32_t i = gw; i < n; i += nw) {
+        const uint2 it = s.items[i];
+        const unsigned long long lo = g.csri_off[it.x] + (unsigned long long)it.y * PIECE;
+        const unsigned long long end = g.csri_off[it.x + 1];
+        const unsigned long long hi = (lo + PIECE < end) ? lo + PIECE : end;
+        for (unsigned long long j0 = lo; j0 < hi; j0 += 32) {
+            const unsigned long long j = j0 + lane;
+            bool add = false;
+            uint32_t tile = 0;
+            if (j < hi) {
+                const uint32_t ch = g.csri[j];
+                const uint32_t word = ch >> 5, bit = 1u << (ch & 31u);
+                if (!(s.chunk_bits[word] & bit)) {
+                    const uint32_t old = atomicOr(&s.chunk_bits[word], bit);
+                    add = ((old >> (ch & 28u)) & 0xFu) == 0u;
+                    tile = ch >> 2;
+                }
+            }
+            const uint32_t m = __ballot_sync(FULL, add);
+            if (m) {
+                const int leader = __ffs(m) - 1;
+                uint32_t b0 = 0;
+                if (lane == leader)
+                    b0 = atomicAdd(&c->tiles, (uint32_t)__popc(m));
+                b0 = __shfl_sync(FULL, b0, leader);
+                if (add)
+                    s.tile_list[b0 + __popc(m & lt)] = tile;
+            }
+        }
+    }
+}
+
+// Clear the bitmap the next pull writes (execution_bfs.c:320-338: swap + memset;
+// execution_cc.c:243-277: clear of the active bitmap).
+__global__ void advance_kernel(DevGraph g, DevState s, uint32_t app)
+{
+    Ctrl* c = s.ctrl;
+    if (c->done)
+        return;
+    uint32_t* fb = (app == WEDGE_APP_BFS) ? next_front(s, app, c->parity) : s.front0;
+    const uint64_t nwords = (g.V + 31) / 32;
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < nwords; i += (uint64_t)gridDim.x * blockDim.x)
+        fb[i] = 0u;
+}
+
+// execution_initialize_{bfs,cc,sssp} bulk part
+__global__ void init_kernel(DevGraph g, DevState s, uint32_t app)
+{
+    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+    const uint64_t tid = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
+    for (uint64_t v = tid; v < g.V; v += stride) {
+        if (app == WEDGE_APP_BFS)
+            s.prop32[v] = NONE32; /* execution_bfs.c:106 */
+        else if (app == WEDGE_APP_CC)
+            s.prop32[v] = (uint32_t)v; /* execution_cc.c:77 */
+        else
+            s.prop64[v] = (g.weight_kind == WEDGE_WEIGHTS_F64) ? 0x7FF0000000000000ull : NONE64; /* execution_sssp.c:78 */
+    }
+    const uint64_t nwords = (g.V + 31) / 32;
+    for (uint64_t i = tid; i < nwords; i += stride) {
+        s.front0[i] = 0u;
+        if (s.front1)
+            s.front1[i] = 0u;
+    }
+    const uint64_t cwords = ((uint64_t)g.T + 7) / 8;
+    for (uint64_t i = tid; i < cwords; i += stride)
+        s.chunk_bits[i] = 0u;
+    if (s.vis_c) {
+        const uint64_t vwords = ((uint64_t)g.Vne + 31) / 32;
+        for (uint64_t i = tid; i < vwords; i += stride)
+            s.vis_c[i] = 0u;
+    }
+}
+
+// root activation (execution_bfs.c:110-117, execution_sssp.c:83-88) and the
+// control block
+__global__ void init_root_kernel(DevGraph g, DevState s, uint32_t app, uint64_t root, uint32_t sched,
+                                 unsigned long long thr, uint32_t max_iter)
+{
+    const uint32_t tid = blockIdx.x * blockDim.x + threadIdx.x;
+    if (app == WEDGE_APP_BFS) {
+        for (uint32_t k = tid; k < g.Vne; k += gridDim.x * blockDim.x)
+            if (g.dst_id[k] == (uint32_t)root)
+                atomicOr(&s.vis_c[k >> 5], 1u << (k & 31u));
+    }
+    if (tid == 0) {
+        Ctrl* c = s.ctrl;
+        c->mass = 0;
+        c->edges_scanned = 0;
+        c->tiles_scanned = 0;
+        c->threshold = thr;
+        c->items = 0;
+        c->tiles = 0;
+        c->iter = 0;
+        c->wedge_iters = 0;
+        c->done = 0;
+        c->not_converged = 0;
+        c->max_iter = max_iter;
+        c->sched = sched;
+        c->parity = 0;
+        c->loop = 1;
+        c->error = 0;
+        c->pull_launches = 0;
+        c->pr_total = 0.0;
+        c->pr_sum = 0.0;
+        if (app == WEDGE_APP_CC) {
+            c->last_mass = g.E;
+            c->mode = MODE_DENSE; /* first CC pull is always dense, execution_cc.c:103 */
+        } else {
+            if (app == WEDGE_APP_SSSP)
+                s.prop64[root] = 0ull; /* 0.0 has the same bits */
+            s.front0[root >> 5] |= 1u << (root & 31u);
+            c->last_mass = g.outdeg[root];
+            c->mode = choose_mode(sched, g.outdeg[root], thr);
+        }
+        if (g.T == 0) {
+            c->done = 1;
+            c->loop = 0;
+        }
+    }
+}
+
+/* ------------------------------------------------------------- PageRank */
+
+// execution_initialize_pr (execution_pr.c:380-392)
+__global__ void pr_init_kernel(DevGraph g, DevState s)
+{
+    const double N = (double)g.V;
+    for (uint64_t v = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; v < g.V; v += (uint64_t)gridDim.x * blockDim.x) {
+        const uint32_t od = g.outdeg[v];
+        const double r = __ddiv_rn(__ddiv_rn(1.0, N), od ? (double)od : N);
+        s.acc[v] = 0.0;
+        if (s.precision == WEDGE_PREC_FP32C)
+            s.rank32[v] = (float)r;
+        else
+            s.rank[v] = r;
+    }
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        Ctrl* c = s.ctrl;
+        c->iter = 0;
+        c->wedge_iters = 0;
+        c->edges_scanned = 0;
+        c->tiles_scanned = 0;
+        c->pull_launches = 0;
+        c->done = 0;
+        c->mode = MODE_DENSE;
+        c->parity = 0;
+        c->tiles = 0;
+        c->pr_total = 0.0;
+        c->pr_sum = 0.0;
+    }
+}
+
+// Total rank (fixed-order reduction of the per-block tile sums; phases.c:37-46)
+// and the in-edge sums of destinations that span tiles (fixed tile order; the
+// GPU counterpart of the ordered merge of phases.c:71-114).
+__global__ void pr_finish_kernel(DevGraph g, DevState s, uint32_t nblocks, const unsigned long long* block_cnt)
+{
+    __shared__ double sh[AUX_THREADS / 32];
+    Ctrl* c = s.ctrl;
+    const int lane = threadIdx.x & 31;
+    if (blockIdx.x == 0) {
+        double x = 0.0;
+        for (uint32_t i = threadIdx.x; i < nblocks; i += blockDim.x)
+            x = __dadd_rn(x, s.block_part[i]);
+        x = warp_sum_f64(x);
+        if (lane == 0)
+            sh[threadIdx.x >> 5] = x;
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            double t = 0.0;
+            unsigned long long e = 0, tl = 0;
+            for (int w = 0; w < AUX_THREADS / 32; ++w)
+                t = __dadd_rn(t, sh[w]);
+            for (uint32_t i = 0; i < nblocks; ++i) {
+                e += block_cnt[4u * i + 1u];
+                tl += block_cnt[4u * i + 2u];
+            }
+            c->pr_total = t;
+            c->edges_scanned += e;
+            c->tiles_scanned += tl;
+            c->pull_launches += 1u;
+            c->iter += 1u;
+        }
+    }
+    const uint32_t gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const uint32_t nw = (gridDim.x * blockDim.x) >> 5;
+    const bool c32 = s.precision == WEDGE_PREC_FP32C;
+    for (uint32_t i = gw; i < g.nsplit; i += nw) {
+        const uint32_t t0 = g.split_t0[i], t1 = g.split_t1[i];
+        double x = 0.0;
+        for (uint32_t t = t0 + lane; t < t1; t += 32)
+            x = __dadd_rn(x, c32 ? __dadd_rn((double)s.tail_part32[2u * t], (double)s.tail_part32[2u * t + 1u])
+                                 : s.tail_part[t]);
+        x = warp_sum_f64(x);
+        if (lane == 0) {
+            const double h = c32 ? __dadd_rn((double)s.head_part32[2u * t1], (double)s.head_part32[2u * t1 + 1u])
+                                 : s.head_part[t1];
+            s.acc[g.dst_id[g.split_k[i]]] = __dadd_rn(x, h);
+        }
+    }
+}
+
+// perform_vertex_phase_pr (phase_vertex_pr.c:26-77):
+// rank' = ((acc + (1 - total)/N) * d + (1 - d)/N) / outdegree'
+__global__ void pr_vertex_kernel(DevGraph g, DevState s)
+{
+    const double N = (double)g.V;
+    const double d = s.damping;
+    const double omd = __ddiv_rn(__dsub_rn(1.0, d), N);
+    const double corr = __ddiv_rn(__dsub_rn(1.0, s.ctrl->pr_total), N);
+    const bool c32 = s.precision == WEDGE_PREC_FP32C;
+    for (uint64_t v = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; v < g.V; v += (uint64_t)gridDim.x * blockDim.x) {
+        const uint32_t od = g.outdeg[v];
+        const double odd = od ? (double)od : N;
+        const double r = __ddiv_rn(__dadd_rn(__dmul_rn(__dadd_rn(s.acc[v], corr), d), omd), odd);
+        if (c32)
+            s.rank32[v] = (float)r;
+        else
+            s.rank[v] = r;
+    }
+}
+
+// PageRank Sum (execution_pr.c:63-71): sum of rank' * outdegree' over all vertices
+__global__ void pr_sum_kernel(DevGraph g, DevState s, double* block_out)
+{
+    __shared__ double sh[AUX_THREADS / 32];
+    const double N = (double)g.V;
+    const bool c32 = s.precision == WEDGE_PREC_FP32C;
+    double x = 0.0;
+    for (uint64_t v = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; v < g.V; v += (uint64_t)gridDim.x * blockDim.x) {
+        const uint32_t od = g.outdeg[v];
+        const double r = c32 ? (double)s.rank32[v] : s.rank[v];
+        x = __dadd_rn(x, __dmul_rn(r, od ? (double)od : N));
+    }
+    x = warp_sum_f64(x);
+    if ((threadIdx.x & 31) == 0)
+        sh[threadIdx.x >> 5] = x;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double t = 0.0;
+        for (int w = 0; w < AUX_THREADS / 32; ++w)
+            t = __dadd_rn(t, sh[w]);
+        block_out[blockIdx.x] = t;
+    }
+}
+
+__global__ void pr_sum_final_kernel(DevState s, const double* block_out, uint32_t n)
+{
+    if (threadIdx.x == 0 && blockIdx.x == 0) {
+        double t = 0.0;
+        for (uint32_t i = 0; i < n; ++i)
+            t = __dadd_rn(t, block_out[i]);
+        s.ctrl->pr_sum = t;
+    }
+}
+
+/* --------------------------------------------------------------- results */
+
+// graph_vertex_props in the reference's representation (one 64-bit word per vertex)
+__global__ void export_kernel(DevGraph g, DevState s, uint32_t app, unsigned long long* out)
+{
+    for (uint64_t v = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; v < g.V; v += (uint64_t)gridDim.x * blockDim.x) {
+        unsigned long long x;
+        if (app == WEDGE_APP_BFS) {
+            const uint32_t p = s.prop32[v];
+            x = (p == NONE32) ? NONE64 : (unsigned long long)p;
+        } else if (app == WEDGE_APP_CC) {
+            x = (unsigned long long)__double_as_longlong((double)s.prop32[v]);
+        } else if (app == WEDGE_APP_SSSP) {
+            x = s.prop64[v];
+        } else {
+            x = (unsigned long long)__double_as_longlong(s.precision == WEDGE_PREC_FP32C ? (double)s.rank32[v] : s.rank[v]);
+        }
+        out[v] = x;
+    }
+}
+
+__global__ void export_outdeg_kernel(DevGraph g, unsigned long long* out)
+{
+    for (uint64_t v = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; v < g.V; v += (uint64_t)gridDim.x * blockDim.x)
+        out[v] = g.outdeg[v];
+}
+
+/* ================================================================ host */
+
+int compute_grids(wedge_graph* h)
+{
+    int blocks = 0;
+    WEDGE_CHECK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, pull_kernel<WEDGE_APP_CC>, PULL_THREADS, 0));
+    if (blocks < 1)
+        blocks = 1;
+    h->pull_grid = (uint32_t)(h->num_sms * blocks);
+    h->build_grid = (uint32_t)h->num_sms * 8u;
+    return WEDGE_OK;
+}
+
+// state arrays of one application (allocated on first use, reused by later runs)
+static int ensure_state(wedge_graph* h, int app, int precision)
+{
+    if (h->built_app == app && (app != WEDGE_APP_PR || h->last_precision == precision))
+        return WEDGE_OK;
+    free_state(h);
+    DevGraph& g = h->g;
+    DevState& s = h->s;
+    const uint64_t V = g.V;
+    const uint64_t nwords = (V + 31) / 32 + 1;
+    const uint64_t grid = h->pull_grid;
+    int rc;
+    Ctrl* ctrl;
+    double* bp;
+    // [grid] block sums | [4*grid] block counters | [aux grid] PageRank-sum partials
+    if ((rc = dalloc(h, &ctrl, 1, true)) || (rc = dalloc(h, &bp, grid * 5 + (uint64_t)h->num_sms * 8 + 8, true)))
+        return rc;
+    WEDGE_CHECK(cudaMemset(ctrl, 0, sizeof(Ctrl)));
+    s.ctrl = ctrl;
+    s.block_part = bp; /* [grid] doubles, then 4*grid counters */
+    s.app = (uint32_t)app;
+    if (app == WEDGE_APP_PR) {
+        if ((rc = dalloc(h, &s.acc, V, true)))
+            return rc;
+        if (precision == WEDGE_PREC_FP32C) {
+            if ((rc = dalloc(h, &s.rank32, V, true)) || (rc = dalloc(h, &s.head_part32, 2ull * g.T + 2, true)) ||
+                (rc = dalloc(h, &s.tail_part32, 2ull * g.T + 2, true)))
+                return rc;
+        } else {
+            if ((rc = dalloc(h, &s.rank, V, true)) || (rc = dalloc(h, &s.head_part, (uint64_t)g.T + 1, true)) ||
+                (rc = dalloc(h, &s.tail_part, (uint64_t)g.T + 1, true)))
+                return rc;
+        }
+    } else {
+        if (app == WEDGE_APP_SSSP) {
+            if ((rc = dalloc(h, &s.prop64, V, true)))
+                return rc;
+        } else if ((rc = dalloc(h, &s.prop32, V, true))) {
+            return rc;
+        }
+        if ((rc = dalloc(h, &s.front0, nwords, true)) || (rc = dalloc(h, &s.chunk_bits, (uint64_t)g.T / 8 + 2, true)) ||
+            (rc = dalloc(h, &s.tile_list, (uint64_t)g.T + 1, true)) ||
+            (rc = dalloc(h, &s.items, V + g.E / PIECE + 2, true)))
+            return rc;
+        if (app == WEDGE_APP_BFS) {
+            if ((rc = dalloc(h, &s.front1, nwords, true)) || (rc = dalloc(h, &s.vis_c, (uint64_t)g.Vne / 32 + 2, true)))
+                return rc;
+        }
+    }
+    h->built_app = app;
+    h->last_precision = precision;
+    return WEDGE_OK;
+}
+
+static unsigned long long* counters(wedge_graph* h) { return (unsigned long long*)(h->s.block_part + h->pull_grid); }
+
+static void launch_pull(wedge_graph* h, int app)
+{
+    const uint32_t grid = h->pull_grid;
+    switch (app) {
+    case WEDGE_APP_BFS:
+        pull_kernel<WEDGE_APP_BFS><<<grid, PULL_THREADS, 0, h->stream>>>(h->g, h->s, counters(h));
+        break;
+    case WEDGE_APP_CC:
+        pull_kernel<WEDGE_APP_CC><<<grid, PULL_THREADS, 0, h->stream>>>(h->g, h->s, counters(h));
+        break;
+    case WEDGE_APP_SSSP:
+        pull_kernel<WEDGE_APP_SSSP><<<grid, PULL_THREADS, 0, h->stream>>>(h->g, h->s, counters(h));
+        break;
+    default:
+        pull_kernel<WEDGE_APP_PR><<<grid, PULL_THREADS, 0, h->stream>>>(h->g, h->s, counters(h));
+        break;
+    }
+}
+
+static uint32_t aux_grid(wedge_graph* h, uint64_t work)
+{
+    return grid_for(work, AUX_THREADS, (uint32_t)h->num_sms * 8u);
+}
+
+// iteration tail after a pull: mass/convergence, Wedge frontier, bitmap reset
+static void launch_tail(wedge_graph* h, int app)
+{
+    decide_kernel<<<1, AUX_THREADS, 0, h->stream>>>(h->s, counters(h), h->pull_grid, (uint32_t)app);
+    collect_kernel<<<aux_grid(h, (h->g.V + 31) / 32), AUX_THREADS, 0, h->stream>>>(h->g, h->s, (uint32_t)app);
+    wedge_build_kernel<<<h->build_grid, AUX_THREADS, 0, h->stream>>>(h->g, h->s);
+    advance_kernel<<<aux_grid(h, (h->g.V + 31) / 32), AUX_THREADS, 0, h->stream>>>(h->g, h->s, (uint32_t)app);
+}
+
+static void launch_init(wedge_graph* h, int app, uint64_t root, uint32_t sched, unsigned long long thr, uint32_t max_iter)
+{
+    const uint64_t work = h->g.V > h->g.T ? h->g.V : h->g.T;
+    init_kernel<<<aux_grid(h, work), AUX_THREADS, 0, h->stream>>>(h->g, h->s, (uint32_t)app);
+    init_root_kernel<<<aux_grid(h, h->g.Vne), AUX_THREADS, 0, h->stream>>>(h->g, h->s, (uint32_t)app, root, sched, thr,
+                                                                           max_iter);
+    collect_kernel<<<aux_grid(h, (h->g.V + 31) / 32), AUX_THREADS, 0, h->stream>>>(h->g, h->s, (uint32_t)app);
+    wedge_build_kernel<<<h->build_grid, AUX_THREADS, 0, h->stream>>>(h->g, h->s);
+    advance_kernel<<<aux_grid(h, (h->g.V + 31) / 32), AUX_THREADS, 0, h->stream>>>(h->g, h->s, (uint32_t)app);
+}
+
+static int read_ctrl(wedge_graph* h, Ctrl* out)
+{
+    WEDGE_CHECK(cudaMemcpyAsync(h->h_ctrl, h->s.ctrl, sizeof(Ctrl), cudaMemcpyDeviceToHost, h->stream));
+    WEDGE_CHECK(cudaStreamSynchronize(h->stream));
+    memcpy(out, h->h_ctrl, sizeof(Ctrl));
+    return WEDGE_OK;
+}
+
+// Captures one iteration (pull + tail) as the body of a device-side while
+// loop; the loop condition is Ctrl::loop, set by decide_kernel through
+// loop_cond_kernel.
+__global__ void loop_cond_kernel(DevState s, cudaGraphConditionalHandle handle)
+{
+    cudaGraphSetConditional(handle, s.ctrl->loop);
+}
+
+static int build_graph(wedge_graph* h, int app)
+{
+    if (h->graph_exec && h->graph_app == app)
+        return WEDGE_OK;
+    if (h->graph_exec) {
+        cudaGraphExecDestroy(h->graph_exec);
+        h->graph_exec = nullptr;
+    }
+    cudaGraph_t graph;
+    WEDGE_CHECK(cudaGraphCreate(&graph, 0));
+    cudaGraphConditionalHandle handle;
+    WEDGE_CHECK(cudaGraphConditionalHandleCreate(&handle, graph, 1, cudaGraphCondAssignDefault));
+    cudaGraphNodeParams cparams = {};
+    cparams.type = cudaGraphNodeTypeConditional;
+    cparams.conditional.handle = handle;
+    cparams.conditional.type = cudaGraphCondTypeWhile;
+    cparams.conditional.size = 1;
+    cudaGraphNode_t cnode;
+    WEDGE_CHECK(cudaGraphAddNode(&cnode, graph, nullptr, nullptr, 0, &cparams));
+    cudaGraph_t body = cparams.conditional.phGraph_out[0];
+    WEDGE_CHECK(cudaStreamBeginCaptureToGraph(h->stream, body, nullptr, nullptr, 0, cudaStreamCaptureModeRelaxed));
+    launch_pull(h, app);
+    launch_tail(h, app);
+    loop_cond_kernel<<<1, 1, 0, h->stream>>>(h->s, handle);
+    cudaGraph_t captured;
+    WEDGE_CHECK(cudaStreamEndCapture(h->stream, &captured));
+    WEDGE_CHECK(cudaGraphInstantiate(&h->graph_exec, graph, 0));
+    cudaGraphDestroy(graph);
+    h->graph_app = app;
+    return WEDGE_OK;
+}
+
+static int run_traversal(wedge_graph* h, int app, const wedge_params_t* p, wedge_stats_t* st)
+{
+    const DevGraph& g = h->g;
+    const uint64_t root = p->root < g.V ? p->root : 0; /* main.c:81-85 */
+    const unsigned long long thr = (unsigned long long)((g.E * (unsigned long long)p->threshold_pct) / 100ull);
+    uint64_t cap = p->max_iterations ? p->max_iterations : g.V + 1;
+    if (cap > 0x7fffffffull)
+        cap = 0x7fffffffull;
+    const bool timing = (p->flags & WEDGE_FLAG_TIMING) != 0;
+    const bool use_graph = (p->flags & WEDGE_FLAG_GRAPH) != 0 && !timing;
+    uint64_t launches = 0;
+    double t_pull_dense = 0, t_pull_wedge = 0, t_wedge = 0;
+    if (use_graph) {
+        int rc = build_graph(h, app);
+        if (rc)
+            return rc;
+    }
+    WEDGE_CHECK(cudaEventRecord(h->ev[0], h->stream));
+    launch_init(h, app, root, (uint32_t)p->sched, thr, (uint32_t)cap);
+    launches += 5;
+    Ctrl c;
+    if (use_graph) {
+        WEDGE_CHECK(cudaGraphLaunch(h->graph_exec, h->stream));
+    } else if (timing) {
+        for (;;) {
+            int rc = read_ctrl(h, &c);
+            if (rc)
+                return rc;
+            if (c.done)
+                break;
+            const uint32_t mode = c.mode;
+            WEDGE_CHECK(cudaEventRecord(h->ev[2], h->stream));
+            launch_pull(h, app);
+            WEDGE_CHECK(cudaEventRecord(h->ev[3], h->stream));
+            launch_tail(h, app);
+            WEDGE_CHECK(cudaEventRecord(h->ev[4], h->stream));
+            launches += 5;
+            WEDGE_CHECK(cudaEventSynchronize(h->ev[4]));
+            float a = 0, b = 0;
+            cudaEventElapsedTime(&a, h->ev[2], h->ev[3]);
+            cudaEventElapsedTime(&b, h->ev[3], h->ev[4]);
+            if (mode == MODE_DENSE)
+                t_pull_dense += a;
+            else
+                t_pull_wedge += a;
+            t_wedge += b;
+        }
+    } else {
+        // speculative batches: kernels are no-ops once Ctrl::done is set
+        for (;;) {
+            for (int b = 0; b < 3; ++b) {
+                launch_pull(h, app);
+                launch_tail(h, app);
+                launches += 5;
+            }
+            int rc = read_ctrl(h, &c);
+            if (rc)
+                return rc;
+            if (c.done)
+                break;
+        }
+    }
+    WEDGE_CHECK(cudaEventRecord(h->ev[1], h->stream));
+    WEDGE_CHECK(cudaGetLastError());
+    int rc = read_ctrl(h, &c);
+    if (rc)
+        return rc;
+    float total = 0;
+    cudaEventElapsedTime(&total, h->ev[0], h->ev[1]);
+    h->last_app = app;
+    if (st) {
+        memset(st, 0, sizeof(*st));
+        st->iterations = c.iter;
+        st->wedge_iterations = c.wedge_iters;
+        st->running_ms = total;
+        st->pull_ms_dense = t_pull_dense;
+        st->pull_ms_wedge = t_pull_wedge;
+        st->wedge_ms = t_wedge;
+        st->edges_scanned = c.edges_scanned;
+        st->tiles_scanned = c.tiles_scanned;
+        st->pull_launches = c.pull_launches;
+        st->kernel_launches = use_graph ? (uint64_t)5 + 6ull * c.iter : launches;
+    }
+    if (c.not_converged)
+        return WEDGE_ERR_NOT_CONVERGED;
+    return WEDGE_OK;
+}
+
+static int run_pr(wedge_graph* h, const wedge_params_t* p, wedge_stats_t* st)
+{
+    const DevGraph& g = h->g;
+    const bool timing = (p->flags & WEDGE_FLAG_TIMING) != 0;
+    h->s.damping = p->damping > 0.0 ? p->damping : 0.875;
+    h->s.precision = (uint32_t)p->precision;
+    const uint32_t vgrid = aux_grid(h, g.V);
+    const uint32_t fgrid = aux_grid(h, (uint64_t)g.nsplit * 32 + 1);
+    double t_pull = 0, t_vertex = 0;
+    WEDGE_CHECK(cudaEventRecord(h->ev[0], h->stream));
+    pr_init_kernel<<<vgrid, AUX_THREADS, 0, h->stream>>>(g, h->s);
+    for (uint32_t it = 0; it < p->num_iterations; ++it) {
+        if (timing)
+            WEDGE_CHECK(cudaEventRecord(h->ev[2], h->stream));
+        launch_pull(h, WEDGE_APP_PR);
+        if (timing)
+            WEDGE_CHECK(cudaEventRecord(h->ev[3], h->stream));
+        pr_finish_kernel<<<fgrid, AUX_THREADS, 0, h->stream>>>(g, h->s, h->pull_grid, counters(h));
+        pr_vertex_kernel<<<vgrid, AUX_THREADS, 0, h->stream>>>(g, h->s);
+        if (timing) {
+            WEDGE_CHECK(cudaEventRecord(h->ev[4], h->stream));
+            WEDGE_CHECK(cudaEventSynchronize(h->ev[4]));
+            float a = 0, b = 0;
+            cudaEventElapsedTime(&a, h->ev[2], h->ev[3]);
+            cudaEventElapsedTime(&b, h->ev[3], h->ev[4]);
+            t_pull += a;
+            t_vertex += b;
+        }
+    }
+    WEDGE_CHECK(cudaEventRecord(h->ev[1], h->stream));
+    double* sums = (double*)(counters(h) + 4ull * h->pull_grid);
+    pr_sum_kernel<<<vgrid, AUX_THREADS, 0, h->stream>>>(g, h->s, sums);
+    pr_sum_final_kernel<<<1, 32, 0, h->stream>>>(h->s, sums, vgrid);
+    WEDGE_CHECK(cudaGetLastError());
+    Ctrl c;
+    int rc = read_ctrl(h, &c);
+    if (rc)
+        return rc;
+    float total = 0;
+    cudaEventElapsedTime(&total, h->ev[0], h->ev[1]);
+    h->last_app = WEDGE_APP_PR;
+    if (st) {
+        memset(st, 0, sizeof(*st));
+        st->iterations = p->num_iterations;
+        st->running_ms = total;
+        st->pull_ms_dense = t_pull;
+        st->vertex_ms = t_vertex;
+        st->edges_scanned = c.edges_scanned;
+        st->tiles_scanned = c.tiles_scanned;
+        st->pull_launches = c.pull_launches;
+        st->kernel_launches = 3ull + 3ull * p->num_iterations;
+        st->pr_sum = c.pr_sum;
+    }
+    return WEDGE_OK;
+}
+
+}  // namespace wedge
+
+using namespace wedge;
+
+extern "C" {
+
+int wedge_cuda_abi_version(void) { return WEDGE_CUDA_ABI_VERSION; }
+
+const char* wedge_cuda_status_string(int status)
+{
+    switch (status) {
+    case WEDGE_OK:
+        return "ok";
+    case WEDGE_ERR_IO:
+        return "I/O error";
+    case WEDGE_ERR_FORMAT:
+        return "malformed graph input";
+    case WEDGE_ERR_OOM:
+        return "out of memory";
+    case WEDGE_ERR_CUDA:
+        return "CUDA error";
+    case WEDGE_ERR_NOT_CONVERGED:
+        return "iteration cap reached before convergence";
+    case WEDGE_ERR_ARG:
+        return "invalid argument";
+    case WEDGE_ERR_UNSUPPORTED:
+        return "unsupported";
+    default:
+        return "unknown status";
+    }
+}
+
+static int check_params(const wedge_graph_t* g, int app, const wedge_params_t* p)
+{
+    if (!g || !p || app < WEDGE_APP_BFS || app > WEDGE_APP_SSSP)
+        return WEDGE_ERR_ARG;
+    if (p->threshold_pct > 100 || p->sched < WEDGE_SCHED_PLAIN || p->sched > WEDGE_SCHED_WEDGE)
+        return WEDGE_ERR_ARG;
+    if (app == WEDGE_APP_PR && (p->precision != WEDGE_PREC_FP64 && p->precision != WEDGE_PREC_FP32C))
+        return WEDGE_ERR_ARG;
+    if (app == WEDGE_APP_SSSP && g->weight_kind == WEDGE_WEIGHTS_NONE)
+        return WEDGE_ERR_ARG; /* SSSP needs a weighted load (application.c:171) */
+    return WEDGE_OK;
+}
+
+int wedge_cuda_run(wedge_graph_t* g, int app, const wedge_params_t* params, wedge_stats_t* stats)
+{
+    int rc = check_params(g, app, params);
+    if (rc)
+        return rc;
+    WEDGE_CHECK(cudaSetDevice(g->device));
+    if ((rc = ensure_state(g, app, params->precision)))
+        return rc;
+    if (app == WEDGE_APP_PR)
+        return run_pr(g, params, stats);
+    return run_traversal(g, app, params, stats);
+}
+
+int wedge_cuda_run_phase(wedge_graph_t* g, int app, int phase, const wedge_params_t* params, uint64_t* active_mass)
+{
+    int rc = check_params(g, app, params);
+    if (rc)
+        return rc;
+    WEDGE_CHECK(cudaSetDevice(g->device));
+    if ((rc = ensure_state(g, app, params->precision)))
+        return rc;
+    const DevGraph& dg = g->g;
+    g->s.damping = params->damping > 0.0 ? params->damping : 0.875;
+    g->s.precision = (uint32_t)params->precision;
+    const uint32_t vgrid = aux_grid(g, dg.V);
+    Ctrl c;
+    switch (phase) {
+    case WEDGE_PHASE_INIT:
+        if (app == WEDGE_APP_PR) {
+            pr_init_kernel<<<vgrid, AUX_THREADS, 0, g->stream>>>(dg, g->s);
+        } else {
+            const uint64_t root = params->root < dg.V ? params->root : 0;
+            const unsigned long long thr =
+                (unsigned long long)((dg.E * (unsigned long long)params->threshold_pct) / 100ull);
+            uint64_t cap = params->max_iterations ? params->max_iterations : dg.V + 1;
+            launch_init(g, app, root, (uint32_t)params->sched, thr, (uint32_t)(cap > 0x7fffffffull ? 0x7fffffffull : cap));
+        }
+        break;
+    case WEDGE_PHASE_PULL_DENSE:
+    case WEDGE_PHASE_PULL_WEDGE: {
+        if (app != WEDGE_APP_PR) {
+            if ((rc = read_ctrl(g, &c)))
+                return rc;
+            const uint32_t want = phase == WEDGE_PHASE_PULL_DENSE ? MODE_DENSE : MODE_WEDGE;
+            if (c.mode != want && !c.done) {
+                if (want == MODE_WEDGE)
+                    return WEDGE_ERR_ARG; /* no Wedge frontier was built for this pull */
+                WEDGE_CHECK(cudaMemcpyAsync(&g->s.ctrl->mode, &want, sizeof(want), cudaMemcpyHostToDevice, g->stream));
+            }
+        } else if (phase == WEDGE_PHASE_PULL_WEDGE) {
+            return WEDGE_ERR_UNSUPPORTED; /* PageRank has no Wedge pull (application.c:154) */
+        }
+        launch_pull(g, app);
+        if (app == WEDGE_APP_PR) {
+            pr_finish_kernel<<<aux_grid(g, (uint64_t)dg.nsplit * 32 + 1), AUX_THREADS, 0, g->stream>>>(
+                dg, g->s, g->pull_grid, counters(g));
+        } else {
+            decide_kernel<<<1, AUX_THREADS, 0, g->stream>>>(g->s, counters(g), g->pull_grid, (uint32_t)app);
+        }
+        break;
+    }
+    case WEDGE_PHASE_VERTEX_PR:
+        if (app != WEDGE_APP_PR)
+            return WEDGE_ERR_ARG;
+        pr_vertex_kernel<<<vgrid, AUX_THREADS, 0, g->stream>>>(dg, g->s);
+        break;
+    case WEDGE_PHASE_WEDGE_BUILD:
+        if (app == WEDGE_APP_PR)
+            return WEDGE_ERR_UNSUPPORTED;
+        collect_kernel<<<aux_grid(g, (dg.V + 31) / 32), AUX_THREADS, 0, g->stream>>>(dg, g->s, (uint32_t)app);
+        wedge_build_kernel<<<g->build_grid, AUX_THREADS, 0, g->stream>>>(dg, g->s);
+        break;
+    case WEDGE_PHASE_ADVANCE:
+        if (app == WEDGE_APP_PR)
+            return WEDGE_ERR_UNSUPPORTED;
+        advance_kernel<<<aux_grid(g, (dg.V + 31) / 32), AUX_THREADS, 0, g->stream>>>(dg, g->s, (uint32_t)app);
+        break;
+    default:
+        return WEDGE_ERR_ARG;
+    }
+    WEDGE_CHECK(cudaGetLastError());
+    if ((rc = read_ctrl(g, &c)))
+        return rc;
+    g->last_app = app;
+    if (active_mass)
+        *active_mass = app == WEDGE_APP_PR ? 0 : c.mass;
+    return WEDGE_OK;
+}
+
+int wedge_cuda_read_results(wedge_graph_t* g, void* host_props, uint64_t bytes)
+{
+    if (!g || !host_props || bytes < 8ull * g->g.V || g->last_app < 0)
+        return WEDGE_ERR_ARG;
+    WEDGE_CHECK(cudaSetDevice(g->device));
+    unsigned long long* tmp = nullptr;
+    WEDGE_CHECK(cudaMallocAsync((void**)&tmp, 8ull * (g->g.V ? g->g.V : 1), g->stream));
+    export_kernel<<<aux_grid(g, g->g.V), AUX_THREADS, 0, g->stream>>>(g->g, g->s, (uint32_t)g->last_app, tmp);
+    cudaError_t e = cudaMemcpyAsync(host_props, tmp, 8ull * g->g.V, cudaMemcpyDeviceToHost, g->stream);
+    cudaFreeAsync(tmp, g->stream);
+    WEDGE_CHECK(e);
+    WEDGE_CHECK(cudaStreamSynchronize(g->stream));
+    return WEDGE_OK;
+}
+
+int wedge_cuda_read_outdegrees(wedge_graph_t* g, uint64_t* host_outdeg, uint64_t bytes)
+{
+    if (!g || !host_outdeg || bytes < 8ull * g->g.V)
+        return WEDGE_ERR_ARG;
+    WEDGE_CHECK(cudaSetDevice(g->device));
+    unsigned long long* tmp = nullptr;
+    WEDGE_CHECK(cudaMallocAsync((void**)&tmp, 8ull * (g->g.V ? g->g.V : 1), g->stream));
+    export_outdeg_kernel<<<aux_grid(g, g->g.V), AUX_THREADS, 0, g->stream>>>(g->g, tmp);
+    cudaError_t e = cudaMemcpyAsync(host_outdeg, tmp, 8ull * g->g.V, cudaMemcpyDeviceToHost, g->stream);
+    cudaFreeAsync(tmp, g->stream);
+    WEDGE_CHECK(e);
+    WEDGE_CHECK(cudaStreamSynchronize(g->stream));
+    return WEDGE_OK;
+}
+
+uint64_t wedge_cuda_num_vertices(const wedge_graph_t* g) { return g ? g->g.V : 0; }
+uint64_t wedge_cuda_num_edges(const wedge_graph_t* g) { return g ? g->g.E : 0; }
+void* wedge_cuda_stream(const wedge_graph_t* g) { return g ? (void*)g->stream : nullptr; }
+void wedge_cuda_free(wedge_graph_t* g) { free_handle(g); }
+
+}  // extern "C"

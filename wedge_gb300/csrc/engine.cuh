@@ -1,0 +1,148 @@
+// Shared definitions of the sm_103a edge-pull engine.
+//
+// Device layout of a loaded graph (all resident in HBM):
+//   src[Epad]      uint32 in-edge sources, grouped by destination in file order,
+//                  padded to a multiple of TILE with NONE32
+//   w[Epad]        64-bit weight words (SSSP only; uint64 or IEEE double)
+//   dst_id[Vne]    vertex id of compressed destination k (only vertices with
+//                  in-degree > 0 are listed, ascending)
+//   dst_off[Vne+1] first edge of compressed destination k
+//   tile_dst0[T+1] compressed destination owning the first edge of tile t
+//                  (tile_dst0[T] = Vne)
+//   outdeg[V]      out-degree (graphdata.c:430-490)
+//   csri_off[V+1], csri[E]  for every source, the Wedge chunk (32 in-edges)
+//                  holding each of its out-edges (the CSRI of graphdata.c:493-585)
+// A tile (128 consecutive in-edges) is the unit of work of one warp; a chunk
+// (32 in-edges, one 128-byte line of sources) is the unit the Wedge frontier
+// marks, i.e. the GPU form of the reference's frontier element of 4 edge
+// vectors (include/configuration.h:19-24).
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "wedge_cuda.h"
+
+namespace wedge {
+
+constexpr uint32_t TILE = 128;
+constexpr uint32_t CHUNK = 32;
+constexpr uint32_t CHUNKS_PER_TILE = TILE / CHUNK;        // 4
+constexpr uint32_t TILES_PER_WORD = 32 / CHUNKS_PER_TILE;  // 8 tiles per 32-bit chunk-bitmap word
+constexpr uint32_t PIECE = 1024;                           // CSRI entries per Wedge-build work item
+constexpr uint32_t NONE32 = 0xFFFFFFFFu;
+constexpr unsigned long long NONE64 = ~0ull;
+constexpr uint32_t FULL = 0xFFFFFFFFu;
+
+enum : uint32_t { MODE_DENSE = 0, MODE_WEDGE = 1 };
+
+// Device control block of one traversal; read and written only by the
+// engine's kernels (the host reads it back for statistics).
+struct Ctrl {
+    unsigned long long mass;           // changed out-edge mass of the last pull (phases.c:26-35)
+    unsigned long long last_mass;      // mass that chose the current mode
+    unsigned long long edges_scanned;  // in-edges read by pulls
+    unsigned long long tiles_scanned;  // tiles visited by pulls
+    unsigned long long threshold;      // |E| * t% / 100 (execution_bfs.c:132)
+    unsigned int items;                // Wedge-build work items appended by the last pull
+    unsigned int tiles;                // Wedge tile list length
+    unsigned int mode;                 // MODE_DENSE / MODE_WEDGE for the next pull
+    unsigned int iter;                 // completed pulls
+    unsigned int wedge_iters;          // pulls that used the Wedge frontier
+    unsigned int done;                 // traversal finished
+    unsigned int not_converged;        // iteration cap reached
+    unsigned int max_iter;
+    unsigned int sched;                // enum wedge_sched
+    unsigned int parity;               // BFS frontier double-buffer parity
+    unsigned int loop;                 // 1 while the traversal continues (CUDA-graph loop condition)
+    unsigned int error;                // kernel-detected error (bounds)
+    unsigned int pull_launches;
+    unsigned int pad;
+    double pr_total;                   // sum of all accumulators (phase_vertex_pr.c:161)
+    double pr_sum;                     // PageRank Sum statistic
+};
+
+// Immutable graph, passed to kernels by value.
+struct DevGraph {
+    uint64_t V, E, Epad;
+    uint32_t Vne, T, nsplit, weight_kind;
+    const uint32_t* src;
+    const unsigned long long* w;
+    const uint32_t* dst_id;
+    const unsigned long long* dst_off;
+    const uint32_t* tile_dst0;
+    const uint32_t* outdeg;
+    const unsigned long long* csri_off;
+    const uint32_t* csri;
+    const uint32_t* split_k;   // compressed destinations whose in-edges span tiles
+    const uint32_t* split_t0;  // their first tile
+    const uint32_t* split_t1;  // their last tile
+};
+
+// Mutable per-traversal state, passed to kernels by value.
+struct DevState {
+    uint32_t* prop32;              // BFS parent / CC label
+    unsigned long long* prop64;    // SSSP distance (uint64 or double bits)
+    double* rank;                  // PageRank FP64: rank / outdegree'
+    float* rank32;                 // PageRank FP32C: rank / outdegree'
+    double* acc;                   // PageRank accumulators (graph_vertex_accumulators)
+    double* head_part;             // [T] partial sum of a split destination ending in tile t
+    double* tail_part;             // [T] partial sum of a split destination continuing past tile t
+    float* head_part32;            // FP32C partial sums (value, compensation) interleaved
+    float* tail_part32;
+    double* block_part;            // [grid] per-block sums of tile sums
+    uint32_t* front0;              // V-bit frontier bitmaps (active / snapshot)
+    uint32_t* front1;
+    uint32_t* vis_c;               // Vne-bit visited bitmap (BFS)
+    uint32_t* chunk_bits;          // Wedge frontier: one bit per chunk
+    uint32_t* tile_list;           // tiles holding at least one marked chunk
+    uint2* items;                  // (vertex, piece) Wedge-build work items
+    Ctrl* ctrl;
+    double damping;
+    uint32_t precision;
+    uint32_t app;
+    uint64_t root;
+};
+
+}  // namespace wedge
+
+// host-side handle (opaque to C callers)
+struct wedge_graph {
+    wedge::DevGraph g;
+    wedge::DevState s;
+    cudaStream_t stream;
+    int device;
+    int num_sms;
+    int weight_kind;
+    int built_app;                     // app whose state arrays are sized (-1 none)
+    int last_app;                      // app of the last run (for read_results)
+    int last_precision;
+    uint32_t pull_grid;                // persistent grid of the pull kernels
+    uint32_t build_grid;
+    // allocations owned by the handle
+    void* allocs[32];
+    int nallocs;
+    void* state_allocs[32];
+    int nstate;
+    unsigned long long* h_ctrl;        // pinned mirror of Ctrl (host reads)
+    cudaEvent_t ev[8];
+    cudaGraphExec_t graph_exec;        // captured traversal
+    int graph_app;
+    int graph_key;
+};
+
+namespace wedge {
+// implemented in engine.cu, used by loaders in graph.cu
+int build_from_device_edges(wedge_graph* h, uint64_t V, uint64_t E, uint32_t* d_src, uint32_t* d_dst,
+                            unsigned long long* d_w, int weight_kind);
+int new_handle(wedge_graph** out);
+void free_handle(wedge_graph* h);
+int track(wedge_graph* h, void* p);
+int cuda_status(cudaError_t e);
+}  // namespace wedge
+
+#define WEDGE_CHECK(call)                                          \
+    do {                                                           \
+        cudaError_t e_ = (call);                                   \
+        if (e_ != cudaSuccess) return wedge::cuda_status(e_);      \
+    } while (0)

@@ -1,0 +1,196 @@
+// Edge-pull kernels of the sm_103a engine.
+//
+// One warp owns one 128-edge tile of the destination-grouped CSC at a time:
+// each lane loads 4 consecutive sources with one 128-bit load (a warp reads
+// the tile's 512 bytes in one coalesced request), gathers the 4 source
+// properties, and the warp folds them per destination with a segmented
+// reduction (lane-local runs, then a 5-step shuffle scan).  A destination
+// whose in-edges lie inside one tile is finished by that warp alone; one that
+// spans tiles (a hub) gets one partial per tile, combined with atomicMin for
+// the min-reductions and with a fixed-order fixup pass for PageRank sums.
+// This replaces the reference's per-thread vector loops and merge buffers
+// (phase_edge_pull_*.c, phases.c:54-114): every destination has exactly one
+// owner per tile, so no merge buffer is needed.
+#pragma once
+
+#include "engine.cuh"
+
+namespace wedge {
+
+__device__ __forceinline__ uint4 ld_stream_v4(const uint32_t* p)
+{
+    uint4 r;
+    asm volatile("ld.global.nc.L1::no_allocate.v4.u32 {%0,%1,%2,%3}, [%4];"
+                 : "=r"(r.x), "=r"(r.y), "=r"(r.z), "=r"(r.w)
+                 : "l"(p));
+    return r;
+}
+
+__device__ __forceinline__ ulonglong2 ld_stream_v2u64(const unsigned long long* p)
+{
+    ulonglong2 r;
+    asm volatile("ld.global.nc.L1::no_allocate.v2.u64 {%0,%1}, [%2];" : "=l"(r.x), "=l"(r.y) : "l"(p));
+    return r;
+}
+
+__device__ __forceinline__ bool test_bit32(const uint32_t* bm, uint64_t i)
+{
+    return (bm[i >> 5] >> (i & 31)) & 1u;
+}
+
+// per-lane geometry of a tile
+struct TileGeo {
+    uint64_t base;
+    uint32_t k0;         // compressed destination of position 0
+    uint32_t before;     // heads at positions [1, 4*lane)
+    uint32_t nib;        // heads at the lane's 4 positions (bit 0 for lane 0 = k0 starts at base)
+    bool k0_fresh;       // k0 starts exactly at the tile start
+    bool tail_cont;      // the tile's last destination continues into the next tile
+    uint32_t nib_inner;  // nib without the lane-0 position-0 marker
+};
+
+// Destination ranks inside the tile: position p belongs to compressed
+// destination k0 + (number of destination starts in [1, p]).
+// k0 = tile_dst0[t], kend = tile_dst0[t + 1].
+__device__ __forceinline__ void tile_geometry(const DevGraph& g, uint32_t t, uint32_t k0, uint32_t kend, int lane,
+                                              TileGeo& tg)
+{
+    tg.base = (uint64_t)t * TILE;
+    const uint32_t klim = min(kend, g.Vne - 1u);
+    uint32_t h0 = 0, h1 = 0, h2 = 0, h3 = 0;
+    for (uint32_t j = k0 + 1u + (uint32_t)lane; j <= klim; j += 32u) {
+        const uint64_t p = g.dst_off[j] - tg.base;
+        if (p < TILE) {
+            const uint32_t b = 1u << (uint32_t)(p & 31u);
+            const uint32_t w = (uint32_t)(p >> 5);
+            h0 |= (w == 0) ? b : 0u;
+            h1 |= (w == 1) ? b : 0u;
+            h2 |= (w == 2) ? b : 0u;
+            h3 |= (w == 3) ? b : 0u;
+        }
+    }
+    h0 = __reduce_or_sync(FULL, h0);
+    h1 = __reduce_or_sync(FULL, h1);
+    h2 = __reduce_or_sync(FULL, h2);
+    h3 = __reduce_or_sync(FULL, h3);
+    const uint32_t c0 = __popc(h0), c1 = __popc(h1), c2 = __popc(h2), c3 = __popc(h3);
+    tg.k0 = k0;
+    tg.k0_fresh = g.dst_off[k0] == tg.base;
+    const uint32_t k_last = k0 + c0 + c1 + c2 + c3;
+    tg.tail_cont = (t + 1u < g.T) && (kend == k_last);
+    const uint32_t wi = (uint32_t)lane >> 3, sh = ((uint32_t)lane & 7u) << 2;
+    const uint32_t hw = wi == 0 ? h0 : wi == 1 ? h1 : wi == 2 ? h2 : h3;
+    tg.before = (wi > 0 ? c0 : 0u) + (wi > 1 ? c1 : 0u) + (wi > 2 ? c2 : 0u) + __popc(hw & ((1u << sh) - 1u));
+    tg.nib_inner = (hw >> sh) & 0xFu;
+    tg.nib = tg.nib_inner | ((lane == 0 && tg.k0_fresh) ? 1u : 0u);
+}
+
+__device__ __forceinline__ uint32_t pos_dst(const TileGeo& tg, int i)
+{
+    return tg.k0 + tg.before + __popc(tg.nib_inner & ((2u << i) - 1u));
+}
+
+// (value, compensation) pair for the FP32 compensated PageRank sums
+struct F2 {
+    float s, c;
+};
+// warp shuffle-up of every value type the segmented reduction carries
+template <class T>
+__device__ __forceinline__ T shfl_up(T x, int d)
+{
+    return __shfl_up_sync(FULL, x, d);
+}
+template <>
+__device__ __forceinline__ F2 shfl_up<F2>(F2 x, int d)
+{
+    return F2{__shfl_up_sync(FULL, x.s, d), __shfl_up_sync(FULL, x.c, d)};
+}
+// Knuth two-sum of the leading parts, compensations added
+struct AddF2 {
+    __device__ __forceinline__ F2 operator()(F2 a, F2 b) const
+    {
+        const float t = __fadd_rn(a.s, b.s);
+        const float bp = __fsub_rn(t, a.s);
+        const float err = __fadd_rn(__fsub_rn(a.s, __fsub_rn(t, bp)), __fsub_rn(b.s, bp));
+        return F2{t, __fadd_rn(__fadd_rn(a.c, b.c), err)};
+    }
+};
+
+enum : int { EMIT_COMPLETE = 0, EMIT_HEAD = 1, EMIT_TAIL = 2 };
+
+// Segmented reduction of the tile's 128 values; calls emit(k, value, kind)
+// once per destination segment, on the lane holding the segment's last
+// position.  kind: EMIT_COMPLETE (all in-edges of k are in this tile),
+// EMIT_HEAD (k began in an earlier tile and ends here), EMIT_TAIL (k
+// continues into the next tile).
+template <class T, class Op, class Emit>
+__device__ __forceinline__ void seg_reduce(const T (&v)[4], const TileGeo& tg, int lane, Op op, Emit emit)
+{
+    const uint32_t nib = tg.nib;
+    T run = v[0];
+    T first = v[0];
+    int first_end = -1;
+    int last_start = 0;
+#pragma unroll
+    for (int i = 1; i < 4; ++i) {
+        if ((nib >> i) & 1u) {
+            if (first_end < 0) {
+                first = run;
+                first_end = i - 1;
+                if (nib & 1u) {
+                    const uint32_t k = pos_dst(tg, i - 1);
+                    emit(k, run, (k == tg.k0 && !tg.k0_fresh) ? EMIT_HEAD : EMIT_COMPLETE);
+                }
+            } else {
+                emit(pos_dst(tg, i - 1), run, EMIT_COMPLETE);
+            }
+            run = v[i];
+            last_start = i;
+        } else {
+            run = op(run, v[i]);
+        }
+    }
+    // inclusive segmented scan of the lanes' last runs
+    bool f = (last_start > 0) || (nib & 1u);
+    T s = run;
+#pragma unroll
+    for (int d = 1; d < 32; d <<= 1) {
+        const T y = shfl_up(s, d);
+        const bool gflag = __shfl_up_sync(FULL, f, d);
+        if (lane >= d) {
+            if (!f) s = op(y, s);
+            f = f || gflag;
+        }
+    }
+    const T sp = shfl_up(s, 1);
+    const uint32_t next_fresh = __shfl_down_sync(FULL, nib & 1u, 1);
+    if (first_end >= 0 && !(nib & 1u)) {
+        const uint32_t k = pos_dst(tg, first_end);
+        const T total = lane > 0 ? op(sp, first) : first;
+        emit(k, total, (k == tg.k0 && !tg.k0_fresh) ? EMIT_HEAD : EMIT_COMPLETE);
+    }
+    if (lane == 31 || next_fresh) {
+        const uint32_t k = pos_dst(tg, 3);
+        int kind = EMIT_COMPLETE;
+        if (lane == 31 && tg.tail_cont)
+            kind = EMIT_TAIL;
+        else if (k == tg.k0 && !tg.k0_fresh)
+            kind = EMIT_HEAD;
+        emit(k, s, kind);
+    }
+}
+
+struct MinU32 {
+    __device__ __forceinline__ uint32_t operator()(uint32_t a, uint32_t b) const { return min(a, b); }
+};
+struct MinU64 {
+    __device__ __forceinline__ unsigned long long operator()(unsigned long long a, unsigned long long b) const
+    {
+        return a < b ? a : b;
+    }
+};
+struct AddF64 {
+    __device__ __forceinline__ double operator()(double a, double b) const { return __dadd_rn(a, b); }
+};
+
+}  // namespace wedge

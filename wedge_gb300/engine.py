@@ -1,0 +1,265 @@
+"""ctypes binding of ``libwedge_cuda.so`` (the C ABI declared in include/wedge_cuda.h).
+
+The Python side mirrors the reference's host flow for the edge-pull path
+(source/main.c:33-110):
+
+    app = application_select("bfs")                      # application.c:197-205
+    g = Graph.load("graph.bin", app)                     # graphdata.c:946 + :648
+    stats = g.run(app, Params(root=0))                   # execution_impl_* (execution.h:107-129)
+    props = g.read_results()                             # graph_vertex_props
+
+There is no CPU fallback: if the library cannot be loaded, importing this
+module raises.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+PKG = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(PKG, "lib", "libwedge_cuda.so")
+
+APP_BFS, APP_CC, APP_PR, APP_SSSP = 0, 1, 2, 3
+WEIGHTS_NONE, WEIGHTS_U64, WEIGHTS_F64 = 0, 1, 2
+PREC_FP64, PREC_FP32C = 0, 1
+SCHED_PLAIN, SCHED_DENSE, SCHED_WEDGE = 0, 1, 2
+PHASE_INIT, PHASE_PULL_DENSE, PHASE_PULL_WEDGE, PHASE_VERTEX_PR, PHASE_WEDGE_BUILD, PHASE_ADVANCE = range(6)
+FLAG_GRAPH, FLAG_TIMING = 1, 2
+
+OK = 0
+ERR_IO, ERR_FORMAT, ERR_OOM, ERR_CUDA, ERR_NOT_CONVERGED, ERR_ARG, ERR_UNSUPPORTED = -1, -2, -3, -4, -5, -6, -7
+
+# names accepted by application_select (source/application.c:49-59)
+_APP_NAMES = {
+    APP_BFS: ("bfs", "breadth_first_search", "breadthfirstsearch"),
+    APP_CC: ("cc", "connected_components", "connectedcomponents"),
+    APP_PR: ("pr", "pagerank"),
+    APP_SSSP: ("sssp", "single_source_shortest_path", "singlesourceshortestpath"),
+}
+APP_CANONICAL = {APP_BFS: "Breadth-First Search", APP_CC: "Connected Components", APP_PR: "PageRank",
+                 APP_SSSP: "Single-Source Shortest Path"}
+
+
+def application_select(name: str) -> int:
+    """Application id for a name, as application_select (application.c:197-205); raises ValueError."""
+    n = name.lower()
+    for app, names in _APP_NAMES.items():
+        if n in names:
+            return app
+    raise ValueError(f'Application: ERROR: unable to run "{name}"')
+
+
+class Params(C.Structure):
+    _fields_ = [("root", C.c_uint64), ("threshold_pct", C.c_uint32), ("num_iterations", C.c_uint32),
+                ("damping", C.c_double), ("precision", C.c_int32), ("sched", C.c_int32),
+                ("max_iterations", C.c_uint32), ("flags", C.c_uint32)]
+
+    def __init__(self, root=0, threshold_pct=20, num_iterations=1, damping=0.0, precision=PREC_FP64,
+                 sched=SCHED_PLAIN, max_iterations=0, flags=0):
+        super().__init__(root, threshold_pct, num_iterations, damping, precision, sched, max_iterations, flags)
+
+
+class Stats(C.Structure):
+    _fields_ = [("iterations", C.c_uint64), ("wedge_iterations", C.c_uint64), ("running_ms", C.c_double),
+                ("pull_ms_dense", C.c_double), ("pull_ms_wedge", C.c_double), ("wedge_ms", C.c_double),
+                ("vertex_ms", C.c_double), ("edges_scanned", C.c_uint64), ("tiles_scanned", C.c_uint64),
+                ("pull_launches", C.c_uint64), ("kernel_launches", C.c_uint64), ("pr_sum", C.c_double)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+class WedgeError(RuntimeError):
+    def __init__(self, status: int, what: str):
+        super().__init__(f"{what}: {status_string(status)} ({status})")
+        self.status = status
+
+
+_lib = None
+
+# every symbol include/wedge_cuda.h declares, with its ctypes signature
+_SIGNATURES = {
+    "wedge_cuda_load_graph": (C.c_int, [C.c_char_p, C.c_int, C.POINTER(C.c_void_p)]),
+    "wedge_cuda_load_graph_ex": (C.c_int, [C.c_char_p, C.c_int, C.c_int, C.POINTER(C.c_void_p)]),
+    "wedge_cuda_load_graph_image": (C.c_int, [C.c_void_p, C.c_uint64, C.c_int, C.c_int, C.POINTER(C.c_void_p)]),
+    "wedge_cuda_load_edges": (C.c_int, [C.c_uint64, C.c_uint64, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int,
+                                        C.POINTER(C.c_void_p)]),
+    "wedge_cuda_load_edge_vectors": (C.c_int, [C.c_uint64, C.c_void_p, C.c_uint64, C.c_int, C.c_int,
+                                               C.POINTER(C.c_void_p)]),
+    "wedge_cuda_generate_rmat": (C.c_int, [C.c_uint32, C.c_uint32, C.c_double, C.c_double, C.c_double, C.c_uint64,
+                                           C.c_int, C.c_int, C.POINTER(C.c_void_p)]),
+    "wedge_cuda_generate_grid": (C.c_int, [C.c_uint32, C.c_double, C.c_uint64, C.c_int, C.POINTER(C.c_void_p)]),
+    "wedge_cuda_run": (C.c_int, [C.c_void_p, C.c_int, C.POINTER(Params), C.POINTER(Stats)]),
+    "wedge_cuda_run_phase": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.POINTER(Params), C.POINTER(C.c_uint64)]),
+    "wedge_cuda_read_results": (C.c_int, [C.c_void_p, C.c_void_p, C.c_uint64]),
+    "wedge_cuda_read_outdegrees": (C.c_int, [C.c_void_p, C.c_void_p, C.c_uint64]),
+    "wedge_cuda_num_vertices": (C.c_uint64, [C.c_void_p]),
+    "wedge_cuda_num_edges": (C.c_uint64, [C.c_void_p]),
+    "wedge_cuda_stream": (C.c_void_p, [C.c_void_p]),
+    "wedge_cuda_free": (None, [C.c_void_p]),
+    "wedge_cuda_status_string": (C.c_char_p, [C.c_int]),
+    "wedge_cuda_abi_version": (C.c_int, []),
+}
+
+
+def lib():
+    """The loaded engine library (raises if it has not been built)."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise ImportError(f"{LIB_PATH} is missing: run `python -c 'import __graft_entry__ as g; g.build()'`")
+        L = C.CDLL(LIB_PATH)
+        for name, (res, args) in _SIGNATURES.items():
+            f = getattr(L, name)
+            f.restype = res
+            f.argtypes = args
+        _lib = L
+    return _lib
+
+
+def status_string(status: int) -> str:
+    return lib().wedge_cuda_status_string(status).decode()
+
+
+def _check(rc: int, what: str):
+    if rc != OK:
+        raise WedgeError(rc, what)
+
+
+def _ptr(a: np.ndarray):
+    return a.ctypes.data_as(C.c_void_p)
+
+
+class Graph:
+    """A graph resident on the GPU (the handle of wedge_cuda.h)."""
+
+    def __init__(self, handle: C.c_void_p, weight_kind: int = WEIGHTS_NONE):
+        self._h = handle
+        self.weight_kind = weight_kind
+        self.last_app = None
+
+    # ---------------------------------------------------------------- loading
+    @classmethod
+    def load(cls, path: str, app: int, weight_kind: int = WEIGHTS_U64) -> "Graph":
+        h = C.c_void_p()
+        _check(lib().wedge_cuda_load_graph_ex(path.encode(), app, weight_kind, C.byref(h)), "wedge_cuda_load_graph_ex")
+        return cls(h, weight_kind if app == APP_SSSP else WEIGHTS_NONE)
+
+    @classmethod
+    def load_image(cls, image: bytes | np.ndarray, app: int, weight_kind: int = WEIGHTS_U64) -> "Graph":
+        buf = np.frombuffer(image, np.uint8) if isinstance(image, (bytes, bytearray)) else np.ascontiguousarray(image)
+        h = C.c_void_p()
+        _check(lib().wedge_cuda_load_graph_image(_ptr(buf), buf.nbytes, app, weight_kind, C.byref(h)),
+               "wedge_cuda_load_graph_image")
+        return cls(h, weight_kind if app == APP_SSSP else WEIGHTS_NONE)
+
+    @classmethod
+    def from_edges(cls, V: int, src, dst, weights=None, weight_kind: int = WEIGHTS_U64) -> "Graph":
+        s = np.ascontiguousarray(src, np.uint32)
+        d = np.ascontiguousarray(dst, np.uint32)
+        w = None if weights is None else np.ascontiguousarray(weights, np.uint64)
+        h = C.c_void_p()
+        _check(lib().wedge_cuda_load_edges(V, len(s), _ptr(s), _ptr(d), None if w is None else _ptr(w),
+                                           weight_kind if w is not None else WEIGHTS_NONE, C.byref(h)),
+               "wedge_cuda_load_edges")
+        return cls(h, weight_kind if w is not None else WEIGHTS_NONE)
+
+    @classmethod
+    def from_edge_vectors(cls, V: int, vectors: np.ndarray, weighted: bool, weight_kind: int = WEIGHTS_U64) -> "Graph":
+        v = np.ascontiguousarray(vectors, np.uint64)
+        words = 8 if weighted else 4
+        h = C.c_void_p()
+        _check(lib().wedge_cuda_load_edge_vectors(V, _ptr(v), v.size // words, int(weighted), weight_kind, C.byref(h)),
+               "wedge_cuda_load_edge_vectors")
+        return cls(h, weight_kind if weighted else WEIGHTS_NONE)
+
+    @classmethod
+    def rmat(cls, scale: int, edge_factor: int, seed: int, symmetrise: bool = False, weight_kind: int = WEIGHTS_NONE,
+             abc=(0.57, 0.19, 0.19)) -> "Graph":
+        h = C.c_void_p()
+        _check(lib().wedge_cuda_generate_rmat(scale, edge_factor, abc[0], abc[1], abc[2], seed, int(symmetrise),
+                                              weight_kind, C.byref(h)), "wedge_cuda_generate_rmat")
+        return cls(h, weight_kind)
+
+    @classmethod
+    def grid(cls, side: int, long_range_frac: float, seed: int, weight_kind: int = WEIGHTS_U64) -> "Graph":
+        h = C.c_void_p()
+        _check(lib().wedge_cuda_generate_grid(side, long_range_frac, seed, weight_kind, C.byref(h)),
+               "wedge_cuda_generate_grid")
+        return cls(h, weight_kind)
+
+    # ---------------------------------------------------------------- running
+    @property
+    def V(self) -> int:
+        return lib().wedge_cuda_num_vertices(self._h)
+
+    @property
+    def E(self) -> int:
+        return lib().wedge_cuda_num_edges(self._h)
+
+    @property
+    def stream(self) -> int:
+        return lib().wedge_cuda_stream(self._h) or 0
+
+    def run(self, app: int, params: Params | None = None, allow_not_converged: bool = False) -> dict:
+        p = params or Params()
+        st = Stats()
+        rc = lib().wedge_cuda_run(self._h, app, C.byref(p), C.byref(st))
+        if not (rc == OK or (allow_not_converged and rc == ERR_NOT_CONVERGED)):
+            raise WedgeError(rc, "wedge_cuda_run")
+        self.last_app = app
+        d = st.as_dict()
+        d["status"] = rc
+        return d
+
+    def run_phase(self, app: int, phase: int, params: Params | None = None) -> int:
+        p = params or Params()
+        mass = C.c_uint64()
+        _check(lib().wedge_cuda_run_phase(self._h, app, phase, C.byref(p), C.byref(mass)), "wedge_cuda_run_phase")
+        self.last_app = app
+        return mass.value
+
+    def read_results(self, out: np.ndarray | None = None) -> np.ndarray:
+        V = self.V
+        if out is None:
+            out = np.empty(V, np.uint64)
+        _check(lib().wedge_cuda_read_results(self._h, _ptr(out), out.nbytes), "wedge_cuda_read_results")
+        return out
+
+    def read_outdegrees(self) -> np.ndarray:
+        out = np.empty(self.V, np.uint64)
+        _check(lib().wedge_cuda_read_outdegrees(self._h, _ptr(out), out.nbytes), "wedge_cuda_read_outdegrees")
+        return out
+
+    def close(self):
+        if self._h:
+            lib().wedge_cuda_free(self._h)
+            self._h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def prop_string(app: int, prop: int, outdeg: int, num_vertices: int, sssp_f64: bool = False) -> str:
+    """One -o output value, formatted as execution_get_vertex_prop_string_* does."""
+    if app == APP_BFS:  # execution_bfs.c:69-73
+        return "%d" % np.int64(np.uint64(prop).view(np.int64))
+    d = float(np.uint64(prop).view(np.float64))
+    if app == APP_CC:  # execution_cc.c:47-51
+        return "%.0f" % d
+    if app == APP_PR:  # execution_pr.c:31-35
+        return "%.4e" % (d * (num_vertices if outdeg == 0 else outdeg))
+    if sssp_f64:
+        return "%.17g" % d
+    return "%d" % np.int64(np.uint64(prop).view(np.int64))  # execution_sssp.c:48-52
