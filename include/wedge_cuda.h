@@ -109,10 +109,27 @@ typedef struct wedge_stats {
     double vertex_ms;             /* PageRank vertex phase (needs WEDGE_FLAG_TIMING) */
     uint64_t edges_scanned;       /* in-edges read by the pulls, summed over iterations */
     uint64_t tiles_scanned;       /* 128-edge tiles visited by the pulls */
+    uint64_t dsts_scanned;        /* destinations with in-edges in the visited tiles */
+    uint64_t vertices_activated;  /* vertices whose property changed (BFS: newly visited) */
     uint64_t pull_launches;       /* edge-pull kernel launches */
     uint64_t kernel_launches;     /* all kernel launches of the run */
     double pr_sum;                /* PageRank Sum (execution_pr.c:63-71); 0 for other apps */
 } wedge_stats_t;
+
+/* one iteration of a traversal: the ITERATION_STATS record the reference prints to stderr
+ * (execution_bfs.c:227-232: active edges, used Wedge, pull ms, Wedge ms) plus device counters */
+typedef struct wedge_iteration_record {
+    uint64_t active_edges;        /* changed-edge mass that chose this iteration's pull */
+    uint32_t used_wedge;          /* 1 if the pull used the Wedge frontier */
+    uint32_t iteration;
+    double pull_ms;               /* pull time, or -1 unless the run had WEDGE_FLAG_TIMING */
+    double wedge_ms;              /* Wedge-frontier build time after the pull, or -1 */
+    uint64_t changed_mass;        /* changed-edge mass the pull produced */
+    uint64_t edges_scanned;
+    uint64_t tiles_scanned;
+    uint64_t dsts_scanned;
+    uint64_t vertices_activated;
+} wedge_iteration_record_t;
 
 typedef struct wedge_graph wedge_graph_t;
 
@@ -162,6 +179,11 @@ int wedge_cuda_run_phase(wedge_graph_t* g, int app, int phase, const wedge_param
                          uint64_t* active_mass);
 
 /* ---------------------------------------------------------------- results */
+
+/* per-iteration records of the last run (at most 4096 kept); *count receives the number
+ * of iterations recorded, min(count, max_records) records are written */
+int wedge_cuda_iteration_log(wedge_graph_t* g, wedge_iteration_record_t* out, uint64_t max_records,
+                             uint64_t* count);
 
 /* graph_vertex_props, one 64-bit word per vertex (see the header comment); bytes >= 8*V */
 int wedge_cuda_read_results(wedge_graph_t* g, void* host_props, uint64_t bytes);

@@ -67,9 +67,18 @@ typedef struct {
     int threads, id;
 } rmat_job_t;
 
+static inline uint64_t mix64_inline(uint64_t z)
+{
+    z += 0x9E3779B97F4A7C15ull;
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+    return z ^ (z >> 31);
+}
+
 static void* rmat_worker(void* p)
 {
     rmat_job_t* j = (rmat_job_t*)p;
+    const uint64_t hseed = mix64_inline(j->seed); /* orc_draw's first mix, hoisted */
     const uint64_t per = j->count / j->threads, extra = j->count % j->threads;
     const uint64_t lo = per * j->id + ((uint64_t)j->id < extra ? j->id : extra);
     const uint64_t hi = lo + per + ((uint64_t)j->id < extra ? 1 : 0);
@@ -79,7 +88,7 @@ static void* rmat_worker(void* p)
         uint64_t h = 0;
         for (uint32_t l = 0; l < j->scale; ++l) {
             if ((l & 1u) == 0)
-                h = orc_draw(j->seed, e, l >> 1);
+                h = mix64_inline(hseed + ((e << 4) | (l >> 1))); /* == orc_draw(seed, e, l/2) */
             const uint64_t u = (l & 1u) ? (h >> 32) : (h & 0xffffffffull);
             const uint32_t bit = 1u << (j->scale - 1 - l);
             if (u < j->t[0]) {
@@ -474,62 +483,109 @@ void orc_free(orc_graph_t* g)
     free(g);
 }
 
-/*
- * graphdata.c:946-1133 (+ :648-942): pack dst-grouped edges into vectors, pad to
- * a multiple of 4 vectors with invalid vectors of dst V-1, then build the
- * vertex index (:402-427), out-degrees (:430-490), CSRI (:493-585), the Wedge
- * frontier (:804-842) and the traditional bitmaps (:845-892).
- */
-static int build_common(orc_graph_t* g, const uint32_t* src, const uint32_t* dst, const uint64_t* w)
+/* ---- a small parallel-for over pthreads (the reference uses Spindle tasks) ---- */
+typedef struct {
+    void (*fn)(void* ctx, int id, int n);
+    void* ctx;
+    int id, n;
+} pf_job_t;
+
+static void* pf_main(void* p)
 {
-    const uint64_t V = g->V, E = g->E;
+    pf_job_t* j = (pf_job_t*)p;
+    j->fn(j->ctx, j->id, j->n);
+    return NULL;
+}
+
+static void parallel_run(int n, void (*fn)(void*, int, int), void* ctx)
+{
+    pf_job_t* jobs = (pf_job_t*)calloc((size_t)n, sizeof(pf_job_t));
+    pthread_t* th = (pthread_t*)calloc((size_t)n, sizeof(pthread_t));
+    for (int i = 0; i < n; ++i)
+        jobs[i] = (pf_job_t){fn, ctx, i, n};
+    for (int i = 1; i < n; ++i)
+        pthread_create(&th[i], NULL, pf_main, &jobs[i]);
+    pf_main(&jobs[0]);
+    for (int i = 1; i < n; ++i)
+        pthread_join(th[i], NULL);
+    free(jobs);
+    free(th);
+}
+
+static inline void chunk_of(uint64_t total, int id, int n, uint64_t* lo, uint64_t* hi)
+{
+    const uint64_t per = total / (uint64_t)n, extra = total % (uint64_t)n;
+    *lo = per * (uint64_t)id + ((uint64_t)id < extra ? (uint64_t)id : extra);
+    *hi = *lo + per + ((uint64_t)id < extra ? 1 : 0);
+}
+
+typedef struct {
+    orc_graph_t* g;
+    const uint32_t* src;
+    const uint32_t* dst;
+    const uint64_t* w;
+    uint64_t* cut;  /* [n+1] edge positions, each at the start of a destination run */
+    uint64_t* voff; /* [n+1] vectors before part p (after the prefix) */
+    int* err;
+} build_ctx_t;
+
+/* validation and vector count of one part (graphdata.c:1017-1035, first pass) */
+static void bp_count(void* p, int id, int n)
+{
+    (void)n;
+    build_ctx_t* c = (build_ctx_t*)p;
+    const uint64_t V = c->g->V;
     uint64_t nvec = 0, run = 0;
-    for (uint64_t e = 0; e < E; ++e) {
-        if (e > 0 && dst[e] != dst[e - 1]) {
-            if (dst[e] < dst[e - 1])
-                return ORC_ERR_FORMAT; /* input must be grouped by ascending dst */
-            nvec += (run + 3) / 4;
+    for (uint64_t e = c->cut[id]; e < c->cut[id + 1]; ++e) {
+        if (c->dst[e] >= V || c->src[e] >= V)
+            c->err[id] = ORC_ERR_FORMAT;
+        if (e > 0 && c->dst[e] != c->dst[e - 1]) {
+            if (c->dst[e] < c->dst[e - 1])
+                c->err[id] = ORC_ERR_FORMAT; /* input must be grouped by ascending dst */
+            if (e != c->cut[id])
+                nvec += (run + 3) / 4;
             run = 0;
         }
-        if (dst[e] >= V || src[e] >= V)
-            return ORC_ERR_FORMAT;
         ++run;
     }
-    nvec += (run + 3) / 4;
-    g->nvec = nvec;
-    g->nvec_alloc = nvec + (4ull - (nvec & 3ull));
+    if (run)
+        nvec += (run + 3) / 4;
+    c->voff[id + 1] = nvec;
+}
+
+/* second pass: a stash of up to 4 sources per destination run (graphdata.c:247-319) */
+static void bp_pack(void* p, int id, int n)
+{
+    (void)n;
+    build_ctx_t* c = (build_ctx_t*)p;
+    orc_graph_t* g = c->g;
     const uint64_t words = g->weighted ? 8 : 4;
-    g->vec = (uint64_t*)xalloc(g->nvec_alloc * words * 8, 0);
-    if (!g->vec)
-        return ORC_ERR_OOM;
-    const uint64_t zero[4] = {0, 0, 0, 0};
-    for (uint64_t i = nvec; i < g->nvec_alloc; ++i)
-        write_edge_vector(V - 1, zero, zero, 0, g->weighted, &g->vec[i * words]);
-    /* pass 2: stash of up to 4 sources per destination run (graphdata.c:247-319) */
-    uint64_t stash_s[4] = {0}, stash_w[4] = {0}, stash_d = 0, cnt = 0, wi = 0;
-    for (uint64_t e = 0; e < E; ++e) {
-        if ((cnt != 0 && stash_d != dst[e]) || cnt == 4) {
+    uint64_t stash_s[4] = {0}, stash_w[4] = {0}, stash_d = 0, cnt = 0, wi = c->voff[id];
+    for (uint64_t e = c->cut[id]; e < c->cut[id + 1]; ++e) {
+        if ((cnt != 0 && stash_d != c->dst[e]) || cnt == 4) {
             write_edge_vector(stash_d, stash_s, stash_w, cnt, g->weighted, &g->vec[wi * words]);
             ++wi;
             cnt = 0;
         }
-        stash_d = dst[e];
-        stash_s[cnt] = src[e];
-        stash_w[cnt] = w ? w[e] : 0;
+        stash_d = c->dst[e];
+        stash_s[cnt] = c->src[e];
+        stash_w[cnt] = c->w ? c->w[e] : 0;
         ++cnt;
     }
     if (cnt)
         write_edge_vector(stash_d, stash_s, stash_w, cnt, g->weighted, &g->vec[wi * words]);
+}
 
-    const uint64_t Va = V + (8ull - (V & 7ull));
-    g->index = (uint64_t*)xalloc(Va * 8, 0xff);
-    g->outdeg = (uint64_t*)xalloc(Va * 8, 0);
-    g->props = (uint64_t*)xalloc(Va * 8, 0);
-    g->acc = (uint64_t*)xalloc(Va * 8, 0);
-    if (!g->index || !g->outdeg || !g->props || !g->acc)
-        return ORC_ERR_OOM;
-    uint64_t last = UINT64_MAX;
-    for (uint64_t i = 0; i < nvec; ++i) {
+/* vertex index (graphdata.c:402-427) and out-degrees (graphdata.c:430-490) */
+static void bp_index(void* p, int id, int n)
+{
+    build_ctx_t* c = (build_ctx_t*)p;
+    orc_graph_t* g = c->g;
+    const uint64_t words = g->weighted ? 8 : 4;
+    uint64_t lo, hi;
+    chunk_of(g->nvec, id, n, &lo, &hi);
+    uint64_t last = lo > 0 ? dst_of(&g->vec[(lo - 1) * words]) : UINT64_MAX;
+    for (uint64_t i = lo; i < hi; ++i) {
         const uint64_t d = dst_of(&g->vec[i * words]);
         if (d != last) {
             g->index[d] = i;
@@ -538,48 +594,126 @@ static int build_common(orc_graph_t* g, const uint32_t* src, const uint32_t* dst
         for (int k = 0; k < 4; ++k) {
             const uint64_t x = g->vec[i * words + k];
             if (x & VALID_BIT)
-                g->outdeg[x & SRC_MASK] += 1;
+                __atomic_fetch_add(&g->outdeg[x & SRC_MASK], 1ull, __ATOMIC_RELAXED);
         }
     }
+}
 
-    /* Wedge frontier: (nvec >> 11) + 1 blocks of 512 bits (graphdata.c:810-819) */
-    const uint64_t blocks = (nvec >> (9ull + LOG2_PRECISION)) + 1ull;
-    g->wedge_count = blocks * 8ull;
-    g->wedge = (uint64_t*)xalloc(g->wedge_count * 8, 0);
-    g->csri_index = (uint64_t*)xalloc((V + 1) * 8, 0);
-    g->csri_edges = (uint64_t*)xalloc((nvec * 4 + 1) * 8, 0);
-    const uint64_t fbytes = ((V >> 9) + ((V & 511ull) ? 1 : 0)) << 6;
-    g->frontier_count = fbytes >> 3;
-    g->active = (uint64_t*)xalloc(fbytes + 64, 0);
-    g->snapshot = (uint64_t*)xalloc(fbytes + 64, 0);
-    g->unconverged = (uint64_t*)xalloc(fbytes + 64, 0xff);
-    if (!g->wedge || !g->csri_index || !g->csri_edges || !g->active || !g->snapshot || !g->unconverged)
-        return ORC_ERR_OOM;
-    uint64_t pos = 0;
-    for (uint64_t v = 0; v < V; ++v) {
-        g->csri_index[v] = pos;
-        pos += g->outdeg[v];
-    }
-    g->csri_index[V] = pos;
-    for (uint64_t i = 0; i < nvec; ++i)
+/* CSRI fill with an atomic cursor per source (graphdata.c:535-569) */
+static void bp_csri(void* p, int id, int n)
+{
+    build_ctx_t* c = (build_ctx_t*)p;
+    orc_graph_t* g = c->g;
+    const uint64_t words = g->weighted ? 8 : 4;
+    uint64_t lo, hi;
+    chunk_of(g->nvec, id, n, &lo, &hi);
+    for (uint64_t i = lo; i < hi; ++i)
         for (int k = 0; k < 4; ++k) {
             const uint64_t x = g->vec[i * words + k];
-            if (x & VALID_BIT)
-                g->csri_edges[g->csri_index[x & SRC_MASK]++] = i >> LOG2_PRECISION;
+            if (x & VALID_BIT) {
+                const uint64_t pos = __atomic_fetch_add(&g->csri_index[x & SRC_MASK], 1ull, __ATOMIC_RELAXED);
+                g->csri_edges[pos] = i >> LOG2_PRECISION;
+            }
         }
-    pos = 0;
-    for (uint64_t v = 0; v < V; ++v) {
-        g->csri_index[v] = pos;
-        pos += g->outdeg[v];
+}
+
+/*
+ * graphdata.c:946-1133 (+ :648-942): pack dst-grouped edges into vectors, pad to
+ * a multiple of 4 vectors with invalid vectors of dst V-1, then build the
+ * vertex index (:402-427), out-degrees (:430-490), CSRI (:493-585), the Wedge
+ * frontier (:804-842) and the traditional bitmaps (:845-892).
+ */
+static int build_common(orc_graph_t* g, const uint32_t* src, const uint32_t* dst, const uint64_t* w, int threads)
+{
+    const uint64_t V = g->V, E = g->E;
+    int n = threads > 0 ? threads : orc_online_cores();
+    if ((uint64_t)n > E / 4096 + 1)
+        n = (int)(E / 4096 + 1);
+    build_ctx_t c = {g, src, dst, w, NULL, NULL, NULL};
+    c.cut = (uint64_t*)calloc((size_t)n + 1, 8);
+    c.voff = (uint64_t*)calloc((size_t)n + 1, 8);
+    c.err = (int*)calloc((size_t)n, sizeof(int));
+    if (!c.cut || !c.voff || !c.err) {
+        free(c.cut);
+        free(c.voff);
+        free(c.err);
+        return ORC_ERR_OOM;
     }
-    g->csri_index[V] = pos;
-    return ORC_OK;
+    for (int i = 1; i < n; ++i) {
+        uint64_t b = E * (uint64_t)i / (uint64_t)n;
+        if (b < c.cut[i - 1])
+            b = c.cut[i - 1];
+        while (b > 0 && b < E && dst[b] == dst[b - 1])
+            ++b;
+        c.cut[i] = b;
+    }
+    c.cut[n] = E;
+    parallel_run(n, bp_count, &c);
+    int rc = ORC_OK;
+    for (int i = 0; i < n; ++i)
+        if (c.err[i])
+            rc = c.err[i];
+    for (int i = 0; i < n; ++i)
+        c.voff[i + 1] += c.voff[i];
+    const uint64_t nvec = c.voff[n];
+    if (rc == ORC_OK) {
+        g->nvec = nvec;
+        g->nvec_alloc = nvec + (4ull - (nvec & 3ull));
+        g->vec = (uint64_t*)xalloc(g->nvec_alloc * (g->weighted ? 8 : 4) * 8, 0);
+        if (!g->vec)
+            rc = ORC_ERR_OOM;
+    }
+    if (rc == ORC_OK) {
+        const uint64_t words = g->weighted ? 8 : 4;
+        const uint64_t zero[4] = {0, 0, 0, 0};
+        for (uint64_t i = nvec; i < g->nvec_alloc; ++i)
+            write_edge_vector(V - 1, zero, zero, 0, g->weighted, &g->vec[i * words]);
+        parallel_run(n, bp_pack, &c);
+        const uint64_t Va = V + (8ull - (V & 7ull));
+        g->index = (uint64_t*)xalloc(Va * 8, 0xff);
+        g->outdeg = (uint64_t*)xalloc(Va * 8, 0);
+        g->props = (uint64_t*)xalloc(Va * 8, 0);
+        g->acc = (uint64_t*)xalloc(Va * 8, 0);
+        /* Wedge frontier: (nvec >> 11) + 1 blocks of 512 bits (graphdata.c:810-819) */
+        const uint64_t blocks = (nvec >> (9ull + LOG2_PRECISION)) + 1ull;
+        g->wedge_count = blocks * 8ull;
+        g->wedge = (uint64_t*)xalloc(g->wedge_count * 8, 0);
+        g->csri_index = (uint64_t*)xalloc((V + 1) * 8, 0);
+        g->csri_edges = (uint64_t*)xalloc((nvec * 4 + 1) * 8, 0);
+        const uint64_t fbytes = ((V >> 9) + ((V & 511ull) ? 1 : 0)) << 6;
+        g->frontier_count = fbytes >> 3;
+        g->active = (uint64_t*)xalloc(fbytes + 64, 0);
+        g->snapshot = (uint64_t*)xalloc(fbytes + 64, 0);
+        g->unconverged = (uint64_t*)xalloc(fbytes + 64, 0xff);
+        if (!g->index || !g->outdeg || !g->props || !g->acc || !g->wedge || !g->csri_index || !g->csri_edges ||
+            !g->active || !g->snapshot || !g->unconverged)
+            rc = ORC_ERR_OOM;
+    }
+    if (rc == ORC_OK) {
+        parallel_run(n, bp_index, &c);
+        uint64_t pos = 0;
+        for (uint64_t v = 0; v < V; ++v) {
+            g->csri_index[v] = pos;
+            pos += g->outdeg[v];
+        }
+        g->csri_index[V] = pos;
+        parallel_run(n, bp_csri, &c);
+        pos = 0;
+        for (uint64_t v = 0; v < V; ++v) {
+            g->csri_index[v] = pos;
+            pos += g->outdeg[v];
+        }
+        g->csri_index[V] = pos;
+    }
+    free(c.cut);
+    free(c.voff);
+    free(c.err);
+    return rc;
 }
 
 int orc_build(uint64_t V, uint64_t E, const uint32_t* src, const uint32_t* dst, const uint64_t* weights,
               int app, int threads, orc_graph_t** out)
 {
-    (void)threads;
     *out = NULL;
     if (V == 0)
         return ORC_ERR_FORMAT;
@@ -598,7 +732,7 @@ int orc_build(uint64_t V, uint64_t E, const uint32_t* src, const uint32_t* dst, 
         }
         orc_weights(E, src, dst, ORC_WEIGHTS_U64, w);
     }
-    const int rc = build_common(g, src, dst, weights ? weights : w);
+    const int rc = build_common(g, src, dst, weights ? weights : w, threads);
     free(w);
     if (rc != ORC_OK) {
         orc_free(g);

@@ -49,6 +49,10 @@ int new_handle(wedge_graph** out)
     for (int i = 0; i < 8; ++i)
         WEDGE_CHECK(cudaEventCreate(&h->ev[i]));
     WEDGE_CHECK(cudaMallocHost((void**)&h->h_ctrl, sizeof(Ctrl)));
+    h->iter_pull_ms = (double*)calloc(LOG_CAP, sizeof(double));
+    h->iter_wedge_ms = (double*)calloc(LOG_CAP, sizeof(double));
+    if (!h->iter_pull_ms || !h->iter_wedge_ms)
+        return WEDGE_ERR_OOM;
     *out = h;
     return WEDGE_OK;
 }
@@ -97,6 +101,8 @@ void free_handle(wedge_graph* h)
             cudaEventDestroy(h->ev[i]);
     if (h->h_ctrl)
         cudaFreeHost(h->h_ctrl);
+    free(h->iter_pull_ms);
+    free(h->iter_wedge_ms);
     if (h->stream)
         cudaStreamDestroy(h->stream);
     free(h);
@@ -362,11 +368,12 @@ __device__ __forceinline__ uint32_t* next_front(const DevState& s, uint32_t app,
 }
 
 // Edge pull over all tiles (dense) or over the tiles of the Wedge frontier.
-// block_cnt[4*b + {0,1,2}] = changed mass, in-edges read, tiles visited.
+// block_cnt[NCNT*b + CNT_*] = changed mass, in-edges read, tiles visited,
+// destinations in visited tiles, vertices activated.
 template <int APP>
 __global__ void __launch_bounds__(PULL_THREADS) pull_kernel(DevGraph g, DevState s, unsigned long long* block_cnt)
 {
-    __shared__ unsigned long long sh_cnt[PULL_THREADS / 32][3];
+    __shared__ unsigned long long sh_cnt[PULL_THREADS / 32][5];
     __shared__ double sh_sum[PULL_THREADS / 32];
     Ctrl* c = s.ctrl;
     if (c->done)
@@ -380,7 +387,7 @@ __global__ void __launch_bounds__(PULL_THREADS) pull_kernel(DevGraph g, DevState
     const uint32_t parity = c->parity;
     const uint32_t* cur = cur_front(s, parity);
     uint32_t* nxt = next_front(s, APP, parity);
-    unsigned long long mass = 0, edges = 0, tiles = 0;
+    unsigned long long mass = 0, edges = 0, tiles = 0, dsts = 0, act = 0;
     double psum = 0.0;
 
     for (uint32_t i = gw; i < ntiles; i += nw) {
@@ -415,6 +422,7 @@ __global__ void __launch_bounds__(PULL_THREADS) pull_kernel(DevGraph g, DevState
         }
         TileGeo tg;
         tile_geometry(g, t, k0, kend, lane, tg);
+        dsts += tg.ndst;
         const bool on = (cmask >> (lane >> 3)) & 1u;
         uint4 sv = make_uint4(NONE32, NONE32, NONE32, NONE32);
         if (on)
@@ -442,6 +450,7 @@ __global__ void __launch_bounds__(PULL_THREADS) pull_kernel(DevGraph g, DevState
                     atomicOr(&s.vis_c[k >> 5], 1u << (k & 31u));
                     atomicOr(&nxt[vtx >> 5], 1u << (vtx & 31u));
                     mass += g.outdeg[vtx];
+                    ++act;
                 }
             });
         } else if (APP == WEDGE_APP_CC) {
@@ -460,8 +469,10 @@ __global__ void __launch_bounds__(PULL_THREADS) pull_kernel(DevGraph g, DevState
                     const uint32_t old = atomicMin(&s.prop32[vtx], val);
                     if (val < old) {
                         const uint32_t b = 1u << (vtx & 31u);
-                        if (!(atomicOr(&nxt[vtx >> 5], b) & b))
+                        if (!(atomicOr(&nxt[vtx >> 5], b) & b)) {
                             mass += g.outdeg[vtx];
+                            ++act;
+                        }
                     }
                 }
             });
@@ -495,8 +506,10 @@ __global__ void __launch_bounds__(PULL_THREADS) pull_kernel(DevGraph g, DevState
                     const unsigned long long old = atomicMin(&s.prop64[vtx], val);
                     if (val < old) {
                         const uint32_t b = 1u << (vtx & 31u);
-                        if (!(atomicOr(&nxt[vtx >> 5], b) & b))
+                        if (!(atomicOr(&nxt[vtx >> 5], b) & b)) {
                             mass += g.outdeg[vtx];
+                            ++act;
+                        }
                     }
                 }
             });
@@ -548,27 +561,27 @@ __global__ void __launch_bounds__(PULL_THREADS) pull_kernel(DevGraph g, DevState
     // per-block counters (no same-address atomics): reduced by decide_kernel
     mass = warp_sum_u64(mass);
     edges = warp_sum_u64(edges);
+    act = warp_sum_u64(act);
     if (lane == 0) {
-        sh_cnt[wib][0] = mass;
-        sh_cnt[wib][1] = edges;
-        sh_cnt[wib][2] = tiles;
+        sh_cnt[wib][CNT_MASS] = mass;
+        sh_cnt[wib][CNT_EDGES] = edges;
+        sh_cnt[wib][CNT_TILES] = tiles;  // warp-uniform
+        sh_cnt[wib][CNT_DSTS] = dsts;    // warp-uniform
+        sh_cnt[wib][CNT_ACT] = act;
         sh_sum[wib] = psum;
     }
     __syncthreads();
-    if (threadIdx.x == 0) {
-        unsigned long long a = 0, b = 0, t2 = 0;
+    if (threadIdx.x < 5) {
+        unsigned long long a = 0;
+        for (int w = 0; w < PULL_THREADS / 32; ++w)
+            a += sh_cnt[w][threadIdx.x];
+        block_cnt[NCNT * blockIdx.x + threadIdx.x] = a;
+    }
+    if (APP == WEDGE_APP_PR && threadIdx.x == 0) {
         double ps = 0.0;
-        for (int w = 0; w < PULL_THREADS / 32; ++w) {
-            a += sh_cnt[w][0];
-            b += sh_cnt[w][1];
-            t2 += sh_cnt[w][2];
+        for (int w = 0; w < PULL_THREADS / 32; ++w)
             ps = __dadd_rn(ps, sh_sum[w]);
-        }
-        block_cnt[4u * blockIdx.x + 0u] = a;
-        block_cnt[4u * blockIdx.x + 1u] = b;
-        block_cnt[4u * blockIdx.x + 2u] = t2;
-        if (APP == WEDGE_APP_PR)
-            s.block_part[blockIdx.x] = ps;
+        s.block_part[blockIdx.x] = ps;
     }
 }
 
@@ -584,40 +597,67 @@ __device__ __forceinline__ uint32_t choose_mode(uint32_t sched, unsigned long lo
 // After a pull: reduce the block counters, count the iteration, stop when no
 // edge was activated (execution_bfs.c:239-251) or at the cap, choose the next
 // pull (execution_bfs.c:141, execution_cc.c:103).
+__device__ __forceinline__ void reduce_counters(const unsigned long long* block_cnt, uint32_t nblocks,
+                                                unsigned long long (&out)[5])
+{
+    __shared__ unsigned long long sh[5][AUX_THREADS / 32];
+    unsigned long long x[5] = {0, 0, 0, 0, 0};
+    for (uint32_t i = threadIdx.x; i < nblocks; i += blockDim.x)
+#pragma unroll
+        for (int j = 0; j < 5; ++j)
+            x[j] += block_cnt[NCNT * i + j];
+#pragma unroll
+    for (int j = 0; j < 5; ++j) {
+        x[j] = warp_sum_u64(x[j]);
+        if ((threadIdx.x & 31) == 0)
+            sh[j][threadIdx.x >> 5] = x[j];
+    }
+    __syncthreads();
+#pragma unroll
+    for (int j = 0; j < 5; ++j) {
+        unsigned long long t = 0;
+        for (int w = 0; w < AUX_THREADS / 32; ++w)
+            t += sh[j][w];
+        out[j] = t;
+    }
+}
+
+__device__ __forceinline__ void log_iteration(DevState& s, Ctrl* c, const unsigned long long (&cnt)[5])
+{
+    c->edges_scanned += cnt[CNT_EDGES];
+    c->tiles_scanned += cnt[CNT_TILES];
+    c->dsts_scanned += cnt[CNT_DSTS];
+    c->activated += cnt[CNT_ACT];
+    c->pull_launches += 1u;
+    if (c->iter < LOG_CAP) {
+        IterRec& r = s.log[c->iter];
+        r.mass_in = c->last_mass;
+        r.mass_out = cnt[CNT_MASS];
+        r.edges = cnt[CNT_EDGES];
+        r.tiles = cnt[CNT_TILES];
+        r.dsts = cnt[CNT_DSTS];
+        r.activated = cnt[CNT_ACT];
+        r.mode = c->mode;
+        r.iter = c->iter;
+    }
+    c->iter += 1u;
+}
+
+// After a pull: reduce the block counters, count the iteration, stop when no
+// edge was activated (execution_bfs.c:239-251) or at the cap, choose the next
+// pull (execution_bfs.c:141, execution_cc.c:103).
 __global__ void decide_kernel(DevState s, const unsigned long long* block_cnt, uint32_t nblocks, uint32_t app)
 {
-    __shared__ unsigned long long sh[3][AUX_THREADS / 32];
     Ctrl* c = s.ctrl;
     if (c->done)
         return;
-    unsigned long long m = 0, e = 0, t = 0;
-    for (uint32_t i = threadIdx.x; i < nblocks; i += blockDim.x) {
-        m += block_cnt[4u * i];
-        e += block_cnt[4u * i + 1u];
-        t += block_cnt[4u * i + 2u];
-    }
-    m = warp_sum_u64(m);
-    e = warp_sum_u64(e);
-    t = warp_sum_u64(t);
-    if ((threadIdx.x & 31) == 0) {
-        sh[0][threadIdx.x >> 5] = m;
-        sh[1][threadIdx.x >> 5] = e;
-        sh[2][threadIdx.x >> 5] = t;
-    }
-    __syncthreads();
+    unsigned long long cnt[5];
+    reduce_counters(block_cnt, nblocks, cnt);
     if (threadIdx.x == 0) {
-        m = e = t = 0;
-        for (int w = 0; w < AUX_THREADS / 32; ++w) {
-            m += sh[0][w];
-            e += sh[1][w];
-            t += sh[2][w];
-        }
-        c->edges_scanned += e;
-        c->tiles_scanned += t;
-        c->pull_launches += 1u;
+        const unsigned long long m = cnt[CNT_MASS];
         if (c->mode == MODE_WEDGE)
             c->wedge_iters += 1u;
-        c->iter += 1u;
+        log_iteration(s, c, cnt);
         c->last_mass = m;
         c->mass = m;
         if (app == WEDGE_APP_BFS)
@@ -786,6 +826,8 @@ __global__ void init_root_kernel(DevGraph g, DevState s, uint32_t app, uint64_t 
         c->mass = 0;
         c->edges_scanned = 0;
         c->tiles_scanned = 0;
+        c->dsts_scanned = 0;
+        c->activated = 0;
         c->threshold = thr;
         c->items = 0;
         c->tiles = 0;
@@ -839,7 +881,10 @@ __global__ void pr_init_kernel(DevGraph g, DevState s)
         c->wedge_iters = 0;
         c->edges_scanned = 0;
         c->tiles_scanned = 0;
+        c->dsts_scanned = 0;
+        c->activated = 0;
         c->pull_launches = 0;
+        c->last_mass = 0;
         c->done = 0;
         c->mode = MODE_DENSE;
         c->parity = 0;
@@ -864,21 +909,15 @@ __global__ void pr_finish_kernel(DevGraph g, DevState s, uint32_t nblocks, const
         x = warp_sum_f64(x);
         if (lane == 0)
             sh[threadIdx.x >> 5] = x;
-        __syncthreads();
+        unsigned long long cnt[5];
+        reduce_counters(block_cnt, nblocks, cnt); /* contains __syncthreads */
         if (threadIdx.x == 0) {
             double t = 0.0;
-            unsigned long long e = 0, tl = 0;
             for (int w = 0; w < AUX_THREADS / 32; ++w)
                 t = __dadd_rn(t, sh[w]);
-            for (uint32_t i = 0; i < nblocks; ++i) {
-                e += block_cnt[4u * i + 1u];
-                tl += block_cnt[4u * i + 2u];
-            }
             c->pr_total = t;
-            c->edges_scanned += e;
-            c->tiles_scanned += tl;
-            c->pull_launches += 1u;
-            c->iter += 1u;
+            c->last_mass = 0;
+            log_iteration(s, c, cnt);
         }
     }
     const uint32_t gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
@@ -1008,7 +1047,8 @@ static int ensure_state(wedge_graph* h, int app, int precision)
     Ctrl* ctrl;
     double* bp;
     // [grid] block sums | [4*grid] block counters | [aux grid] PageRank-sum partials
-    if ((rc = dalloc(h, &ctrl, 1, true)) || (rc = dalloc(h, &bp, grid * 5 + (uint64_t)h->num_sms * 8 + 8, true)))
+    if ((rc = dalloc(h, &ctrl, 1, true)) || (rc = dalloc(h, &bp, grid * (1 + NCNT) + (uint64_t)h->num_sms * 8 + 8, true)) ||
+        (rc = dalloc(h, &s.log, LOG_CAP, true)))
         return rc;
     WEDGE_CHECK(cudaMemset(ctrl, 0, sizeof(Ctrl)));
     s.ctrl = ctrl;
@@ -1187,6 +1227,10 @@ static int run_traversal(wedge_graph* h, int app, const wedge_params_t* p, wedge
             else
                 t_pull_wedge += a;
             t_wedge += b;
+            if (c.iter < LOG_CAP) {
+                h->iter_pull_ms[c.iter] = a;
+                h->iter_wedge_ms[c.iter] = b;
+            }
         }
     } else {
         // speculative batches: kernels are no-ops once Ctrl::done is set
@@ -1211,8 +1255,11 @@ static int run_traversal(wedge_graph* h, int app, const wedge_params_t* p, wedge
     float total = 0;
     cudaEventElapsedTime(&total, h->ev[0], h->ev[1]);
     h->last_app = app;
+    h->last_timing = timing;
     if (st) {
         memset(st, 0, sizeof(*st));
+        st->dsts_scanned = c.dsts_scanned;
+        st->vertices_activated = c.activated;
         st->iterations = c.iter;
         st->wedge_iterations = c.wedge_iters;
         st->running_ms = total;
@@ -1256,10 +1303,14 @@ static int run_pr(wedge_graph* h, const wedge_params_t* p, wedge_stats_t* st)
             cudaEventElapsedTime(&b, h->ev[3], h->ev[4]);
             t_pull += a;
             t_vertex += b;
+            if (it < LOG_CAP) {
+                h->iter_pull_ms[it] = a;
+                h->iter_wedge_ms[it] = 0.0;
+            }
         }
     }
     WEDGE_CHECK(cudaEventRecord(h->ev[1], h->stream));
-    double* sums = (double*)(counters(h) + 4ull * h->pull_grid);
+    double* sums = (double*)(counters(h) + (uint64_t)NCNT * h->pull_grid);
     pr_sum_kernel<<<vgrid, AUX_THREADS, 0, h->stream>>>(g, h->s, sums);
     pr_sum_final_kernel<<<1, 32, 0, h->stream>>>(h->s, sums, vgrid);
     WEDGE_CHECK(cudaGetLastError());
@@ -1270,8 +1321,10 @@ static int run_pr(wedge_graph* h, const wedge_params_t* p, wedge_stats_t* st)
     float total = 0;
     cudaEventElapsedTime(&total, h->ev[0], h->ev[1]);
     h->last_app = WEDGE_APP_PR;
+    h->last_timing = timing;
     if (st) {
         memset(st, 0, sizeof(*st));
+        st->dsts_scanned = c.dsts_scanned;
         st->iterations = p->num_iterations;
         st->running_ms = total;
         st->pull_ms_dense = t_pull;
@@ -1446,6 +1499,45 @@ int wedge_cuda_read_outdegrees(wedge_graph_t* g, uint64_t* host_outdeg, uint64_t
     cudaFreeAsync(tmp, g->stream);
     WEDGE_CHECK(e);
     WEDGE_CHECK(cudaStreamSynchronize(g->stream));
+    return WEDGE_OK;
+}
+
+int wedge_cuda_iteration_log(wedge_graph_t* g, wedge_iteration_record_t* out, uint64_t max_records, uint64_t* count)
+{
+    if (!g || !count || (max_records && !out) || g->last_app < 0 || !g->s.log)
+        return WEDGE_ERR_ARG;
+    WEDGE_CHECK(cudaSetDevice(g->device));
+    Ctrl c;
+    int rc = read_ctrl(g, &c);
+    if (rc)
+        return rc;
+    const uint64_t n = c.iter < LOG_CAP ? c.iter : LOG_CAP;
+    *count = n;
+    const uint64_t m = n < max_records ? n : max_records;
+    if (m == 0)
+        return WEDGE_OK;
+    IterRec* tmp = (IterRec*)malloc(m * sizeof(IterRec));
+    if (!tmp)
+        return WEDGE_ERR_OOM;
+    cudaError_t e = cudaMemcpy(tmp, g->s.log, m * sizeof(IterRec), cudaMemcpyDeviceToHost);
+    if (e != cudaSuccess) {
+        free(tmp);
+        return cuda_status(e);
+    }
+    for (uint64_t i = 0; i < m; ++i) {
+        wedge_iteration_record_t& r = out[i];
+        r.active_edges = tmp[i].mass_in;
+        r.used_wedge = tmp[i].mode == MODE_WEDGE ? 1u : 0u;
+        r.iteration = tmp[i].iter;
+        r.pull_ms = g->last_timing ? g->iter_pull_ms[i] : -1.0;
+        r.wedge_ms = g->last_timing ? g->iter_wedge_ms[i] : -1.0;
+        r.changed_mass = tmp[i].mass_out;
+        r.edges_scanned = tmp[i].edges;
+        r.tiles_scanned = tmp[i].tiles;
+        r.dsts_scanned = tmp[i].dsts;
+        r.vertices_activated = tmp[i].activated;
+    }
+    free(tmp);
     return WEDGE_OK;
 }
 

@@ -36,6 +36,24 @@ constexpr uint32_t FULL = 0xFFFFFFFFu;
 
 enum : uint32_t { MODE_DENSE = 0, MODE_WEDGE = 1 };
 
+// per-block counters written by the pulls (NCNT slots per block)
+constexpr uint32_t NCNT = 8;
+enum : uint32_t { CNT_MASS = 0, CNT_EDGES = 1, CNT_TILES = 2, CNT_DSTS = 3, CNT_ACT = 4 };
+constexpr uint32_t LOG_CAP = 4096;  // iterations kept in the per-iteration log
+
+// one iteration of the per-iteration log (the ITERATION_STATS record of
+// execution_bfs.c:227-232, plus device counters)
+struct IterRec {
+    unsigned long long mass_in;    // active edges that chose this iteration's pull
+    unsigned long long mass_out;   // changed-edge mass the pull produced
+    unsigned long long edges;      // in-edges read
+    unsigned long long tiles;      // tiles visited
+    unsigned long long dsts;       // destinations in visited tiles
+    unsigned long long activated;  // vertices activated
+    unsigned int mode;             // MODE_DENSE / MODE_WEDGE
+    unsigned int iter;
+};
+
 // Device control block of one traversal; read and written only by the
 // engine's kernels (the host reads it back for statistics).
 struct Ctrl {
@@ -44,6 +62,8 @@ struct Ctrl {
     unsigned long long edges_scanned;  // in-edges read by pulls
     unsigned long long tiles_scanned;  // tiles visited by pulls
     unsigned long long threshold;      // |E| * t% / 100 (execution_bfs.c:132)
+    unsigned long long dsts_scanned;   // destinations in visited tiles
+    unsigned long long activated;      // vertices activated by pulls
     unsigned int items;                // Wedge-build work items appended by the last pull
     unsigned int tiles;                // Wedge tile list length
     unsigned int mode;                 // MODE_DENSE / MODE_WEDGE for the next pull
@@ -98,6 +118,7 @@ struct DevState {
     uint32_t* tile_list;           // tiles holding at least one marked chunk
     uint2* items;                  // (vertex, piece) Wedge-build work items
     Ctrl* ctrl;
+    IterRec* log;                  // [LOG_CAP] per-iteration records
     double damping;
     uint32_t precision;
     uint32_t app;
@@ -126,6 +147,9 @@ struct wedge_graph {
     int nstate;
     unsigned long long* h_ctrl;        // pinned mirror of Ctrl (host reads)
     cudaEvent_t ev[8];
+    double* iter_pull_ms;              // [LOG_CAP] per-iteration times of a WEDGE_FLAG_TIMING run
+    double* iter_wedge_ms;
+    int last_timing;
     cudaGraphExec_t graph_exec;        // captured traversal
     int graph_app;
     int graph_key;

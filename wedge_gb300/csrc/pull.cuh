@@ -47,6 +47,7 @@ struct TileGeo {
     bool k0_fresh;       // k0 starts exactly at the tile start
     bool tail_cont;      // the tile's last destination continues into the next tile
     uint32_t nib_inner;  // nib without the lane-0 position-0 marker
+    uint32_t ndst;       // destinations with in-edges in this tile
 };
 
 // Destination ranks inside the tile: position p belongs to compressed
@@ -78,6 +79,7 @@ __device__ __forceinline__ void tile_geometry(const DevGraph& g, uint32_t t, uin
     tg.k0_fresh = g.dst_off[k0] == tg.base;
     const uint32_t k_last = k0 + c0 + c1 + c2 + c3;
     tg.tail_cont = (t + 1u < g.T) && (kend == k_last);
+    tg.ndst = k_last - k0 + 1u;
     const uint32_t wi = (uint32_t)lane >> 3, sh = ((uint32_t)lane & 7u) << 2;
     const uint32_t hw = wi == 0 ? h0 : wi == 1 ? h1 : wi == 2 ? h2 : h3;
     tg.before = (wi > 0 ? c0 : 0u) + (wi > 1 ? c1 : 0u) + (wi > 2 ? c2 : 0u) + __popc(hw & ((1u << sh) - 1u));

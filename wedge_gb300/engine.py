@@ -65,7 +65,18 @@ class Stats(C.Structure):
     _fields_ = [("iterations", C.c_uint64), ("wedge_iterations", C.c_uint64), ("running_ms", C.c_double),
                 ("pull_ms_dense", C.c_double), ("pull_ms_wedge", C.c_double), ("wedge_ms", C.c_double),
                 ("vertex_ms", C.c_double), ("edges_scanned", C.c_uint64), ("tiles_scanned", C.c_uint64),
+                ("dsts_scanned", C.c_uint64), ("vertices_activated", C.c_uint64),
                 ("pull_launches", C.c_uint64), ("kernel_launches", C.c_uint64), ("pr_sum", C.c_double)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+class IterationRecord(C.Structure):
+    _fields_ = [("active_edges", C.c_uint64), ("used_wedge", C.c_uint32), ("iteration", C.c_uint32),
+                ("pull_ms", C.c_double), ("wedge_ms", C.c_double), ("changed_mass", C.c_uint64),
+                ("edges_scanned", C.c_uint64), ("tiles_scanned", C.c_uint64), ("dsts_scanned", C.c_uint64),
+                ("vertices_activated", C.c_uint64)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}
@@ -94,6 +105,7 @@ _SIGNATURES = {
     "wedge_cuda_run": (C.c_int, [C.c_void_p, C.c_int, C.POINTER(Params), C.POINTER(Stats)]),
     "wedge_cuda_run_phase": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.POINTER(Params), C.POINTER(C.c_uint64)]),
     "wedge_cuda_read_results": (C.c_int, [C.c_void_p, C.c_void_p, C.c_uint64]),
+    "wedge_cuda_iteration_log": (C.c_int, [C.c_void_p, C.c_void_p, C.c_uint64, C.POINTER(C.c_uint64)]),
     "wedge_cuda_read_outdegrees": (C.c_int, [C.c_void_p, C.c_void_p, C.c_uint64]),
     "wedge_cuda_num_vertices": (C.c_uint64, [C.c_void_p]),
     "wedge_cuda_num_edges": (C.c_uint64, [C.c_void_p]),
@@ -227,6 +239,15 @@ class Graph:
             out = np.empty(V, np.uint64)
         _check(lib().wedge_cuda_read_results(self._h, _ptr(out), out.nbytes), "wedge_cuda_read_results")
         return out
+
+    def iteration_log(self) -> list[dict]:
+        """per-iteration records of the last run (the reference's ITERATION_STATS rows)"""
+        n = C.c_uint64()
+        _check(lib().wedge_cuda_iteration_log(self._h, None, 0, C.byref(n)), "wedge_cuda_iteration_log")
+        recs = (IterationRecord * max(1, n.value))()
+        _check(lib().wedge_cuda_iteration_log(self._h, C.cast(recs, C.c_void_p), n.value, C.byref(n)),
+               "wedge_cuda_iteration_log")
+        return [recs[i].as_dict() for i in range(n.value)]
 
     def read_outdegrees(self) -> np.ndarray:
         out = np.empty(self.V, np.uint64)
