@@ -118,7 +118,7 @@ class ClockSampler:
         sm = sorted(float(r[1]) for r in rows if r[1].strip().replace(".", "").isdigit())
         mx = [float(r[2]) for r in rows if r[2].strip().replace(".", "").isdigit()]
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        reasons = sorted({names[j] for r in rows for j in range(4) if "Active" in r[5 + j]})
+        reasons = sorted({names[j] for r in rows for j in range(4) if r[5 + j].strip() == "Active"})
         return {"sm_mhz": sm[len(sm) // 2] if sm else None, "sm_max_mhz": max(mx) if mx else None,
                 "reasons": reasons, "samples": len(rows),
                 "power_w_max": max((float(r[3]) for r in rows if r[3].strip().replace(".", "").isdigit()),

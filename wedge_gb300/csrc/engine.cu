@@ -367,14 +367,130 @@ __device__ __forceinline__ uint32_t* next_front(const DevState& s, uint32_t app,
     return (app == WEDGE_APP_BFS) ? (parity ? s.front0 : s.front1) : s.front0;
 }
 
+// One tile's inputs, loaded one tile ahead of its processing so their latency
+// overlaps the previous tile's gathers, reduction and emission.
+struct TileIn {
+    uint32_t t, cmask, k0, kend, visw;
+    bool open;
+    uint4 src;
+};
+
+template <int APP>
+__device__ __forceinline__ void tile_prefetch(const DevGraph& g, const DevState& s, uint32_t t, uint32_t cmask, int lane,
+                                              TileIn& in)
+{
+    in.t = t;
+    in.cmask = cmask;
+    in.k0 = g.tile_dst0[t];
+    in.kend = g.tile_dst0[t + 1];
+    in.open = true;
+    in.visw = 0u;
+    if (APP == WEDGE_APP_BFS) {
+        // skip a tile whose destinations are all visited (the reference's jump over
+        // converged vertices, phase_edge_pull_bfs.c:189-204)
+        const uint32_t klim = min(in.kend, g.Vne - 1u);
+        const uint32_t w0 = in.k0 >> 5, w1 = klim >> 5;
+        bool open = false;
+        if ((uint32_t)lane <= w1 - w0) {
+            const uint32_t wi = w0 + lane;
+            const uint32_t lo = (wi == w0) ? (in.k0 & 31u) : 0u;
+            const uint32_t hi = (wi == w1) ? (klim & 31u) : 31u;
+            const uint32_t range = (hi == 31u ? FULL : ((2u << hi) - 1u)) & ~((1u << lo) - 1u);
+            in.visw = s.vis_c[wi];
+            open = (~in.visw & range) != 0u;
+        }
+        in.open = __any_sync(FULL, open);
+    }
+    const bool on = in.open && ((cmask >> (lane >> 3)) & 1u);
+    in.src = on ? ld_stream_v4(g.src + (uint64_t)t * TILE + 4u * (uint32_t)lane)
+                : make_uint4(NONE32, NONE32, NONE32, NONE32);
+}
+
+// The tiles a warp pulls: every tile (dense, static stride), or the tiles of
+// the Wedge frontier, found by walking the chunk bitmap one region
+// (REGION_WORDS words = 256 tiles) at a time, regions handed out dynamically;
+// a region whose summary bit is clear is skipped without reading its words
+// (the reference's 256-bit emptiness test, phase_edge_pull_bfs.c:244-246).
+// Walked words are cleared: the pull consumes the frontier
+// (phase_edge_pull_bfs.c:256).  Warp-uniform.
+struct TileIter {
+    uint32_t i, step;      // dense
+    uint32_t region;       // wedge: region being walked (NONE32 before the first)
+    uint32_t myword;       // this lane's chunk word of the region
+    uint32_t lanes;        // lanes whose words are still to be walked
+    uint32_t word, wlane;  // the word being walked and its lane
+};
+
+__device__ __forceinline__ bool next_tile(const DevGraph& g, const DevState& s, uint32_t mode, TileIter& it, int lane,
+                                          uint32_t& t, uint32_t& cmask)
+{
+    if (mode == MODE_DENSE) {
+        if (it.i >= g.T)
+            return false;
+        t = it.i;
+        cmask = 0xFu;
+        it.i += it.step;
+        return true;
+    }
+    const uint32_t nwords = (g.T + TILES_PER_WORD - 1) / TILES_PER_WORD;
+    const uint32_t nregions = (g.T + TILES_PER_REGION - 1) / TILES_PER_REGION;
+    for (;;) {
+        if (it.word) {
+            const uint32_t j = (uint32_t)(__ffs(it.word) - 1) >> 2;
+            cmask = (it.word >> (4u * j)) & 0xFu;
+            it.word &= ~(0xFu << (4u * j));
+            t = (it.region * REGION_WORDS + it.wlane) * TILES_PER_WORD + j;
+            return true;
+        }
+        if (it.lanes) {
+            it.wlane = (uint32_t)(__ffs(it.lanes) - 1);
+            it.lanes &= it.lanes - 1u;
+            it.word = __shfl_sync(FULL, it.myword, (int)it.wlane);
+            continue;
+        }
+        if (it.region != NONE32 && it.myword)
+            s.chunk_bits[it.region * REGION_WORDS + (uint32_t)lane] = 0u;
+        uint32_t r = 0;
+        if (lane == 0)
+            r = atomicAdd(&s.ctrl->region_next, 1u);
+        r = __shfl_sync(FULL, r, 0);
+        if (r >= nregions) {
+            it.region = NONE32;
+            it.myword = 0u;
+            return false;
+        }
+        it.region = r;
+        it.myword = 0u;
+        it.lanes = 0u;
+        if ((s.summary[r >> 5] >> (r & 31u)) & 1u) {
+            const uint32_t wi = r * REGION_WORDS + (uint32_t)lane;
+            it.myword = wi < nwords ? s.chunk_bits[wi] : 0u;
+            it.lanes = __ballot_sync(FULL, it.myword != 0u);
+        }
+    }
+}
+
+template <int APP>
+struct CurT {
+    using type = uint32_t;
+};
+template <>
+struct CurT<WEDGE_APP_SSSP> {
+    using type = unsigned long long;
+};
+
 // Edge pull over all tiles (dense) or over the tiles of the Wedge frontier.
 // block_cnt[NCNT*b + CNT_*] = changed mass, in-edges read, tiles visited,
 // destinations in visited tiles, vertices activated.
 template <int APP>
 __global__ void __launch_bounds__(PULL_THREADS) pull_kernel(DevGraph g, DevState s, unsigned long long* block_cnt)
 {
-    __shared__ unsigned long long sh_cnt[PULL_THREADS / 32][5];
-    __shared__ double sh_sum[PULL_THREADS / 32];
+    constexpr int WARPS = PULL_THREADS / 32;
+    using cur_t = typename CurT<APP>::type;
+    __shared__ unsigned long long sh_cnt[WARPS][5];
+    __shared__ double sh_sum[WARPS];
+    __shared__ uint32_t tab_id[WARPS][TILE + 1];  // vertex id of each destination of the warp's tile
+    __shared__ cur_t tab_cur[WARPS][TILE + 1];    // its property before the tile (min apps)
     Ctrl* c = s.ctrl;
     if (c->done)
         return;
@@ -383,68 +499,61 @@ __global__ void __launch_bounds__(PULL_THREADS) pull_kernel(DevGraph g, DevState
     const uint32_t gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const uint32_t nw = (gridDim.x * blockDim.x) >> 5;
     const uint32_t mode = c->mode;
-    const uint32_t ntiles = (mode == MODE_DENSE) ? g.T : c->tiles;
     const uint32_t parity = c->parity;
     const uint32_t* cur = cur_front(s, parity);
     uint32_t* nxt = next_front(s, APP, parity);
+    uint32_t* my_id = tab_id[wib];
+    cur_t* my_cur = tab_cur[wib];
     unsigned long long mass = 0, edges = 0, tiles = 0, dsts = 0, act = 0;
     double psum = 0.0;
 
-    for (uint32_t i = gw; i < ntiles; i += nw) {
-        uint32_t t = i, cmask = 0xFu;
-        if (mode != MODE_DENSE) {
-            t = s.tile_list[i];
-            if (lane == 0) {
-                const uint32_t sh = (t & 7u) * 4u;
-                cmask = (s.chunk_bits[t >> 3] >> sh) & 0xFu;
-                atomicAnd(&s.chunk_bits[t >> 3], ~(0xFu << sh)); /* consume (phase_edge_pull_bfs.c:256) */
-            }
-            cmask = __shfl_sync(FULL, cmask, 0);
-        }
+    TileIter it;
+    it.i = gw;
+    it.step = nw;
+    it.region = NONE32;
+    it.myword = it.lanes = it.word = it.wlane = 0u;
+    TileIn nextin;
+    uint32_t tn, cn;
+    bool more = next_tile(g, s, mode, it, lane, tn, cn);
+    if (more)
+        tile_prefetch<APP>(g, s, tn, cn, lane, nextin);
+    while (more) {
+        const TileIn in = nextin;
+        more = next_tile(g, s, mode, it, lane, tn, cn);
+        if (more)
+            tile_prefetch<APP>(g, s, tn, cn, lane, nextin);
         ++tiles;
-        const uint32_t k0 = g.tile_dst0[t];
-        const uint32_t kend = g.tile_dst0[t + 1];
-        if (APP == WEDGE_APP_BFS) {
-            // skip a tile whose destinations are all visited (the reference's jump over
-            // converged vertices, phase_edge_pull_bfs.c:189-204)
-            const uint32_t klim = min(kend, g.Vne - 1u);
-            const uint32_t w0 = k0 >> 5, w1 = klim >> 5;
-            bool open = false;
-            if ((uint32_t)lane <= w1 - w0) {
-                const uint32_t wi = w0 + lane;
-                const uint32_t lo = (wi == w0) ? (k0 & 31u) : 0u;
-                const uint32_t hi = (wi == w1) ? (klim & 31u) : 31u;
-                const uint32_t range = (hi == 31u ? FULL : ((2u << hi) - 1u)) & ~((1u << lo) - 1u);
-                open = (~s.vis_c[wi] & range) != 0u;
-            }
-            if (!__any_sync(FULL, open))
-                continue;
-        }
-        TileGeo tg;
-        tile_geometry(g, t, k0, kend, lane, tg);
-        dsts += tg.ndst;
-        const bool on = (cmask >> (lane >> 3)) & 1u;
-        uint4 sv = make_uint4(NONE32, NONE32, NONE32, NONE32);
-        if (on)
-            sv = ld_stream_v4(g.src + tg.base + 4u * (uint32_t)lane);
-        const uint32_t sa[4] = {sv.x, sv.y, sv.z, sv.w};
+        if (!in.open)
+            continue;
+        const uint32_t t = in.t;
+        const uint32_t sa[4] = {in.src.x, in.src.y, in.src.z, in.src.w};
+#pragma unroll
+        for (int q = 0; q < 4; ++q)
+            edges += (sa[q] != NONE32) ? 1u : 0u;
 
         if (APP == WEDGE_APP_BFS) {
+            // frontier-bit gathers first, then the geometry (their latencies overlap)
+            uint32_t fb[4];
+#pragma unroll
+            for (int q = 0; q < 4; ++q)
+                fb[q] = (sa[q] != NONE32) ? ld_ro_u32(cur + (sa[q] >> 5)) : 0u;
+            TileGeo tg;
+            tile_geometry(g, t, in.k0, in.kend, lane, tg,
+                          [&](uint32_t slot, uint32_t k) { my_id[slot] = g.dst_id[k]; });
+            dsts += tg.ndst;
             uint32_t v[4];
+            const uint32_t w0 = in.k0 >> 5;
 #pragma unroll
             for (int q = 0; q < 4; ++q) {
-                v[q] = NONE32;
-                if (sa[q] != NONE32) {
-                    ++edges;
-                    const uint32_t k = pos_dst(tg, q);
-                    if (!test_bit32(s.vis_c, k) && test_bit32(cur, sa[q]))
-                        v[q] = sa[q];
-                }
+                const uint32_t k = pos_dst(tg, q);
+                const uint32_t vw = __shfl_sync(FULL, in.visw, (int)((k >> 5) - w0));
+                const bool visited = (vw >> (k & 31u)) & 1u;
+                v[q] = (sa[q] != NONE32 && !visited && ((fb[q] >> (sa[q] & 31u)) & 1u)) ? sa[q] : NONE32;
             }
             seg_reduce(v, tg, lane, MinU32(), [&](uint32_t k, uint32_t val, int) {
                 if (val == NONE32)
                     return;
-                const uint32_t vtx = g.dst_id[k];
+                const uint32_t vtx = my_id[k - tg.k0];
                 const uint32_t old = atomicMin(&s.prop32[vtx], val);
                 if (old == NONE32) {
                     atomicOr(&s.vis_c[k >> 5], 1u << (k & 31u));
@@ -456,16 +565,19 @@ __global__ void __launch_bounds__(PULL_THREADS) pull_kernel(DevGraph g, DevState
         } else if (APP == WEDGE_APP_CC) {
             uint32_t v[4];
 #pragma unroll
-            for (int q = 0; q < 4; ++q) {
-                v[q] = NONE32;
-                if (sa[q] != NONE32) {
-                    ++edges;
-                    v[q] = s.prop32[sa[q]];
-                }
-            }
-            seg_reduce(v, tg, lane, MinU32(), [&](uint32_t k, uint32_t val, int) {
+            for (int q = 0; q < 4; ++q)
+                v[q] = (sa[q] != NONE32) ? s.prop32[sa[q]] : NONE32;
+            TileGeo tg;
+            tile_geometry(g, t, in.k0, in.kend, lane, tg, [&](uint32_t slot, uint32_t k) {
                 const uint32_t vtx = g.dst_id[k];
-                if (val < s.prop32[vtx]) {
+                my_id[slot] = vtx;
+                my_cur[slot] = s.prop32[vtx];
+            });
+            dsts += tg.ndst;
+            seg_reduce(v, tg, lane, MinU32(), [&](uint32_t k, uint32_t val, int) {
+                const uint32_t slot = k - tg.k0;
+                if (val < (uint32_t)my_cur[slot]) {
+                    const uint32_t vtx = my_id[slot];
                     const uint32_t old = atomicMin(&s.prop32[vtx], val);
                     if (val < old) {
                         const uint32_t b = 1u << (vtx & 31u);
@@ -478,31 +590,42 @@ __global__ void __launch_bounds__(PULL_THREADS) pull_kernel(DevGraph g, DevState
             });
         } else if (APP == WEDGE_APP_SSSP) {
             unsigned long long wv[4] = {0, 0, 0, 0};
-            if (on) {
-                const ulonglong2 a = ld_stream_v2u64(g.w + tg.base + 4u * (uint32_t)lane);
-                const ulonglong2 b = ld_stream_v2u64(g.w + tg.base + 4u * (uint32_t)lane + 2u);
+            const uint64_t base = (uint64_t)t * TILE + 4u * (uint32_t)lane;
+            if (sa[0] != NONE32 || sa[3] != NONE32 || sa[1] != NONE32 || sa[2] != NONE32) {
+                const ulonglong2 a = ld_stream_v2u64(g.w + base);
+                const ulonglong2 b = ld_stream_v2u64(g.w + base + 2u);
                 wv[0] = a.x;
                 wv[1] = a.y;
                 wv[2] = b.x;
                 wv[3] = b.y;
             }
+            unsigned long long dv[4];
+#pragma unroll
+            for (int q = 0; q < 4; ++q)
+                dv[q] = (sa[q] != NONE32) ? s.prop64[sa[q]] : NONE64;
+            TileGeo tg;
+            tile_geometry(g, t, in.k0, in.kend, lane, tg, [&](uint32_t slot, uint32_t k) {
+                const uint32_t vtx = g.dst_id[k];
+                my_id[slot] = vtx;
+                my_cur[slot] = s.prop64[vtx];
+            });
+            dsts += tg.ndst;
             unsigned long long v[4];
 #pragma unroll
             for (int q = 0; q < 4; ++q) {
                 v[q] = NONE64;
                 if (sa[q] != NONE32) {
-                    ++edges;
-                    const unsigned long long d = s.prop64[sa[q]];
                     if (g.weight_kind == WEDGE_WEIGHTS_F64)
                         v[q] = (unsigned long long)__double_as_longlong(
-                            __dadd_rn(__longlong_as_double((long long)d), __longlong_as_double((long long)wv[q])));
+                            __dadd_rn(__longlong_as_double((long long)dv[q]), __longlong_as_double((long long)wv[q])));
                     else
-                        v[q] = (d == NONE64) ? NONE64 : d + wv[q]; /* phase_edge_pull_sssp.c:136-137 */
+                        v[q] = (dv[q] == NONE64) ? NONE64 : dv[q] + wv[q]; /* phase_edge_pull_sssp.c:136-137 */
                 }
             }
             seg_reduce(v, tg, lane, MinU64(), [&](uint32_t k, unsigned long long val, int) {
-                const uint32_t vtx = g.dst_id[k];
-                if (val < s.prop64[vtx]) {
+                const uint32_t slot = k - tg.k0;
+                if (val < (unsigned long long)my_cur[slot]) {
+                    const uint32_t vtx = my_id[slot];
                     const unsigned long long old = atomicMin(&s.prop64[vtx], val);
                     if (val < old) {
                         const uint32_t b = 1u << (vtx & 31u);
@@ -517,19 +640,18 @@ __global__ void __launch_bounds__(PULL_THREADS) pull_kernel(DevGraph g, DevState
             if (s.precision == WEDGE_PREC_FP32C) {
                 F2 v[4];
 #pragma unroll
-                for (int q = 0; q < 4; ++q) {
-                    v[q] = F2{0.0f, 0.0f};
-                    if (sa[q] != NONE32) {
-                        ++edges;
-                        v[q].s = s.rank32[sa[q]];
-                    }
-                }
+                for (int q = 0; q < 4; ++q)
+                    v[q] = F2{(sa[q] != NONE32) ? ld_ro_f32(s.rank32 + sa[q]) : 0.0f, 0.0f};
+                TileGeo tg;
+                tile_geometry(g, t, in.k0, in.kend, lane, tg,
+                              [&](uint32_t slot, uint32_t k) { my_id[slot] = g.dst_id[k]; });
+                dsts += tg.ndst;
                 const AddF2 add;
                 const F2 ls = add(add(v[0], v[1]), add(v[2], v[3]));
                 psum = __dadd_rn(psum, warp_sum_f64(__dadd_rn((double)ls.s, (double)ls.c)));
                 seg_reduce(v, tg, lane, add, [&](uint32_t k, F2 val, int kind) {
                     if (kind == EMIT_COMPLETE) {
-                        s.acc[g.dst_id[k]] = __dadd_rn((double)val.s, (double)val.c);
+                        s.acc[my_id[k - tg.k0]] = __dadd_rn((double)val.s, (double)val.c);
                     } else {
                         float* p = (kind == EMIT_HEAD) ? s.head_part32 : s.tail_part32;
                         p[2u * t] = val.s;
@@ -539,17 +661,16 @@ __global__ void __launch_bounds__(PULL_THREADS) pull_kernel(DevGraph g, DevState
             } else {
                 double v[4];
 #pragma unroll
-                for (int q = 0; q < 4; ++q) {
-                    v[q] = 0.0;
-                    if (sa[q] != NONE32) {
-                        ++edges;
-                        v[q] = s.rank[sa[q]];
-                    }
-                }
+                for (int q = 0; q < 4; ++q)
+                    v[q] = (sa[q] != NONE32) ? ld_ro_f64(s.rank + sa[q]) : 0.0;
+                TileGeo tg;
+                tile_geometry(g, t, in.k0, in.kend, lane, tg,
+                              [&](uint32_t slot, uint32_t k) { my_id[slot] = g.dst_id[k]; });
+                dsts += tg.ndst;
                 psum = __dadd_rn(psum, warp_sum_f64(__dadd_rn(__dadd_rn(v[0], v[1]), __dadd_rn(v[2], v[3]))));
                 seg_reduce(v, tg, lane, AddF64(), [&](uint32_t k, double val, int kind) {
                     if (kind == EMIT_COMPLETE)
-                        s.acc[g.dst_id[k]] = val;
+                        s.acc[my_id[k - tg.k0]] = val;
                     else if (kind == EMIT_HEAD)
                         s.head_part[t] = val;
                     else
@@ -557,6 +678,7 @@ __global__ void __launch_bounds__(PULL_THREADS) pull_kernel(DevGraph g, DevState
                 });
             }
         }
+        __syncwarp(); /* the table is rewritten by the next tile */
     }
     // per-block counters (no same-address atomics): reduced by decide_kernel
     mass = warp_sum_u64(mass);
@@ -573,13 +695,13 @@ __global__ void __launch_bounds__(PULL_THREADS) pull_kernel(DevGraph g, DevState
     __syncthreads();
     if (threadIdx.x < 5) {
         unsigned long long a = 0;
-        for (int w = 0; w < PULL_THREADS / 32; ++w)
+        for (int w = 0; w < WARPS; ++w)
             a += sh_cnt[w][threadIdx.x];
         block_cnt[NCNT * blockIdx.x + threadIdx.x] = a;
     }
     if (APP == WEDGE_APP_PR && threadIdx.x == 0) {
         double ps = 0.0;
-        for (int w = 0; w < PULL_THREADS / 32; ++w)
+        for (int w = 0; w < WARPS; ++w)
             ps = __dadd_rn(ps, sh_sum[w]);
         s.block_part[blockIdx.x] = ps;
     }
@@ -646,11 +768,14 @@ __device__ __forceinline__ void log_iteration(DevState& s, Ctrl* c, const unsign
 // After a pull: reduce the block counters, count the iteration, stop when no
 // edge was activated (execution_bfs.c:239-251) or at the cap, choose the next
 // pull (execution_bfs.c:141, execution_cc.c:103).
-__global__ void decide_kernel(DevState s, const unsigned long long* block_cnt, uint32_t nblocks, uint32_t app)
+__global__ void decide_kernel(DevGraph g, DevState s, const unsigned long long* block_cnt, uint32_t nblocks, uint32_t app)
 {
     Ctrl* c = s.ctrl;
     if (c->done)
         return;
+    const uint32_t nsum = ((g.T + TILES_PER_REGION - 1) / TILES_PER_REGION + 31) / 32;
+    for (uint32_t i = threadIdx.x; i < nsum; i += blockDim.x)
+        s.summary[i] = 0u; /* the pull has cleared every chunk word it walked */
     unsigned long long cnt[5];
     reduce_counters(block_cnt, nblocks, cnt);
     if (threadIdx.x == 0) {
@@ -662,7 +787,7 @@ __global__ void decide_kernel(DevState s, const unsigned long long* block_cnt, u
         c->mass = m;
         if (app == WEDGE_APP_BFS)
             c->parity ^= 1u;
-        c->tiles = 0u;
+        c->region_next = 0u;
         c->items = 0u;
         if (m == 0ull) {
             c->done = 1u;
@@ -677,11 +802,32 @@ __global__ void decide_kernel(DevState s, const unsigned long long* block_cnt, u
     }
 }
 
-// Walk the vertices activated by the last pull (the reference walks
-// graph_frontier_active_vertices, wedge.c:86-153) and emit one work item per
-// PIECE of each vertex's CSRI list; warp-aggregated with a shuffle scan.
+// set the Wedge-frontier bit of chunk ch (wedge.c:22-31) and the summary bit
+// of its region when the chunk word was empty
+__device__ __forceinline__ void mark_chunk(const DevState& s, uint32_t ch, bool valid)
+{
+    if (!valid)
+        return;
+    const uint32_t word = ch >> 5, bit = 1u << (ch & 31u);
+    if (!(s.chunk_bits[word] & bit)) {
+        const uint32_t old = atomicOr(&s.chunk_bits[word], bit);
+        if (old == 0u) {
+            const uint32_t r = word / REGION_WORDS;
+            atomicOr(&s.summary[r >> 5], 1u << (r & 31u));
+        }
+    }
+}
+
+// Wedge frontier generation (wedge.c:63-155): walk the bitmap of vertices the
+// last pull activated and set the chunk bit of each of their out-edges
+// (wedge.c:37-46).  Each warp takes 32 bitmap words; per word, the lanes take
+// the set bits' vertices and expand their CSRI lists cooperatively (shuffle
+// scan of the list lengths, then every lane finds the list that owns each of
+// 32 consecutive entries).  Vertices with more than BIG out-edges are handed to
+// wedge_build_kernel as PIECE-sized work items instead.
 __global__ void collect_kernel(DevGraph g, DevState s, uint32_t app)
 {
+    constexpr unsigned long long BIG = 2048;
     Ctrl* c = s.ctrl;
     if (c->done || c->mode != MODE_WEDGE)
         return;
@@ -691,41 +837,56 @@ __global__ void collect_kernel(DevGraph g, DevState s, uint32_t app)
     const uint64_t gw = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) >> 5;
     const uint64_t nw = ((uint64_t)gridDim.x * blockDim.x) >> 5;
     for (uint64_t base = gw * 32; base < nwords; base += nw * 32) {
-        const uint64_t wi = base + lane;
-        const uint32_t bits = wi < nwords ? fb[wi] : 0u;
-        uint32_t cnt = 0;
-        for (uint32_t b = bits; b; b &= b - 1u) {
-            const uint64_t v = wi * 32 + (uint32_t)(__ffs(b) - 1);
-            const unsigned long long len = g.csri_off[v + 1] - g.csri_off[v];
-            cnt += (uint32_t)((len + PIECE - 1) / PIECE);
-        }
-        uint32_t incl = cnt;
+        const uint32_t myword = (base + lane < nwords) ? fb[base + lane] : 0u;
+        uint32_t nonzero = __ballot_sync(FULL, myword != 0u);
+        while (nonzero) {
+            const int w = __ffs(nonzero) - 1;
+            nonzero &= nonzero - 1u;
+            const uint32_t bits = __shfl_sync(FULL, myword, w);
+            const uint64_t v = (base + (uint64_t)w) * 32 + (uint64_t)lane;
+            unsigned long long start = 0, len = 0;
+            if ((bits >> lane) & 1u) {
+                start = g.csri_off[v];
+                len = g.csri_off[v + 1] - start;
+                if (len > BIG) { /* hub: split into work items */
+                    const uint32_t np = (uint32_t)((len + PIECE - 1) / PIECE);
+                    const uint32_t pos = atomicAdd(&c->items, np);
+                    for (uint32_t q = 0; q < np; ++q)
+                        s.items[pos + q] = make_uint2((uint32_t)v, q);
+                    len = 0;
+                }
+            }
+            unsigned long long incl = len;
 #pragma unroll
-        for (int d = 1; d < 32; d <<= 1) {
-            const uint32_t y = __shfl_up_sync(FULL, incl, d);
-            if (lane >= d)
-                incl += y;
-        }
-        const uint32_t total = __shfl_sync(FULL, incl, 31);
-        if (total == 0)
-            continue;
-        uint32_t pos = 0;
-        if (lane == 31)
-            pos = atomicAdd(&c->items, total);
-        pos = __shfl_sync(FULL, pos, 31) + incl - cnt;
-        for (uint32_t b = bits; b; b &= b - 1u) {
-            const uint64_t v = wi * 32 + (uint32_t)(__ffs(b) - 1);
-            const unsigned long long len = g.csri_off[v + 1] - g.csri_off[v];
-            const uint32_t np = (uint32_t)((len + PIECE - 1) / PIECE);
-            for (uint32_t p = 0; p < np; ++p)
-                s.items[pos++] = make_uint2((uint32_t)v, p);
+            for (int d = 1; d < 32; d <<= 1) {
+                const unsigned long long y = __shfl_up_sync(FULL, incl, d);
+                if (lane >= d)
+                    incl += y;
+            }
+            const unsigned long long total = __shfl_sync(FULL, incl, 31);
+            const unsigned long long excl = incl - len;
+            for (unsigned long long j0 = 0; j0 < total; j0 += 32) {
+                const unsigned long long j = j0 + (unsigned long long)lane;
+                // owner = number of lanes whose inclusive end is <= j
+                int owner = 0;
+#pragma unroll
+                for (int step = 16; step > 0; step >>= 1) {
+                    const unsigned long long e = __shfl_sync(FULL, incl, owner + step - 1);
+                    if (e <= j)
+                        owner += step;
+                }
+                const unsigned long long ost = __shfl_sync(FULL, start, owner & 31);
+                const unsigned long long oex = __shfl_sync(FULL, excl, owner & 31);
+                const bool valid = j < total;
+                const uint32_t ch = valid ? g.csri[ost + (j - oex)] : 0u;
+                mark_chunk(s, ch, valid);
+            }
         }
     }
 }
 
-// Set the Wedge frontier bit of every chunk holding an out-edge of an active
-// vertex (wedge.c:37-46); the first bit set in a tile appends the tile to the
-// tile list (ballot + popc aggregated).
+// Wedge frontier bits of the out-edges of hub vertices, one PIECE of a CSRI
+// list per warp (wedge.c:37-46).
 __global__ void wedge_build_kernel(DevGraph g, DevState s)
 {
     Ctrl* c = s.ctrl;
@@ -735,7 +896,6 @@ __global__ void wedge_build_kernel(DevGraph g, DevState s)
     const uint32_t gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const uint32_t nw = (gridDim.x * blockDim.x) >> 5;
     const uint32_t n = c->items;
-    const uint32_t lt = (1u << lane) - 1u;
     for (uint32_t i = gw; i < n; i += nw) {
         const uint2 it = s.items[i];
         const unsigned long long lo = g.csri_off[it.x] + (unsigned long long)it.y * PIECE;
@@ -743,27 +903,8 @@ __global__ void wedge_build_kernel(DevGraph g, DevState s)
         const unsigned long long hi = (lo + PIECE < end) ? lo + PIECE : end;
         for (unsigned long long j0 = lo; j0 < hi; j0 += 32) {
             const unsigned long long j = j0 + lane;
-            bool add = false;
-            uint32_t tile = 0;
-            if (j < hi) {
-                const uint32_t ch = g.csri[j];
-                const uint32_t word = ch >> 5, bit = 1u << (ch & 31u);
-                if (!(s.chunk_bits[word] & bit)) {
-                    const uint32_t old = atomicOr(&s.chunk_bits[word], bit);
-                    add = ((old >> (ch & 28u)) & 0xFu) == 0u;
-                    tile = ch >> 2;
-                }
-            }
-            const uint32_t m = __ballot_sync(FULL, add);
-            if (m) {
-                const int leader = __ffs(m) - 1;
-                uint32_t b0 = 0;
-                if (lane == leader)
-                    b0 = atomicAdd(&c->tiles, (uint32_t)__popc(m));
-                b0 = __shfl_sync(FULL, b0, leader);
-                if (add)
-                    s.tile_list[b0 + __popc(m & lt)] = tile;
-            }
+            const bool valid = j < hi;
+            mark_chunk(s, valid ? g.csri[j] : 0u, valid);
         }
     }
 }
@@ -803,6 +944,9 @@ __global__ void init_kernel(DevGraph g, DevState s, uint32_t app)
     const uint64_t cwords = ((uint64_t)g.T + 7) / 8;
     for (uint64_t i = tid; i < cwords; i += stride)
         s.chunk_bits[i] = 0u;
+    const uint64_t swords = ((uint64_t)g.T / TILES_PER_REGION + 32) / 32;
+    for (uint64_t i = tid; i < swords; i += stride)
+        s.summary[i] = 0u;
     if (s.vis_c) {
         const uint64_t vwords = ((uint64_t)g.Vne + 31) / 32;
         for (uint64_t i = tid; i < vwords; i += stride)
@@ -830,7 +974,7 @@ __global__ void init_root_kernel(DevGraph g, DevState s, uint32_t app, uint64_t 
         c->activated = 0;
         c->threshold = thr;
         c->items = 0;
-        c->tiles = 0;
+        c->region_next = 0;
         c->iter = 0;
         c->wedge_iters = 0;
         c->done = 0;
@@ -888,7 +1032,7 @@ __global__ void pr_init_kernel(DevGraph g, DevState s)
         c->done = 0;
         c->mode = MODE_DENSE;
         c->parity = 0;
-        c->tiles = 0;
+        c->region_next = 0;
         c->pr_total = 0.0;
         c->pr_sum = 0.0;
     }
@@ -1073,8 +1217,9 @@ static int ensure_state(wedge_graph* h, int app, int precision)
         } else if ((rc = dalloc(h, &s.prop32, V, true))) {
             return rc;
         }
-        if ((rc = dalloc(h, &s.front0, nwords, true)) || (rc = dalloc(h, &s.chunk_bits, (uint64_t)g.T / 8 + 2, true)) ||
-            (rc = dalloc(h, &s.tile_list, (uint64_t)g.T + 1, true)) ||
+        if ((rc = dalloc(h, &s.front0, nwords, true)) ||
+            (rc = dalloc(h, &s.chunk_bits, (uint64_t)g.T / TILES_PER_WORD + REGION_WORDS + 2, true)) ||
+            (rc = dalloc(h, &s.summary, (uint64_t)g.T / TILES_PER_REGION / 32 + 2, true)) ||
             (rc = dalloc(h, &s.items, V + g.E / PIECE + 2, true)))
             return rc;
         if (app == WEDGE_APP_BFS) {
@@ -1116,7 +1261,7 @@ static uint32_t aux_grid(wedge_graph* h, uint64_t work)
 // iteration tail after a pull: mass/convergence, Wedge frontier, bitmap reset
 static void launch_tail(wedge_graph* h, int app)
 {
-    decide_kernel<<<1, AUX_THREADS, 0, h->stream>>>(h->s, counters(h), h->pull_grid, (uint32_t)app);
+    decide_kernel<<<1, AUX_THREADS, 0, h->stream>>>(h->g, h->s, counters(h), h->pull_grid, (uint32_t)app);
     collect_kernel<<<aux_grid(h, (h->g.V + 31) / 32), AUX_THREADS, 0, h->stream>>>(h->g, h->s, (uint32_t)app);
     wedge_build_kernel<<<h->build_grid, AUX_THREADS, 0, h->stream>>>(h->g, h->s);
     advance_kernel<<<aux_grid(h, (h->g.V + 31) / 32), AUX_THREADS, 0, h->stream>>>(h->g, h->s, (uint32_t)app);
@@ -1440,7 +1585,7 @@ int wedge_cuda_run_phase(wedge_graph_t* g, int app, int phase, const wedge_param
             pr_finish_kernel<<<aux_grid(g, (uint64_t)dg.nsplit * 32 + 1), AUX_THREADS, 0, g->stream>>>(
                 dg, g->s, g->pull_grid, counters(g));
         } else {
-            decide_kernel<<<1, AUX_THREADS, 0, g->stream>>>(g->s, counters(g), g->pull_grid, (uint32_t)app);
+            decide_kernel<<<1, AUX_THREADS, 0, g->stream>>>(dg, g->s, counters(g), g->pull_grid, (uint32_t)app);
         }
         break;
     }

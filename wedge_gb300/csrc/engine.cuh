@@ -29,6 +29,8 @@ constexpr uint32_t TILE = 128;
 constexpr uint32_t CHUNK = 32;
 constexpr uint32_t CHUNKS_PER_TILE = TILE / CHUNK;        // 4
 constexpr uint32_t TILES_PER_WORD = 32 / CHUNKS_PER_TILE;  // 8 tiles per 32-bit chunk-bitmap word
+constexpr uint32_t REGION_WORDS = 32;                      // chunk-bitmap words per summary bit
+constexpr uint32_t TILES_PER_REGION = REGION_WORDS * TILES_PER_WORD;  // 256 tiles = 32768 in-edges
 constexpr uint32_t PIECE = 1024;                           // CSRI entries per Wedge-build work item
 constexpr uint32_t NONE32 = 0xFFFFFFFFu;
 constexpr unsigned long long NONE64 = ~0ull;
@@ -65,7 +67,7 @@ struct Ctrl {
     unsigned long long dsts_scanned;   // destinations in visited tiles
     unsigned long long activated;      // vertices activated by pulls
     unsigned int items;                // Wedge-build work items appended by the last pull
-    unsigned int tiles;                // Wedge tile list length
+    unsigned int region_next;          // next Wedge-frontier region a warp takes (dynamic schedule)
     unsigned int mode;                 // MODE_DENSE / MODE_WEDGE for the next pull
     unsigned int iter;                 // completed pulls
     unsigned int wedge_iters;          // pulls that used the Wedge frontier
@@ -115,7 +117,7 @@ struct DevState {
     uint32_t* front1;
     uint32_t* vis_c;               // Vne-bit visited bitmap (BFS)
     uint32_t* chunk_bits;          // Wedge frontier: one bit per chunk
-    uint32_t* tile_list;           // tiles holding at least one marked chunk
+    uint32_t* summary;             // one bit per region of REGION_WORDS chunk words (any chunk marked)
     uint2* items;                  // (vertex, piece) Wedge-build work items
     Ctrl* ctrl;
     IterRec* log;                  // [LOG_CAP] per-iteration records

@@ -38,6 +38,28 @@ __device__ __forceinline__ bool test_bit32(const uint32_t* bm, uint64_t i)
     return (bm[i >> 5] >> (i & 31)) & 1u;
 }
 
+// read-only (non-coherent) path for arrays no kernel writes while it runs
+__device__ __forceinline__ uint32_t ld_ro_u32(const uint32_t* p)
+{
+    uint32_t r;
+    asm volatile("ld.global.nc.u32 %0, [%1];" : "=r"(r) : "l"(p));
+    return r;
+}
+
+__device__ __forceinline__ double ld_ro_f64(const double* p)
+{
+    double r;
+    asm volatile("ld.global.nc.f64 %0, [%1];" : "=d"(r) : "l"(p));
+    return r;
+}
+
+__device__ __forceinline__ float ld_ro_f32(const float* p)
+{
+    float r;
+    asm volatile("ld.global.nc.f32 %0, [%1];" : "=f"(r) : "l"(p));
+    return r;
+}
+
 // per-lane geometry of a tile
 struct TileGeo {
     uint64_t base;
@@ -52,9 +74,13 @@ struct TileGeo {
 
 // Destination ranks inside the tile: position p belongs to compressed
 // destination k0 + (number of destination starts in [1, p]).
-// k0 = tile_dst0[t], kend = tile_dst0[t + 1].
+// k0 = tile_dst0[t], kend = tile_dst0[t + 1].  fill(slot, k) is called once for
+// every destination k with in-edges in the tile (slot = k - k0, on some lane) so
+// the caller can stage per-destination data in the warp's shared-memory table;
+// the table is complete after the __syncwarp at the end.
+template <class Fill>
 __device__ __forceinline__ void tile_geometry(const DevGraph& g, uint32_t t, uint32_t k0, uint32_t kend, int lane,
-                                              TileGeo& tg)
+                                              TileGeo& tg, Fill fill)
 {
     tg.base = (uint64_t)t * TILE;
     const uint32_t klim = min(kend, g.Vne - 1u);
@@ -68,8 +94,11 @@ __device__ __forceinline__ void tile_geometry(const DevGraph& g, uint32_t t, uin
             h1 |= (w == 1) ? b : 0u;
             h2 |= (w == 2) ? b : 0u;
             h3 |= (w == 3) ? b : 0u;
+            fill(j - k0, j);
         }
     }
+    if (lane == 0)
+        fill(0u, k0);
     h0 = __reduce_or_sync(FULL, h0);
     h1 = __reduce_or_sync(FULL, h1);
     h2 = __reduce_or_sync(FULL, h2);
@@ -85,6 +114,7 @@ __device__ __forceinline__ void tile_geometry(const DevGraph& g, uint32_t t, uin
     tg.before = (wi > 0 ? c0 : 0u) + (wi > 1 ? c1 : 0u) + (wi > 2 ? c2 : 0u) + __popc(hw & ((1u << sh) - 1u));
     tg.nib_inner = (hw >> sh) & 0xFu;
     tg.nib = tg.nib_inner | ((lane == 0 && tg.k0_fresh) ? 1u : 0u);
+    __syncwarp();
 }
 
 __device__ __forceinline__ uint32_t pos_dst(const TileGeo& tg, int i)
