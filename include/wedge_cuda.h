@@ -190,6 +190,36 @@ int wedge_cuda_read_results(wedge_graph_t* g, void* host_props, uint64_t bytes);
 /* graph_vertex_outdegrees as uint64 counts; bytes >= 8*V */
 int wedge_cuda_read_outdegrees(wedge_graph_t* g, uint64_t* host_outdeg, uint64_t bytes);
 
+/* ---------------------------------------------------------------- allocation-free iteration */
+
+/* No counterpart in the reference.  One PageRank iteration -- the edge pull
+ * (perform_edge_pull_phase_pr) and the vertex phase -- for callers that cannot
+ * allocate device memory, such as a host framework that owns every device
+ * allocation through its own pool, or code that must not trigger a cudaMalloc in
+ * the middle of its own stream work.  Nothing is allocated: the scratch lives in
+ * a fixed static device array of about 4.2 MB that every GPU loading this
+ * library holds until exit.  The caller owns all inputs and outputs, in device
+ * memory:
+ *   dst_off[num_dsts+1]  first in-edge of each destination that has in-edges
+ *                        (strictly increasing, dst_off[num_dsts] == num_edges)
+ *   dst_id[num_dsts]     vertex id of each such destination, ascending
+ *   src[]                in-edge sources, 16-byte aligned, padded with
+ *                        0xFFFFFFFF to a multiple of 128 entries
+ *   outdeg[num_vertices] out-degree of every vertex
+ *   rank_in, rank_out    [num_vertices] rank / outdegree' (graph_vertex_props of
+ *                        PageRank); rank_out must not alias rank_in
+ * damping <= 0 selects 0.875.  num_edges above WEDGE_NOALLOC_MAX_EDGES is
+ * rejected with WEDGE_ERR_ARG.  Work is queued on `stream` (a cudaStream_t, NULL
+ * for the default stream) and the call returns without waiting.  The first call
+ * on a device looks up the scratch array's device address (make that first call
+ * before any stream capture).  All calls share the one array: calls that
+ * overlap on the GPU race and must be ordered by the caller. */
+#define WEDGE_NOALLOC_MAX_EDGES (1ull << 24)
+int wedge_cuda_pr_iteration_noalloc(uint64_t num_vertices, uint64_t num_dsts, uint64_t num_edges,
+                                    const uint64_t* dst_off, const uint32_t* dst_id, const uint32_t* src,
+                                    const uint32_t* outdeg, const double* rank_in, double* rank_out,
+                                    double damping, void* stream);
+
 uint64_t wedge_cuda_num_vertices(const wedge_graph_t* g);
 uint64_t wedge_cuda_num_edges(const wedge_graph_t* g);
 /* the CUDA stream (cudaStream_t) the graph's kernels run on, as an opaque pointer */

@@ -14,6 +14,7 @@
 //   run_traversal / run_pr    execution_{bfs,cc,sssp}.c:122-365 / execution_pr.c:396-486
 #include <cub/device/device_scan.cuh>
 
+#include <pthread.h>
 #include <stdio.h>
 #include <stdlib.h>
 #include <string.h>
@@ -1692,3 +1693,209 @@ void* wedge_cuda_stream(const wedge_graph_t* g) { return g ? (void*)g->stream : 
 void wedge_cuda_free(wedge_graph_t* g) { free_handle(g); }
 
 }  // extern "C"
+
+/* ===================================== allocation-free PageRank iteration */
+//
+// For callers that cannot allocate device memory -- a host framework that owns
+// every device allocation through its own pool, or code running where a
+// cudaMalloc would stall or break the caller's stream ordering -- one PageRank
+// iteration runs over a CSC the caller already holds in device memory.  The
+// caller passes inputs and outputs; the scratch the edge pull needs (the tile
+// index, per-tile partial sums of destinations that span tiles, per-block
+// totals, the control block) lives in one file-scope static device array of
+// fixed size, which every GPU that loads this library holds until exit.
+namespace wedge {
+
+constexpr uint64_t NOALLOC_MAX_EDGES = WEDGE_NOALLOC_MAX_EDGES;
+constexpr uint32_t NOALLOC_MAX_TILES = (uint32_t)(NOALLOC_MAX_EDGES / TILE);
+constexpr uint32_t NOALLOC_MAX_GRID = 2048;
+constexpr int NOALLOC_MAX_DEVICES = 64;
+
+struct NoAllocScratch {
+    Ctrl ctrl;
+    IterRec log[1];
+    unsigned int nsplit;
+    unsigned long long block_cnt[NCNT * NOALLOC_MAX_GRID];
+    double block_part[NOALLOC_MAX_GRID];
+    uint32_t tile_dst0[NOALLOC_MAX_TILES + 1];
+    uint32_t split_k[NOALLOC_MAX_TILES];
+    uint32_t split_t0[NOALLOC_MAX_TILES];
+    uint32_t split_t1[NOALLOC_MAX_TILES];
+    double head_part[NOALLOC_MAX_TILES];
+    double tail_part[NOALLOC_MAX_TILES];
+};
+
+// about 4.2 MB on every device that loads the library
+static __device__ __align__(256) NoAllocScratch g_noalloc_scratch;
+
+// per-device address of g_noalloc_scratch and the pull grid, set up on the first call
+static NoAllocScratch* g_noalloc_ptr[NOALLOC_MAX_DEVICES];
+static uint32_t g_noalloc_grid[NOALLOC_MAX_DEVICES];
+static pthread_mutex_t g_noalloc_lock = PTHREAD_MUTEX_INITIALIZER;
+
+// control block for one dense pull, tile index (first compressed destination of
+// every tile) and a zeroed split count: everything that must start fresh per call
+__global__ void noalloc_prepare_kernel(const unsigned long long* dst_off, uint32_t num_dsts, uint32_t T)
+{
+    NoAllocScratch* sc = &g_noalloc_scratch;
+    const uint64_t tid = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
+    if (tid == 0) {
+        Ctrl* c = &sc->ctrl;
+        memset(c, 0, sizeof(Ctrl));
+        c->mode = MODE_DENSE;
+        c->iter = LOG_CAP; /* no per-iteration log in this path */
+        sc->nsplit = 0u;
+    }
+    for (uint64_t t = tid; t <= T; t += (uint64_t)gridDim.x * blockDim.x) {
+        if (t == T) {
+            sc->tile_dst0[t] = num_dsts;
+            continue;
+        }
+        // last destination whose first in-edge is at or before edge t*TILE
+        const unsigned long long e = t * (unsigned long long)TILE;
+        uint32_t lo = 0, hi = num_dsts; /* dst_off[lo] <= e < dst_off[hi] */
+        while (hi - lo > 1) {
+            const uint32_t mid = lo + (hi - lo) / 2;
+            if (dst_off[mid] <= e)
+                lo = mid;
+            else
+                hi = mid;
+        }
+        sc->tile_dst0[t] = lo;
+    }
+}
+
+// total rank and the destinations spanning tiles, as pr_finish_kernel, with the
+// split count read from the scratch
+__global__ void noalloc_finish_kernel(DevGraph g, DevState s, uint32_t nblocks)
+{
+    __shared__ double sh[AUX_THREADS / 32];
+    NoAllocScratch* sc = &g_noalloc_scratch;
+    const int lane = threadIdx.x & 31;
+    if (blockIdx.x == 0) {
+        double x = 0.0;
+        for (uint32_t i = threadIdx.x; i < nblocks; i += blockDim.x)
+            x = __dadd_rn(x, sc->block_part[i]);
+        x = warp_sum_f64(x);
+        if (lane == 0)
+            sh[threadIdx.x >> 5] = x;
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            double t = 0.0;
+            for (int w = 0; w < AUX_THREADS / 32; ++w)
+                t = __dadd_rn(t, sh[w]);
+            sc->ctrl.pr_total = t;
+        }
+    }
+    const uint32_t nsplit = sc->nsplit;
+    const uint32_t gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const uint32_t nw = (gridDim.x * blockDim.x) >> 5;
+    for (uint32_t i = gw; i < nsplit; i += nw) {
+        const uint32_t t0 = sc->split_t0[i], t1 = sc->split_t1[i];
+        double x = 0.0;
+        for (uint32_t t = t0 + lane; t < t1; t += 32)
+            x = __dadd_rn(x, sc->tail_part[t]);
+        x = warp_sum_f64(x);
+        if (lane == 0)
+            s.acc[g.dst_id[sc->split_k[i]]] = __dadd_rn(x, sc->head_part[t1]);
+    }
+}
+
+static int noalloc_setup(int dev, NoAllocScratch** sc, uint32_t* grid)
+{
+    if (dev < 0 || dev >= NOALLOC_MAX_DEVICES)
+        return WEDGE_ERR_UNSUPPORTED;
+    pthread_mutex_lock(&g_noalloc_lock);
+    int rc = WEDGE_OK;
+    if (!g_noalloc_ptr[dev]) {
+        void* p = nullptr;
+        cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch); /* device `dev` is current */
+        int sms = 0, blocks = 0;
+        if (e == cudaSuccess)
+            e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        if (e == cudaSuccess)
+            e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, pull_kernel<WEDGE_APP_PR>, PULL_THREADS, 0);
+        if (e != cudaSuccess) {
+            rc = cuda_status(e);
+        } else {
+            uint32_t grid = (uint32_t)(sms * (blocks > 0 ? blocks : 1));
+            g_noalloc_grid[dev] = grid < NOALLOC_MAX_GRID ? grid : NOALLOC_MAX_GRID;
+            g_noalloc_ptr[dev] = (NoAllocScratch*)p;
+        }
+    }
+    *sc = g_noalloc_ptr[dev];
+    *grid = g_noalloc_grid[dev];
+    pthread_mutex_unlock(&g_noalloc_lock);
+    return rc;
+}
+
+}  // namespace wedge
+
+extern "C" int wedge_cuda_pr_iteration_noalloc(uint64_t num_vertices, uint64_t num_dsts, uint64_t num_edges,
+                                               const uint64_t* dst_off, const uint32_t* dst_id, const uint32_t* src,
+                                               const uint32_t* outdeg, const double* rank_in, double* rank_out,
+                                               double damping, void* stream)
+{
+    using namespace wedge;
+    if (num_edges > NOALLOC_MAX_EDGES || num_dsts > num_edges || num_vertices == 0 || num_vertices > 0xFFFFFFFEull ||
+        num_dsts > num_vertices)
+        return WEDGE_ERR_ARG; /* beyond the static scratch, or inconsistent sizes */
+    if (!dst_off || !dst_id || !src || !outdeg || !rank_in || !rank_out || ((uintptr_t)src & 15u) ||
+        (num_edges && !num_dsts))
+        return WEDGE_ERR_ARG;
+    int dev = 0;
+    WEDGE_CHECK(cudaGetDevice(&dev));
+    NoAllocScratch* sc = nullptr;
+    uint32_t grid = 0;
+    int rc = noalloc_setup(dev, &sc, &grid);
+    if (rc)
+        return rc;
+    cudaStream_t st = (cudaStream_t)stream;
+    const uint32_t T = (uint32_t)((num_edges + TILE - 1) / TILE);
+    DevGraph g;
+    memset(&g, 0, sizeof(g));
+    g.V = num_vertices;
+    g.E = num_edges;
+    g.Epad = (uint64_t)T * TILE;
+    g.Vne = (uint32_t)num_dsts;
+    g.T = T;
+    g.weight_kind = WEDGE_WEIGHTS_NONE;
+    g.src = src;
+    g.dst_id = dst_id;
+    g.dst_off = (const unsigned long long*)dst_off;
+    g.tile_dst0 = sc->tile_dst0;
+    g.outdeg = outdeg;
+    g.split_k = sc->split_k;
+    g.split_t0 = sc->split_t0;
+    g.split_t1 = sc->split_t1;
+    DevState s;
+    memset(&s, 0, sizeof(s));
+    s.ctrl = &sc->ctrl;
+    s.log = sc->log;
+    s.head_part = sc->head_part;
+    s.tail_part = sc->tail_part;
+    s.block_part = sc->block_part;
+    s.damping = damping > 0.0 ? damping : 0.875;
+    s.precision = WEDGE_PREC_FP64;
+    s.app = WEDGE_APP_PR;
+    s.acc = rank_out; /* accumulators first, ranks after the vertex phase */
+    const uint32_t aux = (uint32_t)grid_for(num_vertices > T ? num_vertices : (uint64_t)T + 1, AUX_THREADS, grid * 2u);
+    noalloc_prepare_kernel<<<aux, AUX_THREADS, 0, st>>>(g.dst_off, g.Vne, T);
+    if (num_dsts)
+        split_kernel<<<grid_for(num_dsts, AUX_THREADS, grid * 2u), AUX_THREADS, 0, st>>>(
+            g.dst_off, g.Vne, sc->split_k, sc->split_t0, sc->split_t1, &sc->nsplit);
+    WEDGE_CHECK(cudaMemsetAsync(rank_out, 0, num_vertices * sizeof(double), st));
+    DevState sp = s;
+    sp.rank = (double*)rank_in; /* gathered by the pull */
+    if (T)
+        pull_kernel<WEDGE_APP_PR><<<grid, PULL_THREADS, 0, st>>>(g, sp, sc->block_cnt);
+    else
+        WEDGE_CHECK(cudaMemsetAsync(sc->block_part, 0, sizeof(double), st));
+    noalloc_finish_kernel<<<grid_for((uint64_t)T * 32 + 1, AUX_THREADS, grid * 2u), AUX_THREADS, 0, st>>>(
+        g, s, T ? grid : 1u);
+    DevState sv = s;
+    sv.rank = rank_out;
+    pr_vertex_kernel<<<grid_for(num_vertices, AUX_THREADS, grid * 2u), AUX_THREADS, 0, st>>>(g, sv);
+    WEDGE_CHECK(cudaGetLastError());
+    return WEDGE_OK;
+}

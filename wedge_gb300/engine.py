@@ -107,6 +107,9 @@ _SIGNATURES = {
     "wedge_cuda_read_results": (C.c_int, [C.c_void_p, C.c_void_p, C.c_uint64]),
     "wedge_cuda_iteration_log": (C.c_int, [C.c_void_p, C.c_void_p, C.c_uint64, C.POINTER(C.c_uint64)]),
     "wedge_cuda_read_outdegrees": (C.c_int, [C.c_void_p, C.c_void_p, C.c_uint64]),
+    "wedge_cuda_pr_iteration_noalloc": (C.c_int, [C.c_uint64, C.c_uint64, C.c_uint64, C.c_void_p, C.c_void_p,
+                                                  C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_double,
+                                                  C.c_void_p]),
     "wedge_cuda_num_vertices": (C.c_uint64, [C.c_void_p]),
     "wedge_cuda_num_edges": (C.c_uint64, [C.c_void_p]),
     "wedge_cuda_stream": (C.c_void_p, [C.c_void_p]),
