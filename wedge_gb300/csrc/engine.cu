@@ -165,7 +165,7 @@ __global__ void tile_index_kernel(const uint32_t* kidx, uint64_t E, uint32_t T, 
                                   unsigned long long* dst_off)
 {
     for (uint64_t t = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; t <= T; t += (uint64_t)gridDim.x * blockDim.x) {
-        tile_dst0[t] = (t < T) ? kidx[t * TILE] - 1u : Vne;
+        tile_dst0[t] = (t * TILE < E) ? kidx[t * TILE] - 1u : Vne; /* padding edges: no owner */
         if (t == 0)
             dst_off[Vne] = E;
     }
@@ -243,7 +243,7 @@ int build_from_device_edges(wedge_graph* h, uint64_t V, uint64_t E, uint32_t* d_
     DevGraph& g = h->g;
     g.V = V;
     g.E = E;
-    g.Epad = (E + TILE - 1) / TILE * TILE;
+    g.Epad = (E + MAX_TILE_E - 1) / MAX_TILE_E * MAX_TILE_E;
     g.T = (uint32_t)(g.Epad / TILE);
     g.weight_kind = (uint32_t)weight_kind;
     h->weight_kind = weight_kind;
@@ -368,22 +368,36 @@ __device__ __forceinline__ uint32_t* next_front(const DevState& s, uint32_t app,
     return (app == WEDGE_APP_BFS) ? (parity ? s.front0 : s.front1) : s.front0;
 }
 
-// One tile's inputs, loaded one tile ahead of its processing so their latency
-// overlaps the previous tile's gathers, reduction and emission.
+// in-edges per lane of each application's pull (tile = 32 * EPL in-edges)
+template <int APP>
+struct PullEpl {
+    static constexpr int value = 8;
+};
+template <>
+struct PullEpl<WEDGE_APP_CC> {
+    static constexpr int value = 16;
+};
+template <>
+struct PullEpl<WEDGE_APP_PR> {
+    static constexpr int value = 4; /* the PageRank split lists are built for 128-edge tiles */
+};
+
+// One tile's bounds, loaded one tile ahead of its processing so their latency
+// overlaps the previous tile's work.
 struct TileIn {
     uint32_t t, cmask, k0, kend, visw;
     bool open;
-    uint4 src;
 };
 
-template <int APP>
+template <int APP, int EPL>
 __device__ __forceinline__ void tile_prefetch(const DevGraph& g, const DevState& s, uint32_t t, uint32_t cmask, int lane,
                                               TileIn& in)
 {
+    constexpr uint32_t Q = EPL / 4; /* 128-edge index entries per tile */
     in.t = t;
     in.cmask = cmask;
-    in.k0 = g.tile_dst0[t];
-    in.kend = g.tile_dst0[t + 1];
+    in.k0 = g.tile_dst0[(uint64_t)t * Q];
+    in.kend = g.tile_dst0[((uint64_t)t + 1) * Q];
     in.open = true;
     in.visw = 0u;
     if (APP == WEDGE_APP_BFS) {
@@ -392,55 +406,98 @@ __device__ __forceinline__ void tile_prefetch(const DevGraph& g, const DevState&
         const uint32_t klim = min(in.kend, g.Vne - 1u);
         const uint32_t w0 = in.k0 >> 5, w1 = klim >> 5;
         bool open = false;
+        uint32_t visw = 0u;
         if ((uint32_t)lane <= w1 - w0) {
             const uint32_t wi = w0 + lane;
             const uint32_t lo = (wi == w0) ? (in.k0 & 31u) : 0u;
             const uint32_t hi = (wi == w1) ? (klim & 31u) : 31u;
             const uint32_t range = (hi == 31u ? FULL : ((2u << hi) - 1u)) & ~((1u << lo) - 1u);
-            in.visw = s.vis_c[wi];
-            open = (~in.visw & range) != 0u;
+            visw = s.vis_c[wi];
+            open = (~visw & range) != 0u;
         }
+        in.visw = visw;
         in.open = __any_sync(FULL, open);
+        if (!in.open && lane == 0)
+            atomicAnd(&s.tile_open[t >> 5], ~(1u << (t & 31u))); /* closed for good */
     }
-    const bool on = in.open && ((cmask >> (lane >> 3)) & 1u);
-    in.src = on ? ld_stream_v4(g.src + (uint64_t)t * TILE + 4u * (uint32_t)lane)
-                : make_uint4(NONE32, NONE32, NONE32, NONE32);
 }
 
-// The tiles a warp pulls: every tile (dense, static stride), or the tiles of
-// the Wedge frontier, found by walking the chunk bitmap one region
-// (REGION_WORDS words = 256 tiles) at a time, regions handed out dynamically;
-// a region whose summary bit is clear is skipped without reading its words
-// (the reference's 256-bit emptiness test, phase_edge_pull_bfs.c:244-246).
-// Walked words are cleared: the pull consumes the frontier
-// (phase_edge_pull_bfs.c:256).  Warp-uniform.
+// EPL consecutive sources of this lane (positions EPL*lane ..), NONE32 where the
+// lane's chunk is not in the mask; L1-cached vector loads, so the lanes of a
+// warp together read the tile's 128*EPL bytes once.
+template <int EPL>
+__device__ __forceinline__ void load_sources(const DevGraph& g, uint64_t base, uint32_t cmask, int lane,
+                                             uint32_t (&sa)[EPL])
+{
+    const bool on = (cmask >> (((uint32_t)lane * EPL) >> 5)) & 1u;
+    const uint4* p = reinterpret_cast<const uint4*>(g.src + base + (uint64_t)lane * EPL);
+#pragma unroll
+    for (int q = 0; q < EPL / 4; ++q) {
+        uint4 x = make_uint4(NONE32, NONE32, NONE32, NONE32);
+        if (on)
+            x = __ldg(p + q);
+        sa[4 * q + 0] = x.x;
+        sa[4 * q + 1] = x.y;
+        sa[4 * q + 2] = x.z;
+        sa[4 * q + 3] = x.w;
+    }
+}
+
+// The tiles a warp pulls: every tile (dense: static stride, or for BFS the open
+// tiles, 32 per dynamically grabbed word of the open-tile bitmap), or the
+// tiles of the Wedge frontier, found by walking the chunk bitmap one region
+// (REGION_WORDS words) at a time, regions handed out dynamically; a region
+// whose summary bit is clear is skipped without reading its words (the
+// reference's 256-bit emptiness test, phase_edge_pull_bfs.c:244-246).  Walked
+// words are cleared: the pull consumes the frontier (phase_edge_pull_bfs.c:256).
+// Warp-uniform.
 struct TileIter {
     uint32_t i, step;      // dense
+    uint32_t obits, obase; // BFS dense: open tiles left in the current word, its first tile
     uint32_t region;       // wedge: region being walked (NONE32 before the first)
     uint32_t myword;       // this lane's chunk word of the region
     uint32_t lanes;        // lanes whose words are still to be walked
     uint32_t word, wlane;  // the word being walked and its lane
 };
 
-__device__ __forceinline__ bool next_tile(const DevGraph& g, const DevState& s, uint32_t mode, TileIter& it, int lane,
-                                          uint32_t& t, uint32_t& cmask)
+template <int EPL>
+__device__ __forceinline__ bool next_tile(const DevGraph& g, const DevState& s, uint32_t mode, uint32_t T, TileIter& it,
+                                          int lane, uint32_t& t, uint32_t& cmask)
 {
+    constexpr uint32_t TPW = 32 / EPL;  // tiles per chunk word
+    constexpr uint32_t MASK = (EPL >= 32) ? FULL : ((1u << EPL) - 1u);
+    if (mode == MODE_DENSE && s.tile_open) {
+        while (!it.obits) {
+            uint32_t w = 0;
+            if (lane == 0)
+                w = atomicAdd(&s.ctrl->region_next, 1u);
+            w = __shfl_sync(FULL, w, 0);
+            if (w >= (T + 31) / 32)
+                return false;
+            it.obits = s.tile_open[w];
+            it.obase = w * 32;
+        }
+        t = it.obase + (uint32_t)(__ffs(it.obits) - 1);
+        it.obits &= it.obits - 1u;
+        cmask = MASK;
+        return true;
+    }
     if (mode == MODE_DENSE) {
-        if (it.i >= g.T)
+        if (it.i >= T)
             return false;
         t = it.i;
-        cmask = 0xFu;
+        cmask = MASK;
         it.i += it.step;
         return true;
     }
-    const uint32_t nwords = (g.T + TILES_PER_WORD - 1) / TILES_PER_WORD;
-    const uint32_t nregions = (g.T + TILES_PER_REGION - 1) / TILES_PER_REGION;
+    const uint32_t nwords = (g.T + TILES_PER_WORD - 1) / TILES_PER_WORD; /* chunk words (4 per 128 edges / 32) */
+    const uint32_t nregions = (nwords + REGION_WORDS - 1) / REGION_WORDS;
     for (;;) {
         if (it.word) {
-            const uint32_t j = (uint32_t)(__ffs(it.word) - 1) >> 2;
-            cmask = (it.word >> (4u * j)) & 0xFu;
-            it.word &= ~(0xFu << (4u * j));
-            t = (it.region * REGION_WORDS + it.wlane) * TILES_PER_WORD + j;
+            const uint32_t j = (uint32_t)(__ffs(it.word) - 1) / EPL;
+            cmask = (it.word >> (EPL * j)) & MASK;
+            it.word &= ~(MASK << (EPL * j));
+            t = (it.region * REGION_WORDS + it.wlane) * TPW + j;
             return true;
         }
         if (it.lanes) {
@@ -480,18 +537,27 @@ struct CurT<WEDGE_APP_SSSP> {
     using type = unsigned long long;
 };
 
+// resident blocks per SM the register allocation must allow for each pull
+#ifndef WEDGE_PULL_MINB
+#define WEDGE_PULL_MINB 4
+#endif
+
 // Edge pull over all tiles (dense) or over the tiles of the Wedge frontier.
 // block_cnt[NCNT*b + CNT_*] = changed mass, in-edges read, tiles visited,
 // destinations in visited tiles, vertices activated.
-template <int APP>
-__global__ void __launch_bounds__(PULL_THREADS) pull_kernel(DevGraph g, DevState s, unsigned long long* block_cnt)
+template <int APP, int EPL>
+__global__ void __launch_bounds__(PULL_THREADS, WEDGE_PULL_MINB)
+    pull_kernel(DevGraph g, DevState s, unsigned long long* block_cnt)
 {
     constexpr int WARPS = PULL_THREADS / 32;
+    constexpr uint32_t TILE_E = 32u * EPL;
+    constexpr uint32_t TAB = 129; /* staged destinations per tile; more are read from global memory */
     using cur_t = typename CurT<APP>::type;
     __shared__ unsigned long long sh_cnt[WARPS][5];
     __shared__ double sh_sum[WARPS];
-    __shared__ uint32_t tab_id[WARPS][TILE + 1];  // vertex id of each destination of the warp's tile
-    __shared__ cur_t tab_cur[WARPS][TILE + 1];    // its property before the tile (min apps)
+    __shared__ uint32_t tab_id[WARPS][TAB];  // vertex id of each destination of the warp's tile
+    __shared__ cur_t tab_cur[WARPS][TAB];    // its property before the tile (min apps)
+    __shared__ uint32_t sh_heads[WARPS][EPL];
     Ctrl* c = s.ctrl;
     if (c->done)
         return;
@@ -499,62 +565,72 @@ __global__ void __launch_bounds__(PULL_THREADS) pull_kernel(DevGraph g, DevState
     const int wib = threadIdx.x >> 5;
     const uint32_t gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const uint32_t nw = (gridDim.x * blockDim.x) >> 5;
+    const uint32_t T = (uint32_t)((g.E + TILE_E - 1) / TILE_E); /* tiles holding real in-edges */
     const uint32_t mode = c->mode;
     const uint32_t parity = c->parity;
+    const bool first_cc = (APP == WEDGE_APP_CC) && c->iter == 0u; /* labels still equal vertex ids */
     const uint32_t* cur = cur_front(s, parity);
     uint32_t* nxt = next_front(s, APP, parity);
     uint32_t* my_id = tab_id[wib];
     cur_t* my_cur = tab_cur[wib];
+    uint32_t* heads = sh_heads[wib];
     unsigned long long mass = 0, edges = 0, tiles = 0, dsts = 0, act = 0;
     double psum = 0.0;
+    auto vid = [&](uint32_t k, uint32_t slot) -> uint32_t { return slot < TAB ? my_id[slot] : g.dst_id[k]; };
 
     TileIter it;
     it.i = gw;
     it.step = nw;
+    it.obits = it.obase = 0u;
     it.region = NONE32;
     it.myword = it.lanes = it.word = it.wlane = 0u;
     TileIn nextin;
     uint32_t tn, cn;
-    bool more = next_tile(g, s, mode, it, lane, tn, cn);
+    bool more = next_tile<EPL>(g, s, mode, T, it, lane, tn, cn);
     if (more)
-        tile_prefetch<APP>(g, s, tn, cn, lane, nextin);
+        tile_prefetch<APP, EPL>(g, s, tn, cn, lane, nextin);
     while (more) {
         const TileIn in = nextin;
-        more = next_tile(g, s, mode, it, lane, tn, cn);
+        more = next_tile<EPL>(g, s, mode, T, it, lane, tn, cn);
         if (more)
-            tile_prefetch<APP>(g, s, tn, cn, lane, nextin);
+            tile_prefetch<APP, EPL>(g, s, tn, cn, lane, nextin);
         ++tiles;
         if (!in.open)
             continue;
         const uint32_t t = in.t;
-        const uint32_t sa[4] = {in.src.x, in.src.y, in.src.z, in.src.w};
+        const uint64_t base = (uint64_t)t * TILE_E;
+        const bool last_tile = (t + 1u >= T);
+        uint32_t sa[EPL];
+        load_sources<EPL>(g, base, in.cmask, lane, sa);
 #pragma unroll
-        for (int q = 0; q < 4; ++q)
+        for (int q = 0; q < EPL; ++q)
             edges += (sa[q] != NONE32) ? 1u : 0u;
 
         if (APP == WEDGE_APP_BFS) {
             // frontier-bit gathers first, then the geometry (their latencies overlap)
-            uint32_t fb[4];
+            uint32_t fb[EPL];
 #pragma unroll
-            for (int q = 0; q < 4; ++q)
+            for (int q = 0; q < EPL; ++q)
                 fb[q] = (sa[q] != NONE32) ? ld_ro_u32(cur + (sa[q] >> 5)) : 0u;
-            TileGeo tg;
-            tile_geometry(g, t, in.k0, in.kend, lane, tg,
-                          [&](uint32_t slot, uint32_t k) { my_id[slot] = g.dst_id[k]; });
+            TileGeo<EPL> tg;
+            tile_geometry<EPL>(g, base, last_tile, in.k0, in.kend, lane, heads, tg, [&](uint32_t slot, uint32_t k) {
+                if (slot < TAB)
+                    my_id[slot] = g.dst_id[k];
+            });
             dsts += tg.ndst;
-            uint32_t v[4];
+            uint32_t v[EPL];
             const uint32_t w0 = in.k0 >> 5;
 #pragma unroll
-            for (int q = 0; q < 4; ++q) {
+            for (int q = 0; q < EPL; ++q) {
                 const uint32_t k = pos_dst(tg, q);
                 const uint32_t vw = __shfl_sync(FULL, in.visw, (int)((k >> 5) - w0));
                 const bool visited = (vw >> (k & 31u)) & 1u;
                 v[q] = (sa[q] != NONE32 && !visited && ((fb[q] >> (sa[q] & 31u)) & 1u)) ? sa[q] : NONE32;
             }
-            seg_reduce(v, tg, lane, MinU32(), [&](uint32_t k, uint32_t val, int) {
+            seg_reduce<EPL>(v, tg, lane, MinU32(), [&](uint32_t k, uint32_t val, int) {
                 if (val == NONE32)
                     return;
-                const uint32_t vtx = my_id[k - tg.k0];
+                const uint32_t vtx = vid(k, k - tg.k0);
                 const uint32_t old = atomicMin(&s.prop32[vtx], val);
                 if (old == NONE32) {
                     atomicOr(&s.vis_c[k >> 5], 1u << (k & 31u));
@@ -564,21 +640,28 @@ __global__ void __launch_bounds__(PULL_THREADS) pull_kernel(DevGraph g, DevState
                 }
             });
         } else if (APP == WEDGE_APP_CC) {
-            uint32_t v[4];
+            // The first pull reads the initial labels, which are the sources' own
+            // ids (execution_cc.c:77): no gather.  Reading an older label than
+            // the in-place one is always allowed in label propagation, so the
+            // fixed point is unchanged.
+            uint32_t v[EPL];
 #pragma unroll
-            for (int q = 0; q < 4; ++q)
-                v[q] = (sa[q] != NONE32) ? s.prop32[sa[q]] : NONE32;
-            TileGeo tg;
-            tile_geometry(g, t, in.k0, in.kend, lane, tg, [&](uint32_t slot, uint32_t k) {
-                const uint32_t vtx = g.dst_id[k];
-                my_id[slot] = vtx;
-                my_cur[slot] = s.prop32[vtx];
+            for (int q = 0; q < EPL; ++q)
+                v[q] = (sa[q] != NONE32) ? (first_cc ? sa[q] : s.prop32[sa[q]]) : NONE32;
+            TileGeo<EPL> tg;
+            tile_geometry<EPL>(g, base, last_tile, in.k0, in.kend, lane, heads, tg, [&](uint32_t slot, uint32_t k) {
+                if (slot < TAB) {
+                    const uint32_t vtx = g.dst_id[k];
+                    my_id[slot] = vtx;
+                    my_cur[slot] = first_cc ? vtx : s.prop32[vtx];
+                }
             });
             dsts += tg.ndst;
-            seg_reduce(v, tg, lane, MinU32(), [&](uint32_t k, uint32_t val, int) {
+            seg_reduce<EPL>(v, tg, lane, MinU32(), [&](uint32_t k, uint32_t val, int) {
                 const uint32_t slot = k - tg.k0;
-                if (val < (uint32_t)my_cur[slot]) {
-                    const uint32_t vtx = my_id[slot];
+                const uint32_t vtx = vid(k, slot);
+                const uint32_t cv = slot < TAB ? (uint32_t)my_cur[slot] : s.prop32[vtx];
+                if (val < cv) {
                     const uint32_t old = atomicMin(&s.prop32[vtx], val);
                     if (val < old) {
                         const uint32_t b = 1u << (vtx & 31u);
@@ -590,43 +673,44 @@ __global__ void __launch_bounds__(PULL_THREADS) pull_kernel(DevGraph g, DevState
                 }
             });
         } else if (APP == WEDGE_APP_SSSP) {
-            unsigned long long wv[4] = {0, 0, 0, 0};
-            const uint64_t base = (uint64_t)t * TILE + 4u * (uint32_t)lane;
-            if (sa[0] != NONE32 || sa[3] != NONE32 || sa[1] != NONE32 || sa[2] != NONE32) {
-                const ulonglong2 a = ld_stream_v2u64(g.w + base);
-                const ulonglong2 b = ld_stream_v2u64(g.w + base + 2u);
-                wv[0] = a.x;
-                wv[1] = a.y;
-                wv[2] = b.x;
-                wv[3] = b.y;
+            unsigned long long wv[EPL];
+            const bool on = (in.cmask >> (((uint32_t)lane * EPL) >> 5)) & 1u;
+            const ulonglong2* wp = reinterpret_cast<const ulonglong2*>(g.w + base + (uint64_t)lane * EPL);
+#pragma unroll
+            for (int q = 0; q < EPL / 2; ++q) {
+                ulonglong2 x = make_ulonglong2(0ull, 0ull);
+                if (on)
+                    x = __ldg(wp + q);
+                wv[2 * q] = x.x;
+                wv[2 * q + 1] = x.y;
             }
-            unsigned long long dv[4];
+            unsigned long long v[EPL];
 #pragma unroll
-            for (int q = 0; q < 4; ++q)
-                dv[q] = (sa[q] != NONE32) ? s.prop64[sa[q]] : NONE64;
-            TileGeo tg;
-            tile_geometry(g, t, in.k0, in.kend, lane, tg, [&](uint32_t slot, uint32_t k) {
-                const uint32_t vtx = g.dst_id[k];
-                my_id[slot] = vtx;
-                my_cur[slot] = s.prop64[vtx];
-            });
-            dsts += tg.ndst;
-            unsigned long long v[4];
-#pragma unroll
-            for (int q = 0; q < 4; ++q) {
+            for (int q = 0; q < EPL; ++q) {
                 v[q] = NONE64;
                 if (sa[q] != NONE32) {
+                    const unsigned long long d = s.prop64[sa[q]];
                     if (g.weight_kind == WEDGE_WEIGHTS_F64)
                         v[q] = (unsigned long long)__double_as_longlong(
-                            __dadd_rn(__longlong_as_double((long long)dv[q]), __longlong_as_double((long long)wv[q])));
+                            __dadd_rn(__longlong_as_double((long long)d), __longlong_as_double((long long)wv[q])));
                     else
-                        v[q] = (dv[q] == NONE64) ? NONE64 : dv[q] + wv[q]; /* phase_edge_pull_sssp.c:136-137 */
+                        v[q] = (d == NONE64) ? NONE64 : d + wv[q]; /* phase_edge_pull_sssp.c:136-137 */
                 }
             }
-            seg_reduce(v, tg, lane, MinU64(), [&](uint32_t k, unsigned long long val, int) {
+            TileGeo<EPL> tg;
+            tile_geometry<EPL>(g, base, last_tile, in.k0, in.kend, lane, heads, tg, [&](uint32_t slot, uint32_t k) {
+                if (slot < TAB) {
+                    const uint32_t vtx = g.dst_id[k];
+                    my_id[slot] = vtx;
+                    my_cur[slot] = s.prop64[vtx];
+                }
+            });
+            dsts += tg.ndst;
+            seg_reduce<EPL>(v, tg, lane, MinU64(), [&](uint32_t k, unsigned long long val, int) {
                 const uint32_t slot = k - tg.k0;
-                if (val < (unsigned long long)my_cur[slot]) {
-                    const uint32_t vtx = my_id[slot];
+                const uint32_t vtx = vid(k, slot);
+                const unsigned long long cv = slot < TAB ? (unsigned long long)my_cur[slot] : s.prop64[vtx];
+                if (val < cv) {
                     const unsigned long long old = atomicMin(&s.prop64[vtx], val);
                     if (val < old) {
                         const uint32_t b = 1u << (vtx & 31u);
@@ -639,20 +723,26 @@ __global__ void __launch_bounds__(PULL_THREADS) pull_kernel(DevGraph g, DevState
             });
         } else if (APP == WEDGE_APP_PR) {
             if (s.precision == WEDGE_PREC_FP32C) {
-                F2 v[4];
+                F2 v[EPL];
 #pragma unroll
-                for (int q = 0; q < 4; ++q)
+                for (int q = 0; q < EPL; ++q)
                     v[q] = F2{(sa[q] != NONE32) ? ld_ro_f32(s.rank32 + sa[q]) : 0.0f, 0.0f};
-                TileGeo tg;
-                tile_geometry(g, t, in.k0, in.kend, lane, tg,
-                              [&](uint32_t slot, uint32_t k) { my_id[slot] = g.dst_id[k]; });
+                TileGeo<EPL> tg;
+                tile_geometry<EPL>(g, base, last_tile, in.k0, in.kend, lane, heads, tg,
+                                   [&](uint32_t slot, uint32_t k) {
+                                       if (slot < TAB)
+                                           my_id[slot] = g.dst_id[k];
+                                   });
                 dsts += tg.ndst;
                 const AddF2 add;
-                const F2 ls = add(add(v[0], v[1]), add(v[2], v[3]));
+                F2 ls = v[0];
+#pragma unroll
+                for (int q = 1; q < EPL; ++q)
+                    ls = add(ls, v[q]);
                 psum = __dadd_rn(psum, warp_sum_f64(__dadd_rn((double)ls.s, (double)ls.c)));
-                seg_reduce(v, tg, lane, add, [&](uint32_t k, F2 val, int kind) {
+                seg_reduce<EPL>(v, tg, lane, add, [&](uint32_t k, F2 val, int kind) {
                     if (kind == EMIT_COMPLETE) {
-                        s.acc[my_id[k - tg.k0]] = __dadd_rn((double)val.s, (double)val.c);
+                        s.acc[vid(k, k - tg.k0)] = __dadd_rn((double)val.s, (double)val.c);
                     } else {
                         float* p = (kind == EMIT_HEAD) ? s.head_part32 : s.tail_part32;
                         p[2u * t] = val.s;
@@ -660,18 +750,25 @@ __global__ void __launch_bounds__(PULL_THREADS) pull_kernel(DevGraph g, DevState
                     }
                 });
             } else {
-                double v[4];
+                double v[EPL];
 #pragma unroll
-                for (int q = 0; q < 4; ++q)
+                for (int q = 0; q < EPL; ++q)
                     v[q] = (sa[q] != NONE32) ? ld_ro_f64(s.rank + sa[q]) : 0.0;
-                TileGeo tg;
-                tile_geometry(g, t, in.k0, in.kend, lane, tg,
-                              [&](uint32_t slot, uint32_t k) { my_id[slot] = g.dst_id[k]; });
+                TileGeo<EPL> tg;
+                tile_geometry<EPL>(g, base, last_tile, in.k0, in.kend, lane, heads, tg,
+                                   [&](uint32_t slot, uint32_t k) {
+                                       if (slot < TAB)
+                                           my_id[slot] = g.dst_id[k];
+                                   });
                 dsts += tg.ndst;
-                psum = __dadd_rn(psum, warp_sum_f64(__dadd_rn(__dadd_rn(v[0], v[1]), __dadd_rn(v[2], v[3]))));
-                seg_reduce(v, tg, lane, AddF64(), [&](uint32_t k, double val, int kind) {
+                double ls = __dadd_rn(__dadd_rn(v[0], v[1]), __dadd_rn(v[2], v[3]));
+#pragma unroll
+                for (int q = 4; q < EPL; q += 4)
+                    ls = __dadd_rn(ls, __dadd_rn(__dadd_rn(v[q], v[q + 1]), __dadd_rn(v[q + 2], v[q + 3])));
+                psum = __dadd_rn(psum, warp_sum_f64(ls));
+                seg_reduce<EPL>(v, tg, lane, AddF64(), [&](uint32_t k, double val, int kind) {
                     if (kind == EMIT_COMPLETE)
-                        s.acc[my_id[k - tg.k0]] = val;
+                        s.acc[vid(k, k - tg.k0)] = val;
                     else if (kind == EMIT_HEAD)
                         s.head_part[t] = val;
                     else
@@ -923,8 +1020,8 @@ __global__ void advance_kernel(DevGraph g, DevState s, uint32_t app)
         fb[i] = 0u;
 }
 
-// execution_initialize_{bfs,cc,sssp} bulk part
-__global__ void init_kernel(DevGraph g, DevState s, uint32_t app)
+// execution_initialize_{bfs,cc,sssp} bulk part; topen = BFS pull tiles
+__global__ void init_kernel(DevGraph g, DevState s, uint32_t app, uint32_t topen)
 {
     const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
     const uint64_t tid = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
@@ -952,6 +1049,13 @@ __global__ void init_kernel(DevGraph g, DevState s, uint32_t app)
         const uint64_t vwords = ((uint64_t)g.Vne + 31) / 32;
         for (uint64_t i = tid; i < vwords; i += stride)
             s.vis_c[i] = 0u;
+    }
+    if (s.tile_open) {
+        const uint64_t owords = ((uint64_t)topen + 31) / 32;
+        for (uint64_t i = tid; i < owords; i += stride) {
+            const uint64_t left = (uint64_t)topen - i * 32;
+            s.tile_open[i] = left >= 32 ? FULL : ((1u << left) - 1u);
+        }
     }
 }
 
@@ -1169,7 +1273,7 @@ __global__ void export_outdeg_kernel(DevGraph g, unsigned long long* out)
 int compute_grids(wedge_graph* h)
 {
     int blocks = 0;
-    WEDGE_CHECK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, pull_kernel<WEDGE_APP_CC>, PULL_THREADS, 0));
+    WEDGE_CHECK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, pull_kernel<WEDGE_APP_CC, PullEpl<WEDGE_APP_CC>::value>, PULL_THREADS, 0));
     if (blocks < 1)
         blocks = 1;
     h->pull_grid = (uint32_t)(h->num_sms * blocks);
@@ -1224,7 +1328,8 @@ static int ensure_state(wedge_graph* h, int app, int precision)
             (rc = dalloc(h, &s.items, V + g.E / PIECE + 2, true)))
             return rc;
         if (app == WEDGE_APP_BFS) {
-            if ((rc = dalloc(h, &s.front1, nwords, true)) || (rc = dalloc(h, &s.vis_c, (uint64_t)g.Vne / 32 + 2, true)))
+            if ((rc = dalloc(h, &s.front1, nwords, true)) || (rc = dalloc(h, &s.vis_c, (uint64_t)g.Vne / 32 + 2, true)) ||
+                (rc = dalloc(h, &s.tile_open, (uint64_t)g.T / 32 + 2, true)))
                 return rc;
         }
     }
@@ -1240,16 +1345,16 @@ static void launch_pull(wedge_graph* h, int app)
     const uint32_t grid = h->pull_grid;
     switch (app) {
     case WEDGE_APP_BFS:
-        pull_kernel<WEDGE_APP_BFS><<<grid, PULL_THREADS, 0, h->stream>>>(h->g, h->s, counters(h));
+        pull_kernel<WEDGE_APP_BFS, PullEpl<WEDGE_APP_BFS>::value><<<grid, PULL_THREADS, 0, h->stream>>>(h->g, h->s, counters(h));
         break;
     case WEDGE_APP_CC:
-        pull_kernel<WEDGE_APP_CC><<<grid, PULL_THREADS, 0, h->stream>>>(h->g, h->s, counters(h));
+        pull_kernel<WEDGE_APP_CC, PullEpl<WEDGE_APP_CC>::value><<<grid, PULL_THREADS, 0, h->stream>>>(h->g, h->s, counters(h));
         break;
     case WEDGE_APP_SSSP:
-        pull_kernel<WEDGE_APP_SSSP><<<grid, PULL_THREADS, 0, h->stream>>>(h->g, h->s, counters(h));
+        pull_kernel<WEDGE_APP_SSSP, PullEpl<WEDGE_APP_SSSP>::value><<<grid, PULL_THREADS, 0, h->stream>>>(h->g, h->s, counters(h));
         break;
     default:
-        pull_kernel<WEDGE_APP_PR><<<grid, PULL_THREADS, 0, h->stream>>>(h->g, h->s, counters(h));
+        pull_kernel<WEDGE_APP_PR, PullEpl<WEDGE_APP_PR>::value><<<grid, PULL_THREADS, 0, h->stream>>>(h->g, h->s, counters(h));
         break;
     }
 }
@@ -1271,7 +1376,8 @@ static void launch_tail(wedge_graph* h, int app)
 static void launch_init(wedge_graph* h, int app, uint64_t root, uint32_t sched, unsigned long long thr, uint32_t max_iter)
 {
     const uint64_t work = h->g.V > h->g.T ? h->g.V : h->g.T;
-    init_kernel<<<aux_grid(h, work), AUX_THREADS, 0, h->stream>>>(h->g, h->s, (uint32_t)app);
+    const uint32_t topen = (uint32_t)((h->g.E + 32u * PullEpl<WEDGE_APP_BFS>::value - 1) / (32u * PullEpl<WEDGE_APP_BFS>::value));
+    init_kernel<<<aux_grid(h, work), AUX_THREADS, 0, h->stream>>>(h->g, h->s, (uint32_t)app, topen);
     init_root_kernel<<<aux_grid(h, h->g.Vne), AUX_THREADS, 0, h->stream>>>(h->g, h->s, (uint32_t)app, root, sched, thr,
                                                                            max_iter);
     collect_kernel<<<aux_grid(h, (h->g.V + 31) / 32), AUX_THREADS, 0, h->stream>>>(h->g, h->s, (uint32_t)app);
@@ -1814,7 +1920,7 @@ static int noalloc_setup(int dev, NoAllocScratch** sc, uint32_t* grid)
         if (e == cudaSuccess)
             e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
         if (e == cudaSuccess)
-            e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, pull_kernel<WEDGE_APP_PR>, PULL_THREADS, 0);
+            e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, pull_kernel<WEDGE_APP_PR, PullEpl<WEDGE_APP_PR>::value>, PULL_THREADS, 0);
         if (e != cudaSuccess) {
             rc = cuda_status(e);
         } else {
@@ -1888,7 +1994,7 @@ extern "C" int wedge_cuda_pr_iteration_noalloc(uint64_t num_vertices, uint64_t n
     DevState sp = s;
     sp.rank = (double*)rank_in; /* gathered by the pull */
     if (T)
-        pull_kernel<WEDGE_APP_PR><<<grid, PULL_THREADS, 0, st>>>(g, sp, sc->block_cnt);
+        pull_kernel<WEDGE_APP_PR, PullEpl<WEDGE_APP_PR>::value><<<grid, PULL_THREADS, 0, st>>>(g, sp, sc->block_cnt);
     else
         WEDGE_CHECK(cudaMemsetAsync(sc->block_part, 0, sizeof(double), st));
     noalloc_finish_kernel<<<grid_for((uint64_t)T * 32 + 1, AUX_THREADS, grid * 2u), AUX_THREADS, 0, st>>>(

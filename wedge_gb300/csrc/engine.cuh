@@ -7,8 +7,8 @@
 //   dst_id[Vne]    vertex id of compressed destination k (only vertices with
 //                  in-degree > 0 are listed, ascending)
 //   dst_off[Vne+1] first edge of compressed destination k
-//   tile_dst0[T+1] compressed destination owning the first edge of tile t
-//                  (tile_dst0[T] = Vne)
+//   tile_dst0[T+1] compressed destination owning edge 128*t (Vne where that
+//                  edge is padding); pull tiles of 32*EPL edges index it with a stride
 //   outdeg[V]      out-degree (graphdata.c:430-490)
 //   csri_off[V+1], csri[E]  for every source, the Wedge chunk (32 in-edges)
 //                  holding each of its out-edges (the CSRI of graphdata.c:493-585)
@@ -25,7 +25,8 @@
 
 namespace wedge {
 
-constexpr uint32_t TILE = 128;
+constexpr uint32_t TILE = 128;          // granularity of the tile index (tile_dst0)
+constexpr uint32_t MAX_TILE_E = 512;    // largest pull tile; E is padded to a multiple of it
 constexpr uint32_t CHUNK = 32;
 constexpr uint32_t CHUNKS_PER_TILE = TILE / CHUNK;        // 4
 constexpr uint32_t TILES_PER_WORD = 32 / CHUNKS_PER_TILE;  // 8 tiles per 32-bit chunk-bitmap word
@@ -116,6 +117,7 @@ struct DevState {
     uint32_t* front0;              // V-bit frontier bitmaps (active / snapshot)
     uint32_t* front1;
     uint32_t* vis_c;               // Vne-bit visited bitmap (BFS)
+    uint32_t* tile_open;           // T-bit: tile still has an unvisited destination (BFS)
     uint32_t* chunk_bits;          // Wedge frontier: one bit per chunk
     uint32_t* summary;             // one bit per region of REGION_WORDS chunk words (any chunk marked)
     uint2* items;                  // (vertex, piece) Wedge-build work items

@@ -66,14 +66,14 @@ static int fetch(RecordReader& r, void* dst, uint64_t bytes)
 
 static int alloc_edges(uint64_t E, bool weighted, uint32_t** src, uint32_t** dst, unsigned long long** w)
 {
-    const uint64_t Epad = (E + TILE - 1) / TILE * TILE;
+    const uint64_t Epad = (E + MAX_TILE_E - 1) / MAX_TILE_E * MAX_TILE_E;
     *src = nullptr;
     *dst = nullptr;
     *w = nullptr;
-    WEDGE_CHECK(cudaMalloc((void**)src, (Epad ? Epad : TILE) * sizeof(uint32_t)));
+    WEDGE_CHECK(cudaMalloc((void**)src, (Epad ? Epad : MAX_TILE_E) * sizeof(uint32_t)));
     WEDGE_CHECK(cudaMalloc((void**)dst, (E ? E : 1) * sizeof(uint32_t)));
     if (weighted)
-        WEDGE_CHECK(cudaMalloc((void**)w, (Epad ? Epad : TILE) * sizeof(unsigned long long)));
+        WEDGE_CHECK(cudaMalloc((void**)w, (Epad ? Epad : MAX_TILE_E) * sizeof(unsigned long long)));
     return WEDGE_OK;
 }
 

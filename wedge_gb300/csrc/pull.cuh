@@ -60,64 +60,75 @@ __device__ __forceinline__ float ld_ro_f32(const float* p)
     return r;
 }
 
-// per-lane geometry of a tile
+// Per-lane geometry of a tile of TILE_E = 32*EPL consecutive in-edges; lane l
+// owns positions [EPL*l, EPL*l + EPL).
+template <int EPL>
 struct TileGeo {
     uint64_t base;
     uint32_t k0;         // compressed destination of position 0
-    uint32_t before;     // heads at positions [1, 4*lane)
-    uint32_t nib;        // heads at the lane's 4 positions (bit 0 for lane 0 = k0 starts at base)
-    bool k0_fresh;       // k0 starts exactly at the tile start
-    bool tail_cont;      // the tile's last destination continues into the next tile
+    uint32_t before;     // destination starts at positions [1, EPL*lane)
+    uint32_t nib;        // starts at the lane's EPL positions (bit 0 for lane 0 = k0 starts at base)
     uint32_t nib_inner;  // nib without the lane-0 position-0 marker
     uint32_t ndst;       // destinations with in-edges in this tile
+    bool k0_fresh;       // k0 starts exactly at the tile start
+    bool tail_cont;      // the tile's last destination continues into the next tile
 };
 
-// Destination ranks inside the tile: position p belongs to compressed
-// destination k0 + (number of destination starts in [1, p]).
-// k0 = tile_dst0[t], kend = tile_dst0[t + 1].  fill(slot, k) is called once for
-// every destination k with in-edges in the tile (slot = k - k0, on some lane) so
-// the caller can stage per-destination data in the warp's shared-memory table;
-// the table is complete after the __syncwarp at the end.
-template <class Fill>
-__device__ __forceinline__ void tile_geometry(const DevGraph& g, uint32_t t, uint32_t k0, uint32_t kend, int lane,
-                                              TileGeo& tg, Fill fill)
+// Destination ranks inside a tile: position p belongs to compressed destination
+// k0 + (number of destination starts in [1, p]).  k0 / kend are the compressed
+// destinations owning the tile's first edge and the next tile's first edge.
+// The starts are collected in the warp's shared `heads` words (EPL words) and
+// prefix-counted with a shuffle scan.  fill(slot, k) is called once for every
+// destination k with in-edges in the tile (slot = k - k0, on some lane) so the
+// caller can stage per-destination data in shared memory; everything is visible
+// after the final __syncwarp.
+template <int EPL, class Fill>
+__device__ __forceinline__ void tile_geometry(const DevGraph& g, uint64_t base, bool last_tile, uint32_t k0,
+                                              uint32_t kend, int lane, uint32_t* heads, TileGeo<EPL>& tg, Fill fill)
 {
-    tg.base = (uint64_t)t * TILE;
+    constexpr uint32_t TILE_E = 32u * EPL;
+    tg.base = base;
     const uint32_t klim = min(kend, g.Vne - 1u);
-    uint32_t h0 = 0, h1 = 0, h2 = 0, h3 = 0;
+    if (lane < EPL)
+        heads[lane] = 0u;
+    __syncwarp();
     for (uint32_t j = k0 + 1u + (uint32_t)lane; j <= klim; j += 32u) {
-        const uint64_t p = g.dst_off[j] - tg.base;
-        if (p < TILE) {
-            const uint32_t b = 1u << (uint32_t)(p & 31u);
-            const uint32_t w = (uint32_t)(p >> 5);
-            h0 |= (w == 0) ? b : 0u;
-            h1 |= (w == 1) ? b : 0u;
-            h2 |= (w == 2) ? b : 0u;
-            h3 |= (w == 3) ? b : 0u;
+        const uint64_t p = g.dst_off[j] - base;
+        if (p < TILE_E) {
+            atomicOr(&heads[(uint32_t)p >> 5], 1u << (uint32_t)(p & 31u));
             fill(j - k0, j);
         }
     }
     if (lane == 0)
         fill(0u, k0);
-    h0 = __reduce_or_sync(FULL, h0);
-    h1 = __reduce_or_sync(FULL, h1);
-    h2 = __reduce_or_sync(FULL, h2);
-    h3 = __reduce_or_sync(FULL, h3);
-    const uint32_t c0 = __popc(h0), c1 = __popc(h1), c2 = __popc(h2), c3 = __popc(h3);
+    __syncwarp();
+    // prefix popcount of the EPL head words
+    const uint32_t hw_own = (lane < EPL) ? heads[lane] : 0u;
+    uint32_t incl = __popc(hw_own);
+#pragma unroll
+    for (int d = 1; d < EPL; d <<= 1) {
+        const uint32_t y = __shfl_up_sync(FULL, incl, d);
+        if (lane >= d)
+            incl += y;
+    }
+    const uint32_t total = __shfl_sync(FULL, incl, EPL - 1);
+    const uint32_t pos0 = (uint32_t)lane * EPL;
+    const uint32_t wi = pos0 >> 5, sh = pos0 & 31u;
+    const uint32_t word = heads[wi];
+    const uint32_t excl_w = __shfl_sync(FULL, incl - __popc(hw_own), (int)wi);
     tg.k0 = k0;
-    tg.k0_fresh = g.dst_off[k0] == tg.base;
-    const uint32_t k_last = k0 + c0 + c1 + c2 + c3;
-    tg.tail_cont = (t + 1u < g.T) && (kend == k_last);
-    tg.ndst = k_last - k0 + 1u;
-    const uint32_t wi = (uint32_t)lane >> 3, sh = ((uint32_t)lane & 7u) << 2;
-    const uint32_t hw = wi == 0 ? h0 : wi == 1 ? h1 : wi == 2 ? h2 : h3;
-    tg.before = (wi > 0 ? c0 : 0u) + (wi > 1 ? c1 : 0u) + (wi > 2 ? c2 : 0u) + __popc(hw & ((1u << sh) - 1u));
-    tg.nib_inner = (hw >> sh) & 0xFu;
+    tg.k0_fresh = g.dst_off[k0] == base;
+    const uint32_t k_last = k0 + total;
+    tg.tail_cont = !last_tile && (kend == k_last);
+    tg.ndst = total + 1u;
+    tg.before = excl_w + __popc(word & ((1u << sh) - 1u));
+    tg.nib_inner = (word >> sh) & ((EPL >= 32) ? FULL : ((1u << EPL) - 1u));
     tg.nib = tg.nib_inner | ((lane == 0 && tg.k0_fresh) ? 1u : 0u);
     __syncwarp();
 }
 
-__device__ __forceinline__ uint32_t pos_dst(const TileGeo& tg, int i)
+template <int EPL>
+__device__ __forceinline__ uint32_t pos_dst(const TileGeo<EPL>& tg, int i)
 {
     return tg.k0 + tg.before + __popc(tg.nib_inner & ((2u << i) - 1u));
 }
@@ -150,13 +161,13 @@ struct AddF2 {
 
 enum : int { EMIT_COMPLETE = 0, EMIT_HEAD = 1, EMIT_TAIL = 2 };
 
-// Segmented reduction of the tile's 128 values; calls emit(k, value, kind)
+// Segmented reduction of the tile's 32*EPL values; calls emit(k, value, kind)
 // once per destination segment, on the lane holding the segment's last
 // position.  kind: EMIT_COMPLETE (all in-edges of k are in this tile),
 // EMIT_HEAD (k began in an earlier tile and ends here), EMIT_TAIL (k
 // continues into the next tile).
-template <class T, class Op, class Emit>
-__device__ __forceinline__ void seg_reduce(const T (&v)[4], const TileGeo& tg, int lane, Op op, Emit emit)
+template <int EPL, class T, class Op, class Emit>
+__device__ __forceinline__ void seg_reduce(const T (&v)[EPL], const TileGeo<EPL>& tg, int lane, Op op, Emit emit)
 {
     const uint32_t nib = tg.nib;
     T run = v[0];
@@ -164,7 +175,7 @@ __device__ __forceinline__ void seg_reduce(const T (&v)[4], const TileGeo& tg, i
     int first_end = -1;
     int last_start = 0;
 #pragma unroll
-    for (int i = 1; i < 4; ++i) {
+    for (int i = 1; i < EPL; ++i) {
         if ((nib >> i) & 1u) {
             if (first_end < 0) {
                 first = run;
@@ -190,7 +201,8 @@ __device__ __forceinline__ void seg_reduce(const T (&v)[4], const TileGeo& tg, i
         const T y = shfl_up(s, d);
         const bool gflag = __shfl_up_sync(FULL, f, d);
         if (lane >= d) {
-            if (!f) s = op(y, s);
+            if (!f)
+                s = op(y, s);
             f = f || gflag;
         }
     }
@@ -202,7 +214,7 @@ __device__ __forceinline__ void seg_reduce(const T (&v)[4], const TileGeo& tg, i
         emit(k, total, (k == tg.k0 && !tg.k0_fresh) ? EMIT_HEAD : EMIT_COMPLETE);
     }
     if (lane == 31 || next_fresh) {
-        const uint32_t k = pos_dst(tg, 3);
+        const uint32_t k = pos_dst(tg, EPL - 1);
         int kind = EMIT_COMPLETE;
         if (lane == 31 && tg.tail_cont)
             kind = EMIT_TAIL;
