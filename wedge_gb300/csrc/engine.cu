@@ -12,6 +12,7 @@
 //   wedge_build_kernel        wedge.c:37-46 (CSRI walk setting frontier bits)
 //   decide_kernel             execution_*.c driver loop: mass reduce, dense/Wedge choice, convergence
 //   run_traversal / run_pr    execution_{bfs,cc,sssp}.c:122-365 / execution_pr.c:396-486
+#include <cub/device/device_radix_sort.cuh>
 #include <cub/device/device_scan.cuh>
 
 #include <pthread.h>
@@ -233,6 +234,106 @@ static int device_scan(wedge_graph* h, const InT* in, OutT* out, uint64_t n, boo
     return WEDGE_OK;
 }
 
+// key of vertex v for the degree order: descending out-degree, then ascending id
+__global__ void degree_key_kernel(const uint32_t* outdeg, uint64_t V, unsigned long long* key)
+{
+    for (uint64_t v = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; v < V; v += (uint64_t)gridDim.x * blockDim.x)
+        key[v] = ((unsigned long long)(~outdeg[v]) << 32) | (unsigned long long)v;
+}
+
+__global__ void permutation_kernel(const unsigned long long* sorted_key, uint64_t V, uint32_t* new2old, uint32_t* old2new)
+{
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < V; i += (uint64_t)gridDim.x * blockDim.x) {
+        const uint32_t old = (uint32_t)(sorted_key[i] & 0xffffffffull);
+        new2old[i] = old;
+        old2new[old] = (uint32_t)i;
+    }
+}
+
+__global__ void relabel_edges_kernel(const uint32_t* src, const uint32_t* dst, uint64_t E, const uint32_t* old2new,
+                                     unsigned long long* key)
+{
+    for (uint64_t e = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; e < E; e += (uint64_t)gridDim.x * blockDim.x)
+        key[e] = ((unsigned long long)old2new[dst[e]] << 32) | old2new[src[e]];
+}
+
+__global__ void unpack_edges_kernel(const unsigned long long* key, uint64_t E, uint32_t* src, uint32_t* dst)
+{
+    for (uint64_t e = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; e < E; e += (uint64_t)gridDim.x * blockDim.x) {
+        src[e] = (uint32_t)(key[e] & 0xffffffffull);
+        dst[e] = (uint32_t)(key[e] >> 32);
+    }
+}
+
+// Degree relabelling: vertices are renumbered by descending out-degree (ties
+// by id), so the sources gathered most often are the lowest ids and share cache
+// lines; edges are renumbered and re-sorted by (destination, source).  The
+// permutations stay on the device: roots are mapped in, results mapped back.
+static int relabel_by_degree(wedge_graph* h, uint64_t V, uint64_t E, uint32_t* d_src, uint32_t* d_dst,
+                             unsigned long long* d_w, uint32_t** new2old, uint32_t** old2new)
+{
+    cudaStream_t st = h->stream;
+    const uint32_t cap = (uint32_t)h->num_sms * 16u;
+    int rc;
+    if ((rc = dalloc(h, new2old, V)) || (rc = dalloc(h, old2new, V)))
+        return rc;
+    uint32_t* deg = nullptr;
+    unsigned long long *vk = nullptr, *vk2 = nullptr;
+    WEDGE_CHECK(cudaMallocAsync((void**)&deg, V * sizeof(uint32_t), st));
+    WEDGE_CHECK(cudaMallocAsync((void**)&vk, V * sizeof(unsigned long long), st));
+    WEDGE_CHECK(cudaMallocAsync((void**)&vk2, V * sizeof(unsigned long long), st));
+    WEDGE_CHECK(cudaMemsetAsync(deg, 0, V * sizeof(uint32_t), st));
+    if (E)
+        outdeg_kernel<<<grid_for(E, AUX_THREADS, cap), AUX_THREADS, 0, st>>>(d_src, E, deg);
+    degree_key_kernel<<<grid_for(V, AUX_THREADS, cap), AUX_THREADS, 0, st>>>(deg, V, vk);
+    {
+        cub::DoubleBuffer<unsigned long long> db(vk, vk2);
+        size_t tb = 0;
+        WEDGE_CHECK(cub::DeviceRadixSort::SortKeys(nullptr, tb, db, (long long)V, 0, 64, st));
+        void* tmp = nullptr;
+        WEDGE_CHECK(cudaMallocAsync(&tmp, tb ? tb : 1, st));
+        WEDGE_CHECK(cub::DeviceRadixSort::SortKeys(tmp, tb, db, (long long)V, 0, 64, st));
+        cudaFreeAsync(tmp, st);
+        permutation_kernel<<<grid_for(V, AUX_THREADS, cap), AUX_THREADS, 0, st>>>(db.Current(), V, *new2old, *old2new);
+    }
+    cudaFreeAsync(deg, st);
+    cudaFreeAsync(vk, st);
+    cudaFreeAsync(vk2, st);
+    if (E == 0)
+        return WEDGE_OK;
+    int vbits = 1;
+    while (vbits < 32 && (1ull << vbits) < V)
+        ++vbits;
+    unsigned long long *ek = nullptr, *ek2 = nullptr, *w2 = nullptr;
+    WEDGE_CHECK(cudaMallocAsync((void**)&ek, E * sizeof(unsigned long long), st));
+    WEDGE_CHECK(cudaMallocAsync((void**)&ek2, E * sizeof(unsigned long long), st));
+    relabel_edges_kernel<<<grid_for(E, AUX_THREADS, cap), AUX_THREADS, 0, st>>>(d_src, d_dst, E, *old2new, ek);
+    cub::DoubleBuffer<unsigned long long> kb(ek, ek2);
+    size_t tb = 0;
+    void* tmp = nullptr;
+    if (d_w) {
+        WEDGE_CHECK(cudaMallocAsync((void**)&w2, E * sizeof(unsigned long long), st));
+        cub::DoubleBuffer<unsigned long long> vb(d_w, w2);
+        WEDGE_CHECK(cub::DeviceRadixSort::SortPairs(nullptr, tb, kb, vb, (long long)E, 0, 32 + vbits, st));
+        WEDGE_CHECK(cudaMallocAsync(&tmp, tb ? tb : 1, st));
+        WEDGE_CHECK(cub::DeviceRadixSort::SortPairs(tmp, tb, kb, vb, (long long)E, 0, 32 + vbits, st));
+        if (vb.Current() != d_w)
+            WEDGE_CHECK(cudaMemcpyAsync(d_w, vb.Current(), E * sizeof(unsigned long long), cudaMemcpyDeviceToDevice, st));
+    } else {
+        WEDGE_CHECK(cub::DeviceRadixSort::SortKeys(nullptr, tb, kb, (long long)E, 0, 32 + vbits, st));
+        WEDGE_CHECK(cudaMallocAsync(&tmp, tb ? tb : 1, st));
+        WEDGE_CHECK(cub::DeviceRadixSort::SortKeys(tmp, tb, kb, (long long)E, 0, 32 + vbits, st));
+    }
+    unpack_edges_kernel<<<grid_for(E, AUX_THREADS, cap), AUX_THREADS, 0, st>>>(kb.Current(), E, d_src, d_dst);
+    cudaFreeAsync(tmp, st);
+    cudaFreeAsync(ek, st);
+    cudaFreeAsync(ek2, st);
+    if (w2)
+        cudaFreeAsync(w2, st);
+    WEDGE_CHECK(cudaGetLastError());
+    return WEDGE_OK;
+}
+
 // Builds the device CSC from destination-sorted device edge arrays.  d_src and
 // d_w (if any) must hold roundup(E, TILE) entries and become owned by the
 // handle; d_dst is consumed and freed.
@@ -263,6 +364,14 @@ int build_from_device_edges(wedge_graph* h, uint64_t V, uint64_t E, uint32_t* d_
     if (herr) {
         cudaFreeAsync(d_dst, st);
         return WEDGE_ERR_FORMAT;
+    }
+    {
+        uint32_t *n2o = nullptr, *o2n = nullptr;
+        int rc = relabel_by_degree(h, V, E, d_src, d_dst, d_w, &n2o, &o2n);
+        if (rc)
+            return rc;
+        g.new2old = n2o;
+        g.old2new = o2n;
     }
 
     // compressed destinations
@@ -444,27 +553,17 @@ __device__ __forceinline__ void load_sources(const DevGraph& g, uint64_t base, u
 }
 
 // The tiles a warp pulls: every tile (dense: static stride, or for BFS the open
-// tiles, 32 per dynamically grabbed word of the open-tile bitmap), or the
-// tiles of the Wedge frontier, found by walking the chunk bitmap one region
-// (REGION_WORDS words) at a time, regions handed out dynamically; a region
-// whose summary bit is clear is skipped without reading its words (the
-// reference's 256-bit emptiness test, phase_edge_pull_bfs.c:244-246).  Walked
-// words are cleared: the pull consumes the frontier (phase_edge_pull_bfs.c:256).
-// Warp-uniform.
+// tiles, 32 per dynamically grabbed word of the open-tile bitmap), or the tiles
+// of the Wedge frontier from the list compact_kernel built.  Warp-uniform.
 struct TileIter {
     uint32_t i, step;      // dense
     uint32_t obits, obase; // BFS dense: open tiles left in the current word, its first tile
-    uint32_t region;       // wedge: region being walked (NONE32 before the first)
-    uint32_t myword;       // this lane's chunk word of the region
-    uint32_t lanes;        // lanes whose words are still to be walked
-    uint32_t word, wlane;  // the word being walked and its lane
 };
 
 template <int EPL>
 __device__ __forceinline__ bool next_tile(const DevGraph& g, const DevState& s, uint32_t mode, uint32_t T, TileIter& it,
                                           int lane, uint32_t& t, uint32_t& cmask)
 {
-    constexpr uint32_t TPW = 32 / EPL;  // tiles per chunk word
     constexpr uint32_t MASK = (EPL >= 32) ? FULL : ((1u << EPL) - 1u);
     if (mode == MODE_DENSE && s.tile_open) {
         while (!it.obits) {
@@ -490,42 +589,15 @@ __device__ __forceinline__ bool next_tile(const DevGraph& g, const DevState& s, 
         it.i += it.step;
         return true;
     }
-    const uint32_t nwords = (g.T + TILES_PER_WORD - 1) / TILES_PER_WORD; /* chunk words (4 per 128 edges / 32) */
-    const uint32_t nregions = (nwords + REGION_WORDS - 1) / REGION_WORDS;
-    for (;;) {
-        if (it.word) {
-            const uint32_t j = (uint32_t)(__ffs(it.word) - 1) / EPL;
-            cmask = (it.word >> (EPL * j)) & MASK;
-            it.word &= ~(MASK << (EPL * j));
-            t = (it.region * REGION_WORDS + it.wlane) * TPW + j;
-            return true;
-        }
-        if (it.lanes) {
-            it.wlane = (uint32_t)(__ffs(it.lanes) - 1);
-            it.lanes &= it.lanes - 1u;
-            it.word = __shfl_sync(FULL, it.myword, (int)it.wlane);
-            continue;
-        }
-        if (it.region != NONE32 && it.myword)
-            s.chunk_bits[it.region * REGION_WORDS + (uint32_t)lane] = 0u;
-        uint32_t r = 0;
-        if (lane == 0)
-            r = atomicAdd(&s.ctrl->region_next, 1u);
-        r = __shfl_sync(FULL, r, 0);
-        if (r >= nregions) {
-            it.region = NONE32;
-            it.myword = 0u;
-            return false;
-        }
-        it.region = r;
-        it.myword = 0u;
-        it.lanes = 0u;
-        if ((s.summary[r >> 5] >> (r & 31u)) & 1u) {
-            const uint32_t wi = r * REGION_WORDS + (uint32_t)lane;
-            it.myword = wi < nwords ? s.chunk_bits[wi] : 0u;
-            it.lanes = __ballot_sync(FULL, it.myword != 0u);
-        }
-    }
+    // Wedge: the (tile, chunk mask) list compact_kernel built from the frontier
+    const uint32_t n = s.ctrl->tiles;
+    if (it.i >= n)
+        return false;
+    const unsigned long long e = s.tile_list[it.i];
+    it.i += it.step;
+    t = (uint32_t)(e >> 32);
+    cmask = (uint32_t)e & MASK;
+    return true;
 }
 
 template <int APP>
@@ -568,7 +640,6 @@ __global__ void __launch_bounds__(PULL_THREADS, WEDGE_PULL_MINB)
     const uint32_t T = (uint32_t)((g.E + TILE_E - 1) / TILE_E); /* tiles holding real in-edges */
     const uint32_t mode = c->mode;
     const uint32_t parity = c->parity;
-    const bool first_cc = (APP == WEDGE_APP_CC) && c->iter == 0u; /* labels still equal vertex ids */
     const uint32_t* cur = cur_front(s, parity);
     uint32_t* nxt = next_front(s, APP, parity);
     uint32_t* my_id = tab_id[wib];
@@ -582,8 +653,6 @@ __global__ void __launch_bounds__(PULL_THREADS, WEDGE_PULL_MINB)
     it.i = gw;
     it.step = nw;
     it.obits = it.obase = 0u;
-    it.region = NONE32;
-    it.myword = it.lanes = it.word = it.wlane = 0u;
     TileIn nextin;
     uint32_t tn, cn;
     bool more = next_tile<EPL>(g, s, mode, T, it, lane, tn, cn);
@@ -640,20 +709,16 @@ __global__ void __launch_bounds__(PULL_THREADS, WEDGE_PULL_MINB)
                 }
             });
         } else if (APP == WEDGE_APP_CC) {
-            // The first pull reads the initial labels, which are the sources' own
-            // ids (execution_cc.c:77): no gather.  Reading an older label than
-            // the in-place one is always allowed in label propagation, so the
-            // fixed point is unchanged.
             uint32_t v[EPL];
 #pragma unroll
             for (int q = 0; q < EPL; ++q)
-                v[q] = (sa[q] != NONE32) ? (first_cc ? sa[q] : s.prop32[sa[q]]) : NONE32;
+                v[q] = (sa[q] != NONE32) ? s.prop32[sa[q]] : NONE32;
             TileGeo<EPL> tg;
             tile_geometry<EPL>(g, base, last_tile, in.k0, in.kend, lane, heads, tg, [&](uint32_t slot, uint32_t k) {
                 if (slot < TAB) {
                     const uint32_t vtx = g.dst_id[k];
                     my_id[slot] = vtx;
-                    my_cur[slot] = first_cc ? vtx : s.prop32[vtx];
+                    my_cur[slot] = s.prop32[vtx];
                 }
             });
             dsts += tg.ndst;
@@ -886,6 +951,7 @@ __global__ void decide_kernel(DevGraph g, DevState s, const unsigned long long* 
         if (app == WEDGE_APP_BFS)
             c->parity ^= 1u;
         c->region_next = 0u;
+        c->tiles = 0u;
         c->items = 0u;
         if (m == 0ull) {
             c->done = 1u;
@@ -1007,6 +1073,66 @@ __global__ void wedge_build_kernel(DevGraph g, DevState s)
     }
 }
 
+// Wedge frontier -> tile list for the next pull.  Each warp takes a region of
+// REGION_WORDS chunk-bitmap words, skips it when its summary bit is clear (the
+// reference skips empty 256-bit frontier groups, phase_edge_pull_bfs.c:244-246),
+// and appends one (tile, chunk mask) entry per tile with a marked chunk -- one
+// atomic per warp -- then clears the words: the pull consumes the frontier
+// (phase_edge_pull_bfs.c:256).  BFS drops tiles already closed (all visited).
+template <int EPL>
+__global__ void compact_kernel(DevGraph g, DevState s)
+{
+    constexpr uint32_t TPW = 32 / EPL;
+    constexpr uint32_t MASK = (EPL >= 32) ? FULL : ((1u << EPL) - 1u);
+    Ctrl* c = s.ctrl;
+    if (c->done || c->mode != MODE_WEDGE)
+        return;
+    const int lane = threadIdx.x & 31;
+    const uint32_t gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const uint32_t nw = (gridDim.x * blockDim.x) >> 5;
+    const uint32_t nwords = (g.T + TILES_PER_WORD - 1) / TILES_PER_WORD;
+    const uint32_t nregions = (nwords + REGION_WORDS - 1) / REGION_WORDS;
+    for (uint32_t r = gw; r < nregions; r += nw) {
+        if (!((s.summary[r >> 5] >> (r & 31u)) & 1u))
+            continue;
+        const uint32_t wi = r * REGION_WORDS + (uint32_t)lane;
+        uint32_t word = wi < nwords ? s.chunk_bits[wi] : 0u;
+        if (word && s.tile_open) {
+            // tiles of this word: wi*TPW .. +TPW (TPW <= 32 of them, all in one open word)
+            const uint32_t t0 = wi * TPW;
+            const uint32_t open = (s.tile_open[t0 >> 5] >> (t0 & 31u)) & ((TPW >= 32) ? FULL : ((1u << TPW) - 1u));
+#pragma unroll
+            for (uint32_t j = 0; j < TPW; ++j)
+                if (!((open >> j) & 1u))
+                    word &= ~(MASK << (EPL * j));
+        }
+        uint32_t cnt = 0;
+#pragma unroll
+        for (uint32_t j = 0; j < TPW; ++j)
+            cnt += ((word >> (EPL * j)) & MASK) ? 1u : 0u;
+        uint32_t incl = cnt;
+#pragma unroll
+        for (int d = 1; d < 32; d <<= 1) {
+            const uint32_t y = __shfl_up_sync(FULL, incl, d);
+            if (lane >= d)
+                incl += y;
+        }
+        const uint32_t total = __shfl_sync(FULL, incl, 31);
+        uint32_t pos = 0;
+        if (lane == 31 && total)
+            pos = atomicAdd(&c->tiles, total);
+        pos = __shfl_sync(FULL, pos, 31) + incl - cnt;
+#pragma unroll
+        for (uint32_t j = 0; j < TPW; ++j) {
+            const uint32_t m = (word >> (EPL * j)) & MASK;
+            if (m)
+                s.tile_list[pos++] = ((unsigned long long)(wi * TPW + j) << 32) | m;
+        }
+        if (wi < nwords)
+            s.chunk_bits[wi] = 0u;
+    }
+}
+
 // Clear the bitmap the next pull writes (execution_bfs.c:320-338: swap + memset;
 // execution_cc.c:243-277: clear of the active bitmap).
 __global__ void advance_kernel(DevGraph g, DevState s, uint32_t app)
@@ -1029,7 +1155,7 @@ __global__ void init_kernel(DevGraph g, DevState s, uint32_t app, uint32_t topen
         if (app == WEDGE_APP_BFS)
             s.prop32[v] = NONE32; /* execution_bfs.c:106 */
         else if (app == WEDGE_APP_CC)
-            s.prop32[v] = (uint32_t)v; /* execution_cc.c:77 */
+            s.prop32[v] = g.new2old[v]; /* execution_cc.c:77: labels are the caller's vertex ids */
         else
             s.prop64[v] = (g.weight_kind == WEDGE_WEIGHTS_F64) ? 0x7FF0000000000000ull : NONE64; /* execution_sssp.c:78 */
     }
@@ -1061,10 +1187,11 @@ __global__ void init_kernel(DevGraph g, DevState s, uint32_t app, uint32_t topen
 
 // root activation (execution_bfs.c:110-117, execution_sssp.c:83-88) and the
 // control block
-__global__ void init_root_kernel(DevGraph g, DevState s, uint32_t app, uint64_t root, uint32_t sched,
+__global__ void init_root_kernel(DevGraph g, DevState s, uint32_t app, uint64_t root_in, uint32_t sched,
                                  unsigned long long thr, uint32_t max_iter)
 {
     const uint32_t tid = blockIdx.x * blockDim.x + threadIdx.x;
+    const uint64_t root = g.old2new[root_in]; /* the caller's id -> relabelled id */
     if (app == WEDGE_APP_BFS) {
         for (uint32_t k = tid; k < g.Vne; k += gridDim.x * blockDim.x)
             if (g.dst_id[k] == (uint32_t)root)
@@ -1080,6 +1207,7 @@ __global__ void init_root_kernel(DevGraph g, DevState s, uint32_t app, uint64_t 
         c->threshold = thr;
         c->items = 0;
         c->region_next = 0;
+        c->tiles = 0;
         c->iter = 0;
         c->wedge_iters = 0;
         c->done = 0;
@@ -1246,11 +1374,12 @@ __global__ void pr_sum_final_kernel(DevState s, const double* block_out, uint32_
 // graph_vertex_props in the reference's representation (one 64-bit word per vertex)
 __global__ void export_kernel(DevGraph g, DevState s, uint32_t app, unsigned long long* out)
 {
-    for (uint64_t v = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; v < g.V; v += (uint64_t)gridDim.x * blockDim.x) {
+    for (uint64_t o = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; o < g.V; o += (uint64_t)gridDim.x * blockDim.x) {
+        const uint32_t v = g.old2new[o]; /* results come back in the caller's numbering */
         unsigned long long x;
         if (app == WEDGE_APP_BFS) {
             const uint32_t p = s.prop32[v];
-            x = (p == NONE32) ? NONE64 : (unsigned long long)p;
+            x = (p == NONE32) ? NONE64 : (unsigned long long)g.new2old[p];
         } else if (app == WEDGE_APP_CC) {
             x = (unsigned long long)__double_as_longlong((double)s.prop32[v]);
         } else if (app == WEDGE_APP_SSSP) {
@@ -1258,14 +1387,14 @@ __global__ void export_kernel(DevGraph g, DevState s, uint32_t app, unsigned lon
         } else {
             x = (unsigned long long)__double_as_longlong(s.precision == WEDGE_PREC_FP32C ? (double)s.rank32[v] : s.rank[v]);
         }
-        out[v] = x;
+        out[o] = x;
     }
 }
 
 __global__ void export_outdeg_kernel(DevGraph g, unsigned long long* out)
 {
-    for (uint64_t v = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; v < g.V; v += (uint64_t)gridDim.x * blockDim.x)
-        out[v] = g.outdeg[v];
+    for (uint64_t o = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; o < g.V; o += (uint64_t)gridDim.x * blockDim.x)
+        out[o] = g.outdeg[g.old2new[o]];
 }
 
 /* ================================================================ host */
@@ -1325,6 +1454,7 @@ static int ensure_state(wedge_graph* h, int app, int precision)
         if ((rc = dalloc(h, &s.front0, nwords, true)) ||
             (rc = dalloc(h, &s.chunk_bits, (uint64_t)g.T / TILES_PER_WORD + REGION_WORDS + 2, true)) ||
             (rc = dalloc(h, &s.summary, (uint64_t)g.T / TILES_PER_REGION / 32 + 2, true)) ||
+            (rc = dalloc(h, &s.tile_list, (uint64_t)g.T + 1, true)) ||
             (rc = dalloc(h, &s.items, V + g.E / PIECE + 2, true)))
             return rc;
         if (app == WEDGE_APP_BFS) {
@@ -1364,12 +1494,26 @@ static uint32_t aux_grid(wedge_graph* h, uint64_t work)
     return grid_for(work, AUX_THREADS, (uint32_t)h->num_sms * 8u);
 }
 
+// Wedge frontier -> tile list, with the tile size of the application's pull
+static void launch_compact(wedge_graph* h, int app)
+{
+    const uint64_t regions = ((uint64_t)h->g.T / TILES_PER_WORD + REGION_WORDS) / REGION_WORDS;
+    const uint32_t grid = aux_grid(h, regions * 32);
+    if (app == WEDGE_APP_BFS)
+        compact_kernel<PullEpl<WEDGE_APP_BFS>::value><<<grid, AUX_THREADS, 0, h->stream>>>(h->g, h->s);
+    else if (app == WEDGE_APP_CC)
+        compact_kernel<PullEpl<WEDGE_APP_CC>::value><<<grid, AUX_THREADS, 0, h->stream>>>(h->g, h->s);
+    else
+        compact_kernel<PullEpl<WEDGE_APP_SSSP>::value><<<grid, AUX_THREADS, 0, h->stream>>>(h->g, h->s);
+}
+
 // iteration tail after a pull: mass/convergence, Wedge frontier, bitmap reset
 static void launch_tail(wedge_graph* h, int app)
 {
     decide_kernel<<<1, AUX_THREADS, 0, h->stream>>>(h->g, h->s, counters(h), h->pull_grid, (uint32_t)app);
     collect_kernel<<<aux_grid(h, (h->g.V + 31) / 32), AUX_THREADS, 0, h->stream>>>(h->g, h->s, (uint32_t)app);
     wedge_build_kernel<<<h->build_grid, AUX_THREADS, 0, h->stream>>>(h->g, h->s);
+    launch_compact(h, app);
     advance_kernel<<<aux_grid(h, (h->g.V + 31) / 32), AUX_THREADS, 0, h->stream>>>(h->g, h->s, (uint32_t)app);
 }
 
@@ -1382,6 +1526,7 @@ static void launch_init(wedge_graph* h, int app, uint64_t root, uint32_t sched, 
                                                                            max_iter);
     collect_kernel<<<aux_grid(h, (h->g.V + 31) / 32), AUX_THREADS, 0, h->stream>>>(h->g, h->s, (uint32_t)app);
     wedge_build_kernel<<<h->build_grid, AUX_THREADS, 0, h->stream>>>(h->g, h->s);
+    launch_compact(h, app);
     advance_kernel<<<aux_grid(h, (h->g.V + 31) / 32), AUX_THREADS, 0, h->stream>>>(h->g, h->s, (uint32_t)app);
 }
 
@@ -1452,7 +1597,7 @@ static int run_traversal(wedge_graph* h, int app, const wedge_params_t* p, wedge
     }
     WEDGE_CHECK(cudaEventRecord(h->ev[0], h->stream));
     launch_init(h, app, root, (uint32_t)p->sched, thr, (uint32_t)cap);
-    launches += 5;
+    launches += 6;
     Ctrl c;
     if (use_graph) {
         WEDGE_CHECK(cudaGraphLaunch(h->graph_exec, h->stream));
@@ -1469,7 +1614,7 @@ static int run_traversal(wedge_graph* h, int app, const wedge_params_t* p, wedge
             WEDGE_CHECK(cudaEventRecord(h->ev[3], h->stream));
             launch_tail(h, app);
             WEDGE_CHECK(cudaEventRecord(h->ev[4], h->stream));
-            launches += 5;
+            launches += 6;
             WEDGE_CHECK(cudaEventSynchronize(h->ev[4]));
             float a = 0, b = 0;
             cudaEventElapsedTime(&a, h->ev[2], h->ev[3]);
@@ -1490,7 +1635,7 @@ static int run_traversal(wedge_graph* h, int app, const wedge_params_t* p, wedge
             for (int b = 0; b < 3; ++b) {
                 launch_pull(h, app);
                 launch_tail(h, app);
-                launches += 5;
+                launches += 6;
             }
             int rc = read_ctrl(h, &c);
             if (rc)
@@ -1521,7 +1666,7 @@ static int run_traversal(wedge_graph* h, int app, const wedge_params_t* p, wedge
         st->edges_scanned = c.edges_scanned;
         st->tiles_scanned = c.tiles_scanned;
         st->pull_launches = c.pull_launches;
-        st->kernel_launches = use_graph ? (uint64_t)5 + 6ull * c.iter : launches;
+        st->kernel_launches = use_graph ? (uint64_t)6 + 7ull * c.iter : launches;
     }
     if (c.not_converged)
         return WEDGE_ERR_NOT_CONVERGED;
@@ -1706,6 +1851,7 @@ int wedge_cuda_run_phase(wedge_graph_t* g, int app, int phase, const wedge_param
             return WEDGE_ERR_UNSUPPORTED;
         collect_kernel<<<aux_grid(g, (dg.V + 31) / 32), AUX_THREADS, 0, g->stream>>>(dg, g->s, (uint32_t)app);
         wedge_build_kernel<<<g->build_grid, AUX_THREADS, 0, g->stream>>>(dg, g->s);
+        launch_compact(g, app);
         break;
     case WEDGE_PHASE_ADVANCE:
         if (app == WEDGE_APP_PR)

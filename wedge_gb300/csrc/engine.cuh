@@ -68,7 +68,8 @@ struct Ctrl {
     unsigned long long dsts_scanned;   // destinations in visited tiles
     unsigned long long activated;      // vertices activated by pulls
     unsigned int items;                // Wedge-build work items appended by the last pull
-    unsigned int region_next;          // next Wedge-frontier region a warp takes (dynamic schedule)
+    unsigned int region_next;          // next open-tile word a warp takes (BFS dense, dynamic schedule)
+    unsigned int tiles;                // length of the Wedge tile list
     unsigned int mode;                 // MODE_DENSE / MODE_WEDGE for the next pull
     unsigned int iter;                 // completed pulls
     unsigned int wedge_iters;          // pulls that used the Wedge frontier
@@ -100,6 +101,8 @@ struct DevGraph {
     const uint32_t* split_k;   // compressed destinations whose in-edges span tiles
     const uint32_t* split_t0;  // their first tile
     const uint32_t* split_t1;  // their last tile
+    const uint32_t* new2old;   // degree relabelling: engine id -> caller's id
+    const uint32_t* old2new;   // caller's id -> engine id
 };
 
 // Mutable per-traversal state, passed to kernels by value.
@@ -120,6 +123,7 @@ struct DevState {
     uint32_t* tile_open;           // T-bit: tile still has an unvisited destination (BFS)
     uint32_t* chunk_bits;          // Wedge frontier: one bit per chunk
     uint32_t* summary;             // one bit per region of REGION_WORDS chunk words (any chunk marked)
+    unsigned long long* tile_list; // (tile << 32 | chunk mask) of the next Wedge pull
     uint2* items;                  // (vertex, piece) Wedge-build work items
     Ctrl* ctrl;
     IterRec* log;                  // [LOG_CAP] per-iteration records
