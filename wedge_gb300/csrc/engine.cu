@@ -25,7 +25,7 @@
 
 namespace wedge {
 
-constexpr int PULL_THREADS = 256;
+constexpr int PULL_THREADS = 1024; /* one block per SM: its shared memory holds the hub cache */
 constexpr int AUX_THREADS = 256;
 
 int compute_grids(wedge_graph* h);
@@ -482,9 +482,12 @@ template <int APP>
 struct PullEpl {
     static constexpr int value = 8;
 };
+#ifndef WEDGE_EPL_CC
+#define WEDGE_EPL_CC 16
+#endif
 template <>
 struct PullEpl<WEDGE_APP_CC> {
-    static constexpr int value = 16;
+    static constexpr int value = WEDGE_EPL_CC;
 };
 template <>
 struct PullEpl<WEDGE_APP_PR> {
@@ -495,7 +498,8 @@ struct PullEpl<WEDGE_APP_PR> {
 // overlaps the previous tile's work.
 struct TileIn {
     uint32_t t, cmask, k0, kend, visw;
-    bool open;
+    bool open;     // some destination of the tile is not finished
+    bool anydone;  // some destination of the tile is finished (its in-edges need no gathers)
 };
 
 template <int APP, int EPL>
@@ -508,13 +512,15 @@ __device__ __forceinline__ void tile_prefetch(const DevGraph& g, const DevState&
     in.k0 = g.tile_dst0[(uint64_t)t * Q];
     in.kend = g.tile_dst0[((uint64_t)t + 1) * Q];
     in.open = true;
+    in.anydone = false;
     in.visw = 0u;
-    if (APP == WEDGE_APP_BFS) {
-        // skip a tile whose destinations are all visited (the reference's jump over
-        // converged vertices, phase_edge_pull_bfs.c:189-204)
+    if (APP == WEDGE_APP_BFS || APP == WEDGE_APP_CC) {
+        // skip a tile whose destinations are all finished: visited (BFS; the
+        // reference's jump over converged vertices, phase_edge_pull_bfs.c:189-204)
+        // or holding label 0, the smallest label there is (CC)
         const uint32_t klim = min(in.kend, g.Vne - 1u);
         const uint32_t w0 = in.k0 >> 5, w1 = klim >> 5;
-        bool open = false;
+        bool open = false, done = false;
         uint32_t visw = 0u;
         if ((uint32_t)lane <= w1 - w0) {
             const uint32_t wi = w0 + lane;
@@ -523,32 +529,52 @@ __device__ __forceinline__ void tile_prefetch(const DevGraph& g, const DevState&
             const uint32_t range = (hi == 31u ? FULL : ((2u << hi) - 1u)) & ~((1u << lo) - 1u);
             visw = s.vis_c[wi];
             open = (~visw & range) != 0u;
+            done = (visw & range) != 0u;
         }
         in.visw = visw;
         in.open = __any_sync(FULL, open);
-        if (!in.open && lane == 0)
+        in.anydone = __any_sync(FULL, done);
+        if (APP == WEDGE_APP_BFS && !in.open && lane == 0)
             atomicAnd(&s.tile_open[t >> 5], ~(1u << (t & 31u))); /* closed for good */
     }
 }
 
 // EPL consecutive sources of this lane (positions EPL*lane ..), NONE32 where the
-// lane's chunk is not in the mask; L1-cached vector loads, so the lanes of a
-// warp together read the tile's 128*EPL bytes once.
+// lane's chunk is not in the mask.  Whole 32-byte sectors per lane (256-bit
+// loads) for EPL >= 8, one 128-bit load for EPL = 4: each sector of the tile
+// is requested once, with no reliance on L1 reuse.
 template <int EPL>
 __device__ __forceinline__ void load_sources(const DevGraph& g, uint64_t base, uint32_t cmask, int lane,
                                              uint32_t (&sa)[EPL])
 {
     const bool on = (cmask >> (((uint32_t)lane * EPL) >> 5)) & 1u;
-    const uint4* p = reinterpret_cast<const uint4*>(g.src + base + (uint64_t)lane * EPL);
+    const uint32_t* p = g.src + base + (uint64_t)lane * EPL;
+    if constexpr (EPL % 8 == 0) {
 #pragma unroll
-    for (int q = 0; q < EPL / 4; ++q) {
-        uint4 x = make_uint4(NONE32, NONE32, NONE32, NONE32);
-        if (on)
-            x = __ldg(p + q);
-        sa[4 * q + 0] = x.x;
-        sa[4 * q + 1] = x.y;
-        sa[4 * q + 2] = x.z;
-        sa[4 * q + 3] = x.w;
+        for (int q = 0; q < EPL / 8; ++q) {
+            uint32_t x[8];
+            if (on) {
+                ld_stream_v8(p + 8 * q, x);
+            } else {
+#pragma unroll
+                for (int j = 0; j < 8; ++j)
+                    x[j] = NONE32;
+            }
+#pragma unroll
+            for (int j = 0; j < 8; ++j)
+                sa[8 * q + j] = x[j];
+        }
+    } else {
+#pragma unroll
+        for (int q = 0; q < EPL / 4; ++q) {
+            uint4 x = make_uint4(NONE32, NONE32, NONE32, NONE32);
+            if (on)
+                x = __ldg(reinterpret_cast<const uint4*>(p) + q);
+            sa[4 * q + 0] = x.x;
+            sa[4 * q + 1] = x.y;
+            sa[4 * q + 2] = x.z;
+            sa[4 * q + 3] = x.w;
+        }
     }
 }
 
@@ -557,24 +583,27 @@ __device__ __forceinline__ void load_sources(const DevGraph& g, uint64_t base, u
 // of the Wedge frontier from the list compact_kernel built.  Warp-uniform.
 struct TileIter {
     uint32_t i, step;      // dense
-    uint32_t obits, obase; // BFS dense: open tiles left in the current word, its first tile
+    uint32_t obits, obase; // BFS dense: open tiles left in the current unit, its first tile
 };
 
+constexpr uint32_t OPEN_UNIT = 8; /* tiles a warp takes per grab of the open-tile bitmap */
+
 template <int EPL>
-__device__ __forceinline__ bool next_tile(const DevGraph& g, const DevState& s, uint32_t mode, uint32_t T, TileIter& it,
-                                          int lane, uint32_t& t, uint32_t& cmask)
+__device__ __forceinline__ bool next_tile(const DevGraph& g, const DevState& s, uint32_t mode, uint32_t t_end,
+                                          TileIter& it, int lane, uint32_t& t, uint32_t& cmask)
 {
     constexpr uint32_t MASK = (EPL >= 32) ? FULL : ((1u << EPL) - 1u);
     if (mode == MODE_DENSE && s.tile_open) {
         while (!it.obits) {
-            uint32_t w = 0;
+            uint32_t u = 0;
             if (lane == 0)
-                w = atomicAdd(&s.ctrl->region_next, 1u);
-            w = __shfl_sync(FULL, w, 0);
-            if (w >= (T + 31) / 32)
+                u = atomicAdd(&s.ctrl->region_next, 1u);
+            u = __shfl_sync(FULL, u, 0);
+            if (u >= (t_end + OPEN_UNIT - 1) / OPEN_UNIT)
                 return false;
-            it.obits = s.tile_open[w];
-            it.obase = w * 32;
+            constexpr uint32_t PER_WORD = 32 / OPEN_UNIT;
+            it.obits = (s.tile_open[u / PER_WORD] >> ((u % PER_WORD) * OPEN_UNIT)) & ((1u << OPEN_UNIT) - 1u);
+            it.obase = u * OPEN_UNIT;
         }
         t = it.obase + (uint32_t)(__ffs(it.obits) - 1);
         it.obits &= it.obits - 1u;
@@ -582,7 +611,7 @@ __device__ __forceinline__ bool next_tile(const DevGraph& g, const DevState& s, 
         return true;
     }
     if (mode == MODE_DENSE) {
-        if (it.i >= T)
+        if (it.i >= t_end)
             return false;
         t = it.i;
         cmask = MASK;
@@ -609,17 +638,30 @@ struct CurT<WEDGE_APP_SSSP> {
     using type = unsigned long long;
 };
 
-// resident blocks per SM the register allocation must allow for each pull
-#ifndef WEDGE_PULL_MINB
-#define WEDGE_PULL_MINB 4
-#endif
+// bounded mbarrier probes before a pull gives up on its hub-cache copy
+constexpr uint32_t HUB_WAIT_TRIES = 1u << 20;
+enum : uint32_t { ERR_HUB_TIMEOUT = 2u };
+
+// pull phases: 0 = all tiles; CC/SSSP dense pulls run as two launches,
+// 1 = tiles [0, hub_tile) (the hub destinations), 2 = tiles [hub_tile, T),
+// so the second launch caches hub values that no tile of it can change
+enum : uint32_t { PHASE_ALL = 0, PHASE_HUBS = 1, PHASE_REST = 2 };
+
+__host__ __device__ constexpr bool two_phase_app(int app)
+{
+    return app == WEDGE_APP_CC || app == WEDGE_APP_SSSP;
+}
 
 // Edge pull over all tiles (dense) or over the tiles of the Wedge frontier.
 // block_cnt[NCNT*b + CNT_*] = changed mass, in-edges read, tiles visited,
 // destinations in visited tiles, vertices activated.
+// One 1024-thread block per SM; dynamic shared memory holds the hub cache:
+// elements [0, s.hub_n) of the gathered array (BFS frontier words, CC labels,
+// SSSP distances, PageRank ranks), bulk-copied at the start of the launch.
+// Warps start on global memory and switch to the cache once its copy landed.
 template <int APP, int EPL>
-__global__ void __launch_bounds__(PULL_THREADS, WEDGE_PULL_MINB)
-    pull_kernel(DevGraph g, DevState s, unsigned long long* block_cnt)
+__global__ void __launch_bounds__(PULL_THREADS, 1)
+    pull_kernel(DevGraph g, DevState s, unsigned long long* block_cnt, uint32_t phase)
 {
     constexpr int WARPS = PULL_THREADS / 32;
     constexpr uint32_t TILE_E = 32u * EPL;
@@ -630,15 +672,31 @@ __global__ void __launch_bounds__(PULL_THREADS, WEDGE_PULL_MINB)
     __shared__ uint32_t tab_id[WARPS][TAB];  // vertex id of each destination of the warp's tile
     __shared__ cur_t tab_cur[WARPS][TAB];    // its property before the tile (min apps)
     __shared__ uint32_t sh_heads[WARPS][EPL];
+    __shared__ unsigned long long hub_bar;
+    extern __shared__ __align__(16) unsigned char hub_smem[];
     Ctrl* c = s.ctrl;
     if (c->done)
         return;
+    const uint32_t mode = c->mode;
+    if (phase == PHASE_REST && mode != MODE_DENSE) {
+        // a Wedge pull ran whole in the first launch: this one only reports zeros
+        if (threadIdx.x < 5)
+            block_cnt[NCNT * blockIdx.x + threadIdx.x] = 0ull;
+        return;
+    }
     const int lane = threadIdx.x & 31;
     const int wib = threadIdx.x >> 5;
     const uint32_t gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const uint32_t nw = (gridDim.x * blockDim.x) >> 5;
     const uint32_t T = (uint32_t)((g.E + TILE_E - 1) / TILE_E); /* tiles holding real in-edges */
-    const uint32_t mode = c->mode;
+    uint32_t t_begin = 0, t_end = T;
+    if (two_phase_app(APP) && mode == MODE_DENSE) {
+        const uint32_t split = min(s.hub_tile, T);
+        if (phase == PHASE_HUBS)
+            t_end = split;
+        else
+            t_begin = split;
+    }
     const uint32_t parity = c->parity;
     const uint32_t* cur = cur_front(s, parity);
     uint32_t* nxt = next_front(s, APP, parity);
@@ -649,23 +707,59 @@ __global__ void __launch_bounds__(PULL_THREADS, WEDGE_PULL_MINB)
     double psum = 0.0;
     auto vid = [&](uint32_t k, uint32_t slot) -> uint32_t { return slot < TAB ? my_id[slot] : g.dst_id[k]; };
 
+    // ---- hub cache
+    const bool wide = (APP == WEDGE_APP_SSSP) || (APP == WEDGE_APP_PR && s.precision != WEDGE_PREC_FP32C);
+    const void* hub_src = (APP == WEDGE_APP_BFS)    ? (const void*)cur
+                          : (APP == WEDGE_APP_CC)   ? (const void*)s.prop32
+                          : (APP == WEDGE_APP_SSSP) ? (const void*)s.prop64
+                          : wide                    ? (const void*)s.rank
+                                                    : (const void*)s.rank32;
+    const uint64_t hub_have = ((APP == WEDGE_APP_BFS) ? (g.V + 31) / 32 : g.V) * (wide ? 8u : 4u);
+    const uint64_t hub_fit = hub_have & ~15ull;
+    const uint32_t hub_bytes = (uint64_t)s.hub_bytes < hub_fit ? s.hub_bytes : (uint32_t)hub_fit; /* within smem and the array */
+    bool use_hub = hub_bytes != 0u && ((uintptr_t)hub_src & 15u) == 0u && (smem_u32(hub_smem) & 15u) == 0u;
+    if (APP == WEDGE_APP_BFS)
+        use_hub = use_hub && (mode == MODE_DENSE || c->tiles >= T / 16u);
+    else if (two_phase_app(APP))
+        use_hub = use_hub && mode == MODE_DENSE;
+    uint32_t* hub32 = reinterpret_cast<uint32_t*>(hub_smem);
+    unsigned long long* hub64 = reinterpret_cast<unsigned long long*>(hub_smem);
+    if (use_hub) {
+        if (threadIdx.x == 0) {
+            mbar_init(&hub_bar, 1u);
+            mbar_arrive_expect_tx(&hub_bar, hub_bytes);
+            for (uint32_t off = 0; off < hub_bytes; off += 32768u)
+                bulk_g2s(hub_smem + off, static_cast<const unsigned char*>(hub_src) + off, min(32768u, hub_bytes - off),
+                         &hub_bar);
+        }
+        __syncthreads();
+    }
+    uint32_t hub_lim = 0; /* elements of the cache this warp reads: 0 until the copy completed */
+
     TileIter it;
-    it.i = gw;
+    it.i = t_begin + gw;
     it.step = nw;
     it.obits = it.obase = 0u;
     TileIn nextin;
     uint32_t tn, cn;
-    bool more = next_tile<EPL>(g, s, mode, T, it, lane, tn, cn);
+    bool more = next_tile<EPL>(g, s, mode, t_end, it, lane, tn, cn);
     if (more)
         tile_prefetch<APP, EPL>(g, s, tn, cn, lane, nextin);
     while (more) {
         const TileIn in = nextin;
-        more = next_tile<EPL>(g, s, mode, T, it, lane, tn, cn);
+        more = next_tile<EPL>(g, s, mode, t_end, it, lane, tn, cn);
         if (more)
             tile_prefetch<APP, EPL>(g, s, tn, cn, lane, nextin);
         ++tiles;
         if (!in.open)
             continue;
+        if (use_hub && hub_lim == 0u) {
+            uint32_t ready = 0u;
+            if (lane == 0)
+                ready = mbar_test_wait(&hub_bar, 0u) ? 1u : 0u;
+            if (__shfl_sync(FULL, ready, 0))
+                hub_lim = hub_bytes / (wide ? 8u : 4u);
+        }
         const uint32_t t = in.t;
         const uint64_t base = (uint64_t)t * TILE_E;
         const bool last_tile = (t + 1u >= T);
@@ -676,31 +770,42 @@ __global__ void __launch_bounds__(PULL_THREADS, WEDGE_PULL_MINB)
             edges += (sa[q] != NONE32) ? 1u : 0u;
 
         if (APP == WEDGE_APP_BFS) {
-            // frontier-bit gathers first, then the geometry (their latencies overlap)
-            uint32_t fb[EPL];
-#pragma unroll
-            for (int q = 0; q < EPL; ++q)
-                fb[q] = (sa[q] != NONE32) ? ld_ro_u32(cur + (sa[q] >> 5)) : 0u;
-            TileGeo<EPL> tg;
-            tile_geometry<EPL>(g, base, last_tile, in.k0, in.kend, lane, heads, tg, [&](uint32_t slot, uint32_t k) {
-                if (slot < TAB)
-                    my_id[slot] = g.dst_id[k];
-            });
-            dsts += tg.ndst;
+            // Frontier-bit gathers.  A tile with no visited destination gathers at
+            // once (the latency overlaps the geometry's); otherwise the geometry
+            // comes first and only the in-edges of unvisited destinations gather.
             uint32_t v[EPL];
-            const uint32_t w0 = in.k0 >> 5;
+            auto gather = [&](uint32_t x) -> uint32_t {
+                const uint32_t wi = x >> 5; /* NONE32 >> 5 lies beyond any cache */
+                const uint32_t fb = (wi < hub_lim) ? hub32[wi] : ((x != NONE32) ? ld_ro_u32(cur + wi) : 0u);
+                return ((fb >> (x & 31u)) & 1u) ? x : NONE32;
+            };
+            if (!in.anydone) {
 #pragma unroll
-            for (int q = 0; q < EPL; ++q) {
-                const uint32_t k = pos_dst(tg, q);
-                const uint32_t vw = __shfl_sync(FULL, in.visw, (int)((k >> 5) - w0));
-                const bool visited = (vw >> (k & 31u)) & 1u;
-                v[q] = (sa[q] != NONE32 && !visited && ((fb[q] >> (sa[q] & 31u)) & 1u)) ? sa[q] : NONE32;
+                for (int q = 0; q < EPL; ++q)
+                    v[q] = gather(sa[q]);
             }
-            seg_reduce<EPL>(v, tg, lane, MinU32(), [&](uint32_t k, uint32_t val, int) {
+            TileGeo<EPL> tg;
+            tile_geometry<EPL>(g, base, last_tile, in.k0, in.kend, lane, heads, tg, [](uint32_t, uint32_t) {});
+            dsts += tg.ndst;
+            if (in.anydone) {
+                const uint32_t w0 = in.k0 >> 5;
+#pragma unroll
+                for (int q = 0; q < EPL; ++q) {
+                    const uint32_t k = pos_dst(tg, q);
+                    const uint32_t vw = __shfl_sync(FULL, in.visw, (int)((k >> 5) - w0));
+                    v[q] = gather(((vw >> (k & 31u)) & 1u) ? NONE32 : sa[q]);
+                }
+            }
+            for (uint32_t slot = (uint32_t)lane; slot < min(tg.ndst, TAB); slot += 32u)
+                my_id[slot] = g.dst_id[tg.k0 + slot];
+            __syncwarp();
+            seg_reduce<EPL>(v, tg, lane, MinU32(), [&](uint32_t k, uint32_t val, int kind) {
                 if (val == NONE32)
                     return;
                 const uint32_t vtx = vid(k, k - tg.k0);
-                const uint32_t old = atomicMin(&s.prop32[vtx], val);
+                // a destination whose in-edges all lie in this tile has no other
+                // writer in this pull, and it was unvisited when the tile began
+                const uint32_t old = (kind == EMIT_COMPLETE) ? (s.prop32[vtx] = val, NONE32) : atomicMin(&s.prop32[vtx], val);
                 if (old == NONE32) {
                     atomicOr(&s.vis_c[k >> 5], 1u << (k & 31u));
                     atomicOr(&nxt[vtx >> 5], 1u << (vtx & 31u));
@@ -709,27 +814,54 @@ __global__ void __launch_bounds__(PULL_THREADS, WEDGE_PULL_MINB)
                 }
             });
         } else if (APP == WEDGE_APP_CC) {
+            // Label gathers.  A tile whose destinations all may still drop gathers at
+            // once (the latency overlaps the geometry's); otherwise the geometry
+            // comes first and destinations holding label 0 gather nothing.
             uint32_t v[EPL];
+            auto gather = [&](uint32_t x) -> uint32_t {
+                return (x < hub_lim) ? hub32[x] : ((x != NONE32) ? s.prop32[x] : NONE32);
+            };
+            if (!in.anydone) {
 #pragma unroll
-            for (int q = 0; q < EPL; ++q)
-                v[q] = (sa[q] != NONE32) ? s.prop32[sa[q]] : NONE32;
+                for (int q = 0; q < EPL; ++q)
+                    v[q] = gather(sa[q]);
+            }
             TileGeo<EPL> tg;
-            tile_geometry<EPL>(g, base, last_tile, in.k0, in.kend, lane, heads, tg, [&](uint32_t slot, uint32_t k) {
-                if (slot < TAB) {
-                    const uint32_t vtx = g.dst_id[k];
-                    my_id[slot] = vtx;
-                    my_cur[slot] = s.prop32[vtx];
-                }
-            });
+            tile_geometry<EPL>(g, base, last_tile, in.k0, in.kend, lane, heads, tg, [](uint32_t, uint32_t) {});
             dsts += tg.ndst;
-            seg_reduce<EPL>(v, tg, lane, MinU32(), [&](uint32_t k, uint32_t val, int) {
+            if (in.anydone) {
+                const uint32_t w0 = in.k0 >> 5;
+#pragma unroll
+                for (int q = 0; q < EPL; ++q) {
+                    const uint32_t k = pos_dst(tg, q);
+                    const uint32_t vw = __shfl_sync(FULL, in.visw, (int)((k >> 5) - w0));
+                    v[q] = gather(((vw >> (k & 31u)) & 1u) ? NONE32 : sa[q]);
+                }
+            }
+            for (uint32_t slot = (uint32_t)lane; slot < min(tg.ndst, TAB); slot += 32u) {
+                const uint32_t vtx = g.dst_id[tg.k0 + slot];
+                my_id[slot] = vtx;
+                my_cur[slot] = s.prop32[vtx];
+            }
+            __syncwarp();
+            seg_reduce<EPL>(v, tg, lane, MinU32(), [&](uint32_t k, uint32_t val, int kind) {
                 const uint32_t slot = k - tg.k0;
                 const uint32_t vtx = vid(k, slot);
                 const uint32_t cv = slot < TAB ? (uint32_t)my_cur[slot] : s.prop32[vtx];
                 if (val < cv) {
-                    const uint32_t old = atomicMin(&s.prop32[vtx], val);
-                    if (val < old) {
-                        const uint32_t b = 1u << (vtx & 31u);
+                    if (vtx < hub_lim)
+                        atomicMin(&hub32[vtx], val); /* keeps this block's cache current (hub phase) */
+                    if (val == 0u)
+                        atomicOr(&s.vis_c[k >> 5], 1u << (k & 31u)); /* label 0 is final */
+                    const uint32_t b = 1u << (vtx & 31u);
+                    if (kind == EMIT_COMPLETE) {
+                        // sole writer of vtx in this pull: cv is current and its
+                        // changed bit (cleared before the pull) is still clear
+                        s.prop32[vtx] = val;
+                        atomicOr(&nxt[vtx >> 5], b);
+                        mass += g.outdeg[vtx];
+                        ++act;
+                    } else if (val < atomicMin(&s.prop32[vtx], val)) {
                         if (!(atomicOr(&nxt[vtx >> 5], b) & b)) {
                             mass += g.outdeg[vtx];
                             ++act;
@@ -740,21 +872,22 @@ __global__ void __launch_bounds__(PULL_THREADS, WEDGE_PULL_MINB)
         } else if (APP == WEDGE_APP_SSSP) {
             unsigned long long wv[EPL];
             const bool on = (in.cmask >> (((uint32_t)lane * EPL) >> 5)) & 1u;
-            const ulonglong2* wp = reinterpret_cast<const ulonglong2*>(g.w + base + (uint64_t)lane * EPL);
+            const unsigned long long* wp = g.w + base + (uint64_t)lane * EPL;
 #pragma unroll
-            for (int q = 0; q < EPL / 2; ++q) {
-                ulonglong2 x = make_ulonglong2(0ull, 0ull);
+            for (int q = 0; q < EPL / 4; ++q) {
+                unsigned long long x[4] = {0ull, 0ull, 0ull, 0ull};
                 if (on)
-                    x = __ldg(wp + q);
-                wv[2 * q] = x.x;
-                wv[2 * q + 1] = x.y;
+                    ld_stream_v4u64(wp + 4 * q, x);
+#pragma unroll
+                for (int j = 0; j < 4; ++j)
+                    wv[4 * q + j] = x[j];
             }
             unsigned long long v[EPL];
 #pragma unroll
             for (int q = 0; q < EPL; ++q) {
                 v[q] = NONE64;
                 if (sa[q] != NONE32) {
-                    const unsigned long long d = s.prop64[sa[q]];
+                    const unsigned long long d = (sa[q] < hub_lim) ? hub64[sa[q]] : s.prop64[sa[q]];
                     if (g.weight_kind == WEDGE_WEIGHTS_F64)
                         v[q] = (unsigned long long)__double_as_longlong(
                             __dadd_rn(__longlong_as_double((long long)d), __longlong_as_double((long long)wv[q])));
@@ -771,14 +904,20 @@ __global__ void __launch_bounds__(PULL_THREADS, WEDGE_PULL_MINB)
                 }
             });
             dsts += tg.ndst;
-            seg_reduce<EPL>(v, tg, lane, MinU64(), [&](uint32_t k, unsigned long long val, int) {
+            seg_reduce<EPL>(v, tg, lane, MinU64(), [&](uint32_t k, unsigned long long val, int kind) {
                 const uint32_t slot = k - tg.k0;
                 const uint32_t vtx = vid(k, slot);
                 const unsigned long long cv = slot < TAB ? (unsigned long long)my_cur[slot] : s.prop64[vtx];
                 if (val < cv) {
-                    const unsigned long long old = atomicMin(&s.prop64[vtx], val);
-                    if (val < old) {
-                        const uint32_t b = 1u << (vtx & 31u);
+                    if (vtx < hub_lim)
+                        atomicMin(&hub64[vtx], val);
+                    const uint32_t b = 1u << (vtx & 31u);
+                    if (kind == EMIT_COMPLETE) {
+                        s.prop64[vtx] = val; /* sole writer, as for CC */
+                        atomicOr(&nxt[vtx >> 5], b);
+                        mass += g.outdeg[vtx];
+                        ++act;
+                    } else if (val < atomicMin(&s.prop64[vtx], val)) {
                         if (!(atomicOr(&nxt[vtx >> 5], b) & b)) {
                             mass += g.outdeg[vtx];
                             ++act;
@@ -791,7 +930,10 @@ __global__ void __launch_bounds__(PULL_THREADS, WEDGE_PULL_MINB)
                 F2 v[EPL];
 #pragma unroll
                 for (int q = 0; q < EPL; ++q)
-                    v[q] = F2{(sa[q] != NONE32) ? ld_ro_f32(s.rank32 + sa[q]) : 0.0f, 0.0f};
+                    v[q] = F2{(sa[q] < hub_lim)    ? reinterpret_cast<const float*>(hub_smem)[sa[q]]
+                              : (sa[q] != NONE32) ? ld_ro_f32(s.rank32 + sa[q])
+                                                  : 0.0f,
+                              0.0f};
                 TileGeo<EPL> tg;
                 tile_geometry<EPL>(g, base, last_tile, in.k0, in.kend, lane, heads, tg,
                                    [&](uint32_t slot, uint32_t k) {
@@ -818,7 +960,9 @@ __global__ void __launch_bounds__(PULL_THREADS, WEDGE_PULL_MINB)
                 double v[EPL];
 #pragma unroll
                 for (int q = 0; q < EPL; ++q)
-                    v[q] = (sa[q] != NONE32) ? ld_ro_f64(s.rank + sa[q]) : 0.0;
+                    v[q] = (sa[q] < hub_lim)    ? reinterpret_cast<const double*>(hub_smem)[sa[q]]
+                           : (sa[q] != NONE32) ? ld_ro_f64(s.rank + sa[q])
+                                               : 0.0;
                 TileGeo<EPL> tg;
                 tile_geometry<EPL>(g, base, last_tile, in.k0, in.kend, lane, heads, tg,
                                    [&](uint32_t slot, uint32_t k) {
@@ -842,6 +986,11 @@ __global__ void __launch_bounds__(PULL_THREADS, WEDGE_PULL_MINB)
             }
         }
         __syncwarp(); /* the table is rewritten by the next tile */
+    }
+    // the block may not retire with its bulk copy in flight
+    if (use_hub && threadIdx.x == 0 && !mbar_wait_bounded(&hub_bar, 0u, HUB_WAIT_TRIES)) {
+        atomicOr(&c->error, ERR_HUB_TIMEOUT);
+        mbar_wait_bounded(&hub_bar, 0u, HUB_WAIT_TRIES);
     }
     // per-block counters (no same-address atomics): reduced by decide_kernel
     mass = warp_sum_u64(mass);
@@ -913,7 +1062,7 @@ __device__ __forceinline__ void log_iteration(DevState& s, Ctrl* c, const unsign
     c->tiles_scanned += cnt[CNT_TILES];
     c->dsts_scanned += cnt[CNT_DSTS];
     c->activated += cnt[CNT_ACT];
-    c->pull_launches += 1u;
+    c->pull_launches += two_phase_app((int)s.app) ? 2u : 1u;
     if (c->iter < LOG_CAP) {
         IterRec& r = s.log[c->iter];
         r.mass_in = c->last_mass;
@@ -1192,9 +1341,11 @@ __global__ void init_root_kernel(DevGraph g, DevState s, uint32_t app, uint64_t 
 {
     const uint32_t tid = blockIdx.x * blockDim.x + threadIdx.x;
     const uint64_t root = g.old2new[root_in]; /* the caller's id -> relabelled id */
-    if (app == WEDGE_APP_BFS) {
+    if (app == WEDGE_APP_BFS || app == WEDGE_APP_CC) {
+        // BFS: the root is visited; CC: the vertex the caller numbers 0 holds label 0 already
+        const uint32_t done = (app == WEDGE_APP_BFS) ? (uint32_t)root : g.old2new[0];
         for (uint32_t k = tid; k < g.Vne; k += gridDim.x * blockDim.x)
-            if (g.dst_id[k] == (uint32_t)root)
+            if (g.dst_id[k] == done)
                 atomicOr(&s.vis_c[k >> 5], 1u << (k & 31u));
     }
     if (tid == 0) {
@@ -1266,6 +1417,7 @@ __global__ void pr_init_kernel(DevGraph g, DevState s)
         c->mode = MODE_DENSE;
         c->parity = 0;
         c->region_next = 0;
+        c->error = 0;
         c->pr_total = 0.0;
         c->pr_sum = 0.0;
     }
@@ -1397,6 +1549,23 @@ __global__ void export_outdeg_kernel(DevGraph g, unsigned long long* out)
         out[o] = g.outdeg[g.old2new[o]];
 }
 
+// first tile of the second dense-pull launch: the tile holding the first
+// in-edge of the first destination with id >= hub_n, rounded up, so no tile of
+// that launch writes a cached value (dst_id is ascending)
+__global__ void hub_split_kernel(DevGraph g, uint32_t hub_n, uint32_t tile_e, uint32_t* out)
+{
+    uint32_t lo = 0, hi = g.Vne;
+    while (lo < hi) {
+        const uint32_t mid = lo + (hi - lo) / 2u;
+        if (g.dst_id[mid] < hub_n)
+            lo = mid + 1u;
+        else
+            hi = mid;
+    }
+    const unsigned long long pos = g.dst_off[lo]; /* dst_off[Vne] = E */
+    *out = (uint32_t)((pos + tile_e - 1u) / tile_e);
+}
+
 /* ================================================================ host */
 
 int compute_grids(wedge_graph* h)
@@ -1404,9 +1573,80 @@ int compute_grids(wedge_graph* h)
     int blocks = 0;
     WEDGE_CHECK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, pull_kernel<WEDGE_APP_CC, PullEpl<WEDGE_APP_CC>::value>, PULL_THREADS, 0));
     if (blocks < 1)
-        blocks = 1;
-    h->pull_grid = (uint32_t)(h->num_sms * blocks);
+        return WEDGE_ERR_CUDA;
+    h->pull_grid = (uint32_t)h->num_sms; /* one block per SM: the hub cache takes the SM's shared memory */
     h->build_grid = (uint32_t)h->num_sms * 8u;
+    return WEDGE_OK;
+}
+
+static const void* pull_fn(int app)
+{
+    switch (app) {
+    case WEDGE_APP_BFS:
+        return (const void*)pull_kernel<WEDGE_APP_BFS, PullEpl<WEDGE_APP_BFS>::value>;
+    case WEDGE_APP_CC:
+        return (const void*)pull_kernel<WEDGE_APP_CC, PullEpl<WEDGE_APP_CC>::value>;
+    case WEDGE_APP_SSSP:
+        return (const void*)pull_kernel<WEDGE_APP_SSSP, PullEpl<WEDGE_APP_SSSP>::value>;
+    default:
+        return (const void*)pull_kernel<WEDGE_APP_PR, PullEpl<WEDGE_APP_PR>::value>;
+    }
+}
+
+static uint32_t pull_tile_e(int app)
+{
+    switch (app) {
+    case WEDGE_APP_BFS:
+        return 32u * PullEpl<WEDGE_APP_BFS>::value;
+    case WEDGE_APP_CC:
+        return 32u * PullEpl<WEDGE_APP_CC>::value;
+    case WEDGE_APP_SSSP:
+        return 32u * PullEpl<WEDGE_APP_SSSP>::value;
+    default:
+        return 32u * PullEpl<WEDGE_APP_PR>::value;
+    }
+}
+
+// Size the hub cache of an application's pull, in whole 16-byte lines of the
+// gathered array (frontier words for BFS, one property per vertex otherwise):
+// HUB_BYTES_DEFAULT, or WEDGE_HUB_BYTES (0 turns the cache off), within the
+// shared memory a block can opt into beside the kernel's static tables.  The
+// cache comes out of the SM's L1: on R-MAT scale 24 a 64 KB cache beat both no
+// cache and the largest one, whose small L1 left too few gather misses in flight.
+constexpr uint64_t HUB_BYTES_DEFAULT = 65536;
+
+static int setup_hub(wedge_graph* h, int app, int precision)
+{
+    const void* fn = pull_fn(app);
+    cudaFuncAttributes fa;
+    WEDGE_CHECK(cudaFuncGetAttributes(&fa, fn));
+    int optin = 0;
+    WEDGE_CHECK(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, h->device));
+    const uint64_t elem = (app == WEDGE_APP_SSSP || (app == WEDGE_APP_PR && precision != WEDGE_PREC_FP32C)) ? 8 : 4;
+    uint64_t avail = (uint64_t)optin > fa.sharedSizeBytes + 64u ? (uint64_t)optin - fa.sharedSizeBytes - 64u : 0u;
+    const char* cap = getenv("WEDGE_HUB_BYTES");
+    const uint64_t want = cap ? strtoull(cap, nullptr, 10) : HUB_BYTES_DEFAULT;
+    if (want < avail)
+        avail = want;
+    const uint64_t have = (app == WEDGE_APP_BFS) ? (h->g.V + 31) / 32 : h->g.V;
+    uint64_t n = avail / elem;
+    if (n > have)
+        n = have;
+    n &= ~3ull;
+    h->s.hub_n = (uint32_t)n;
+    h->s.hub_tile = 0;
+    h->hub_bytes = (uint32_t)(n * elem);
+    h->s.hub_bytes = h->hub_bytes;
+    WEDGE_CHECK(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)h->hub_bytes));
+    if (two_phase_app(app) && n) {
+        uint32_t* d = (uint32_t*)(h->s.block_part + h->pull_grid); /* counters: scratch until the first pull */
+        hub_split_kernel<<<1, 1, 0, h->stream>>>(h->g, (uint32_t)n, pull_tile_e(app), d);
+        WEDGE_CHECK(cudaGetLastError());
+        uint32_t t = 0;
+        WEDGE_CHECK(cudaMemcpyAsync(&t, d, sizeof(t), cudaMemcpyDeviceToHost, h->stream));
+        WEDGE_CHECK(cudaStreamSynchronize(h->stream));
+        h->s.hub_tile = t;
+    }
     return WEDGE_OK;
 }
 
@@ -1424,13 +1664,14 @@ static int ensure_state(wedge_graph* h, int app, int precision)
     int rc;
     Ctrl* ctrl;
     double* bp;
-    // [grid] block sums | [4*grid] block counters | [aux grid] PageRank-sum partials
-    if ((rc = dalloc(h, &ctrl, 1, true)) || (rc = dalloc(h, &bp, grid * (1 + NCNT) + (uint64_t)h->num_sms * 8 + 8, true)) ||
+    // [grid] block sums | [2*NCNT*grid] block counters (two launches) | [aux grid] PageRank-sum partials
+    if ((rc = dalloc(h, &ctrl, 1, true)) || (rc = dalloc(h, &bp, grid * (1 + 2 * NCNT) + (uint64_t)h->num_sms * 8 + 8, true)) ||
         (rc = dalloc(h, &s.log, LOG_CAP, true)))
         return rc;
     WEDGE_CHECK(cudaMemset(ctrl, 0, sizeof(Ctrl)));
     s.ctrl = ctrl;
-    s.block_part = bp; /* [grid] doubles, then 4*grid counters */
+    s.block_part = bp; /* [grid] doubles, then the counters */
+    WEDGE_CHECK(cudaMemset(bp, 0, sizeof(double) * (grid * (1 + 2 * NCNT))));
     s.app = (uint32_t)app;
     if (app == WEDGE_APP_PR) {
         if ((rc = dalloc(h, &s.acc, V, true)))
@@ -1457,12 +1698,17 @@ static int ensure_state(wedge_graph* h, int app, int precision)
             (rc = dalloc(h, &s.tile_list, (uint64_t)g.T + 1, true)) ||
             (rc = dalloc(h, &s.items, V + g.E / PIECE + 2, true)))
             return rc;
+        if (app == WEDGE_APP_BFS || app == WEDGE_APP_CC) {
+            if ((rc = dalloc(h, &s.vis_c, (uint64_t)g.Vne / 32 + 2, true)))
+                return rc;
+        }
         if (app == WEDGE_APP_BFS) {
-            if ((rc = dalloc(h, &s.front1, nwords, true)) || (rc = dalloc(h, &s.vis_c, (uint64_t)g.Vne / 32 + 2, true)) ||
-                (rc = dalloc(h, &s.tile_open, (uint64_t)g.T / 32 + 2, true)))
+            if ((rc = dalloc(h, &s.front1, nwords, true)) || (rc = dalloc(h, &s.tile_open, (uint64_t)g.T / 32 + 2, true)))
                 return rc;
         }
     }
+    if ((rc = setup_hub(h, app, precision)))
+        return rc;
     h->built_app = app;
     h->last_precision = precision;
     return WEDGE_OK;
@@ -1470,24 +1716,46 @@ static int ensure_state(wedge_graph* h, int app, int precision)
 
 static unsigned long long* counters(wedge_graph* h) { return (unsigned long long*)(h->s.block_part + h->pull_grid); }
 
+// counter slots the pulls of one iteration fill (two launches for CC/SSSP)
+static uint32_t pull_slots(wedge_graph* h, int app) { return h->pull_grid * (two_phase_app(app) ? 2u : 1u); }
+
+// PageRank-sum partials after the counters
+static double* pr_sums(wedge_graph* h) { return (double*)(counters(h) + 2ull * NCNT * h->pull_grid); }
+
+template <int APP>
+static void launch_pull_app(wedge_graph* h)
+{
+    constexpr int EPL = PullEpl<APP>::value;
+    const uint32_t grid = h->pull_grid;
+    if (two_phase_app(APP)) {
+        pull_kernel<APP, EPL><<<grid, PULL_THREADS, h->hub_bytes, h->stream>>>(h->g, h->s, counters(h), PHASE_HUBS);
+        pull_kernel<APP, EPL><<<grid, PULL_THREADS, h->hub_bytes, h->stream>>>(h->g, h->s, counters(h) + NCNT * grid,
+                                                                               PHASE_REST);
+    } else {
+        pull_kernel<APP, EPL><<<grid, PULL_THREADS, h->hub_bytes, h->stream>>>(h->g, h->s, counters(h), PHASE_ALL);
+    }
+}
+
 static void launch_pull(wedge_graph* h, int app)
 {
-    const uint32_t grid = h->pull_grid;
     switch (app) {
     case WEDGE_APP_BFS:
-        pull_kernel<WEDGE_APP_BFS, PullEpl<WEDGE_APP_BFS>::value><<<grid, PULL_THREADS, 0, h->stream>>>(h->g, h->s, counters(h));
+        launch_pull_app<WEDGE_APP_BFS>(h);
         break;
     case WEDGE_APP_CC:
-        pull_kernel<WEDGE_APP_CC, PullEpl<WEDGE_APP_CC>::value><<<grid, PULL_THREADS, 0, h->stream>>>(h->g, h->s, counters(h));
+        launch_pull_app<WEDGE_APP_CC>(h);
         break;
     case WEDGE_APP_SSSP:
-        pull_kernel<WEDGE_APP_SSSP, PullEpl<WEDGE_APP_SSSP>::value><<<grid, PULL_THREADS, 0, h->stream>>>(h->g, h->s, counters(h));
+        launch_pull_app<WEDGE_APP_SSSP>(h);
         break;
     default:
-        pull_kernel<WEDGE_APP_PR, PullEpl<WEDGE_APP_PR>::value><<<grid, PULL_THREADS, 0, h->stream>>>(h->g, h->s, counters(h));
+        launch_pull_app<WEDGE_APP_PR>(h);
         break;
     }
 }
+
+// kernels one iteration launches: the pull(s) and the five of the tail
+static uint64_t iteration_launches(int app) { return 5ull + (two_phase_app(app) ? 2ull : 1ull); }
 
 static uint32_t aux_grid(wedge_graph* h, uint64_t work)
 {
@@ -1510,7 +1778,7 @@ static void launch_compact(wedge_graph* h, int app)
 // iteration tail after a pull: mass/convergence, Wedge frontier, bitmap reset
 static void launch_tail(wedge_graph* h, int app)
 {
-    decide_kernel<<<1, AUX_THREADS, 0, h->stream>>>(h->g, h->s, counters(h), h->pull_grid, (uint32_t)app);
+    decide_kernel<<<1, AUX_THREADS, 0, h->stream>>>(h->g, h->s, counters(h), pull_slots(h, app), (uint32_t)app);
     collect_kernel<<<aux_grid(h, (h->g.V + 31) / 32), AUX_THREADS, 0, h->stream>>>(h->g, h->s, (uint32_t)app);
     wedge_build_kernel<<<h->build_grid, AUX_THREADS, 0, h->stream>>>(h->g, h->s);
     launch_compact(h, app);
@@ -1614,7 +1882,7 @@ static int run_traversal(wedge_graph* h, int app, const wedge_params_t* p, wedge
             WEDGE_CHECK(cudaEventRecord(h->ev[3], h->stream));
             launch_tail(h, app);
             WEDGE_CHECK(cudaEventRecord(h->ev[4], h->stream));
-            launches += 6;
+            launches += iteration_launches(app);
             WEDGE_CHECK(cudaEventSynchronize(h->ev[4]));
             float a = 0, b = 0;
             cudaEventElapsedTime(&a, h->ev[2], h->ev[3]);
@@ -1635,7 +1903,7 @@ static int run_traversal(wedge_graph* h, int app, const wedge_params_t* p, wedge
             for (int b = 0; b < 3; ++b) {
                 launch_pull(h, app);
                 launch_tail(h, app);
-                launches += 6;
+                launches += iteration_launches(app);
             }
             int rc = read_ctrl(h, &c);
             if (rc)
@@ -1666,8 +1934,10 @@ static int run_traversal(wedge_graph* h, int app, const wedge_params_t* p, wedge
         st->edges_scanned = c.edges_scanned;
         st->tiles_scanned = c.tiles_scanned;
         st->pull_launches = c.pull_launches;
-        st->kernel_launches = use_graph ? (uint64_t)6 + 7ull * c.iter : launches;
+        st->kernel_launches = use_graph ? (uint64_t)6 + (iteration_launches(app) + 1ull) * c.iter : launches;
     }
+    if (c.error)
+        return WEDGE_ERR_CUDA;
     if (c.not_converged)
         return WEDGE_ERR_NOT_CONVERGED;
     return WEDGE_OK;
@@ -1707,7 +1977,7 @@ static int run_pr(wedge_graph* h, const wedge_params_t* p, wedge_stats_t* st)
         }
     }
     WEDGE_CHECK(cudaEventRecord(h->ev[1], h->stream));
-    double* sums = (double*)(counters(h) + (uint64_t)NCNT * h->pull_grid);
+    double* sums = pr_sums(h);
     pr_sum_kernel<<<vgrid, AUX_THREADS, 0, h->stream>>>(g, h->s, sums);
     pr_sum_final_kernel<<<1, 32, 0, h->stream>>>(h->s, sums, vgrid);
     WEDGE_CHECK(cudaGetLastError());
@@ -1732,6 +2002,8 @@ static int run_pr(wedge_graph* h, const wedge_params_t* p, wedge_stats_t* st)
         st->kernel_launches = 3ull + 3ull * p->num_iterations;
         st->pr_sum = c.pr_sum;
     }
+    if (c.error)
+        return WEDGE_ERR_CUDA;
     return WEDGE_OK;
 }
 
@@ -1837,7 +2109,7 @@ int wedge_cuda_run_phase(wedge_graph_t* g, int app, int phase, const wedge_param
             pr_finish_kernel<<<aux_grid(g, (uint64_t)dg.nsplit * 32 + 1), AUX_THREADS, 0, g->stream>>>(
                 dg, g->s, g->pull_grid, counters(g));
         } else {
-            decide_kernel<<<1, AUX_THREADS, 0, g->stream>>>(dg, g->s, counters(g), g->pull_grid, (uint32_t)app);
+            decide_kernel<<<1, AUX_THREADS, 0, g->stream>>>(dg, g->s, counters(g), pull_slots(g, app), (uint32_t)app);
         }
         break;
     }
@@ -2140,7 +2412,8 @@ extern "C" int wedge_cuda_pr_iteration_noalloc(uint64_t num_vertices, uint64_t n
     DevState sp = s;
     sp.rank = (double*)rank_in; /* gathered by the pull */
     if (T)
-        pull_kernel<WEDGE_APP_PR, PullEpl<WEDGE_APP_PR>::value><<<grid, PULL_THREADS, 0, st>>>(g, sp, sc->block_cnt);
+        pull_kernel<WEDGE_APP_PR, PullEpl<WEDGE_APP_PR>::value><<<grid, PULL_THREADS, 0, st>>>(g, sp, sc->block_cnt,
+                                                                                           PHASE_ALL); /* no hub cache */
     else
         WEDGE_CHECK(cudaMemsetAsync(sc->block_part, 0, sizeof(double), st));
     noalloc_finish_kernel<<<grid_for((uint64_t)T * 32 + 1, AUX_THREADS, grid * 2u), AUX_THREADS, 0, st>>>(

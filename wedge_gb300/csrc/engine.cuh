@@ -119,7 +119,7 @@ struct DevState {
     double* block_part;            // [grid] per-block sums of tile sums
     uint32_t* front0;              // V-bit frontier bitmaps (active / snapshot)
     uint32_t* front1;
-    uint32_t* vis_c;               // Vne-bit visited bitmap (BFS)
+    uint32_t* vis_c;               // Vne-bit: destination finished (BFS visited; CC label 0, the least label)
     uint32_t* tile_open;           // T-bit: tile still has an unvisited destination (BFS)
     uint32_t* chunk_bits;          // Wedge frontier: one bit per chunk
     uint32_t* summary;             // one bit per region of REGION_WORDS chunk words (any chunk marked)
@@ -131,6 +131,9 @@ struct DevState {
     uint32_t precision;
     uint32_t app;
     uint64_t root;
+    uint32_t hub_n;                // elements of the gathered array cached in shared memory by dense pulls
+    uint32_t hub_bytes;            // their bytes: the pulls' dynamic shared memory (a multiple of 16)
+    uint32_t hub_tile;             // CC/SSSP: first tile whose destinations all have ids >= hub_n
 };
 
 }  // namespace wedge
@@ -146,8 +149,9 @@ struct wedge_graph {
     int built_app;                     // app whose state arrays are sized (-1 none)
     int last_app;                      // app of the last run (for read_results)
     int last_precision;
-    uint32_t pull_grid;                // persistent grid of the pull kernels
+    uint32_t pull_grid;                // persistent grid of the pull kernels (one 1024-thread block per SM)
     uint32_t build_grid;
+    uint32_t hub_bytes;                // dynamic shared memory of the pull kernels (the hub cache)
     // allocations owned by the handle
     void* allocs[32];
     int nallocs;

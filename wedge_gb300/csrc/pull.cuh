@@ -26,6 +26,23 @@ __device__ __forceinline__ uint4 ld_stream_v4(const uint32_t* p)
     return r;
 }
 
+// 256-bit streaming loads (sm_100+): one lane reads a whole 32-byte sector, so
+// a warp's strided per-lane runs cost one L2 request per sector and need no
+// L1 reuse (the L1 is mostly given to the hub cache)
+__device__ __forceinline__ void ld_stream_v8(const uint32_t* p, uint32_t (&r)[8])
+{
+    asm volatile("ld.global.nc.L1::no_allocate.v8.u32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
+                 : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7])
+                 : "l"(p));
+}
+
+__device__ __forceinline__ void ld_stream_v4u64(const unsigned long long* p, unsigned long long (&r)[4])
+{
+    asm volatile("ld.global.nc.L1::no_allocate.v4.u64 {%0,%1,%2,%3}, [%4];"
+                 : "=l"(r[0]), "=l"(r[1]), "=l"(r[2]), "=l"(r[3])
+                 : "l"(p));
+}
+
 __device__ __forceinline__ ulonglong2 ld_stream_v2u64(const unsigned long long* p)
 {
     ulonglong2 r;
@@ -36,6 +53,62 @@ __device__ __forceinline__ ulonglong2 ld_stream_v2u64(const unsigned long long* 
 __device__ __forceinline__ bool test_bit32(const uint32_t* bm, uint64_t i)
 {
     return (bm[i >> 5] >> (i & 31)) & 1u;
+}
+
+/* ---- hub cache: a bulk (TMA) copy of the low-id end of the gathered array
+ * into shared memory, completed on an mbarrier.  Vertices are relabelled by
+ * descending out-degree, so ids [0, hub_n) are the sources most in-edges
+ * name; their gathers then hit shared memory instead of L1/L2. */
+__device__ __forceinline__ uint32_t smem_u32(const void* p)
+{
+    return (uint32_t)__cvta_generic_to_shared(p);
+}
+
+__device__ __forceinline__ void mbar_init(unsigned long long* bar, uint32_t count)
+{
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
+
+__device__ __forceinline__ void mbar_arrive_expect_tx(unsigned long long* bar, uint32_t bytes)
+{
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes) : "memory");
+}
+
+// non-blocking probe of the barrier's phase `parity`
+__device__ __forceinline__ bool mbar_test_wait(unsigned long long* bar, uint32_t parity)
+{
+    uint32_t ok;
+    asm volatile("{\n\t.reg .pred p;\n\tmbarrier.test_wait.parity.shared::cta.b64 p, [%1], %2;\n\tselp.u32 %0, 1, 0, p;\n\t}"
+                 : "=r"(ok)
+                 : "r"(smem_u32(bar)), "r"(parity)
+                 : "memory");
+    return ok != 0u;
+}
+
+// bounded wait: false when the phase did not complete within `tries` probes
+__device__ __forceinline__ bool mbar_wait_bounded(unsigned long long* bar, uint32_t parity, uint32_t tries)
+{
+    for (uint32_t i = 0; i < tries; ++i) {
+        uint32_t ok;
+        asm volatile("{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\tselp.u32 %0, 1, 0, p;\n\t}"
+                     : "=r"(ok)
+                     : "r"(smem_u32(bar)), "r"(parity)
+                     : "memory");
+        if (ok)
+            return true;
+    }
+    return false;
+}
+
+// global -> shared bulk copy (16-byte aligned addresses, size a multiple of 16)
+__device__ __forceinline__ void bulk_g2s(void* dst, const void* src, uint32_t bytes, unsigned long long* bar)
+{
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                     smem_u32(dst)),
+                 "l"(src), "r"(bytes), "r"(smem_u32(bar))
+                 : "memory");
 }
 
 // read-only (non-coherent) path for arrays no kernel writes while it runs
