@@ -429,12 +429,18 @@ int build_from_device_edges(wedge_graph* h, uint64_t V, uint64_t E, uint32_t* d_
                                                                              d_cnt);
     unsigned int nsplit = 0;
     WEDGE_CHECK(cudaMemcpyAsync(&nsplit, d_cnt, sizeof(unsigned int), cudaMemcpyDeviceToHost, st));
+    // dst_id ascends, so it is the identity when its last entry is Vne-1 (symmetric
+    // graphs after the degree relabelling: in-degree > 0 exactly for ids < Vne)
+    uint32_t last_dst = 0;
+    if (Vne)
+        WEDGE_CHECK(cudaMemcpyAsync(&last_dst, dst_id + (Vne - 1), sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
     if (g.Epad > E)
         pad_kernel<<<1, 128, 0, st>>>(d_src, d_w, E, g.Epad);
     WEDGE_CHECK(cudaStreamSynchronize(st));
     cudaFreeAsync(d_cnt, st);
     WEDGE_CHECK(cudaGetLastError());
     g.nsplit = nsplit;
+    g.dst_ident = (Vne && last_dst == Vne - 1) ? 1u : 0u;
     g.dst_id = dst_id;
     g.dst_off = dst_off;
     g.tile_dst0 = tile_dst0;
@@ -773,6 +779,11 @@ __global__ void __launch_bounds__(PULL_THREADS, 1)
             // Frontier-bit gathers.  A tile with no visited destination gathers at
             // once (the latency overlaps the geometry's); otherwise the geometry
             // comes first and only the in-edges of unvisited destinations gather.
+            // ids of the tile's first 32 destinations: loaded now, staged after the gathers
+            const uint32_t nst = min(min(in.kend, g.Vne - 1u) - in.k0 + 1u, TAB);
+            uint32_t st_id = 0u;
+            if ((uint32_t)lane < nst)
+                st_id = g.dst_ident ? in.k0 + (uint32_t)lane : g.dst_id[in.k0 + (uint32_t)lane];
             uint32_t v[EPL];
             auto gather = [&](uint32_t x) -> uint32_t {
                 const uint32_t wi = x >> 5; /* NONE32 >> 5 lies beyond any cache */
@@ -796,7 +807,9 @@ __global__ void __launch_bounds__(PULL_THREADS, 1)
                     v[q] = gather(((vw >> (k & 31u)) & 1u) ? NONE32 : sa[q]);
                 }
             }
-            for (uint32_t slot = (uint32_t)lane; slot < min(tg.ndst, TAB); slot += 32u)
+            if ((uint32_t)lane < nst)
+                my_id[lane] = st_id;
+            for (uint32_t slot = (uint32_t)lane + 32u; slot < min(tg.ndst, TAB); slot += 32u)
                 my_id[slot] = g.dst_id[tg.k0 + slot];
             __syncwarp();
             seg_reduce<EPL>(v, tg, lane, MinU32(), [&](uint32_t k, uint32_t val, int kind) {
@@ -817,6 +830,11 @@ __global__ void __launch_bounds__(PULL_THREADS, 1)
             // Label gathers.  A tile whose destinations all may still drop gathers at
             // once (the latency overlaps the geometry's); otherwise the geometry
             // comes first and destinations holding label 0 gather nothing.
+            // the tile's first 32 destinations: ids and labels loaded now, staged after the gathers
+            const uint32_t nst = min(min(in.kend, g.Vne - 1u) - in.k0 + 1u, TAB);
+            uint32_t st_id = 0u;
+            if ((uint32_t)lane < nst)
+                st_id = g.dst_ident ? in.k0 + (uint32_t)lane : g.dst_id[in.k0 + (uint32_t)lane];
             uint32_t v[EPL];
             auto gather = [&](uint32_t x) -> uint32_t {
                 return (x < hub_lim) ? hub32[x] : ((x != NONE32) ? s.prop32[x] : NONE32);
@@ -838,7 +856,11 @@ __global__ void __launch_bounds__(PULL_THREADS, 1)
                     v[q] = gather(((vw >> (k & 31u)) & 1u) ? NONE32 : sa[q]);
                 }
             }
-            for (uint32_t slot = (uint32_t)lane; slot < min(tg.ndst, TAB); slot += 32u) {
+            if ((uint32_t)lane < nst) {
+                my_id[lane] = st_id;
+                my_cur[lane] = s.prop32[st_id];
+            }
+            for (uint32_t slot = (uint32_t)lane + 32u; slot < min(tg.ndst, TAB); slot += 32u) {
                 const uint32_t vtx = g.dst_id[tg.k0 + slot];
                 my_id[slot] = vtx;
                 my_cur[slot] = s.prop32[vtx];

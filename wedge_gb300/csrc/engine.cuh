@@ -90,6 +90,8 @@ struct Ctrl {
 struct DevGraph {
     uint64_t V, E, Epad;
     uint32_t Vne, T, nsplit, weight_kind;
+    uint32_t dst_ident;        // dst_id[k] == k for every k (the vertices with in-edges are [0, Vne))
+    uint32_t pad0;
     const uint32_t* src;
     const unsigned long long* w;
     const uint32_t* dst_id;
