@@ -285,11 +285,14 @@ def run_ours(args, dist: Dist):
         "roofline": {"bound": "hbm", "kernel": "pull_kernel (BFS + CC, all iterations)",
                      "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
                      "frac": round(achieved / peak, 4), "peak_source": peak_kind,
-                     "traffic": traffic, "launches": n_launch,
+                     "traffic": traffic,
+                     "traffic_scope": "achieved, algorithmic_bytes and traffic are per step: all pull launches of "
+                                      "one BFS + one CC traversal (traffic: ncu DRAM bytes, profiles/)",
+                     "pull_iterations": n_launch,
                      "algorithmic_bytes": int(pull_bytes_tot), "pull_ms": round(pull_ms, 4),
                      "dense_only": {"achieved": round(dense_bytes / (dense_ms / 1e3) / 1e9, 1) if dense_ms else None,
                                     "frac": round(dense_bytes / (dense_ms / 1e3) / 1e9 / peak, 4) if dense_ms else None,
-                                    "launches": len(dense)}},
+                                    "pull_iterations": len(dense)}},
         "clocks": clocks,
         "gpu_launches": int(counts["launches"]),
         "wall_s_timed": round(wall, 4),
@@ -310,11 +313,12 @@ def _timed_records(W, g, app, p):
 
 
 def _ncu_traffic():
-    """DRAM bytes per pull launch from the committed ncu summary, if present"""
+    """DRAM bytes of one step's pull launches (ncu, full-size workload, one pass), if the
+    committed profile summary holds them"""
     path = os.path.join(ROOT, "profiles", "pull_kernel_traffic.json")
     try:
         with open(path) as f:
-            return json.load(f).get("traffic_bytes_per_launch")
+            return json.load(f).get("traffic_bytes_per_step")
     except Exception:
         return None
 
