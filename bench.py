@@ -223,6 +223,9 @@ def run_ours(args, dist: Dist):
     edges_step = E_bfs + E_cc
     value = dist.world * steps * edges_step / t_max / 1e9
 
+    # ---- the same steps under the learned scheduler (on-device network, plain-rule fallback)
+    learned = _learned_arm(W, gb, gc, p_bfs, p_cc, steps, warmup, s_bfs, s_cc, edges_step, dist, value)
+
     # ---- end to end through the C ABI with host buffers: query parameters in,
     # full property arrays (8 bytes per vertex, graph_vertex_props) out, every step
     host_bfs = torch.empty(V, dtype=torch.int64, pin_memory=True).numpy().view(np.uint64)
@@ -293,6 +296,7 @@ def run_ours(args, dist: Dist):
                      "dense_only": {"achieved": round(dense_bytes / (dense_ms / 1e3) / 1e9, 1) if dense_ms else None,
                                     "frac": round(dense_bytes / (dense_ms / 1e3) / 1e9 / peak, 4) if dense_ms else None,
                                     "pull_iterations": len(dense)}},
+        "learned": learned,
         "clocks": clocks,
         "gpu_launches": int(counts["launches"]),
         "wall_s_timed": round(wall, 4),
@@ -304,6 +308,46 @@ def run_ours(args, dist: Dist):
     if dist.rank == 0:
         print(json.dumps(line), flush=True)
     dist.done()
+
+
+def _learned_arm(W, gb, gc, p_bfs, p_cc, steps, warmup, s_bfs, s_cc, edges_step, dist, plain_value):
+    """GTEPS of the same workload with WEDGE_SCHED_LEARNED and the committed network"""
+    import torch
+    from wedge_gb300 import scheduler as S
+
+    try:
+        blob = S.load()
+    except Exception as e:  # no trained network: report it, do not guess
+        return {"unavailable": f"no scheduler network: {e}"}
+    gb.set_scheduler(blob)
+    gc.set_scheduler(blob)
+    lb = W.Params(root=p_bfs.root, threshold_pct=p_bfs.threshold_pct, flags=p_bfs.flags, sched=W.SCHED_LEARNED)
+    lc = W.Params(threshold_pct=p_cc.threshold_pct, flags=p_cc.flags, sched=W.SCHED_LEARNED)
+    for _ in range(warmup):
+        gb.run(W.APP_BFS, lb)
+        gc.run(W.APP_CC, lc)
+    dist.barrier()
+    torch.cuda.synchronize()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(s_bfs)
+    for _ in range(steps):
+        gb.run(W.APP_BFS, lb)
+        gc.run(W.APP_CC, lc)
+    e1.record(s_cc)
+    e1.synchronize()
+    t = dist.max(e0.elapsed_time(e1) / 1e3)
+    # which iterations the network changed (one timed-free run per app)
+    changed = {}
+    for name, g, app, p in (("bfs", gb, W.APP_BFS, lb), ("cc", gc, W.APP_CC, lc)):
+        g.run(app, p)
+        log = g.iteration_log()
+        changed[name] = {"iterations": len(log), "chosen_by_network": sum(r["learned"] for r in log),
+                         "modes": [r["mode"] for r in log]}
+    value = dist.world * steps * edges_step / t / 1e9
+    return {"value": round(value, 4), "unit": "GTEPS", "ms_per_step": round(t * 1e3 / steps, 4),
+            "ratio_vs_plain": round(value / plain_value, 4), "network": "wedge_gb300/data/sched_net.f32",
+            "per_app": changed}
 
 
 def _timed_records(W, g, app, p):

@@ -34,7 +34,7 @@
 extern "C" {
 #endif
 
-#define WEDGE_CUDA_ABI_VERSION 1
+#define WEDGE_CUDA_ABI_VERSION 2
 
 /* application ids; names and aliases as in source/application.c:49-68 */
 enum wedge_app {
@@ -67,11 +67,24 @@ enum wedge_precision {
     WEDGE_PREC_FP32C = 1  /* FP32 ranks, per-destination two-sum compensated sums, FP64 global terms */
 };
 
-/* how each iteration chooses between the dense pull and the Wedge pull */
+/* how each iteration chooses its pull strategy (enum wedge_mode) */
 enum wedge_sched {
-    WEDGE_SCHED_PLAIN = 0,   /* fixed threshold: dense iff active out-edge mass > t% of |E| (execution_bfs.c:132,141) */
-    WEDGE_SCHED_DENSE = 1,   /* always dense */
-    WEDGE_SCHED_WEDGE = 2    /* Wedge whenever the frontier allows it */
+    WEDGE_SCHED_PLAIN = 0,     /* fixed threshold: dense iff active out-edge mass > t% of |E| (execution_bfs.c:132,141) */
+    WEDGE_SCHED_DENSE = 1,     /* always dense */
+    WEDGE_SCHED_WEDGE = 2,     /* Wedge whenever the frontier allows it */
+    WEDGE_SCHED_FILTERED = 3,  /* source-filtered sweep whenever the frontier allows it */
+    WEDGE_SCHED_LEARNED = 4,   /* the scheduler network set by wedge_cuda_set_scheduler, evaluated on the
+                                  device after every pull; the plain rule where its features leave the
+                                  trained range or its predicted gain is below the network's margin */
+    WEDGE_SCHED_PROBE = 5      /* plain, except that iteration probe_iter uses probe_mode (timing data) */
+};
+
+/* pull strategy of one iteration (no counterpart in the reference beyond dense / Wedge) */
+enum wedge_mode {
+    WEDGE_MODE_DENSE = 0,    /* every tile (perform_edge_pull_phase_*) */
+    WEDGE_MODE_WEDGE = 1,    /* the tiles of the Wedge frontier (*_with_wedge_frontier) */
+    WEDGE_MODE_FILTERED = 2  /* every tile, gathering only from sources the previous pull changed
+                                (CC/SSSP; BFS runs it as dense, whose gathers are frontier bits) */
 };
 
 /* single phases, for hosts that keep the reference's own driver loop (include/phases.h:58-88, wedge.h:24-27) */
@@ -96,6 +109,8 @@ typedef struct wedge_params {
     int32_t sched;            /* enum wedge_sched */
     uint32_t max_iterations;  /* cap for BFS/CC/SSSP; 0 = |V| + 1 */
     uint32_t flags;           /* WEDGE_FLAG_* */
+    uint32_t probe_iter;      /* WEDGE_SCHED_PROBE: the iteration whose strategy is forced */
+    int32_t probe_mode;       /* WEDGE_SCHED_PROBE: its enum wedge_mode */
 } wedge_params_t;
 
 /* EXECUTION STATISTICS block of source/main.c:153-182, plus device counters */
@@ -116,6 +131,21 @@ typedef struct wedge_stats {
     double pr_sum;                /* PageRank Sum (execution_pr.c:63-71); 0 for other apps */
 } wedge_stats_t;
 
+/* scheduler network: WEDGE_SCHED_FEATURES inputs -> 64 -> 64 -> 3 (ReLU, FP32); the outputs are
+ * predicted log2 costs (microseconds) of the three enum wedge_mode strategies */
+#define WEDGE_SCHED_FEATURES 16
+#define WEDGE_SCHED_HIDDEN 64
+#define WEDGE_SCHED_OUTPUTS 3
+/* float layout of a network blob (WEDGE_SCHED_BLOB floats):
+ *   mu[16] sd[16]      feature standardisation x' = (x - mu) / sd
+ *   lo[16] hi[16]      trained feature range (outside it: the plain rule)
+ *   W1[64][16] b1[64] W2[64][64] b2[64] W3[3][64] b3[3]
+ *   margin             least predicted log2 gain over the plain choice to take the network's choice
+ * The trainable part (W1..b3, WEDGE_SCHED_PARAMS floats) starts at WEDGE_SCHED_PARAM_OFFSET. */
+#define WEDGE_SCHED_PARAM_OFFSET 64
+#define WEDGE_SCHED_PARAMS (64 * 16 + 64 + 64 * 64 + 64 + 3 * 64 + 3)
+#define WEDGE_SCHED_BLOB (WEDGE_SCHED_PARAM_OFFSET + WEDGE_SCHED_PARAMS + 1)
+
 /* one iteration of a traversal: the ITERATION_STATS record the reference prints to stderr
  * (execution_bfs.c:227-232: active edges, used Wedge, pull ms, Wedge ms) plus device counters */
 typedef struct wedge_iteration_record {
@@ -129,6 +159,9 @@ typedef struct wedge_iteration_record {
     uint64_t tiles_scanned;
     uint64_t dsts_scanned;
     uint64_t vertices_activated;
+    uint32_t mode;                /* enum wedge_mode of the pull */
+    uint32_t learned;             /* 1 if the scheduler network chose it */
+    float features[WEDGE_SCHED_FEATURES]; /* the scheduler features the mode was chosen on (iterations >= 1) */
 } wedge_iteration_record_t;
 
 typedef struct wedge_graph wedge_graph_t;
@@ -189,6 +222,30 @@ int wedge_cuda_iteration_log(wedge_graph_t* g, wedge_iteration_record_t* out, ui
 int wedge_cuda_read_results(wedge_graph_t* g, void* host_props, uint64_t bytes);
 /* graph_vertex_outdegrees as uint64 counts; bytes >= 8*V */
 int wedge_cuda_read_outdegrees(wedge_graph_t* g, uint64_t* host_outdeg, uint64_t bytes);
+
+/* ---------------------------------------------------------------- learned scheduler */
+
+/* No counterpart in the reference.  Loads a scheduler network (count =
+ * WEDGE_SCHED_BLOB floats in host memory, layout above) that the
+ * WEDGE_SCHED_LEARNED runs of g evaluate on the device after every pull: the
+ * features of the next iteration go through the network, and the strategy with
+ * the least predicted cost runs unless a feature lies outside [lo, hi] or the
+ * predicted gain over the plain rule's choice is below the margin.  CC's first
+ * pull stays dense (execution_cc.c:103), and so does every iteration 0. */
+int wedge_cuda_set_scheduler(wedge_graph_t* g, const float* blob, uint64_t count);
+
+/* Training and checking of a scheduler network with the engine's own CUDA
+ * kernels on the current device.  X[n][16] features, Y[n][3] target log2 costs,
+ * M[n][3] = 1 where the target was measured, else 0; the loss is the sum over
+ * measured entries of (y - target)^2 divided by n.  Blobs are host memory of
+ * WEDGE_SCHED_BLOB floats; mu/sd standardise the features inside the network. */
+int wedge_mlp_forward(const float* blob, const float* X, uint64_t n, float* out /* [n][3] */);
+int wedge_mlp_loss_grad(const float* blob, const float* X, const float* Y, const float* M, uint64_t n,
+                        double* loss, float* grad /* [WEDGE_SCHED_PARAMS], d loss / d params */);
+/* Adam on minibatches of `batch` samples in an order drawn from `seed`; blob
+ * holds the initial parameters on entry and the trained ones on return. */
+int wedge_mlp_train(float* blob, const float* X, const float* Y, const float* M, uint64_t n, uint32_t epochs,
+                    uint32_t batch, float lr, uint64_t seed, double* final_loss);
 
 /* ---------------------------------------------------------------- allocation-free iteration */
 

@@ -15,7 +15,7 @@ HEADER = os.path.join(ROOT, "include", "wedge_cuda.h")
 def declared_functions():
     text = open(HEADER).read()
     text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
-    return sorted(set(re.findall(r"\b(wedge_cuda_\w+)\s*\(", text)))
+    return sorted(set(re.findall(r"\b(wedge_(?:cuda|mlp)_\w+)\s*\(", text)))
 
 
 def test_header_declares_the_boundary():
@@ -41,7 +41,7 @@ def test_status_strings_and_version(engine_lib):
     W = engine_lib
     assert W.status_string(0) == "ok"
     assert "format" in W.status_string(-2) or "malformed" in W.status_string(-2)
-    assert W.lib().wedge_cuda_abi_version() == 1
+    assert W.lib().wedge_cuda_abi_version() == 2
 
 
 def test_null_handles_are_rejected(engine_lib):
@@ -55,23 +55,22 @@ def test_null_handles_are_rejected(engine_lib):
 
 
 def test_struct_layout_matches_c(engine_lib, tmp_path):
-    from wedge_gb300.engine import Params, Stats
+    from wedge_gb300.engine import IterationRecord, Params, Stats
 
     src = tmp_path / "layout.c"
-    fields_p = [f for f, _ in Params._fields_]
-    fields_s = [f for f, _ in Stats._fields_]
     lines = ['#include <stdio.h>', '#include <stddef.h>', '#include "wedge_cuda.h"', "int main(void){"]
-    lines.append('printf("%zu\\n", sizeof(wedge_params_t));')
-    lines += [f'printf("%zu\\n", offsetof(wedge_params_t, {f}));' for f in fields_p]
-    lines.append('printf("%zu\\n", sizeof(wedge_stats_t));')
-    lines += [f'printf("%zu\\n", offsetof(wedge_stats_t, {f}));' for f in fields_s]
+    want = []
+    for cls, cname in ((Params, "wedge_params_t"), (Stats, "wedge_stats_t"),
+                       (IterationRecord, "wedge_iteration_record_t")):
+        fields = [f for f, _ in cls._fields_]
+        lines.append(f'printf("%zu\\n", sizeof({cname}));')
+        lines += [f'printf("%zu\\n", offsetof({cname}, {f}));' for f in fields]
+        want += [C.sizeof(cls)] + [getattr(cls, f).offset for f in fields]
     lines.append("return 0;}")
     src.write_text("\n".join(lines))
     exe = tmp_path / "layout"
     subprocess.run(["gcc", "-I", os.path.join(ROOT, "include"), str(src), "-o", str(exe)], check=True)
     out = [int(x) for x in subprocess.run([str(exe)], capture_output=True, text=True, check=True).stdout.split()]
-    want = [C.sizeof(Params)] + [getattr(Params, f).offset for f in fields_p]
-    want += [C.sizeof(Stats)] + [getattr(Stats, f).offset for f in fields_s]
     assert out == want
 
 

@@ -22,6 +22,7 @@
 
 #include "engine.cuh"
 #include "pull.cuh"
+#include "sched.cuh"
 
 namespace wedge {
 
@@ -81,6 +82,7 @@ static void free_state(wedge_graph* h)
         cudaFree(h->state_allocs[i]);
     h->nstate = 0;
     memset(&h->s, 0, sizeof(h->s));
+    h->s.net = h->net; /* the scheduler network outlives the state arrays */
     h->built_app = -1;
     if (h->graph_exec) {
         cudaGraphExecDestroy(h->graph_exec);
@@ -103,6 +105,8 @@ void free_handle(wedge_graph* h)
             cudaEventDestroy(h->ev[i]);
     if (h->h_ctrl)
         cudaFreeHost(h->h_ctrl);
+    if (h->net)
+        cudaFree(h->net);
     free(h->iter_pull_ms);
     free(h->iter_wedge_ms);
     if (h->stream)
@@ -477,10 +481,12 @@ __device__ __forceinline__ const uint32_t* cur_front(const DevState& s, uint32_t
     return parity ? s.front1 : s.front0;
 }
 
-// pull output bitmap: BFS writes the other half of its double buffer
-__device__ __forceinline__ uint32_t* next_front(const DevState& s, uint32_t app, uint32_t parity)
+// pull output bitmap: the other half of the double buffer.  The pull reads the
+// vertices the previous pull activated (BFS frontier; CC/SSSP changed
+// vertices, read by the source-filtered pull) and writes the ones it activates.
+__device__ __forceinline__ uint32_t* next_front(const DevState& s, uint32_t parity)
 {
-    return (app == WEDGE_APP_BFS) ? (parity ? s.front0 : s.front1) : s.front0;
+    return parity ? s.front0 : s.front1;
 }
 
 // in-edges per lane of each application's pull (tile = 32 * EPL in-edges)
@@ -599,7 +605,7 @@ __device__ __forceinline__ bool next_tile(const DevGraph& g, const DevState& s, 
                                           TileIter& it, int lane, uint32_t& t, uint32_t& cmask)
 {
     constexpr uint32_t MASK = (EPL >= 32) ? FULL : ((1u << EPL) - 1u);
-    if (mode == MODE_DENSE && s.tile_open) {
+    if (mode != MODE_WEDGE && s.tile_open) {
         while (!it.obits) {
             uint32_t u = 0;
             if (lane == 0)
@@ -616,7 +622,7 @@ __device__ __forceinline__ bool next_tile(const DevGraph& g, const DevState& s, 
         cmask = MASK;
         return true;
     }
-    if (mode == MODE_DENSE) {
+    if (mode != MODE_WEDGE) {
         if (it.i >= t_end)
             return false;
         t = it.i;
@@ -673,20 +679,21 @@ __global__ void __launch_bounds__(PULL_THREADS, 1)
     constexpr uint32_t TILE_E = 32u * EPL;
     constexpr uint32_t TAB = 129; /* staged destinations per tile; more are read from global memory */
     using cur_t = typename CurT<APP>::type;
-    __shared__ unsigned long long sh_cnt[WARPS][5];
+    __shared__ unsigned long long sh_cnt[WARPS][NCNT];
     __shared__ double sh_sum[WARPS];
     __shared__ uint32_t tab_id[WARPS][TAB];  // vertex id of each destination of the warp's tile
     __shared__ cur_t tab_cur[WARPS][TAB];    // its property before the tile (min apps)
     __shared__ uint32_t sh_heads[WARPS][EPL];
     __shared__ unsigned long long hub_bar;
+    __shared__ unsigned int sh_deg[3];
     extern __shared__ __align__(16) unsigned char hub_smem[];
     Ctrl* c = s.ctrl;
     if (c->done)
         return;
     const uint32_t mode = c->mode;
-    if (phase == PHASE_REST && mode != MODE_DENSE) {
+    if (phase == PHASE_REST && mode == MODE_WEDGE) {
         // a Wedge pull ran whole in the first launch: this one only reports zeros
-        if (threadIdx.x < 5)
+        if (threadIdx.x < NCNT)
             block_cnt[NCNT * blockIdx.x + threadIdx.x] = 0ull;
         return;
     }
@@ -696,7 +703,7 @@ __global__ void __launch_bounds__(PULL_THREADS, 1)
     const uint32_t nw = (gridDim.x * blockDim.x) >> 5;
     const uint32_t T = (uint32_t)((g.E + TILE_E - 1) / TILE_E); /* tiles holding real in-edges */
     uint32_t t_begin = 0, t_end = T;
-    if (two_phase_app(APP) && mode == MODE_DENSE) {
+    if (two_phase_app(APP) && mode != MODE_WEDGE) {
         const uint32_t split = min(s.hub_tile, T);
         if (phase == PHASE_HUBS)
             t_end = split;
@@ -705,12 +712,20 @@ __global__ void __launch_bounds__(PULL_THREADS, 1)
     }
     const uint32_t parity = c->parity;
     const uint32_t* cur = cur_front(s, parity);
-    uint32_t* nxt = next_front(s, APP, parity);
+    const bool filtered = (APP == WEDGE_APP_CC || APP == WEDGE_APP_SSSP) && mode == MODE_FILTERED;
+    uint32_t* nxt = next_front(s, parity);
     uint32_t* my_id = tab_id[wib];
     cur_t* my_cur = tab_cur[wib];
     uint32_t* heads = sh_heads[wib];
     unsigned long long mass = 0, edges = 0, tiles = 0, dsts = 0, act = 0;
     double psum = 0.0;
+    auto count_act = [&](uint32_t d) {
+        mass += d;
+        ++act;
+        const uint32_t b = degree_bucket(d);
+        if (b < 3u)
+            atomicAdd(&sh_deg[b], 1u); /* activated vertices per out-degree bucket 0..2 */
+    };
     auto vid = [&](uint32_t k, uint32_t slot) -> uint32_t { return slot < TAB ? my_id[slot] : g.dst_id[k]; };
 
     // ---- hub cache
@@ -725,11 +740,14 @@ __global__ void __launch_bounds__(PULL_THREADS, 1)
     const uint32_t hub_bytes = (uint64_t)s.hub_bytes < hub_fit ? s.hub_bytes : (uint32_t)hub_fit; /* within smem and the array */
     bool use_hub = hub_bytes != 0u && ((uintptr_t)hub_src & 15u) == 0u && (smem_u32(hub_smem) & 15u) == 0u;
     if (APP == WEDGE_APP_BFS)
-        use_hub = use_hub && (mode == MODE_DENSE || c->tiles >= T / 16u);
+        use_hub = use_hub && (mode != MODE_WEDGE || c->tiles >= T / 16u);
     else if (two_phase_app(APP))
-        use_hub = use_hub && mode == MODE_DENSE;
+        use_hub = use_hub && mode != MODE_WEDGE;
     uint32_t* hub32 = reinterpret_cast<uint32_t*>(hub_smem);
     unsigned long long* hub64 = reinterpret_cast<unsigned long long*>(hub_smem);
+    if (threadIdx.x < 3)
+        sh_deg[threadIdx.x] = 0u;
+    __syncthreads();
     if (use_hub) {
         if (threadIdx.x == 0) {
             mbar_init(&hub_bar, 1u);
@@ -822,8 +840,7 @@ __global__ void __launch_bounds__(PULL_THREADS, 1)
                 if (old == NONE32) {
                     atomicOr(&s.vis_c[k >> 5], 1u << (k & 31u));
                     atomicOr(&nxt[vtx >> 5], 1u << (vtx & 31u));
-                    mass += g.outdeg[vtx];
-                    ++act;
+                    count_act(g.outdeg[vtx]);
                 }
             });
         } else if (APP == WEDGE_APP_CC) {
@@ -837,6 +854,8 @@ __global__ void __launch_bounds__(PULL_THREADS, 1)
                 st_id = g.dst_ident ? in.k0 + (uint32_t)lane : g.dst_id[in.k0 + (uint32_t)lane];
             uint32_t v[EPL];
             auto gather = [&](uint32_t x) -> uint32_t {
+                if (filtered && x != NONE32 && !((ld_ro_u32(cur + (x >> 5)) >> (x & 31u)) & 1u))
+                    return NONE32; /* source unchanged by the previous pull */
                 return (x < hub_lim) ? hub32[x] : ((x != NONE32) ? s.prop32[x] : NONE32);
             };
             if (!in.anydone) {
@@ -881,12 +900,10 @@ __global__ void __launch_bounds__(PULL_THREADS, 1)
                         // changed bit (cleared before the pull) is still clear
                         s.prop32[vtx] = val;
                         atomicOr(&nxt[vtx >> 5], b);
-                        mass += g.outdeg[vtx];
-                        ++act;
+                        count_act(g.outdeg[vtx]);
                     } else if (val < atomicMin(&s.prop32[vtx], val)) {
                         if (!(atomicOr(&nxt[vtx >> 5], b) & b)) {
-                            mass += g.outdeg[vtx];
-                            ++act;
+                            count_act(g.outdeg[vtx]);
                         }
                     }
                 }
@@ -908,7 +925,7 @@ __global__ void __launch_bounds__(PULL_THREADS, 1)
 #pragma unroll
             for (int q = 0; q < EPL; ++q) {
                 v[q] = NONE64;
-                if (sa[q] != NONE32) {
+                if (sa[q] != NONE32 && (!filtered || ((ld_ro_u32(cur + (sa[q] >> 5)) >> (sa[q] & 31u)) & 1u))) {
                     const unsigned long long d = (sa[q] < hub_lim) ? hub64[sa[q]] : s.prop64[sa[q]];
                     if (g.weight_kind == WEDGE_WEIGHTS_F64)
                         v[q] = (unsigned long long)__double_as_longlong(
@@ -937,12 +954,10 @@ __global__ void __launch_bounds__(PULL_THREADS, 1)
                     if (kind == EMIT_COMPLETE) {
                         s.prop64[vtx] = val; /* sole writer, as for CC */
                         atomicOr(&nxt[vtx >> 5], b);
-                        mass += g.outdeg[vtx];
-                        ++act;
+                        count_act(g.outdeg[vtx]);
                     } else if (val < atomicMin(&s.prop64[vtx], val)) {
                         if (!(atomicOr(&nxt[vtx >> 5], b) & b)) {
-                            mass += g.outdeg[vtx];
-                            ++act;
+                            count_act(g.outdeg[vtx]);
                         }
                     }
                 }
@@ -1024,13 +1039,18 @@ __global__ void __launch_bounds__(PULL_THREADS, 1)
         sh_cnt[wib][CNT_TILES] = tiles;  // warp-uniform
         sh_cnt[wib][CNT_DSTS] = dsts;    // warp-uniform
         sh_cnt[wib][CNT_ACT] = act;
+        sh_cnt[wib][CNT_DEG0] = 0ull;
+        sh_cnt[wib][CNT_DEG1] = 0ull;
+        sh_cnt[wib][CNT_DEG2] = 0ull;
         sh_sum[wib] = psum;
     }
     __syncthreads();
-    if (threadIdx.x < 5) {
+    if (threadIdx.x < NCNT) {
         unsigned long long a = 0;
         for (int w = 0; w < WARPS; ++w)
             a += sh_cnt[w][threadIdx.x];
+        if (threadIdx.x >= CNT_DEG0)
+            a = sh_deg[threadIdx.x - CNT_DEG0];
         block_cnt[NCNT * blockIdx.x + threadIdx.x] = a;
     }
     if (APP == WEDGE_APP_PR && threadIdx.x == 0) {
@@ -1041,36 +1061,76 @@ __global__ void __launch_bounds__(PULL_THREADS, 1)
     }
 }
 
+// the fixed schedules; WEDGE_SCHED_LEARNED and WEDGE_SCHED_PROBE fall back to
+// the plain rule here (decide_kernel overrides it where they apply)
 __device__ __forceinline__ uint32_t choose_mode(uint32_t sched, unsigned long long mass, unsigned long long thr)
 {
     if (sched == WEDGE_SCHED_DENSE)
         return MODE_DENSE;
     if (sched == WEDGE_SCHED_WEDGE)
         return MODE_WEDGE;
+    if (sched == WEDGE_SCHED_FILTERED)
+        return MODE_FILTERED;
     return mass > thr ? MODE_DENSE : MODE_WEDGE; /* execution_bfs.c:141 */
+}
+
+__device__ __forceinline__ float log2_1p(double x) { return (float)log2(1.0 + x); }
+
+// Scheduler features of the next iteration, from the pull just finished (its
+// reduced counters) and the traversal so far.  Every feature is O(1) in size.
+__device__ void sched_features(const DevGraph& g, const Ctrl* c, uint32_t app, const unsigned long long (&cnt)[NCNT],
+                               float* f)
+{
+    const double V = (double)(g.V ? g.V : 1), E = (double)(g.E ? g.E : 1);
+    const double m = (double)cnt[CNT_MASS], act = (double)cnt[CNT_ACT];
+    const uint32_t tile_e = (app == WEDGE_APP_CC) ? 32u * PullEpl<WEDGE_APP_CC>::value
+                            : (app == WEDGE_APP_BFS) ? 32u * PullEpl<WEDGE_APP_BFS>::value
+                                                    : 32u * PullEpl<WEDGE_APP_SSSP>::value;
+    const double T = (double)((g.E + tile_e - 1) / tile_e) + 1.0;
+    const double a = act > 0.0 ? act : 1.0;
+    const double b0 = (double)cnt[CNT_DEG0], b1 = (double)cnt[CNT_DEG1], b2 = (double)cnt[CNT_DEG2];
+    f[0] = log2_1p(m) / 32.0f;              // out-edge mass of the activated vertices
+    f[1] = (float)(m / E);
+    f[2] = log2_1p(act) / 32.0f;            // activated vertices
+    f[3] = (float)(act / V);                // frontier bitmap density
+    f[4] = (float)((double)cnt[CNT_TILES] / T); // tiles the last pull visited
+    f[5] = (float)(b0 / a);                 // out-degree histogram of the activated vertices
+    f[6] = (float)(b1 / a);
+    f[7] = (float)(b2 / a);
+    f[8] = (float)((act - b0 - b1 - b2) / a);
+    f[9] = (float)((double)c->activated / V); // activated so far (BFS: visited fraction)
+    f[10] = log2_1p((double)c->iter) / 8.0f;
+    f[11] = (float)(log2(E) / 40.0);
+    f[12] = app == WEDGE_APP_BFS ? 1.0f : 0.0f;
+    f[13] = app == WEDGE_APP_CC ? 1.0f : 0.0f;
+    f[14] = app == WEDGE_APP_SSSP ? 1.0f : 0.0f;
+    f[15] = (float)(log2(E / V) / 8.0);     // average degree
 }
 
 // After a pull: reduce the block counters, count the iteration, stop when no
 // edge was activated (execution_bfs.c:239-251) or at the cap, choose the next
 // pull (execution_bfs.c:141, execution_cc.c:103).
 __device__ __forceinline__ void reduce_counters(const unsigned long long* block_cnt, uint32_t nblocks,
-                                                unsigned long long (&out)[5])
+                                                unsigned long long (&out)[NCNT])
 {
-    __shared__ unsigned long long sh[5][AUX_THREADS / 32];
-    unsigned long long x[5] = {0, 0, 0, 0, 0};
+    __shared__ unsigned long long sh[NCNT][AUX_THREADS / 32];
+    unsigned long long x[NCNT];
+#pragma unroll
+    for (int j = 0; j < (int)NCNT; ++j)
+        x[j] = 0ull;
     for (uint32_t i = threadIdx.x; i < nblocks; i += blockDim.x)
 #pragma unroll
-        for (int j = 0; j < 5; ++j)
+        for (int j = 0; j < (int)NCNT; ++j)
             x[j] += block_cnt[NCNT * i + j];
 #pragma unroll
-    for (int j = 0; j < 5; ++j) {
+    for (int j = 0; j < (int)NCNT; ++j) {
         x[j] = warp_sum_u64(x[j]);
         if ((threadIdx.x & 31) == 0)
             sh[j][threadIdx.x >> 5] = x[j];
     }
     __syncthreads();
 #pragma unroll
-    for (int j = 0; j < 5; ++j) {
+    for (int j = 0; j < (int)NCNT; ++j) {
         unsigned long long t = 0;
         for (int w = 0; w < AUX_THREADS / 32; ++w)
             t += sh[j][w];
@@ -1078,7 +1138,7 @@ __device__ __forceinline__ void reduce_counters(const unsigned long long* block_
     }
 }
 
-__device__ __forceinline__ void log_iteration(DevState& s, Ctrl* c, const unsigned long long (&cnt)[5])
+__device__ __forceinline__ void log_iteration(DevState& s, Ctrl* c, const unsigned long long (&cnt)[NCNT])
 {
     c->edges_scanned += cnt[CNT_EDGES];
     c->tiles_scanned += cnt[CNT_TILES];
@@ -1110,8 +1170,10 @@ __global__ void decide_kernel(DevGraph g, DevState s, const unsigned long long* 
     const uint32_t nsum = ((g.T + TILES_PER_REGION - 1) / TILES_PER_REGION + 31) / 32;
     for (uint32_t i = threadIdx.x; i < nsum; i += blockDim.x)
         s.summary[i] = 0u; /* the pull has cleared every chunk word it walked */
-    unsigned long long cnt[5];
+    unsigned long long cnt[NCNT];
     reduce_counters(block_cnt, nblocks, cnt);
+    __shared__ float feat[NF], xs[NF], h1[NH], h2[NH], pred[NO];
+    __shared__ uint32_t go;
     if (threadIdx.x == 0) {
         const unsigned long long m = cnt[CNT_MASS];
         if (c->mode == MODE_WEDGE)
@@ -1119,11 +1181,11 @@ __global__ void decide_kernel(DevGraph g, DevState s, const unsigned long long* 
         log_iteration(s, c, cnt);
         c->last_mass = m;
         c->mass = m;
-        if (app == WEDGE_APP_BFS)
-            c->parity ^= 1u;
+        c->parity ^= 1u;
         c->region_next = 0u;
         c->tiles = 0u;
         c->items = 0u;
+        go = 0u;
         if (m == 0ull) {
             c->done = 1u;
             c->loop = 0u;
@@ -1133,6 +1195,39 @@ __global__ void decide_kernel(DevGraph g, DevState s, const unsigned long long* 
             c->loop = 0u;
         } else {
             c->mode = choose_mode(c->sched, m, c->threshold);
+            if (c->sched == WEDGE_SCHED_PROBE && c->iter == c->probe_iter)
+                c->mode = c->probe_mode;
+            sched_features(g, c, app, cnt, feat);
+            if (c->iter < LOG_CAP) {
+                for (int i = 0; i < NF; ++i)
+                    s.log[c->iter].feat[i] = feat[i];
+                s.log[c->iter].learned = 0u;
+            }
+            go = (c->sched == WEDGE_SCHED_LEARNED && s.net) ? 1u : 0u;
+        }
+    }
+    __syncthreads();
+    if (!go)
+        return;
+    // the scheduler network: predicted log2 cost of each strategy
+    sched_forward_block(s.net, feat, xs, h1, h2, pred);
+    if (threadIdx.x == 0) {
+        const float* net = s.net;
+        bool in_range = true;
+        for (int i = 0; i < NF; ++i)
+            in_range = in_range && feat[i] >= net[OFF_LO + i] && feat[i] <= net[OFF_HI + i];
+        uint32_t best = MODE_DENSE;
+        for (uint32_t k = 1; k < (uint32_t)NO; ++k)
+            if (pred[k] < pred[best])
+                best = k;
+        if (app == WEDGE_APP_BFS && best == MODE_FILTERED)
+            best = MODE_DENSE; /* the BFS pull has no separate filtered form */
+        const uint32_t plain = c->mode;
+        if (in_range && best != plain && pred[plain] - pred[best] >= net[OFF_MARGIN]) {
+            c->mode = best;
+            c->learned_iters += 1u;
+            if (c->iter < LOG_CAP)
+                s.log[c->iter].learned = 1u;
         }
     }
 }
@@ -1158,15 +1253,16 @@ __device__ __forceinline__ void mark_chunk(const DevState& s, uint32_t ch, bool 
 // (wedge.c:37-46).  Each warp takes 32 bitmap words; per word, the lanes take
 // the set bits' vertices and expand their CSRI lists cooperatively (shuffle
 // scan of the list lengths, then every lane finds the list that owns each of
-// 32 consecutive entries).  Vertices with more than BIG out-edges are handed to
-// wedge_build_kernel as PIECE-sized work items instead.
+// 32 consecutive entries).  Lists longer than BIG_LIST go to
+// wedge_build_kernel as PIECE-sized work items instead (appended with one
+// atomic per warp): the degree relabelling puts the longest lists in the first
+// bitmap words, and one warp must not expand them alone.
 __global__ void collect_kernel(DevGraph g, DevState s, uint32_t app)
 {
-    constexpr unsigned long long BIG = 2048;
     Ctrl* c = s.ctrl;
     if (c->done || c->mode != MODE_WEDGE)
         return;
-    const uint32_t* fb = (app == WEDGE_APP_BFS) ? cur_front(s, c->parity) : s.front0;
+    const uint32_t* fb = cur_front(s, c->parity);
     const uint64_t nwords = (g.V + 31) / 32;
     const int lane = threadIdx.x & 31;
     const uint64_t gw = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) >> 5;
@@ -1180,16 +1276,30 @@ __global__ void collect_kernel(DevGraph g, DevState s, uint32_t app)
             const uint32_t bits = __shfl_sync(FULL, myword, w);
             const uint64_t v = (base + (uint64_t)w) * 32 + (uint64_t)lane;
             unsigned long long start = 0, len = 0;
+            uint32_t np = 0;
             if ((bits >> lane) & 1u) {
                 start = g.csri_off[v];
                 len = g.csri_off[v + 1] - start;
-                if (len > BIG) { /* hub: split into work items */
-                    const uint32_t np = (uint32_t)((len + PIECE - 1) / PIECE);
-                    const uint32_t pos = atomicAdd(&c->items, np);
-                    for (uint32_t q = 0; q < np; ++q)
-                        s.items[pos + q] = make_uint2((uint32_t)v, q);
+                if (len > BIG_LIST) { /* long list: work items */
+                    np = (uint32_t)((len + PIECE - 1) / PIECE);
                     len = 0;
                 }
+            }
+            uint32_t np_incl = np;
+#pragma unroll
+            for (int d = 1; d < 32; d <<= 1) {
+                const uint32_t y = __shfl_up_sync(FULL, np_incl, d);
+                if (lane >= d)
+                    np_incl += y;
+            }
+            const uint32_t np_total = __shfl_sync(FULL, np_incl, 31);
+            if (np_total) {
+                uint32_t pos = 0;
+                if (lane == 0)
+                    pos = atomicAdd(&c->items, np_total);
+                pos = __shfl_sync(FULL, pos, 0) + (np_incl - np);
+                for (uint32_t q = 0; q < np; ++q)
+                    s.items[pos + q] = make_uint2((uint32_t)v, q);
             }
             unsigned long long incl = len;
 #pragma unroll
@@ -1220,8 +1330,6 @@ __global__ void collect_kernel(DevGraph g, DevState s, uint32_t app)
     }
 }
 
-// Wedge frontier bits of the out-edges of hub vertices, one PIECE of a CSRI
-// list per warp (wedge.c:37-46).
 __global__ void wedge_build_kernel(DevGraph g, DevState s)
 {
     Ctrl* c = s.ctrl;
@@ -1311,7 +1419,7 @@ __global__ void advance_kernel(DevGraph g, DevState s, uint32_t app)
     Ctrl* c = s.ctrl;
     if (c->done)
         return;
-    uint32_t* fb = (app == WEDGE_APP_BFS) ? next_front(s, app, c->parity) : s.front0;
+    uint32_t* fb = next_front(s, c->parity);
     const uint64_t nwords = (g.V + 31) / 32;
     for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < nwords; i += (uint64_t)gridDim.x * blockDim.x)
         fb[i] = 0u;
@@ -1359,7 +1467,7 @@ __global__ void init_kernel(DevGraph g, DevState s, uint32_t app, uint32_t topen
 // root activation (execution_bfs.c:110-117, execution_sssp.c:83-88) and the
 // control block
 __global__ void init_root_kernel(DevGraph g, DevState s, uint32_t app, uint64_t root_in, uint32_t sched,
-                                 unsigned long long thr, uint32_t max_iter)
+                                 unsigned long long thr, uint32_t max_iter, uint32_t probe_iter, uint32_t probe_mode)
 {
     const uint32_t tid = blockIdx.x * blockDim.x + threadIdx.x;
     const uint64_t root = g.old2new[root_in]; /* the caller's id -> relabelled id */
@@ -1391,6 +1499,9 @@ __global__ void init_root_kernel(DevGraph g, DevState s, uint32_t app, uint64_t 
         c->loop = 1;
         c->error = 0;
         c->pull_launches = 0;
+        c->probe_iter = probe_iter;
+        c->probe_mode = probe_mode;
+        c->learned_iters = 0;
         c->pr_total = 0.0;
         c->pr_sum = 0.0;
         if (app == WEDGE_APP_CC) {
@@ -1402,6 +1513,13 @@ __global__ void init_root_kernel(DevGraph g, DevState s, uint32_t app, uint64_t 
             s.front0[root >> 5] |= 1u << (root & 31u);
             c->last_mass = g.outdeg[root];
             c->mode = choose_mode(sched, g.outdeg[root], thr);
+            if (sched == WEDGE_SCHED_PROBE && probe_iter == 0u)
+                c->mode = probe_mode;
+        }
+        if (s.log) {
+            for (int i = 0; i < 16; ++i)
+                s.log[0].feat[i] = 0.0f; /* iteration 0 is chosen before any pull: no features */
+            s.log[0].learned = 0u;
         }
         if (g.T == 0) {
             c->done = 1;
@@ -1460,7 +1578,7 @@ __global__ void pr_finish_kernel(DevGraph g, DevState s, uint32_t nblocks, const
         x = warp_sum_f64(x);
         if (lane == 0)
             sh[threadIdx.x >> 5] = x;
-        unsigned long long cnt[5];
+        unsigned long long cnt[NCNT];
         reduce_counters(block_cnt, nblocks, cnt); /* contains __syncthreads */
         if (threadIdx.x == 0) {
             double t = 0.0;
@@ -1714,7 +1832,7 @@ static int ensure_state(wedge_graph* h, int app, int precision)
         } else if ((rc = dalloc(h, &s.prop32, V, true))) {
             return rc;
         }
-        if ((rc = dalloc(h, &s.front0, nwords, true)) ||
+        if ((rc = dalloc(h, &s.front0, nwords, true)) || (rc = dalloc(h, &s.front1, nwords, true)) ||
             (rc = dalloc(h, &s.chunk_bits, (uint64_t)g.T / TILES_PER_WORD + REGION_WORDS + 2, true)) ||
             (rc = dalloc(h, &s.summary, (uint64_t)g.T / TILES_PER_REGION / 32 + 2, true)) ||
             (rc = dalloc(h, &s.tile_list, (uint64_t)g.T + 1, true)) ||
@@ -1725,7 +1843,7 @@ static int ensure_state(wedge_graph* h, int app, int precision)
                 return rc;
         }
         if (app == WEDGE_APP_BFS) {
-            if ((rc = dalloc(h, &s.front1, nwords, true)) || (rc = dalloc(h, &s.tile_open, (uint64_t)g.T / 32 + 2, true)))
+            if ((rc = dalloc(h, &s.tile_open, (uint64_t)g.T / 32 + 2, true)))
                 return rc;
         }
     }
@@ -1807,13 +1925,14 @@ static void launch_tail(wedge_graph* h, int app)
     advance_kernel<<<aux_grid(h, (h->g.V + 31) / 32), AUX_THREADS, 0, h->stream>>>(h->g, h->s, (uint32_t)app);
 }
 
-static void launch_init(wedge_graph* h, int app, uint64_t root, uint32_t sched, unsigned long long thr, uint32_t max_iter)
+static void launch_init(wedge_graph* h, int app, uint64_t root, uint32_t sched, unsigned long long thr, uint32_t max_iter,
+                        uint32_t probe_iter = 0xFFFFFFFFu, uint32_t probe_mode = MODE_DENSE)
 {
     const uint64_t work = h->g.V > h->g.T ? h->g.V : h->g.T;
     const uint32_t topen = (uint32_t)((h->g.E + 32u * PullEpl<WEDGE_APP_BFS>::value - 1) / (32u * PullEpl<WEDGE_APP_BFS>::value));
     init_kernel<<<aux_grid(h, work), AUX_THREADS, 0, h->stream>>>(h->g, h->s, (uint32_t)app, topen);
     init_root_kernel<<<aux_grid(h, h->g.Vne), AUX_THREADS, 0, h->stream>>>(h->g, h->s, (uint32_t)app, root, sched, thr,
-                                                                           max_iter);
+                                                                           max_iter, probe_iter, probe_mode);
     collect_kernel<<<aux_grid(h, (h->g.V + 31) / 32), AUX_THREADS, 0, h->stream>>>(h->g, h->s, (uint32_t)app);
     wedge_build_kernel<<<h->build_grid, AUX_THREADS, 0, h->stream>>>(h->g, h->s);
     launch_compact(h, app);
@@ -1886,7 +2005,7 @@ static int run_traversal(wedge_graph* h, int app, const wedge_params_t* p, wedge
             return rc;
     }
     WEDGE_CHECK(cudaEventRecord(h->ev[0], h->stream));
-    launch_init(h, app, root, (uint32_t)p->sched, thr, (uint32_t)cap);
+    launch_init(h, app, root, (uint32_t)p->sched, thr, (uint32_t)cap, p->probe_iter, (uint32_t)p->probe_mode);
     launches += 6;
     Ctrl c;
     if (use_graph) {
@@ -1909,7 +2028,7 @@ static int run_traversal(wedge_graph* h, int app, const wedge_params_t* p, wedge
             float a = 0, b = 0;
             cudaEventElapsedTime(&a, h->ev[2], h->ev[3]);
             cudaEventElapsedTime(&b, h->ev[3], h->ev[4]);
-            if (mode == MODE_DENSE)
+            if (mode != MODE_WEDGE)
                 t_pull_dense += a;
             else
                 t_pull_wedge += a;
@@ -2065,7 +2184,9 @@ static int check_params(const wedge_graph_t* g, int app, const wedge_params_t* p
 {
     if (!g || !p || app < WEDGE_APP_BFS || app > WEDGE_APP_SSSP)
         return WEDGE_ERR_ARG;
-    if (p->threshold_pct > 100 || p->sched < WEDGE_SCHED_PLAIN || p->sched > WEDGE_SCHED_WEDGE)
+    if (p->threshold_pct > 100 || p->sched < WEDGE_SCHED_PLAIN || p->sched > WEDGE_SCHED_PROBE)
+        return WEDGE_ERR_ARG;
+    if (p->sched == WEDGE_SCHED_PROBE && (p->probe_mode < WEDGE_MODE_DENSE || p->probe_mode > WEDGE_MODE_FILTERED))
         return WEDGE_ERR_ARG;
     if (app == WEDGE_APP_PR && (p->precision != WEDGE_PREC_FP64 && p->precision != WEDGE_PREC_FP32C))
         return WEDGE_ERR_ARG;
@@ -2228,8 +2349,36 @@ int wedge_cuda_iteration_log(wedge_graph_t* g, wedge_iteration_record_t* out, ui
         r.tiles_scanned = tmp[i].tiles;
         r.dsts_scanned = tmp[i].dsts;
         r.vertices_activated = tmp[i].activated;
+        r.mode = tmp[i].mode;
+        r.learned = tmp[i].learned;
+        for (int f = 0; f < WEDGE_SCHED_FEATURES; ++f)
+            r.features[f] = tmp[i].feat[f];
     }
     free(tmp);
+    return WEDGE_OK;
+}
+
+int wedge_cuda_set_scheduler(wedge_graph_t* g, const float* blob, uint64_t count)
+{
+    if (!g || !blob || count != (uint64_t)WEDGE_SCHED_BLOB)
+        return WEDGE_ERR_ARG;
+    for (uint64_t i = 0; i < (uint64_t)NF; ++i)
+        if (!(blob[OFF_SD + i] > 0.0f))
+            return WEDGE_ERR_ARG; /* standardisation divides by sd */
+    WEDGE_CHECK(cudaSetDevice(g->device));
+    if (!g->net) {
+        void* p = nullptr;
+        WEDGE_CHECK(cudaMalloc(&p, sizeof(float) * WEDGE_SCHED_BLOB));
+        g->net = (float*)p;
+    }
+    WEDGE_CHECK(cudaMemcpyAsync(g->net, blob, sizeof(float) * WEDGE_SCHED_BLOB, cudaMemcpyHostToDevice, g->stream));
+    WEDGE_CHECK(cudaStreamSynchronize(g->stream));
+    g->s.net = g->net;
+    if (g->graph_exec) { /* the captured kernels hold the state by value */
+        cudaGraphExecDestroy(g->graph_exec);
+        g->graph_exec = nullptr;
+        g->graph_app = -1;
+    }
     return WEDGE_OK;
 }
 

@@ -32,16 +32,23 @@ constexpr uint32_t CHUNKS_PER_TILE = TILE / CHUNK;        // 4
 constexpr uint32_t TILES_PER_WORD = 32 / CHUNKS_PER_TILE;  // 8 tiles per 32-bit chunk-bitmap word
 constexpr uint32_t REGION_WORDS = 32;                      // chunk-bitmap words per summary bit
 constexpr uint32_t TILES_PER_REGION = REGION_WORDS * TILES_PER_WORD;  // 256 tiles = 32768 in-edges
-constexpr uint32_t PIECE = 1024;                           // CSRI entries per Wedge-build work item
+constexpr uint32_t PIECE = 256;                            // CSRI entries per Wedge-build work item
+constexpr uint32_t BIG_LIST = 64;                          // longer CSRI lists are split into work items
 constexpr uint32_t NONE32 = 0xFFFFFFFFu;
 constexpr unsigned long long NONE64 = ~0ull;
 constexpr uint32_t FULL = 0xFFFFFFFFu;
 
-enum : uint32_t { MODE_DENSE = 0, MODE_WEDGE = 1 };
+// pull strategies: every tile; the tiles of the Wedge frontier; every tile with
+// gathers only from sources the previous pull changed (CC/SSSP; BFS = dense,
+// whose gathers are frontier bits already)
+enum : uint32_t { MODE_DENSE = 0, MODE_WEDGE = 1, MODE_FILTERED = 2 };
 
 // per-block counters written by the pulls (NCNT slots per block)
 constexpr uint32_t NCNT = 8;
-enum : uint32_t { CNT_MASS = 0, CNT_EDGES = 1, CNT_TILES = 2, CNT_DSTS = 3, CNT_ACT = 4 };
+enum : uint32_t { CNT_MASS = 0, CNT_EDGES = 1, CNT_TILES = 2, CNT_DSTS = 3, CNT_ACT = 4, CNT_DEG0 = 5, CNT_DEG1 = 6,
+                  CNT_DEG2 = 7 };
+// out-degree buckets of activated vertices (scheduler features): <= 4, <= 32, <= 256, more
+__host__ __device__ constexpr uint32_t degree_bucket(uint32_t d) { return d <= 4u ? 0u : d <= 32u ? 1u : d <= 256u ? 2u : 3u; }
 constexpr uint32_t LOG_CAP = 4096;  // iterations kept in the per-iteration log
 
 // one iteration of the per-iteration log (the ITERATION_STATS record of
@@ -53,8 +60,11 @@ struct IterRec {
     unsigned long long tiles;      // tiles visited
     unsigned long long dsts;       // destinations in visited tiles
     unsigned long long activated;  // vertices activated
-    unsigned int mode;             // MODE_DENSE / MODE_WEDGE
+    unsigned int mode;             // MODE_DENSE / MODE_WEDGE / MODE_FILTERED
     unsigned int iter;
+    float feat[16];                // scheduler features this iteration's mode was chosen on
+    unsigned int learned;          // 1 if the scheduler network chose the mode
+    unsigned int pad;
 };
 
 // Device control block of one traversal; read and written only by the
@@ -81,6 +91,9 @@ struct Ctrl {
     unsigned int loop;                 // 1 while the traversal continues (CUDA-graph loop condition)
     unsigned int error;                // kernel-detected error (bounds)
     unsigned int pull_launches;
+    unsigned int probe_iter;           // WEDGE_SCHED_PROBE: iteration whose mode is forced
+    unsigned int probe_mode;
+    unsigned int learned_iters;        // iterations whose mode the scheduler network chose
     unsigned int pad;
     double pr_total;                   // sum of all accumulators (phase_vertex_pr.c:161)
     double pr_sum;                     // PageRank Sum statistic
@@ -136,6 +149,7 @@ struct DevState {
     uint32_t hub_n;                // elements of the gathered array cached in shared memory by dense pulls
     uint32_t hub_bytes;            // their bytes: the pulls' dynamic shared memory (a multiple of 16)
     uint32_t hub_tile;             // CC/SSSP: first tile whose destinations all have ids >= hub_n
+    const float* net;              // scheduler network blob (WEDGE_SCHED_LEARNED), or null
 };
 
 }  // namespace wedge
@@ -154,6 +168,7 @@ struct wedge_graph {
     uint32_t pull_grid;                // persistent grid of the pull kernels (one 1024-thread block per SM)
     uint32_t build_grid;
     uint32_t hub_bytes;                // dynamic shared memory of the pull kernels (the hub cache)
+    float* net;                        // device copy of the scheduler network (wedge_cuda_set_scheduler)
     // allocations owned by the handle
     void* allocs[32];
     int nallocs;

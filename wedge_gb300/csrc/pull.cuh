@@ -1,16 +1,16 @@
-// Edge-pull kernels of the sm_103a engine.
+// Edge-pull building blocks of the sm_103a engine.
 //
-// One warp owns one 128-edge tile of the destination-grouped CSC at a time:
-// each lane loads 4 consecutive sources with one 128-bit load (a warp reads
-// the tile's 512 bytes in one coalesced request), gathers the 4 source
-// properties, and the warp folds them per destination with a segmented
-// reduction (lane-local runs, then a 5-step shuffle scan).  A destination
-// whose in-edges lie inside one tile is finished by that warp alone; one that
-// spans tiles (a hub) gets one partial per tile, combined with atomicMin for
-// the min-reductions and with a fixed-order fixup pass for PageRank sums.
-// This replaces the reference's per-thread vector loops and merge buffers
-// (phase_edge_pull_*.c, phases.c:54-114): every destination has exactly one
-// owner per tile, so no merge buffer is needed.
+// One warp owns one tile of 32*EPL consecutive in-edges of the
+// destination-grouped CSC at a time: lane l loads its EPL consecutive sources
+// (whole 32-byte sectors per lane), gathers the EPL source properties, and the
+// warp folds them per destination with a segmented reduction (lane-local runs,
+// then a 5-step shuffle scan).  A destination whose in-edges lie inside one
+// tile is finished by that warp alone; one that spans tiles (a hub) gets one
+// partial per tile, combined with atomicMin for the min-reductions and with a
+// fixed-order fixup pass for PageRank sums.  This replaces the reference's
+// per-thread vector loops and merge buffers (phase_edge_pull_*.c,
+// phases.c:54-114): every destination has exactly one owner per tile, so no
+// merge buffer is needed.
 #pragma once
 
 #include "engine.cuh"

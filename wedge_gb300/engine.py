@@ -24,7 +24,12 @@ LIB_PATH = os.path.join(PKG, "lib", "libwedge_cuda.so")
 APP_BFS, APP_CC, APP_PR, APP_SSSP = 0, 1, 2, 3
 WEIGHTS_NONE, WEIGHTS_U64, WEIGHTS_F64 = 0, 1, 2
 PREC_FP64, PREC_FP32C = 0, 1
-SCHED_PLAIN, SCHED_DENSE, SCHED_WEDGE = 0, 1, 2
+SCHED_PLAIN, SCHED_DENSE, SCHED_WEDGE, SCHED_FILTERED, SCHED_LEARNED, SCHED_PROBE = 0, 1, 2, 3, 4, 5
+MODE_DENSE, MODE_WEDGE, MODE_FILTERED = 0, 1, 2
+SCHED_FEATURES, SCHED_HIDDEN, SCHED_OUTPUTS = 16, 64, 3
+SCHED_PARAM_OFFSET = 64
+SCHED_PARAMS = 64 * 16 + 64 + 64 * 64 + 64 + 3 * 64 + 3
+SCHED_BLOB = SCHED_PARAM_OFFSET + SCHED_PARAMS + 1
 PHASE_INIT, PHASE_PULL_DENSE, PHASE_PULL_WEDGE, PHASE_VERTEX_PR, PHASE_WEDGE_BUILD, PHASE_ADVANCE = range(6)
 FLAG_GRAPH, FLAG_TIMING = 1, 2
 
@@ -54,11 +59,13 @@ def application_select(name: str) -> int:
 class Params(C.Structure):
     _fields_ = [("root", C.c_uint64), ("threshold_pct", C.c_uint32), ("num_iterations", C.c_uint32),
                 ("damping", C.c_double), ("precision", C.c_int32), ("sched", C.c_int32),
-                ("max_iterations", C.c_uint32), ("flags", C.c_uint32)]
+                ("max_iterations", C.c_uint32), ("flags", C.c_uint32), ("probe_iter", C.c_uint32),
+                ("probe_mode", C.c_int32)]
 
     def __init__(self, root=0, threshold_pct=20, num_iterations=1, damping=0.0, precision=PREC_FP64,
-                 sched=SCHED_PLAIN, max_iterations=0, flags=0):
-        super().__init__(root, threshold_pct, num_iterations, damping, precision, sched, max_iterations, flags)
+                 sched=SCHED_PLAIN, max_iterations=0, flags=0, probe_iter=0xFFFFFFFF, probe_mode=MODE_DENSE):
+        super().__init__(root, threshold_pct, num_iterations, damping, precision, sched, max_iterations, flags,
+                         probe_iter, probe_mode)
 
 
 class Stats(C.Structure):
@@ -76,10 +83,13 @@ class IterationRecord(C.Structure):
     _fields_ = [("active_edges", C.c_uint64), ("used_wedge", C.c_uint32), ("iteration", C.c_uint32),
                 ("pull_ms", C.c_double), ("wedge_ms", C.c_double), ("changed_mass", C.c_uint64),
                 ("edges_scanned", C.c_uint64), ("tiles_scanned", C.c_uint64), ("dsts_scanned", C.c_uint64),
-                ("vertices_activated", C.c_uint64)]
+                ("vertices_activated", C.c_uint64), ("mode", C.c_uint32), ("learned", C.c_uint32),
+                ("features", C.c_float * SCHED_FEATURES)]
 
     def as_dict(self):
-        return {k: getattr(self, k) for k, _ in self._fields_}
+        d = {k: getattr(self, k) for k, _ in self._fields_}
+        d["features"] = list(self.features)
+        return d
 
 
 class WedgeError(RuntimeError):
@@ -107,6 +117,12 @@ _SIGNATURES = {
     "wedge_cuda_read_results": (C.c_int, [C.c_void_p, C.c_void_p, C.c_uint64]),
     "wedge_cuda_iteration_log": (C.c_int, [C.c_void_p, C.c_void_p, C.c_uint64, C.POINTER(C.c_uint64)]),
     "wedge_cuda_read_outdegrees": (C.c_int, [C.c_void_p, C.c_void_p, C.c_uint64]),
+    "wedge_cuda_set_scheduler": (C.c_int, [C.c_void_p, C.c_void_p, C.c_uint64]),
+    "wedge_mlp_forward": (C.c_int, [C.c_void_p, C.c_void_p, C.c_uint64, C.c_void_p]),
+    "wedge_mlp_loss_grad": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_uint64,
+                                      C.POINTER(C.c_double), C.c_void_p]),
+    "wedge_mlp_train": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_uint64, C.c_uint32,
+                                  C.c_uint32, C.c_float, C.c_uint64, C.POINTER(C.c_double)]),
     "wedge_cuda_pr_iteration_noalloc": (C.c_int, [C.c_uint64, C.c_uint64, C.c_uint64, C.c_void_p, C.c_void_p,
                                                   C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_double,
                                                   C.c_void_p]),
@@ -252,6 +268,11 @@ class Graph:
                "wedge_cuda_iteration_log")
         return [recs[i].as_dict() for i in range(n.value)]
 
+    def set_scheduler(self, blob: np.ndarray):
+        """load a scheduler network (SCHED_BLOB float32) for SCHED_LEARNED runs"""
+        b = np.ascontiguousarray(blob, np.float32)
+        _check(lib().wedge_cuda_set_scheduler(self._h, _ptr(b), b.size), "wedge_cuda_set_scheduler")
+
     def read_outdegrees(self) -> np.ndarray:
         out = np.empty(self.V, np.uint64)
         _check(lib().wedge_cuda_read_outdegrees(self._h, _ptr(out), out.nbytes), "wedge_cuda_read_outdegrees")
@@ -287,3 +308,44 @@ def prop_string(app: int, prop: int, outdeg: int, num_vertices: int, sssp_f64: b
     if sssp_f64:
         return "%.17g" % d
     return "%d" % np.int64(np.uint64(prop).view(np.int64))  # execution_sssp.c:48-52
+
+
+# ---------------------------------------------------------------- scheduler network (CUDA kernels)
+def _f32(a, shape):
+    a = np.ascontiguousarray(a, np.float32)
+    if a.shape != shape:
+        raise ValueError(f"expected shape {shape}, got {a.shape}")
+    return a
+
+
+def mlp_forward(blob: np.ndarray, X: np.ndarray) -> np.ndarray:
+    """network outputs [n][3] for features X [n][16], computed by the engine's CUDA kernel"""
+    b = _f32(blob, (SCHED_BLOB,))
+    X = _f32(X, (len(X), SCHED_FEATURES))
+    out = np.empty((len(X), SCHED_OUTPUTS), np.float32)
+    _check(lib().wedge_mlp_forward(_ptr(b), _ptr(X), len(X), _ptr(out)), "wedge_mlp_forward")
+    return out
+
+
+def mlp_loss_grad(blob: np.ndarray, X: np.ndarray, Y: np.ndarray, M: np.ndarray):
+    """(loss, gradient over the trainable parameters) from the engine's CUDA kernels"""
+    n = len(X)
+    b = _f32(blob, (SCHED_BLOB,))
+    X, Y, M = _f32(X, (n, SCHED_FEATURES)), _f32(Y, (n, SCHED_OUTPUTS)), _f32(M, (n, SCHED_OUTPUTS))
+    g = np.empty(SCHED_PARAMS, np.float32)
+    loss = C.c_double()
+    _check(lib().wedge_mlp_loss_grad(_ptr(b), _ptr(X), _ptr(Y), _ptr(M), n, C.byref(loss), _ptr(g)),
+           "wedge_mlp_loss_grad")
+    return loss.value, g
+
+
+def mlp_train(blob: np.ndarray, X: np.ndarray, Y: np.ndarray, M: np.ndarray, epochs: int, batch: int = 256,
+              lr: float = 1e-3, seed: int = 1):
+    """Adam training on the GPU; returns (trained blob, final loss)"""
+    n = len(X)
+    b = np.array(_f32(blob, (SCHED_BLOB,)))
+    X, Y, M = _f32(X, (n, SCHED_FEATURES)), _f32(Y, (n, SCHED_OUTPUTS)), _f32(M, (n, SCHED_OUTPUTS))
+    loss = C.c_double()
+    _check(lib().wedge_mlp_train(_ptr(b), _ptr(X), _ptr(Y), _ptr(M), n, epochs, batch, C.c_float(lr), seed,
+                                 C.byref(loss)), "wedge_mlp_train")
+    return b, loss.value

@@ -1,0 +1,223 @@
+"""Learned scheduler: timing collection, training and evaluation.
+
+The engine can run each iteration's edge pull three ways (enum wedge_mode):
+dense (every tile), Wedge (the tiles of the Wedge frontier, built from the
+CSRI after the previous pull) and source-filtered (every tile, gathering only
+from sources the previous pull changed; CC and SSSP).  The reference picks
+between its two with a fixed threshold on the active out-edge mass
+(execution_bfs.c:132,141).  Here a small network (16 features -> 64 -> 64 -> 3)
+predicts the log2 cost of each strategy from features the engine computes on
+the device after every pull, and the engine takes the cheapest one
+(WEDGE_SCHED_LEARNED), keeping the fixed rule where the features leave the
+trained range or the predicted gain is below a margin.
+
+Training data are the engine's own per-iteration timings: for every iteration
+i of a traversal, the run is repeated with iteration i forced to each strategy
+(WEDGE_SCHED_PROBE) and the cost of the choice -- the tail of iteration i-1,
+which builds the Wedge frontier when i uses it, plus the pull of iteration i --
+is read from the iteration log (WEDGE_FLAG_TIMING).  Training runs on the GPU
+with the engine's forward/backward kernels (wedge_mlp_train).
+
+    python -m wedge_gb300.scheduler --out DIR     # collect, train, evaluate, write DIR/sched_net.f32
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import time
+
+import numpy as np
+
+from . import engine as W
+
+NF, NO = W.SCHED_FEATURES, W.SCHED_OUTPUTS
+DATA = os.path.join(os.path.dirname(os.path.abspath(__file__)), "data")
+DEFAULT_NET = os.path.join(DATA, "sched_net.f32")
+DEFAULT_SAMPLES = os.path.join(DATA, "sched_samples.json")
+
+
+def modes_for(app: int):
+    """strategies that differ for an application (BFS's pull is frontier-filtered already)"""
+    return (W.MODE_DENSE, W.MODE_WEDGE) if app == W.APP_BFS else (W.MODE_DENSE, W.MODE_WEDGE, W.MODE_FILTERED)
+
+
+def _cost_us(recs, i):
+    """cost of iteration i's choice: the tail of iteration i-1 (it builds the Wedge frontier i uses) + pull i"""
+    return 1e3 * (recs[i - 1]["wedge_ms"] + recs[i]["pull_ms"])
+
+
+def probe_costs(g: W.Graph, app: int, root: int = 0, threshold_pct: int = 20, reps: int = 3, max_probes: int = 24,
+                tag: str = ""):
+    """Per-iteration features and the measured cost of each strategy.
+
+    Returns a list of dicts: features[16], costs[3] (microseconds, NaN where not
+    measured), plain (the fixed rule's mode), iteration, app, tag."""
+    base = dict(root=root, threshold_pct=threshold_pct, flags=W.FLAG_TIMING)
+    g.run(app, W.Params(**base), allow_not_converged=True)  # warm-up
+    g.run(app, W.Params(**base), allow_not_converged=True)
+    plain = g.iteration_log()
+    n = len(plain)
+    its = list(range(1, n))
+    if len(its) > max_probes:  # long traversals (grids): evenly spaced iterations
+        its = sorted(set(int(round(x)) for x in np.linspace(1, n - 1, max_probes)))
+    out = []
+    for i in its:
+        costs = [math.nan] * NO
+        for m in modes_for(app):
+            ts = []
+            for _ in range(reps):
+                g.run(app, W.Params(sched=W.SCHED_PROBE, probe_iter=i, probe_mode=m, **base), allow_not_converged=True)
+                recs = g.iteration_log()
+                if len(recs) > i and recs[i]["mode"] == m:
+                    ts.append(_cost_us(recs, i))
+            if ts:
+                costs[m] = float(np.median(ts))
+        out.append({"features": list(plain[i]["features"]), "costs": costs, "plain": int(plain[i]["mode"]),
+                    "iteration": i, "app": app, "tag": tag})
+    return out
+
+
+def to_arrays(samples):
+    X = np.array([s["features"] for s in samples], np.float32)
+    C = np.array([s["costs"] for s in samples], np.float64)
+    M = np.isfinite(C).astype(np.float32)
+    Y = np.where(np.isfinite(C), np.log2(np.maximum(np.nan_to_num(C, nan=1.0), 1e-3)), 0.0).astype(np.float32)
+    return X, Y, M
+
+
+def init_blob(X: np.ndarray, seed: int, margin: float = 0.1) -> np.ndarray:
+    """Standardisation and trained range from the training features, He-initialised weights."""
+    rng = np.random.default_rng(seed)
+    mu = X.mean(0)
+    sd = np.maximum(X.std(0), 1e-3)
+    span = X.max(0) - X.min(0)
+    lo = X.min(0) - 0.1 * span - 1e-4
+    hi = X.max(0) + 0.1 * span + 1e-4
+    parts = [mu, sd, lo, hi]
+    for fan_in, shape in ((NF, (64, NF)), (None, (64,)), (64, (64, 64)), (None, (64,)), (64, (NO, 64)), (None, (NO,))):
+        if fan_in is None:
+            parts.append(np.zeros(shape))
+        else:
+            parts.append(rng.normal(0.0, math.sqrt(2.0 / fan_in), shape).ravel())
+    parts.append(np.array([margin]))
+    blob = np.concatenate([np.ravel(p) for p in parts]).astype(np.float32)
+    assert blob.size == W.SCHED_BLOB
+    return blob
+
+
+def choose(blob: np.ndarray, samples, pred=None):
+    """The engine's decision rule (decide_kernel) applied on the host to recorded samples:
+    network choice where in range and predicted to gain at least the margin, else the plain mode."""
+    X, _, _ = to_arrays(samples)
+    if pred is None:
+        pred = W.mlp_forward(blob, X)
+    lo, hi, margin = blob[2 * NF:3 * NF], blob[3 * NF:4 * NF], float(blob[-1])
+    out = []
+    for s, x, p in zip(samples, X, pred):
+        best = int(np.argmin(p))
+        if s["app"] == W.APP_BFS and best == W.MODE_FILTERED:
+            best = W.MODE_DENSE
+        plain = s["plain"]
+        in_range = bool(np.all(x >= lo) and np.all(x <= hi))
+        out.append(best if (in_range and best != plain and p[plain] - p[best] >= margin) else plain)
+    return out
+
+
+def evaluate(blob: np.ndarray, samples, pred=None):
+    """Cost of the plain, learned and per-iteration best choices over recorded samples (microseconds).
+    pred: network outputs for the samples (default: the engine's CUDA forward)."""
+    picks = choose(blob, samples, pred)
+    plain = learned = best = 0.0
+    changed = 0
+    for s, c in zip(samples, picks):
+        costs = s["costs"]
+        if not all(math.isfinite(costs[m]) for m in modes_for(s["app"])):
+            continue
+        plain += costs[s["plain"]]
+        learned += costs[c]
+        best += min(costs[m] for m in modes_for(s["app"]))
+        changed += int(c != s["plain"])
+    return {"plain_us": plain, "learned_us": learned, "best_us": best,
+            "gain": plain / learned if learned > 0 else 1.0, "regret_us": learned - best,
+            "plain_regret_us": plain - best, "iterations_changed": changed, "iterations": len(samples)}
+
+
+def train(samples, epochs: int = 1500, batch: int = 64, lr: float = 2e-3, seed: int = 7, margin: float = 0.1):
+    X, Y, M = to_arrays(samples)
+    blob = init_blob(X, seed, margin)
+    blob, loss = W.mlp_train(blob, X, Y, M, epochs=epochs, batch=batch, lr=lr, seed=seed)
+    return blob, loss
+
+
+def save(blob: np.ndarray, path: str):
+    os.makedirs(os.path.dirname(path) or ".", exist_ok=True)
+    np.asarray(blob, np.float32).tofile(path)
+
+
+def load(path: str = DEFAULT_NET) -> np.ndarray:
+    b = np.fromfile(path, np.float32)
+    if b.size != W.SCHED_BLOB:
+        raise ValueError(f"{path}: {b.size} floats, expected {W.SCHED_BLOB}")
+    return b
+
+
+# ---------------------------------------------------------------- training set
+TRAIN_RMAT = [(18, 16, 11), (20, 16, 12), (22, 16, 13), (24, 16, 14), (20, 8, 15), (22, 32, 16)]
+EVAL_RMAT = [(19, 16, 21), (21, 16, 22), (23, 16, 23)]
+TRAIN_GRID = [(512, 17), (1024, 18)]
+EVAL_GRID = [(768, 27)]
+
+
+def collect(rmat, grids, reps=3, log=print):
+    samples = []
+    for scale, ef, seed in rmat:
+        for app, sym, wk in ((W.APP_BFS, False, W.WEIGHTS_NONE), (W.APP_CC, True, W.WEIGHTS_NONE),
+                             (W.APP_SSSP, False, W.WEIGHTS_U64)):
+            t0 = time.time()
+            with W.Graph.rmat(scale, ef, seed, symmetrise=sym, weight_kind=wk) as g:
+                s = probe_costs(g, app, reps=reps, tag=f"rmat{scale}e{ef}s{seed}")
+            samples += s
+            log(f"rmat s{scale} ef{ef} seed{seed} app{app}: {len(s)} iterations probed in {time.time() - t0:.1f}s")
+    for side, seed in grids:
+        t0 = time.time()
+        with W.Graph.grid(side, 0.01, seed, W.WEIGHTS_U64) as g:
+            s = probe_costs(g, W.APP_SSSP, reps=reps, tag=f"grid{side}s{seed}")
+            samples += s
+        with W.Graph.grid(side, 0.01, seed, W.WEIGHTS_NONE) as g:
+            s2 = probe_costs(g, W.APP_BFS, reps=reps, tag=f"grid{side}s{seed}")
+            samples += s2
+        log(f"grid {side} seed{seed}: {len(s) + len(s2)} iterations probed in {time.time() - t0:.1f}s")
+    return samples
+
+
+def main():
+    ap = argparse.ArgumentParser(description=__doc__.split("\n")[0])
+    ap.add_argument("--out", required=True, help="directory for sched_net.f32, the samples and the summary")
+    ap.add_argument("--reps", type=int, default=3)
+    ap.add_argument("--epochs", type=int, default=1500)
+    ap.add_argument("--seed", type=int, default=7)
+    ap.add_argument("--margin", type=float, default=0.1)
+    a = ap.parse_args()
+    os.makedirs(a.out, exist_ok=True)
+    train_s = collect(TRAIN_RMAT, TRAIN_GRID, a.reps)
+    eval_s = collect(EVAL_RMAT, EVAL_GRID, a.reps)
+    t0 = time.time()
+    blob, loss = train(train_s, epochs=a.epochs, seed=a.seed, margin=a.margin)
+    t_train = time.time() - t0
+    save(blob, os.path.join(a.out, "sched_net.f32"))
+    with open(os.path.join(a.out, "sched_samples.json"), "w") as f:
+        json.dump({"train": train_s, "eval": eval_s}, f)
+    summary = {"train_samples": len(train_s), "eval_samples": len(eval_s), "final_loss": loss,
+               "train_seconds": t_train, "epochs": a.epochs, "margin": a.margin,
+               "train": evaluate(blob, train_s), "eval": evaluate(blob, eval_s)}
+    for app in (W.APP_BFS, W.APP_CC, W.APP_SSSP):
+        summary[f"eval_app{app}"] = evaluate(blob, [s for s in eval_s if s["app"] == app])
+    with open(os.path.join(a.out, "sched_summary.json"), "w") as f:
+        json.dump(summary, f, indent=1)
+    print(json.dumps(summary, indent=1))
+
+
+if __name__ == "__main__":
+    main()
