@@ -90,3 +90,17 @@ def rel_l1(a, b):
     a = np.asarray(a, np.float64)
     b = np.asarray(b, np.float64)
     return float(np.abs(a - b).sum() / np.abs(b).sum())
+
+
+def check_bfs_sorted(parents, V, src, dst, root, expect_levels):
+    """check_bfs for large graphs whose edges are sorted by (dst, src): levels equal
+    to expect_levels, every parent an in-neighbour, without sorting the edge list"""
+    level = levels_from_parents(parents, root)
+    assert np.array_equal(level, expect_levels), "BFS levels differ"
+    v = np.nonzero((parents != UNREACHED) & (np.arange(V) != root))[0]
+    q = (v.astype(np.uint64) << np.uint64(32)) | parents[v].astype(np.uint64)
+    keys = (dst.astype(np.uint64) << np.uint64(32)) | src.astype(np.uint64)
+    assert np.all(keys[1:] >= keys[:-1]), "edges are not sorted by (dst, src)"
+    pos = np.minimum(np.searchsorted(keys, q), len(keys) - 1)
+    assert np.all(keys[pos] == q), "a parent is not an in-neighbour"
+    return level
