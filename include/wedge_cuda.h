@@ -247,6 +247,51 @@ int wedge_mlp_loss_grad(const float* blob, const float* X, const float* Y, const
 int wedge_mlp_train(float* blob, const float* X, const float* Y, const float* M, uint64_t n, uint32_t epochs,
                     uint32_t batch, float lr, uint64_t seed, double* final_loss);
 
+/* ---------------------------------------------------------------- batched queries */
+
+/* No counterpart in the reference, which runs one query per process.  Many
+ * BFS and SSSP queries over many graphs run together in one persistent
+ * cooperative kernel: every iteration of every unfinished query is split into
+ * 32-edge chunks on one device work queue, and the Wedge frontiers of all
+ * queries are built in the same pass, so small and large queries share the
+ * GPU.  Results equal those of wedge_cuda_run on each query alone. */
+typedef struct wedge_query {
+    uint32_t graph;           /* index into the batch's graph array */
+    int32_t app;              /* WEDGE_APP_BFS or WEDGE_APP_SSSP (SSSP needs a weighted graph) */
+    uint64_t root;            /* the caller's vertex id; out of range selects 0 (main.c:81-85) */
+} wedge_query_t;
+
+typedef struct wedge_batch_tuning {
+    uint32_t threshold_pct;   /* dense pull iff active out-edge mass > t% of the query's edges (0: 20) */
+    uint32_t grab;            /* 32-edge chunks a warp takes from the queue at a time (0: 8) */
+    uint32_t blocks_per_sm;   /* persistent blocks per SM, at most the occupancy limit (0: that limit) */
+    uint32_t split;           /* out-degree above which the Wedge build expands a vertex with the whole
+                                 warp instead of one lane (0: 32) */
+} wedge_batch_tuning_t;
+
+typedef struct wedge_batch_stats {
+    double running_ms;        /* the persistent launch (and its setup kernels), CUDA events */
+    uint64_t rounds;          /* iterations of the slowest query */
+    uint64_t chunks_pulled;   /* queue items over all rounds */
+    uint64_t iterations;      /* iterations summed over queries */
+    uint32_t captured;        /* 1 if the run replayed a captured CUDA graph */
+    uint32_t blocks;          /* persistent blocks */
+} wedge_batch_stats_t;
+
+typedef struct wedge_batch wedge_batch_t;
+
+/* graphs: loaded handles on one device (kept alive by the caller until the batch is freed) */
+int wedge_cuda_batch_create(wedge_graph_t* const* graphs, uint32_t num_graphs, const wedge_query_t* queries,
+                            uint32_t num_queries, wedge_batch_t** out);
+/* tuning may be NULL (defaults); flags: WEDGE_FLAG_GRAPH captures setup + launch once and replays it */
+int wedge_cuda_batch_run(wedge_batch_t* b, const wedge_batch_tuning_t* tuning, uint32_t flags,
+                         wedge_batch_stats_t* stats);
+/* one query's graph_vertex_props (8 bytes per vertex of its graph, as wedge_cuda_read_results) */
+int wedge_cuda_batch_read_result(wedge_batch_t* b, uint32_t query, void* host_props, uint64_t bytes);
+/* iterations each query ran, host array of num_queries */
+int wedge_cuda_batch_iterations(wedge_batch_t* b, uint32_t* host_iterations, uint32_t num_queries);
+void wedge_cuda_batch_free(wedge_batch_t* b);
+
 /* ---------------------------------------------------------------- allocation-free iteration */
 
 /* No counterpart in the reference.  One PageRank iteration -- the edge pull

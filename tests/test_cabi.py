@@ -55,13 +55,14 @@ def test_null_handles_are_rejected(engine_lib):
 
 
 def test_struct_layout_matches_c(engine_lib, tmp_path):
-    from wedge_gb300.engine import IterationRecord, Params, Stats
+    from wedge_gb300.engine import BatchStats, BatchTuning, IterationRecord, Params, Query, Stats
 
     src = tmp_path / "layout.c"
     lines = ['#include <stdio.h>', '#include <stddef.h>', '#include "wedge_cuda.h"', "int main(void){"]
     want = []
     for cls, cname in ((Params, "wedge_params_t"), (Stats, "wedge_stats_t"),
-                       (IterationRecord, "wedge_iteration_record_t")):
+                       (IterationRecord, "wedge_iteration_record_t"), (Query, "wedge_query_t"),
+                       (BatchTuning, "wedge_batch_tuning_t"), (BatchStats, "wedge_batch_stats_t")):
         fields = [f for f, _ in cls._fields_]
         lines.append(f'printf("%zu\\n", sizeof({cname}));')
         lines += [f'printf("%zu\\n", offsetof({cname}, {f}));' for f in fields]

@@ -7,5 +7,5 @@ Build with ``wedge_gb300.build.build_all()``.
 from .engine import (APP_BFS, APP_CC, APP_PR, APP_SSSP, FLAG_GRAPH, FLAG_TIMING, MODE_DENSE,  # noqa: F401
                      MODE_FILTERED, MODE_WEDGE, PREC_FP32C, PREC_FP64, SCHED_BLOB, SCHED_DENSE, SCHED_FEATURES,
                      SCHED_FILTERED, SCHED_LEARNED, SCHED_PARAMS, SCHED_PLAIN, SCHED_PROBE, SCHED_WEDGE, WEIGHTS_F64,
-                     WEIGHTS_NONE, WEIGHTS_U64, Graph, Params, WedgeError, application_select, lib, mlp_forward,
+                     WEIGHTS_NONE, WEIGHTS_U64, Batch, BatchTuning, Graph, Params, Query, WedgeError, application_select, lib, mlp_forward,
                      mlp_loss_grad, mlp_train, prop_string, status_string)

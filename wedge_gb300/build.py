@@ -29,7 +29,7 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-I" + INCLUDE, "-I" + CSRC]
 NVCC_FLAGS += os.environ.get("WEDGE_NVCC_EXTRA", "").split()  # tuning experiments only
 
-CUDA_SOURCES = ["engine.cu", "graph.cu", "sched.cu"]
+CUDA_SOURCES = ["engine.cu", "graph.cu", "sched.cu", "batch.cu"]
 HOST_SOURCES = ["main.c", "cmdline.c", "application.c"]
 
 

@@ -92,6 +92,23 @@ class IterationRecord(C.Structure):
         return d
 
 
+class Query(C.Structure):
+    _fields_ = [("graph", C.c_uint32), ("app", C.c_int32), ("root", C.c_uint64)]
+
+
+class BatchTuning(C.Structure):
+    _fields_ = [("threshold_pct", C.c_uint32), ("grab", C.c_uint32), ("blocks_per_sm", C.c_uint32),
+                ("split", C.c_uint32)]
+
+
+class BatchStats(C.Structure):
+    _fields_ = [("running_ms", C.c_double), ("rounds", C.c_uint64), ("chunks_pulled", C.c_uint64),
+                ("iterations", C.c_uint64), ("captured", C.c_uint32), ("blocks", C.c_uint32)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
 class WedgeError(RuntimeError):
     def __init__(self, status: int, what: str):
         super().__init__(f"{what}: {status_string(status)} ({status})")
@@ -118,6 +135,11 @@ _SIGNATURES = {
     "wedge_cuda_iteration_log": (C.c_int, [C.c_void_p, C.c_void_p, C.c_uint64, C.POINTER(C.c_uint64)]),
     "wedge_cuda_read_outdegrees": (C.c_int, [C.c_void_p, C.c_void_p, C.c_uint64]),
     "wedge_cuda_set_scheduler": (C.c_int, [C.c_void_p, C.c_void_p, C.c_uint64]),
+    "wedge_cuda_batch_create": (C.c_int, [C.c_void_p, C.c_uint32, C.c_void_p, C.c_uint32, C.POINTER(C.c_void_p)]),
+    "wedge_cuda_batch_run": (C.c_int, [C.c_void_p, C.POINTER(BatchTuning), C.c_uint32, C.POINTER(BatchStats)]),
+    "wedge_cuda_batch_read_result": (C.c_int, [C.c_void_p, C.c_uint32, C.c_void_p, C.c_uint64]),
+    "wedge_cuda_batch_iterations": (C.c_int, [C.c_void_p, C.c_void_p, C.c_uint32]),
+    "wedge_cuda_batch_free": (None, [C.c_void_p]),
     "wedge_mlp_forward": (C.c_int, [C.c_void_p, C.c_void_p, C.c_uint64, C.c_void_p]),
     "wedge_mlp_loss_grad": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_uint64,
                                       C.POINTER(C.c_double), C.c_void_p]),
@@ -349,3 +371,52 @@ def mlp_train(blob: np.ndarray, X: np.ndarray, Y: np.ndarray, M: np.ndarray, epo
     _check(lib().wedge_mlp_train(_ptr(b), _ptr(X), _ptr(Y), _ptr(M), n, epochs, batch, C.c_float(lr), seed,
                                  C.byref(loss)), "wedge_mlp_train")
     return b, loss.value
+
+
+# ---------------------------------------------------------------- batched queries
+class Batch:
+    """Many BFS / SSSP queries over many resident graphs, run together in one
+    persistent kernel (wedge_cuda_batch_*).  queries: (graph index, app, root)."""
+
+    def __init__(self, graphs, queries):
+        self._graphs = list(graphs)  # kept alive: the batch uses their device arrays
+        hs = (C.c_void_p * len(self._graphs))(*[g._h.value if isinstance(g._h, C.c_void_p) else g._h
+                                                for g in self._graphs])
+        qs = (Query * len(queries))(*[Query(int(gi), int(app), int(root)) for gi, app, root in queries])
+        self.queries = list(queries)
+        self._h = C.c_void_p()
+        _check(lib().wedge_cuda_batch_create(C.cast(hs, C.c_void_p), len(self._graphs), C.cast(qs, C.c_void_p),
+                                             len(queries), C.byref(self._h)), "wedge_cuda_batch_create")
+
+    def run(self, tuning: BatchTuning | None = None, flags: int = 0) -> dict:
+        st = BatchStats()
+        _check(lib().wedge_cuda_batch_run(self._h, C.byref(tuning) if tuning is not None else None, flags,
+                                          C.byref(st)), "wedge_cuda_batch_run")
+        return st.as_dict()
+
+    def read_result(self, q: int) -> np.ndarray:
+        out = np.empty(self._graphs[self.queries[q][0]].V, np.uint64)
+        _check(lib().wedge_cuda_batch_read_result(self._h, q, _ptr(out), out.nbytes), "wedge_cuda_batch_read_result")
+        return out
+
+    def iterations(self) -> np.ndarray:
+        out = np.empty(len(self.queries), np.uint32)
+        _check(lib().wedge_cuda_batch_iterations(self._h, _ptr(out), len(out)), "wedge_cuda_batch_iterations")
+        return out
+
+    def close(self):
+        if self._h:
+            lib().wedge_cuda_batch_free(self._h)
+            self._h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
