@@ -198,6 +198,14 @@ int wedge_cuda_generate_rmat(uint32_t scale, uint32_t edge_factor, double a, dou
 /* side x side 4-neighbour grid, both directions, plus floor(frac * 4*side*(side-1)) random directed pairs */
 int wedge_cuda_generate_grid(uint32_t side, double long_range_frac, uint64_t seed, int weight_kind,
                              wedge_graph_t** out);
+/* The same generators' edge lists, sorted by (dst, src) as the reference's file format
+ * orders them (README.md:42-50), into host arrays of `capacity` entries (the wedge-gen
+ * writer).  With src == NULL only *V and *E are returned. */
+int wedge_cuda_rmat_edge_list(uint32_t scale, uint32_t edge_factor, double a, double b, double c, uint64_t seed,
+                              int symmetrise, uint64_t* V, uint64_t* E, uint32_t* src, uint32_t* dst,
+                              uint64_t capacity);
+int wedge_cuda_grid_edge_list(uint32_t side, double long_range_frac, uint64_t seed, uint64_t* V, uint64_t* E,
+                              uint32_t* src, uint32_t* dst, uint64_t capacity);
 
 /* ---------------------------------------------------------------- running */
 
@@ -222,6 +230,12 @@ int wedge_cuda_iteration_log(wedge_graph_t* g, wedge_iteration_record_t* out, ui
 int wedge_cuda_read_results(wedge_graph_t* g, void* host_props, uint64_t bytes);
 /* graph_vertex_outdegrees as uint64 counts; bytes >= 8*V */
 int wedge_cuda_read_outdegrees(wedge_graph_t* g, uint64_t* host_outdeg, uint64_t bytes);
+/* The -o output of the last run (source/main.c:112-150: one "%llu %s\n" line per vertex in
+ * the format of execution_get_vertex_prop_string_*), written to `path`.  BFS, CC and
+ * uint64 SSSP lines are formatted on the GPU (a length pass, a scan, a write pass) and
+ * written with one fwrite; PageRank's %.4le and FP64 SSSP distances are formatted on the
+ * host.  *gpu_formatted tells which; format_ms is the formatting time (both optional). */
+int wedge_cuda_write_output(wedge_graph_t* g, const char* path, int* gpu_formatted, double* format_ms);
 
 /* ---------------------------------------------------------------- learned scheduler */
 

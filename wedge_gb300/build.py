@@ -88,9 +88,22 @@ def build_cli(force: bool = False) -> str:
     return exe
 
 
+def build_gen(force: bool = False) -> str:
+    """Compile bin/wedge-gen, the writer of the synthetic graphs in the reference's file format."""
+    os.makedirs(OUT_BIN, exist_ok=True)
+    exe = os.path.join(OUT_BIN, "wedge-gen")
+    src = os.path.join(HOST, "gen.c")
+    lib = os.path.join(OUT_LIB, LIB_NAME)
+    if force or _stale(exe, [src, lib] + _headers()):
+        _run(["gcc", "-O2", "-std=gnu11", "-Wall", "-I" + INCLUDE, src, "-o", exe, "-L" + OUT_LIB, "-lwedge_cuda",
+              "-Wl,-rpath,$ORIGIN/../lib"])
+    return exe
+
+
 def build_all(force: bool = False, verbose: bool = False) -> None:
     build_lib(force=force, verbose=verbose)
     build_cli(force=force)
+    build_gen(force=force)
 
 
 if __name__ == "__main__":

@@ -17,6 +17,7 @@
 
 #include <pthread.h>
 #include <stdio.h>
+#include <time.h>
 #include <stdlib.h>
 #include <string.h>
 
@@ -1683,6 +1684,75 @@ __global__ void export_kernel(DevGraph g, DevState s, uint32_t app, unsigned lon
     }
 }
 
+// -o output on the device (source/main.c:112-150): "%llu %s\n" per vertex, with
+// the value as execution_get_vertex_prop_string_{bfs,cc,sssp} print it:
+// BFS and SSSP "%lld" of the 64-bit word (UINT64_MAX prints -1), CC "%.0lf" of
+// an integer label (exact).  A length pass, an exclusive scan, a write pass.
+__device__ __forceinline__ void out_value(const DevGraph& g, const DevState& s, uint32_t app, uint64_t o, bool& neg,
+                                          unsigned long long& x)
+{
+    const uint32_t v = g.old2new[o];
+    neg = false;
+    if (app == WEDGE_APP_BFS) {
+        const uint32_t p = s.prop32[v];
+        neg = p == NONE32;
+        x = neg ? 1ull : (unsigned long long)g.new2old[p];
+    } else if (app == WEDGE_APP_CC) {
+        x = s.prop32[v];
+    } else {
+        const unsigned long long d = s.prop64[v];
+        neg = (long long)d < 0;
+        x = neg ? (unsigned long long)(-(long long)d) : d;
+    }
+}
+
+__device__ __forceinline__ uint32_t dec_len(unsigned long long x)
+{
+    uint32_t n = 1;
+    while (x >= 10ull) {
+        x /= 10ull;
+        ++n;
+    }
+    return n;
+}
+
+__device__ __forceinline__ void dec_put(char* p, unsigned long long x, uint32_t n)
+{
+    for (uint32_t i = n; i-- > 0;) {
+        p[i] = (char)('0' + (int)(x % 10ull));
+        x /= 10ull;
+    }
+}
+
+__global__ void out_len_kernel(DevGraph g, DevState s, uint32_t app, unsigned long long* len)
+{
+    for (uint64_t o = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; o < g.V; o += (uint64_t)gridDim.x * blockDim.x) {
+        bool neg;
+        unsigned long long x;
+        out_value(g, s, app, o, neg, x);
+        len[o] = dec_len(o) + 1u + (neg ? 1u : 0u) + dec_len(x) + 1u;
+    }
+}
+
+__global__ void out_write_kernel(DevGraph g, DevState s, uint32_t app, const unsigned long long* off, char* buf)
+{
+    for (uint64_t o = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; o < g.V; o += (uint64_t)gridDim.x * blockDim.x) {
+        bool neg;
+        unsigned long long x;
+        out_value(g, s, app, o, neg, x);
+        char* p = buf + off[o];
+        const uint32_t n0 = dec_len(o);
+        dec_put(p, o, n0);
+        p += n0;
+        *p++ = ' ';
+        if (neg)
+            *p++ = '-';
+        const uint32_t n1 = dec_len(x);
+        dec_put(p, x, n1);
+        p[n1] = '\n';
+    }
+}
+
 __global__ void export_outdeg_kernel(DevGraph g, unsigned long long* out)
 {
     for (uint64_t o = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; o < g.V; o += (uint64_t)gridDim.x * blockDim.x)
@@ -2298,6 +2368,88 @@ int wedge_cuda_read_results(wedge_graph_t* g, void* host_props, uint64_t bytes)
     WEDGE_CHECK(e);
     WEDGE_CHECK(cudaStreamSynchronize(g->stream));
     return WEDGE_OK;
+}
+
+int wedge_cuda_write_output(wedge_graph_t* g, const char* path, int* gpu_formatted, double* format_ms)
+{
+    if (!g || !path || g->last_app < 0)
+        return WEDGE_ERR_ARG;
+    WEDGE_CHECK(cudaSetDevice(g->device));
+    const uint64_t V = g->g.V;
+    const int app = g->last_app;
+    const bool on_gpu = app == WEDGE_APP_BFS || app == WEDGE_APP_CC ||
+                        (app == WEDGE_APP_SSSP && g->g.weight_kind != WEDGE_WEIGHTS_F64);
+    FILE* f = fopen(path, "w");
+    if (!f)
+        return WEDGE_ERR_IO;
+    int rc = WEDGE_OK;
+    float ms = 0.0f;
+    if (on_gpu) {
+        unsigned long long *len = nullptr, *off = nullptr;
+        char* dbuf = nullptr;
+        char* hbuf = nullptr;
+        unsigned long long total = 0;
+        cudaEventRecord(g->ev[0], g->stream);
+        if (cudaMalloc((void**)&len, 8ull * (V + 1)) != cudaSuccess || cudaMalloc((void**)&off, 8ull * (V + 1)) != cudaSuccess) {
+            rc = WEDGE_ERR_OOM;
+        } else {
+            cudaMemsetAsync(len + V, 0, 8, g->stream);
+            out_len_kernel<<<aux_grid(g, V), AUX_THREADS, 0, g->stream>>>(g->g, g->s, (uint32_t)app, len);
+            rc = device_scan(g, len, off, V + 1, false);
+            if (!rc && (cudaMemcpyAsync(&total, off + V, 8, cudaMemcpyDeviceToHost, g->stream) != cudaSuccess ||
+                        cudaStreamSynchronize(g->stream) != cudaSuccess))
+                rc = WEDGE_ERR_CUDA;
+            if (!rc && (cudaMalloc((void**)&dbuf, total ? total : 1) != cudaSuccess ||
+                        cudaMallocHost((void**)&hbuf, total ? total : 1) != cudaSuccess))
+                rc = WEDGE_ERR_OOM;
+            if (!rc) {
+                out_write_kernel<<<aux_grid(g, V), AUX_THREADS, 0, g->stream>>>(g->g, g->s, (uint32_t)app, off, dbuf);
+                if (cudaMemcpyAsync(hbuf, dbuf, total, cudaMemcpyDeviceToHost, g->stream) != cudaSuccess ||
+                    cudaEventRecord(g->ev[1], g->stream) != cudaSuccess || cudaStreamSynchronize(g->stream) != cudaSuccess)
+                    rc = WEDGE_ERR_CUDA;
+                cudaEventElapsedTime(&ms, g->ev[0], g->ev[1]);
+            }
+            if (!rc && fwrite(hbuf, 1, total, f) != total)
+                rc = WEDGE_ERR_IO;
+        }
+        cudaFree(len);
+        cudaFree(off);
+        cudaFree(dbuf);
+        if (hbuf)
+            cudaFreeHost(hbuf);
+    } else {
+        /* execution_pr.c:31-35 (%.4le of rank * outdegree'), FP64 SSSP distances (%.17g) */
+        uint64_t* props = (uint64_t*)malloc(8 * (V ? V : 1));
+        uint64_t* od = (uint64_t*)malloc(8 * (V ? V : 1));
+        if (!props || !od) {
+            rc = WEDGE_ERR_OOM;
+        } else if ((rc = wedge_cuda_read_results(g, props, 8 * V)) == WEDGE_OK &&
+                   (rc = wedge_cuda_read_outdegrees(g, od, 8 * V)) == WEDGE_OK) {
+            struct timespec t0, t1;
+            clock_gettime(CLOCK_MONOTONIC, &t0);
+            for (uint64_t v = 0; v < V && !ferror(f); ++v) {
+                double d;
+                memcpy(&d, &props[v], sizeof(d));
+                if (app == WEDGE_APP_PR)
+                    fprintf(f, "%llu %.4le\n", (unsigned long long)v, d * (od[v] == 0 ? (double)V : (double)od[v]));
+                else
+                    fprintf(f, "%llu %.17g\n", (unsigned long long)v, d);
+            }
+            clock_gettime(CLOCK_MONOTONIC, &t1);
+            ms = (float)((t1.tv_sec - t0.tv_sec) * 1e3 + (t1.tv_nsec - t0.tv_nsec) / 1e6);
+            if (ferror(f))
+                rc = WEDGE_ERR_IO;
+        }
+        free(props);
+        free(od);
+    }
+    if (fclose(f) != 0 && rc == WEDGE_OK)
+        rc = WEDGE_ERR_IO;
+    if (gpu_formatted)
+        *gpu_formatted = on_gpu ? 1 : 0;
+    if (format_ms)
+        *format_ms = ms;
+    return rc;
 }
 
 int wedge_cuda_read_outdegrees(wedge_graph_t* g, uint64_t* host_outdeg, uint64_t bytes)

@@ -593,4 +593,84 @@ int wedge_cuda_generate_grid(uint32_t side, double long_range_frac, uint64_t see
     return WEDGE_OK;
 }
 
+// generated keys -> (dst, src)-sorted host arrays
+static int keys_to_host(unsigned long long* keys, uint64_t E, uint32_t sbits, uint32_t* src, uint32_t* dst)
+{
+    cudaStream_t st = nullptr;
+    unsigned long long* alt = nullptr;
+    uint32_t *ds = nullptr, *dd = nullptr;
+    void* tmp = nullptr;
+    int rc = WEDGE_OK;
+    cub::DoubleBuffer<unsigned long long> db(keys, nullptr);
+    size_t tb = 0;
+    if (cudaMalloc((void**)&alt, (E ? E : 1) * sizeof(unsigned long long)) != cudaSuccess ||
+        cudaMalloc((void**)&ds, (E ? E : 1) * sizeof(uint32_t)) != cudaSuccess ||
+        cudaMalloc((void**)&dd, (E ? E : 1) * sizeof(uint32_t)) != cudaSuccess) {
+        rc = WEDGE_ERR_OOM;
+    } else {
+        db = cub::DoubleBuffer<unsigned long long>(keys, alt);
+        if (cub::DeviceRadixSort::SortKeys(nullptr, tb, db, (long long)E, 0, (int)(2 * sbits), st) != cudaSuccess ||
+            cudaMalloc(&tmp, tb ? tb : 1) != cudaSuccess ||
+            cub::DeviceRadixSort::SortKeys(tmp, tb, db, (long long)E, 0, (int)(2 * sbits), st) != cudaSuccess) {
+            rc = WEDGE_ERR_CUDA;
+        } else {
+            if (E)
+                unpack_keys_kernel<<<grid_of(E, 152), 256, 0, st>>>(db.Current(), E, sbits, WEDGE_WEIGHTS_NONE, ds, dd,
+                                                                    nullptr);
+            if (cudaMemcpy(src, ds, E * sizeof(uint32_t), cudaMemcpyDeviceToHost) != cudaSuccess ||
+                cudaMemcpy(dst, dd, E * sizeof(uint32_t), cudaMemcpyDeviceToHost) != cudaSuccess)
+                rc = WEDGE_ERR_CUDA;
+        }
+    }
+    cudaFree(tmp);
+    cudaFree(alt);
+    cudaFree(ds);
+    cudaFree(dd);
+    cudaFree(keys);
+    return rc;
+}
+
+int wedge_cuda_rmat_edge_list(uint32_t scale, uint32_t edge_factor, double a, double b, double c, uint64_t seed,
+                              int symmetrise, uint64_t* V, uint64_t* E, uint32_t* src, uint32_t* dst, uint64_t capacity)
+{
+    if (!V || !E || scale < 1 || scale > 31 || edge_factor == 0 || a < 0 || b < 0 || c < 0 || a + b + c > 1.0)
+        return WEDGE_ERR_ARG;
+    const uint64_t E0 = (uint64_t)edge_factor << scale;
+    *V = 1ull << scale;
+    *E = symmetrise ? 2 * E0 : E0;
+    if (!src)
+        return WEDGE_OK;
+    if (!dst || capacity < *E)
+        return WEDGE_ERR_ARG;
+    unsigned long long* keys = nullptr;
+    if (cudaMalloc((void**)&keys, *E * sizeof(unsigned long long)) != cudaSuccess)
+        return WEDGE_ERR_OOM;
+    const unsigned long long ta = (unsigned long long)(a * 4294967296.0);
+    const unsigned long long tab = (unsigned long long)((a + b) * 4294967296.0);
+    const unsigned long long tabc = (unsigned long long)((a + b + c) * 4294967296.0);
+    rmat_kernel<<<grid_of(E0, 152), 256>>>(scale, ta, tab, tabc, seed, E0, symmetrise ? 1 : 0, scale, keys);
+    return keys_to_host(keys, *E, scale, src, dst);
+}
+
+int wedge_cuda_grid_edge_list(uint32_t side, double long_range_frac, uint64_t seed, uint64_t* V, uint64_t* E,
+                              uint32_t* src, uint32_t* dst, uint64_t capacity)
+{
+    if (!V || !E || side < 2 || side > 65535 || long_range_frac < 0.0)
+        return WEDGE_ERR_ARG;
+    const uint64_t base = 4ull * side * (side - 1ull);
+    const uint64_t lr = (uint64_t)(long_range_frac * (double)base);
+    *V = (uint64_t)side * side;
+    *E = base + lr;
+    if (!src)
+        return WEDGE_OK;
+    if (!dst || capacity < *E)
+        return WEDGE_ERR_ARG;
+    const uint32_t sbits = bits_for(*V);
+    unsigned long long* keys = nullptr;
+    if (cudaMalloc((void**)&keys, *E * sizeof(unsigned long long)) != cudaSuccess)
+        return WEDGE_ERR_OOM;
+    grid_kernel<<<grid_of(*E, 152), 256>>>(side, lr, seed, sbits, keys);
+    return keys_to_host(keys, *E, sbits, src, dst);
+}
+
 }  // extern "C"

@@ -135,6 +135,12 @@ _SIGNATURES = {
     "wedge_cuda_iteration_log": (C.c_int, [C.c_void_p, C.c_void_p, C.c_uint64, C.POINTER(C.c_uint64)]),
     "wedge_cuda_read_outdegrees": (C.c_int, [C.c_void_p, C.c_void_p, C.c_uint64]),
     "wedge_cuda_set_scheduler": (C.c_int, [C.c_void_p, C.c_void_p, C.c_uint64]),
+    "wedge_cuda_write_output": (C.c_int, [C.c_void_p, C.c_char_p, C.POINTER(C.c_int), C.POINTER(C.c_double)]),
+    "wedge_cuda_rmat_edge_list": (C.c_int, [C.c_uint32, C.c_uint32, C.c_double, C.c_double, C.c_double, C.c_uint64,
+                                            C.c_int, C.POINTER(C.c_uint64), C.POINTER(C.c_uint64), C.c_void_p,
+                                            C.c_void_p, C.c_uint64]),
+    "wedge_cuda_grid_edge_list": (C.c_int, [C.c_uint32, C.c_double, C.c_uint64, C.POINTER(C.c_uint64),
+                                            C.POINTER(C.c_uint64), C.c_void_p, C.c_void_p, C.c_uint64]),
     "wedge_cuda_batch_create": (C.c_int, [C.c_void_p, C.c_uint32, C.c_void_p, C.c_uint32, C.POINTER(C.c_void_p)]),
     "wedge_cuda_batch_run": (C.c_int, [C.c_void_p, C.POINTER(BatchTuning), C.c_uint32, C.POINTER(BatchStats)]),
     "wedge_cuda_batch_read_result": (C.c_int, [C.c_void_p, C.c_uint32, C.c_void_p, C.c_uint64]),
@@ -294,6 +300,13 @@ class Graph:
         """load a scheduler network (SCHED_BLOB float32) for SCHED_LEARNED runs"""
         b = np.ascontiguousarray(blob, np.float32)
         _check(lib().wedge_cuda_set_scheduler(self._h, _ptr(b), b.size), "wedge_cuda_set_scheduler")
+
+    def write_output(self, path: str):
+        """the -o file of the last run; returns (formatted on the GPU, formatting ms)"""
+        on_gpu, ms = C.c_int(), C.c_double()
+        _check(lib().wedge_cuda_write_output(self._h, path.encode(), C.byref(on_gpu), C.byref(ms)),
+               "wedge_cuda_write_output")
+        return bool(on_gpu.value), ms.value
 
     def read_outdegrees(self) -> np.ndarray:
         out = np.empty(self.V, np.uint64)

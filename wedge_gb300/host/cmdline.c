@@ -32,7 +32,10 @@ static void usage_and_exit(const char* argv0)
            CMDLINE_DEFAULT_FRONTIER_THRESHOLD_PCT);
     printf("  -u node[,node...]     Accepted for compatibility; ignored on the GPU.\n");
     printf("  -V                    Prints version information and exits.\n");
-    printf("  --sched=plain|dense|wedge   iteration strategy (default plain = fixed threshold)\n");
+    printf("  --sched=plain|dense|wedge|filtered|learned\n");
+    printf("                              iteration strategy (default plain = fixed threshold)\n");
+    printf("  --scheduler=<file>          network for --sched=learned (WEDGE_SCHED_BLOB floats)\n");
+    printf("  --iteration-stats           per-iteration CSV on stderr: active edges, used Wedge, pull ms, Wedge ms\n");
     printf("  --prec=fp64|fp32c           PageRank arithmetic (default fp64)\n");
     printf("  --damping=<d>               PageRank damping (default 0.875, as the reference)\n");
     printf("  --weights=u64|f64           SSSP weight words (default u64, as the reference)\n");
@@ -71,6 +74,16 @@ static int parse_long_option(const char* arg)
         opts.timing = 1;
         return 1;
     }
+    if (strcmp(arg, "--iteration-stats") == 0) {
+        opts.iteration_stats = 1;
+        return 1;
+    }
+    if (strncmp(arg, "--scheduler=", 12) == 0) {
+        if (!arg[12])
+            return -1;
+        opts.scheduler_file = (char*)arg + 12;
+        return 1;
+    }
     if (strncmp(arg, "--sched=", 8) == 0) {
         const char* v = arg + 8;
         if (!strcmp(v, "plain"))
@@ -79,6 +92,10 @@ static int parse_long_option(const char* arg)
             opts.sched = WEDGE_SCHED_DENSE;
         else if (!strcmp(v, "wedge"))
             opts.sched = WEDGE_SCHED_WEDGE;
+        else if (!strcmp(v, "filtered"))
+            opts.sched = WEDGE_SCHED_FILTERED;
+        else if (!strcmp(v, "learned"))
+            opts.sched = WEDGE_SCHED_LEARNED;
         else
             return -1;
         return 1;

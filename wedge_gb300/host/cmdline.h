@@ -23,12 +23,14 @@ typedef struct cmdline_opts {
     uint32_t num_threads;            /* -n (ignored) */
     uint64_t root_vertex;            /* -r */
     uint64_t frontier_threshold_pct; /* -t */
-    int sched;                       /* --sched=plain|dense|wedge */
+    int sched;                       /* --sched=plain|dense|wedge|filtered|learned */
     int precision;                   /* --prec=fp64|fp32c */
     double damping;                  /* --damping=<d>, 0 = reference value */
     int weights_f64;                 /* --weights=u64|f64 */
     int use_graph;                   /* --graph: CUDA-graph traversal loop */
     int timing;                      /* --timing: per-phase CUDA events */
+    int iteration_stats;             /* --iteration-stats: the ITERATION_STATS CSV on stderr */
+    char* scheduler_file;            /* --scheduler=<file>: network for --sched=learned */
 } cmdline_opts_t;
 
 void cmdline_parse_options_or_die(int argc, char* argv[]);

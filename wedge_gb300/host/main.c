@@ -63,7 +63,25 @@ int main(int argc, char* argv[])
     p.damping = o->damping;
     p.precision = o->precision;
     p.sched = o->sched;
-    p.flags = (o->use_graph ? WEDGE_FLAG_GRAPH : 0u) | (o->timing ? WEDGE_FLAG_TIMING : 0u);
+    /* the ITERATION_STATS rows carry measured pull and Wedge times (execution_bfs.c:227-232) */
+    p.flags = (o->use_graph ? WEDGE_FLAG_GRAPH : 0u) | ((o->timing || o->iteration_stats) ? WEDGE_FLAG_TIMING : 0u);
+    if (o->sched == WEDGE_SCHED_LEARNED) {
+        if (!o->scheduler_file) {
+            printf("Application: ERROR: --sched=learned needs --scheduler=<file>\n");
+            wedge_cuda_free(g);
+            return __LINE__;
+        }
+        float blob[WEDGE_SCHED_BLOB];
+        FILE* nf = fopen(o->scheduler_file, "rb");
+        const size_t got = nf ? fread(blob, sizeof(float), WEDGE_SCHED_BLOB, nf) : 0;
+        if (nf)
+            fclose(nf);
+        if (got != WEDGE_SCHED_BLOB || wedge_cuda_set_scheduler(g, blob, WEDGE_SCHED_BLOB) != WEDGE_OK) {
+            printf("Application: ERROR: unable to load the scheduler network \"%s\"\n", o->scheduler_file);
+            wedge_cuda_free(g);
+            return __LINE__;
+        }
+    }
     printf("Application: starting execution\n");
     wedge_stats_t st;
     rc = wedge_cuda_run(g, app.app, &p, &st);
@@ -76,30 +94,33 @@ int main(int argc, char* argv[])
         printf("Application: WARNING: %s\n", wedge_cuda_status_string(rc));
     printf("Application: completed execution\n");
 
-    if (o->graph_application_output_filename) {
-        FILE* f = fopen(o->graph_application_output_filename, "w");
-        uint64_t* props = (uint64_t*)malloc(8 * V);
-        uint64_t* od = (uint64_t*)malloc(8 * V);
-        if (f && props && od && wedge_cuda_read_results(g, props, 8 * V) == WEDGE_OK &&
-            wedge_cuda_read_outdegrees(g, od, 8 * V) == WEDGE_OK) {
-            const double t1 = now_ms();
-            printf("Application: writing output to \"%s\"\n", o->graph_application_output_filename);
-            char buf[256];
-            for (uint64_t v = 0; v < V && !ferror(f); ++v) {
-                application_prop_string(&app, props[v], od[v], V, wk == WEDGE_WEIGHTS_F64, buf, sizeof(buf));
-                fprintf(f, "%llu %s\n", (unsigned long long)v, buf);
-            }
-            if (ferror(f))
-                printf("Application: ERROR: file I/O error during write\n");
-            else
-                printf("Application: writing completed in %.2lf msec\n", now_ms() - t1);
-        } else {
-            printf("Application: ERROR: unable to write to \"%s\"\n", o->graph_application_output_filename);
+    if (o->iteration_stats && app.app != WEDGE_APP_PR) {
+        /* EXPERIMENT_ITERATION_STATS rows (execution_bfs.c:227-232), one per iteration */
+        uint64_t n = 0;
+        if (wedge_cuda_iteration_log(g, NULL, 0, &n) == WEDGE_OK && n) {
+            wedge_iteration_record_t* recs = (wedge_iteration_record_t*)malloc(n * sizeof(*recs));
+            if (recs && wedge_cuda_iteration_log(g, recs, n, &n) == WEDGE_OK)
+                for (uint64_t i = 0; i < n; ++i)
+                    fprintf(stderr, "%llu,%s,%lf,%lf\n", (unsigned long long)recs[i].active_edges,
+                            recs[i].used_wedge ? "true" : "false", recs[i].pull_ms, recs[i].wedge_ms);
+            free(recs);
         }
-        if (f)
-            fclose(f);
-        free(props);
-        free(od);
+    }
+
+    if (o->graph_application_output_filename) {
+        /* source/main.c:112-150, formatted on the GPU where the format allows */
+        const double t1 = now_ms();
+        printf("Application: writing output to \"%s\"\n", o->graph_application_output_filename);
+        int on_gpu = 0;
+        double fmt_ms = 0.0;
+        rc = wedge_cuda_write_output(g, o->graph_application_output_filename, &on_gpu, &fmt_ms);
+        if (rc == WEDGE_ERR_IO)
+            printf("Application: ERROR: unable to write to \"%s\"\n", o->graph_application_output_filename);
+        else if (rc != WEDGE_OK)
+            printf("Application: ERROR: %s\n", wedge_cuda_status_string(rc));
+        else
+            printf("Application: writing completed in %.2lf msec (formatting %.2lf msec on the %s)\n", now_ms() - t1,
+                   fmt_ms, on_gpu ? "GPU" : "host");
     }
 
     /* source/main.c:153-182 */
