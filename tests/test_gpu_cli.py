@@ -102,6 +102,7 @@ def test_cli_outputs_every_application(O, tmp_path):
     r = _run([_bin("wedge"), "-i", str(f), "-a", "pr", "-N", "4", "-o", str(o)])
     assert "on the host" in r.stdout
     ref, od, _ = O.Graph.from_edges(V, s, d, O.PR).run(iterations=4)
+    od = od.view(np.float64)  # PageRank keeps out-degrees as doubles (graph_vertex_outdegrees)
     got = _lines(o)
     want = ref.view(np.float64) * np.where(od == 0, V, od)
     assert np.allclose([float(got[v]) for v in range(V)], want, rtol=1e-4)
