@@ -313,7 +313,7 @@ void wedge_cuda_batch_free(wedge_batch_t* b);
  * allocate device memory, such as a host framework that owns every device
  * allocation through its own pool, or code that must not trigger a cudaMalloc in
  * the middle of its own stream work.  Nothing is allocated: the scratch lives in
- * a fixed static device array of about 4.2 MB that every GPU loading this
+ * a fixed static device array of about 6.3 MB that every GPU loading this
  * library holds until exit.  The caller owns all inputs and outputs, in device
  * memory:
  *   dst_off[num_dsts+1]  first in-edge of each destination that has in-edges

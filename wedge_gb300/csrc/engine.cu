@@ -198,6 +198,15 @@ __global__ void csri_fill_kernel(const uint32_t* src, uint64_t E, unsigned long 
     }
 }
 
+// bit dst_off[k] of the destination-start bitmap, for every compressed destination
+__global__ void dst_start_kernel(const unsigned long long* dst_off, uint32_t num_dsts, uint32_t* start)
+{
+    for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < num_dsts; k += gridDim.x * blockDim.x) {
+        const unsigned long long p = dst_off[k];
+        atomicOr(&start[p >> 5], 1u << (uint32_t)(p & 31u));
+    }
+}
+
 __global__ void split_kernel(const unsigned long long* dst_off, uint32_t Vne, uint32_t* split_k, uint32_t* split_t0,
                              uint32_t* split_t1, unsigned int* count)
 {
@@ -422,6 +431,15 @@ int build_from_device_edges(wedge_graph* h, uint64_t V, uint64_t E, uint32_t* d_
         csri_fill_kernel<<<grid_for(E, AUX_THREADS, cap), AUX_THREADS, 0, st>>>(d_src, E, wide, csri);
     cudaFreeAsync(wide, st);
 
+    // destination starts, one bit per in-edge (the pulls' tile geometry)
+    uint32_t* dst_start = nullptr;
+    const uint64_t start_words = g.Epad / 32 + 1;
+    if ((rc = dalloc(h, &dst_start, start_words)))
+        return rc;
+    WEDGE_CHECK(cudaMemsetAsync(dst_start, 0, start_words * sizeof(uint32_t), st));
+    if (Vne)
+        dst_start_kernel<<<grid_for(Vne, AUX_THREADS, cap), AUX_THREADS, 0, st>>>(dst_off, Vne, dst_start);
+
     // destinations whose in-edges span tiles (PageRank fixup list)
     uint32_t *split_k, *split_t0, *split_t1;
     if ((rc = dalloc(h, &split_k, g.T)) || (rc = dalloc(h, &split_t0, g.T)) || (rc = dalloc(h, &split_t1, g.T)))
@@ -449,6 +467,7 @@ int build_from_device_edges(wedge_graph* h, uint64_t V, uint64_t E, uint32_t* d_
     g.dst_id = dst_id;
     g.dst_off = dst_off;
     g.tile_dst0 = tile_dst0;
+    g.dst_start = dst_start;
     g.outdeg = outdeg;
     g.csri_off = csri_off;
     g.csri = csri;
@@ -684,7 +703,6 @@ __global__ void __launch_bounds__(PULL_THREADS, 1)
     __shared__ double sh_sum[WARPS];
     __shared__ uint32_t tab_id[WARPS][TAB];  // vertex id of each destination of the warp's tile
     __shared__ cur_t tab_cur[WARPS][TAB];    // its property before the tile (min apps)
-    __shared__ uint32_t sh_heads[WARPS][EPL];
     __shared__ unsigned long long hub_bar;
     __shared__ unsigned int sh_deg[3];
     extern __shared__ __align__(16) unsigned char hub_smem[];
@@ -717,7 +735,6 @@ __global__ void __launch_bounds__(PULL_THREADS, 1)
     uint32_t* nxt = next_front(s, parity);
     uint32_t* my_id = tab_id[wib];
     cur_t* my_cur = tab_cur[wib];
-    uint32_t* heads = sh_heads[wib];
     unsigned long long mass = 0, edges = 0, tiles = 0, dsts = 0, act = 0;
     double psum = 0.0;
     auto count_act = [&](uint32_t d) {
@@ -815,7 +832,7 @@ __global__ void __launch_bounds__(PULL_THREADS, 1)
                     v[q] = gather(sa[q]);
             }
             TileGeo<EPL> tg;
-            tile_geometry<EPL>(g, base, last_tile, in.k0, in.kend, lane, heads, tg, [](uint32_t, uint32_t) {});
+            tile_geometry_bits<EPL>(g, base, last_tile, in.k0, in.kend, lane, tg);
             dsts += tg.ndst;
             if (in.anydone) {
                 const uint32_t w0 = in.k0 >> 5;
@@ -865,7 +882,7 @@ __global__ void __launch_bounds__(PULL_THREADS, 1)
                     v[q] = gather(sa[q]);
             }
             TileGeo<EPL> tg;
-            tile_geometry<EPL>(g, base, last_tile, in.k0, in.kend, lane, heads, tg, [](uint32_t, uint32_t) {});
+            tile_geometry_bits<EPL>(g, base, last_tile, in.k0, in.kend, lane, tg);
             dsts += tg.ndst;
             if (in.anydone) {
                 const uint32_t w0 = in.k0 >> 5;
@@ -936,14 +953,14 @@ __global__ void __launch_bounds__(PULL_THREADS, 1)
                 }
             }
             TileGeo<EPL> tg;
-            tile_geometry<EPL>(g, base, last_tile, in.k0, in.kend, lane, heads, tg, [&](uint32_t slot, uint32_t k) {
-                if (slot < TAB) {
-                    const uint32_t vtx = g.dst_id[k];
-                    my_id[slot] = vtx;
-                    my_cur[slot] = s.prop64[vtx];
-                }
-            });
+            tile_geometry_bits<EPL>(g, base, last_tile, in.k0, in.kend, lane, tg);
             dsts += tg.ndst;
+            for (uint32_t slot = (uint32_t)lane; slot < min(tg.ndst, TAB); slot += 32u) {
+                const uint32_t vtx = g.dst_ident ? tg.k0 + slot : g.dst_id[tg.k0 + slot];
+                my_id[slot] = vtx;
+                my_cur[slot] = s.prop64[vtx];
+            }
+            __syncwarp();
             seg_reduce<EPL>(v, tg, lane, MinU64(), [&](uint32_t k, unsigned long long val, int kind) {
                 const uint32_t slot = k - tg.k0;
                 const uint32_t vtx = vid(k, slot);
@@ -973,12 +990,11 @@ __global__ void __launch_bounds__(PULL_THREADS, 1)
                                                   : 0.0f,
                               0.0f};
                 TileGeo<EPL> tg;
-                tile_geometry<EPL>(g, base, last_tile, in.k0, in.kend, lane, heads, tg,
-                                   [&](uint32_t slot, uint32_t k) {
-                                       if (slot < TAB)
-                                           my_id[slot] = g.dst_id[k];
-                                   });
+                tile_geometry_bits<EPL>(g, base, last_tile, in.k0, in.kend, lane, tg);
                 dsts += tg.ndst;
+                for (uint32_t slot = (uint32_t)lane; slot < min(tg.ndst, TAB); slot += 32u)
+                    my_id[slot] = g.dst_ident ? tg.k0 + slot : g.dst_id[tg.k0 + slot];
+                __syncwarp();
                 const AddF2 add;
                 F2 ls = v[0];
 #pragma unroll
@@ -1002,12 +1018,11 @@ __global__ void __launch_bounds__(PULL_THREADS, 1)
                            : (sa[q] != NONE32) ? ld_ro_f64(s.rank + sa[q])
                                                : 0.0;
                 TileGeo<EPL> tg;
-                tile_geometry<EPL>(g, base, last_tile, in.k0, in.kend, lane, heads, tg,
-                                   [&](uint32_t slot, uint32_t k) {
-                                       if (slot < TAB)
-                                           my_id[slot] = g.dst_id[k];
-                                   });
+                tile_geometry_bits<EPL>(g, base, last_tile, in.k0, in.kend, lane, tg);
                 dsts += tg.ndst;
+                for (uint32_t slot = (uint32_t)lane; slot < min(tg.ndst, TAB); slot += 32u)
+                    my_id[slot] = g.dst_ident ? tg.k0 + slot : g.dst_id[tg.k0 + slot];
+                __syncwarp();
                 double ls = __dadd_rn(__dadd_rn(v[0], v[1]), __dadd_rn(v[2], v[3]));
 #pragma unroll
                 for (int q = 4; q < EPL; q += 4)
@@ -2565,6 +2580,7 @@ struct NoAllocScratch {
     unsigned long long block_cnt[NCNT * NOALLOC_MAX_GRID];
     double block_part[NOALLOC_MAX_GRID];
     uint32_t tile_dst0[NOALLOC_MAX_TILES + 1];
+    uint32_t dst_start[NOALLOC_MAX_EDGES / 32 + 8];
     uint32_t split_k[NOALLOC_MAX_TILES];
     uint32_t split_t0[NOALLOC_MAX_TILES];
     uint32_t split_t1[NOALLOC_MAX_TILES];
@@ -2572,7 +2588,7 @@ struct NoAllocScratch {
     double tail_part[NOALLOC_MAX_TILES];
 };
 
-// about 4.2 MB on every device that loads the library
+// about 6.3 MB on every device that loads the library
 static __device__ __align__(256) NoAllocScratch g_noalloc_scratch;
 
 // per-device address of g_noalloc_scratch and the pull grid, set up on the first call
@@ -2593,6 +2609,8 @@ __global__ void noalloc_prepare_kernel(const unsigned long long* dst_off, uint32
         c->iter = LOG_CAP; /* no per-iteration log in this path */
         sc->nsplit = 0u;
     }
+    for (uint64_t i = tid; i < (uint64_t)T * TILE / 32 + 1; i += (uint64_t)gridDim.x * blockDim.x)
+        sc->dst_start[i] = 0u; /* set by dst_start_kernel next */
     for (uint64_t t = tid; t <= T; t += (uint64_t)gridDim.x * blockDim.x) {
         if (t == T) {
             sc->tile_dst0[t] = num_dsts;
@@ -2711,6 +2729,7 @@ extern "C" int wedge_cuda_pr_iteration_noalloc(uint64_t num_vertices, uint64_t n
     g.dst_id = dst_id;
     g.dst_off = (const unsigned long long*)dst_off;
     g.tile_dst0 = sc->tile_dst0;
+    g.dst_start = sc->dst_start;
     g.outdeg = outdeg;
     g.split_k = sc->split_k;
     g.split_t0 = sc->split_t0;
@@ -2728,6 +2747,9 @@ extern "C" int wedge_cuda_pr_iteration_noalloc(uint64_t num_vertices, uint64_t n
     s.acc = rank_out; /* accumulators first, ranks after the vertex phase */
     const uint32_t aux = (uint32_t)grid_for(num_vertices > T ? num_vertices : (uint64_t)T + 1, AUX_THREADS, grid * 2u);
     noalloc_prepare_kernel<<<aux, AUX_THREADS, 0, st>>>(g.dst_off, g.Vne, T);
+    if (num_dsts)
+        dst_start_kernel<<<grid_for(num_dsts, AUX_THREADS, grid * 2u), AUX_THREADS, 0, st>>>(g.dst_off, g.Vne,
+                                                                                          sc->dst_start);
     if (num_dsts)
         split_kernel<<<grid_for(num_dsts, AUX_THREADS, grid * 2u), AUX_THREADS, 0, st>>>(
             g.dst_off, g.Vne, sc->split_k, sc->split_t0, sc->split_t1, &sc->nsplit);

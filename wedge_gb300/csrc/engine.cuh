@@ -7,6 +7,7 @@
 //   dst_id[Vne]    vertex id of compressed destination k (only vertices with
 //                  in-degree > 0 are listed, ascending)
 //   dst_off[Vne+1] first edge of compressed destination k
+//   dst_start[Epad/32] one bit per in-edge: the first in-edge of its destination
 //   tile_dst0[T+1] compressed destination owning edge 128*t (Vne where that
 //                  edge is padding); pull tiles of 32*EPL edges index it with a stride
 //   outdeg[V]      out-degree (graphdata.c:430-490)
@@ -110,6 +111,7 @@ struct DevGraph {
     const uint32_t* dst_id;
     const unsigned long long* dst_off;
     const uint32_t* tile_dst0;
+    const uint32_t* dst_start; // [Epad/32] bit p: in-edge p is the first of its destination
     const uint32_t* outdeg;
     const unsigned long long* csri_off;
     const uint32_t* csri;

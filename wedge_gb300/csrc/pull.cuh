@@ -200,6 +200,41 @@ __device__ __forceinline__ void tile_geometry(const DevGraph& g, uint64_t base, 
     __syncwarp();
 }
 
+// The same geometry from the destination-start bitmap (bit p of g.dst_start:
+// in-edge p is the first in-edge of its destination): lane l < EPL loads word
+// l of the tile, no loads of dst_off and no shared memory.  base is a multiple
+// of 32*EPL.
+template <int EPL>
+__device__ __forceinline__ void tile_geometry_bits(const DevGraph& g, uint64_t base, bool last_tile, uint32_t k0,
+                                                   uint32_t kend, int lane, TileGeo<EPL>& tg)
+{
+    tg.base = base;
+    uint32_t hw_own = (lane < EPL) ? g.dst_start[(base >> 5) + (uint32_t)lane] : 0u;
+    const uint32_t w0 = __shfl_sync(FULL, hw_own, 0);
+    tg.k0_fresh = (w0 & 1u) != 0u; /* k0 starts exactly at the tile start */
+    if (lane == 0)
+        hw_own &= ~1u; /* heads count the starts at positions [1, 32*EPL) */
+    uint32_t incl = __popc(hw_own);
+#pragma unroll
+    for (int d = 1; d < EPL; d <<= 1) {
+        const uint32_t y = __shfl_up_sync(FULL, incl, d);
+        if (lane >= d)
+            incl += y;
+    }
+    const uint32_t total = __shfl_sync(FULL, incl, EPL - 1);
+    const uint32_t pos0 = (uint32_t)lane * EPL;
+    const uint32_t wi = pos0 >> 5, sh = pos0 & 31u;
+    const uint32_t word = __shfl_sync(FULL, hw_own, (int)wi);
+    const uint32_t excl_w = __shfl_sync(FULL, incl - __popc(hw_own), (int)wi);
+    tg.k0 = k0;
+    const uint32_t k_last = k0 + total;
+    tg.tail_cont = !last_tile && (kend == k_last);
+    tg.ndst = total + 1u;
+    tg.before = excl_w + __popc(word & ((1u << sh) - 1u));
+    tg.nib_inner = (word >> sh) & ((EPL >= 32) ? FULL : ((1u << EPL) - 1u));
+    tg.nib = tg.nib_inner | ((lane == 0 && tg.k0_fresh) ? 1u : 0u);
+}
+
 template <int EPL>
 __device__ __forceinline__ uint32_t pos_dst(const TileGeo<EPL>& tg, int i)
 {
