@@ -1090,37 +1090,37 @@ __device__ __forceinline__ uint32_t choose_mode(uint32_t sched, unsigned long lo
     return mass > thr ? MODE_DENSE : MODE_WEDGE; /* execution_bfs.c:141 */
 }
 
-__device__ __forceinline__ float log2_1p(double x) { return (float)log2(1.0 + x); }
-
 // Scheduler features of the next iteration, from the pull just finished (its
 // reduced counters) and the traversal so far.  Every feature is O(1) in size.
+// Single-precision arithmetic: one thread computes them after every pull, and
+// the FP64 units of this GPU are slow.
 __device__ void sched_features(const DevGraph& g, const Ctrl* c, uint32_t app, const unsigned long long (&cnt)[NCNT],
                                float* f)
 {
-    const double V = (double)(g.V ? g.V : 1), E = (double)(g.E ? g.E : 1);
-    const double m = (double)cnt[CNT_MASS], act = (double)cnt[CNT_ACT];
+    const float V = (float)(g.V ? g.V : 1), E = (float)(g.E ? g.E : 1);
+    const float m = (float)cnt[CNT_MASS], act = (float)cnt[CNT_ACT];
     const uint32_t tile_e = (app == WEDGE_APP_CC) ? 32u * PullEpl<WEDGE_APP_CC>::value
                             : (app == WEDGE_APP_BFS) ? 32u * PullEpl<WEDGE_APP_BFS>::value
                                                     : 32u * PullEpl<WEDGE_APP_SSSP>::value;
-    const double T = (double)((g.E + tile_e - 1) / tile_e) + 1.0;
-    const double a = act > 0.0 ? act : 1.0;
-    const double b0 = (double)cnt[CNT_DEG0], b1 = (double)cnt[CNT_DEG1], b2 = (double)cnt[CNT_DEG2];
-    f[0] = log2_1p(m) / 32.0f;              // out-edge mass of the activated vertices
-    f[1] = (float)(m / E);
-    f[2] = log2_1p(act) / 32.0f;            // activated vertices
-    f[3] = (float)(act / V);                // frontier bitmap density
-    f[4] = (float)((double)cnt[CNT_TILES] / T); // tiles the last pull visited
-    f[5] = (float)(b0 / a);                 // out-degree histogram of the activated vertices
-    f[6] = (float)(b1 / a);
-    f[7] = (float)(b2 / a);
-    f[8] = (float)((act - b0 - b1 - b2) / a);
-    f[9] = (float)((double)c->activated / V); // activated so far (BFS: visited fraction)
-    f[10] = log2_1p((double)c->iter) / 8.0f;
-    f[11] = (float)(log2(E) / 40.0);
+    const float T = (float)((g.E + tile_e - 1) / tile_e) + 1.0f;
+    const float a = act > 0.0f ? act : 1.0f;
+    const float b0 = (float)cnt[CNT_DEG0], b1 = (float)cnt[CNT_DEG1], b2 = (float)cnt[CNT_DEG2];
+    f[0] = log2f(1.0f + m) / 32.0f;         // out-edge mass of the activated vertices
+    f[1] = m / E;
+    f[2] = log2f(1.0f + act) / 32.0f;       // activated vertices
+    f[3] = act / V;                         // frontier bitmap density
+    f[4] = (float)cnt[CNT_TILES] / T;       // tiles the last pull visited
+    f[5] = b0 / a;                          // out-degree histogram of the activated vertices
+    f[6] = b1 / a;
+    f[7] = b2 / a;
+    f[8] = (act - b0 - b1 - b2) / a;
+    f[9] = (float)c->activated / V;         // activated so far (BFS: visited fraction)
+    f[10] = log2f(1.0f + (float)c->iter) / 8.0f;
+    f[11] = log2f(E) / 40.0f;
     f[12] = app == WEDGE_APP_BFS ? 1.0f : 0.0f;
     f[13] = app == WEDGE_APP_CC ? 1.0f : 0.0f;
     f[14] = app == WEDGE_APP_SSSP ? 1.0f : 0.0f;
-    f[15] = (float)(log2(E / V) / 8.0);     // average degree
+    f[15] = log2f(E / V) / 8.0f;            // average degree
 }
 
 // After a pull: reduce the block counters, count the iteration, stop when no
@@ -1201,6 +1201,7 @@ __global__ void decide_kernel(DevGraph g, DevState s, const unsigned long long* 
         c->region_next = 0u;
         c->tiles = 0u;
         c->items = 0u;
+        c->alist_n = 0u;
         go = 0u;
         if (m == 0ull) {
             c->done = 1u;
@@ -1264,15 +1265,16 @@ __device__ __forceinline__ void mark_chunk(const DevState& s, uint32_t ch, bool 
     }
 }
 
-// Wedge frontier generation (wedge.c:63-155): walk the bitmap of vertices the
-// last pull activated and set the chunk bit of each of their out-edges
-// (wedge.c:37-46).  Each warp takes 32 bitmap words; per word, the lanes take
-// the set bits' vertices and expand their CSRI lists cooperatively (shuffle
-// scan of the list lengths, then every lane finds the list that owns each of
-// 32 consecutive entries).  Lists longer than BIG_LIST go to
-// wedge_build_kernel as PIECE-sized work items instead (appended with one
-// atomic per warp): the degree relabelling puts the longest lists in the first
-// bitmap words, and one warp must not expand them alone.
+// Wedge frontier generation (wedge.c:63-155), in three launches:
+//   collect_kernel  the bitmap of vertices the last pull activated -> a vertex
+//                   list (one warp per 32 words, one atomic per warp)
+//   expand_kernel   one thread per listed vertex marks the chunk of each of its
+//                   out-edges (wedge.c:37-46); lists longer than BIG_LIST go to
+//                   PIECE-sized work items instead (one atomic per warp)
+//   wedge_build_kernel  one warp per work item
+// Threads, not warps, expand the short lists so that enough independent
+// CSRI reads are in flight: the degree relabelling puts the activated
+// low-degree vertices of a BFS level in long runs of dense bitmap words.
 __global__ void collect_kernel(DevGraph g, DevState s, uint32_t app)
 {
     Ctrl* c = s.ctrl;
@@ -1284,64 +1286,71 @@ __global__ void collect_kernel(DevGraph g, DevState s, uint32_t app)
     const uint64_t gw = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) >> 5;
     const uint64_t nw = ((uint64_t)gridDim.x * blockDim.x) >> 5;
     for (uint64_t base = gw * 32; base < nwords; base += nw * 32) {
-        const uint32_t myword = (base + lane < nwords) ? fb[base + lane] : 0u;
-        uint32_t nonzero = __ballot_sync(FULL, myword != 0u);
-        while (nonzero) {
-            const int w = __ffs(nonzero) - 1;
-            nonzero &= nonzero - 1u;
-            const uint32_t bits = __shfl_sync(FULL, myword, w);
-            const uint64_t v = (base + (uint64_t)w) * 32 + (uint64_t)lane;
-            unsigned long long start = 0, len = 0;
-            uint32_t np = 0;
-            if ((bits >> lane) & 1u) {
-                start = g.csri_off[v];
-                len = g.csri_off[v + 1] - start;
-                if (len > BIG_LIST) { /* long list: work items */
-                    np = (uint32_t)((len + PIECE - 1) / PIECE);
-                    len = 0;
-                }
-            }
-            uint32_t np_incl = np;
+        const uint32_t word = (base + lane < nwords) ? fb[base + lane] : 0u;
+        const uint32_t n = __popc(word);
+        uint32_t incl = n;
 #pragma unroll
-            for (int d = 1; d < 32; d <<= 1) {
-                const uint32_t y = __shfl_up_sync(FULL, np_incl, d);
-                if (lane >= d)
-                    np_incl += y;
+        for (int d = 1; d < 32; d <<= 1) {
+            const uint32_t y = __shfl_up_sync(FULL, incl, d);
+            if (lane >= d)
+                incl += y;
+        }
+        const uint32_t total = __shfl_sync(FULL, incl, 31);
+        if (total == 0u)
+            continue;
+        uint32_t pos = 0;
+        if (lane == 0)
+            pos = atomicAdd(&c->alist_n, total);
+        pos = __shfl_sync(FULL, pos, 0) + (incl - n);
+        uint32_t bits = word;
+        const uint32_t v0 = (uint32_t)((base + (uint64_t)lane) * 32u);
+        while (bits) {
+            const int b = __ffs(bits) - 1;
+            bits &= bits - 1u;
+            s.alist[pos++] = v0 + (uint32_t)b;
+        }
+    }
+}
+
+__global__ void expand_kernel(DevGraph g, DevState s)
+{
+    Ctrl* c = s.ctrl;
+    if (c->done || c->mode != MODE_WEDGE)
+        return;
+    const int lane = threadIdx.x & 31;
+    const uint32_t n = c->alist_n;
+    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+    // every lane of a warp runs the same rounds (warp-wide item appends)
+    for (uint64_t i0 = (blockIdx.x * (uint64_t)blockDim.x) + (threadIdx.x & ~31u); i0 < n; i0 += stride) {
+        const uint64_t i = i0 + (uint64_t)lane;
+        uint32_t v = 0, np = 0;
+        unsigned long long start = 0, len = 0;
+        if (i < n) {
+            v = s.alist[i];
+            start = g.csri_off[v];
+            len = g.csri_off[v + 1] - start;
+            if (len > BIG_LIST) {
+                np = (uint32_t)((len + PIECE - 1) / PIECE);
+                len = 0;
             }
-            const uint32_t np_total = __shfl_sync(FULL, np_incl, 31);
-            if (np_total) {
-                uint32_t pos = 0;
-                if (lane == 0)
-                    pos = atomicAdd(&c->items, np_total);
-                pos = __shfl_sync(FULL, pos, 0) + (np_incl - np);
-                for (uint32_t q = 0; q < np; ++q)
-                    s.items[pos + q] = make_uint2((uint32_t)v, q);
-            }
-            unsigned long long incl = len;
+        }
+        for (unsigned long long j = 0; j < len; ++j)
+            mark_chunk(s, g.csri[start + j], true);
+        uint32_t incl = np;
 #pragma unroll
-            for (int d = 1; d < 32; d <<= 1) {
-                const unsigned long long y = __shfl_up_sync(FULL, incl, d);
-                if (lane >= d)
-                    incl += y;
-            }
-            const unsigned long long total = __shfl_sync(FULL, incl, 31);
-            const unsigned long long excl = incl - len;
-            for (unsigned long long j0 = 0; j0 < total; j0 += 32) {
-                const unsigned long long j = j0 + (unsigned long long)lane;
-                // owner = number of lanes whose inclusive end is <= j
-                int owner = 0;
-#pragma unroll
-                for (int step = 16; step > 0; step >>= 1) {
-                    const unsigned long long e = __shfl_sync(FULL, incl, owner + step - 1);
-                    if (e <= j)
-                        owner += step;
-                }
-                const unsigned long long ost = __shfl_sync(FULL, start, owner & 31);
-                const unsigned long long oex = __shfl_sync(FULL, excl, owner & 31);
-                const bool valid = j < total;
-                const uint32_t ch = valid ? g.csri[ost + (j - oex)] : 0u;
-                mark_chunk(s, ch, valid);
-            }
+        for (int d = 1; d < 32; d <<= 1) {
+            const uint32_t y = __shfl_up_sync(FULL, incl, d);
+            if (lane >= d)
+                incl += y;
+        }
+        const uint32_t total = __shfl_sync(FULL, incl, 31);
+        if (total) {
+            uint32_t pos = 0;
+            if (lane == 0)
+                pos = atomicAdd(&c->items, total);
+            pos = __shfl_sync(FULL, pos, 0) + (incl - np);
+            for (uint32_t q = 0; q < np; ++q)
+                s.items[pos + q] = make_uint2(v, q);
         }
     }
 }
@@ -1490,9 +1499,18 @@ __global__ void init_root_kernel(DevGraph g, DevState s, uint32_t app, uint64_t 
     if (app == WEDGE_APP_BFS || app == WEDGE_APP_CC) {
         // BFS: the root is visited; CC: the vertex the caller numbers 0 holds label 0 already
         const uint32_t done = (app == WEDGE_APP_BFS) ? (uint32_t)root : g.old2new[0];
-        for (uint32_t k = tid; k < g.Vne; k += gridDim.x * blockDim.x)
-            if (g.dst_id[k] == done)
-                atomicOr(&s.vis_c[k >> 5], 1u << (k & 31u));
+        if (tid == 0 && g.Vne) { /* its compressed index: dst_id ascends */
+            uint32_t lo = 0, hi = g.Vne;
+            while (lo < hi) {
+                const uint32_t mid = lo + (hi - lo) / 2u;
+                if (g.dst_id[mid] < done)
+                    lo = mid + 1u;
+                else
+                    hi = mid;
+            }
+            if (lo < g.Vne && g.dst_id[lo] == done)
+                atomicOr(&s.vis_c[lo >> 5], 1u << (lo & 31u));
+        }
     }
     if (tid == 0) {
         Ctrl* c = s.ctrl;
@@ -1503,6 +1521,7 @@ __global__ void init_root_kernel(DevGraph g, DevState s, uint32_t app, uint64_t 
         c->activated = 0;
         c->threshold = thr;
         c->items = 0;
+        c->alist_n = 0;
         c->region_next = 0;
         c->tiles = 0;
         c->iter = 0;
@@ -1921,7 +1940,7 @@ static int ensure_state(wedge_graph* h, int app, int precision)
             (rc = dalloc(h, &s.chunk_bits, (uint64_t)g.T / TILES_PER_WORD + REGION_WORDS + 2, true)) ||
             (rc = dalloc(h, &s.summary, (uint64_t)g.T / TILES_PER_REGION / 32 + 2, true)) ||
             (rc = dalloc(h, &s.tile_list, (uint64_t)g.T + 1, true)) ||
-            (rc = dalloc(h, &s.items, V + g.E / PIECE + 2, true)))
+            (rc = dalloc(h, &s.items, V + g.E / PIECE + 2, true)) || (rc = dalloc(h, &s.alist, V + 1, true)))
             return rc;
         if (app == WEDGE_APP_BFS || app == WEDGE_APP_CC) {
             if ((rc = dalloc(h, &s.vis_c, (uint64_t)g.Vne / 32 + 2, true)))
@@ -1980,7 +1999,7 @@ static void launch_pull(wedge_graph* h, int app)
 }
 
 // kernels one iteration launches: the pull(s) and the five of the tail
-static uint64_t iteration_launches(int app) { return 5ull + (two_phase_app(app) ? 2ull : 1ull); }
+static uint64_t iteration_launches(int app) { return 6ull + (two_phase_app(app) ? 2ull : 1ull); }
 
 static uint32_t aux_grid(wedge_graph* h, uint64_t work)
 {
@@ -2000,13 +2019,20 @@ static void launch_compact(wedge_graph* h, int app)
         compact_kernel<PullEpl<WEDGE_APP_SSSP>::value><<<grid, AUX_THREADS, 0, h->stream>>>(h->g, h->s);
 }
 
+// Wedge frontier of the next pull (no-ops unless it is a Wedge pull)
+static void launch_wedge_build(wedge_graph* h, const DevGraph& g, int app)
+{
+    collect_kernel<<<aux_grid(h, (g.V + 31) / 32), AUX_THREADS, 0, h->stream>>>(g, h->s, (uint32_t)app);
+    expand_kernel<<<h->build_grid, AUX_THREADS, 0, h->stream>>>(g, h->s);
+    wedge_build_kernel<<<h->build_grid, AUX_THREADS, 0, h->stream>>>(g, h->s);
+    launch_compact(h, app);
+}
+
 // iteration tail after a pull: mass/convergence, Wedge frontier, bitmap reset
 static void launch_tail(wedge_graph* h, int app)
 {
     decide_kernel<<<1, AUX_THREADS, 0, h->stream>>>(h->g, h->s, counters(h), pull_slots(h, app), (uint32_t)app);
-    collect_kernel<<<aux_grid(h, (h->g.V + 31) / 32), AUX_THREADS, 0, h->stream>>>(h->g, h->s, (uint32_t)app);
-    wedge_build_kernel<<<h->build_grid, AUX_THREADS, 0, h->stream>>>(h->g, h->s);
-    launch_compact(h, app);
+    launch_wedge_build(h, h->g, app);
     advance_kernel<<<aux_grid(h, (h->g.V + 31) / 32), AUX_THREADS, 0, h->stream>>>(h->g, h->s, (uint32_t)app);
 }
 
@@ -2016,11 +2042,9 @@ static void launch_init(wedge_graph* h, int app, uint64_t root, uint32_t sched, 
     const uint64_t work = h->g.V > h->g.T ? h->g.V : h->g.T;
     const uint32_t topen = (uint32_t)((h->g.E + 32u * PullEpl<WEDGE_APP_BFS>::value - 1) / (32u * PullEpl<WEDGE_APP_BFS>::value));
     init_kernel<<<aux_grid(h, work), AUX_THREADS, 0, h->stream>>>(h->g, h->s, (uint32_t)app, topen);
-    init_root_kernel<<<aux_grid(h, h->g.Vne), AUX_THREADS, 0, h->stream>>>(h->g, h->s, (uint32_t)app, root, sched, thr,
+    init_root_kernel<<<1, 32, 0, h->stream>>>(h->g, h->s, (uint32_t)app, root, sched, thr,
                                                                            max_iter, probe_iter, probe_mode);
-    collect_kernel<<<aux_grid(h, (h->g.V + 31) / 32), AUX_THREADS, 0, h->stream>>>(h->g, h->s, (uint32_t)app);
-    wedge_build_kernel<<<h->build_grid, AUX_THREADS, 0, h->stream>>>(h->g, h->s);
-    launch_compact(h, app);
+    launch_wedge_build(h, h->g, app);
     advance_kernel<<<aux_grid(h, (h->g.V + 31) / 32), AUX_THREADS, 0, h->stream>>>(h->g, h->s, (uint32_t)app);
 }
 
@@ -2349,9 +2373,7 @@ int wedge_cuda_run_phase(wedge_graph_t* g, int app, int phase, const wedge_param
     case WEDGE_PHASE_WEDGE_BUILD:
         if (app == WEDGE_APP_PR)
             return WEDGE_ERR_UNSUPPORTED;
-        collect_kernel<<<aux_grid(g, (dg.V + 31) / 32), AUX_THREADS, 0, g->stream>>>(dg, g->s, (uint32_t)app);
-        wedge_build_kernel<<<g->build_grid, AUX_THREADS, 0, g->stream>>>(dg, g->s);
-        launch_compact(g, app);
+        launch_wedge_build(g, dg, app);
         break;
     case WEDGE_PHASE_ADVANCE:
         if (app == WEDGE_APP_PR)

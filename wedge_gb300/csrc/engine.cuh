@@ -95,7 +95,7 @@ struct Ctrl {
     unsigned int probe_iter;           // WEDGE_SCHED_PROBE: iteration whose mode is forced
     unsigned int probe_mode;
     unsigned int learned_iters;        // iterations whose mode the scheduler network chose
-    unsigned int pad;
+    unsigned int alist_n;              // vertices in the Wedge-build vertex list
     double pr_total;                   // sum of all accumulators (phase_vertex_pr.c:161)
     double pr_sum;                     // PageRank Sum statistic
 };
@@ -142,6 +142,7 @@ struct DevState {
     uint32_t* summary;             // one bit per region of REGION_WORDS chunk words (any chunk marked)
     unsigned long long* tile_list; // (tile << 32 | chunk mask) of the next Wedge pull
     uint2* items;                  // (vertex, piece) Wedge-build work items
+    uint32_t* alist;               // vertices the last pull activated (Wedge build)
     Ctrl* ctrl;
     IterRec* log;                  // [LOG_CAP] per-iteration records
     double damping;
