@@ -1250,18 +1250,19 @@ __global__ void decide_kernel(DevGraph g, DevState s, const unsigned long long* 
 }
 
 // set the Wedge-frontier bit of chunk ch (wedge.c:22-31) and the summary bit
-// of its region when the chunk word was empty
+// of its region.  Fire-and-forget atomics behind plain-load checks: bits are
+// only set while the frontier is built, so a stale read can only cost a
+// redundant atomic, and no thread waits for an atomic's return.
 __device__ __forceinline__ void mark_chunk(const DevState& s, uint32_t ch, bool valid)
 {
     if (!valid)
         return;
     const uint32_t word = ch >> 5, bit = 1u << (ch & 31u);
     if (!(s.chunk_bits[word] & bit)) {
-        const uint32_t old = atomicOr(&s.chunk_bits[word], bit);
-        if (old == 0u) {
-            const uint32_t r = word / REGION_WORDS;
-            atomicOr(&s.summary[r >> 5], 1u << (r & 31u));
-        }
+        atomicOr(&s.chunk_bits[word], bit);
+        const uint32_t r = word / REGION_WORDS, rb = 1u << (r & 31u);
+        if (!(s.summary[r >> 5] & rb))
+            atomicOr(&s.summary[r >> 5], rb);
     }
 }
 
