@@ -133,6 +133,25 @@ def test_pagerank_fp64(W, O, scale, ef, seed, damping):
     assert abs(st["pr_sum"] - 1.0) < 1e-9
 
 
+def test_pagerank_graph_matches_stream(W, O):
+    """the captured iteration loop gives the stream-launched ranks bit for bit, across
+    iteration counts, damping factors and precisions (each change re-keys or rebuilds the capture)"""
+    V, s, d = graph_edges(O, "rmat", dict(scale=12, edge_factor=16, seed=4))
+    ref, _, _ = O.Graph.from_edges(V, s, d, O.PR).run(iterations=7, damping=0.85, threads=4)
+    with W.Graph.from_edges(V, s, d) as g:
+        for iters, damping, prec in ((16, 0.875, W.PREC_FP64), (7, 0.85, W.PREC_FP64), (16, 0.875, W.PREC_FP64),
+                                     (30, 0.875, W.PREC_FP32C), (1, 0.875, W.PREC_FP32C)):
+            p = dict(num_iterations=iters, damping=damping, precision=prec)
+            st0 = g.run(W.APP_PR, W.Params(**p))
+            a = g.read_results()
+            st1 = g.run(W.APP_PR, W.Params(flags=W.FLAG_GRAPH, **p))
+            b = g.read_results()
+            assert np.array_equal(a, b), (iters, damping, prec)
+            assert st1["iterations"] == iters and st0["pr_sum"] == st1["pr_sum"]
+            if (iters, damping) == (7, 0.85):
+                assert rel_l1(b.view(np.float64), ref.view(np.float64)) < PR_TOL
+
+
 @pytest.mark.parametrize("scale,ef,seed", SIZES)
 def test_pagerank_fp32_compensated(W, O, scale, ef, seed):
     V, s, d = graph_edges(O, "rmat", dict(scale=scale, edge_factor=ef, seed=seed))

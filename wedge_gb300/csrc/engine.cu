@@ -90,6 +90,10 @@ static void free_state(wedge_graph* h)
         h->graph_exec = nullptr;
         h->graph_app = -1;
     }
+    if (h->pr_exec) {
+        cudaGraphExecDestroy(h->pr_exec);
+        h->pr_exec = nullptr;
+    }
 }
 
 void free_handle(wedge_graph* h)
@@ -207,14 +211,19 @@ __global__ void dst_start_kernel(const unsigned long long* dst_off, uint32_t num
     }
 }
 
-__global__ void split_kernel(const unsigned long long* dst_off, uint32_t Vne, uint32_t* split_k, uint32_t* split_t0,
-                             uint32_t* split_t1, unsigned int* count)
+// Destinations whose in-edges span tiles, for the PageRank merge: those spanning
+// at most SPLIT_SERIAL tile boundaries from the front of the lists (count[0]),
+// the longer ones from the back (count[1]; entry cap-1-j).  Every split holds a
+// distinct tile boundary, so the two ends never meet in lists of T entries.
+constexpr uint32_t SPLIT_SERIAL = 8;
+__global__ void split_kernel(const unsigned long long* dst_off, uint32_t Vne, uint32_t cap, uint32_t* split_k,
+                             uint32_t* split_t0, uint32_t* split_t1, unsigned int* count)
 {
     for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < Vne; k += gridDim.x * blockDim.x) {
         const uint32_t t0 = (uint32_t)(dst_off[k] / TILE);
         const uint32_t t1 = (uint32_t)((dst_off[k + 1] - 1) / TILE);
         if (t0 != t1) {
-            const unsigned int i = atomicAdd(count, 1u);
+            const unsigned int i = t1 - t0 <= SPLIT_SERIAL ? atomicAdd(&count[0], 1u) : cap - 1u - atomicAdd(&count[1], 1u);
             split_k[i] = k;
             split_t0[i] = t0;
             split_t1[i] = t1;
@@ -445,13 +454,13 @@ int build_from_device_edges(wedge_graph* h, uint64_t V, uint64_t E, uint32_t* d_
     if ((rc = dalloc(h, &split_k, g.T)) || (rc = dalloc(h, &split_t0, g.T)) || (rc = dalloc(h, &split_t1, g.T)))
         return rc;
     unsigned int* d_cnt = nullptr;
-    WEDGE_CHECK(cudaMallocAsync((void**)&d_cnt, sizeof(unsigned int), st));
-    WEDGE_CHECK(cudaMemsetAsync(d_cnt, 0, sizeof(unsigned int), st));
+    WEDGE_CHECK(cudaMallocAsync((void**)&d_cnt, 2 * sizeof(unsigned int), st));
+    WEDGE_CHECK(cudaMemsetAsync(d_cnt, 0, 2 * sizeof(unsigned int), st));
     if (Vne)
-        split_kernel<<<grid_for(Vne, AUX_THREADS, cap), AUX_THREADS, 0, st>>>(dst_off, Vne, split_k, split_t0, split_t1,
-                                                                             d_cnt);
-    unsigned int nsplit = 0;
-    WEDGE_CHECK(cudaMemcpyAsync(&nsplit, d_cnt, sizeof(unsigned int), cudaMemcpyDeviceToHost, st));
+        split_kernel<<<grid_for(Vne, AUX_THREADS, cap), AUX_THREADS, 0, st>>>(dst_off, Vne, g.T, split_k, split_t0,
+                                                                             split_t1, d_cnt);
+    unsigned int nsplit[2] = {0, 0};
+    WEDGE_CHECK(cudaMemcpyAsync(nsplit, d_cnt, 2 * sizeof(unsigned int), cudaMemcpyDeviceToHost, st));
     // dst_id ascends, so it is the identity when its last entry is Vne-1 (symmetric
     // graphs after the degree relabelling: in-degree > 0 exactly for ids < Vne)
     uint32_t last_dst = 0;
@@ -462,7 +471,8 @@ int build_from_device_edges(wedge_graph* h, uint64_t V, uint64_t E, uint32_t* d_
     WEDGE_CHECK(cudaStreamSynchronize(st));
     cudaFreeAsync(d_cnt, st);
     WEDGE_CHECK(cudaGetLastError());
-    g.nsplit = nsplit;
+    g.nsplit = nsplit[0];
+    g.nwide = nsplit[1];
     g.dst_ident = (Vne && last_dst == Vne - 1) ? 1u : 0u;
     g.dst_id = dst_id;
     g.dst_off = dst_off;
@@ -700,7 +710,6 @@ __global__ void __launch_bounds__(PULL_THREADS, 1)
     constexpr uint32_t TAB = 129; /* staged destinations per tile; more are read from global memory */
     using cur_t = typename CurT<APP>::type;
     __shared__ unsigned long long sh_cnt[WARPS][NCNT];
-    __shared__ double sh_sum[WARPS];
     __shared__ uint32_t tab_id[WARPS][TAB];  // vertex id of each destination of the warp's tile
     __shared__ cur_t tab_cur[WARPS][TAB];    // its property before the tile (min apps)
     __shared__ unsigned long long hub_bar;
@@ -736,7 +745,6 @@ __global__ void __launch_bounds__(PULL_THREADS, 1)
     uint32_t* my_id = tab_id[wib];
     cur_t* my_cur = tab_cur[wib];
     unsigned long long mass = 0, edges = 0, tiles = 0, dsts = 0, act = 0;
-    double psum = 0.0;
     auto count_act = [&](uint32_t d) {
         mass += d;
         ++act;
@@ -996,11 +1004,6 @@ __global__ void __launch_bounds__(PULL_THREADS, 1)
                     my_id[slot] = g.dst_ident ? tg.k0 + slot : g.dst_id[tg.k0 + slot];
                 __syncwarp();
                 const AddF2 add;
-                F2 ls = v[0];
-#pragma unroll
-                for (int q = 1; q < EPL; ++q)
-                    ls = add(ls, v[q]);
-                psum = __dadd_rn(psum, warp_sum_f64(__dadd_rn((double)ls.s, (double)ls.c)));
                 seg_reduce<EPL>(v, tg, lane, add, [&](uint32_t k, F2 val, int kind) {
                     if (kind == EMIT_COMPLETE) {
                         s.acc[vid(k, k - tg.k0)] = __dadd_rn((double)val.s, (double)val.c);
@@ -1023,11 +1026,6 @@ __global__ void __launch_bounds__(PULL_THREADS, 1)
                 for (uint32_t slot = (uint32_t)lane; slot < min(tg.ndst, TAB); slot += 32u)
                     my_id[slot] = g.dst_ident ? tg.k0 + slot : g.dst_id[tg.k0 + slot];
                 __syncwarp();
-                double ls = __dadd_rn(__dadd_rn(v[0], v[1]), __dadd_rn(v[2], v[3]));
-#pragma unroll
-                for (int q = 4; q < EPL; q += 4)
-                    ls = __dadd_rn(ls, __dadd_rn(__dadd_rn(v[q], v[q + 1]), __dadd_rn(v[q + 2], v[q + 3])));
-                psum = __dadd_rn(psum, warp_sum_f64(ls));
                 seg_reduce<EPL>(v, tg, lane, AddF64(), [&](uint32_t k, double val, int kind) {
                     if (kind == EMIT_COMPLETE)
                         s.acc[vid(k, k - tg.k0)] = val;
@@ -1058,7 +1056,6 @@ __global__ void __launch_bounds__(PULL_THREADS, 1)
         sh_cnt[wib][CNT_DEG0] = 0ull;
         sh_cnt[wib][CNT_DEG1] = 0ull;
         sh_cnt[wib][CNT_DEG2] = 0ull;
-        sh_sum[wib] = psum;
     }
     __syncthreads();
     if (threadIdx.x < NCNT) {
@@ -1068,12 +1065,6 @@ __global__ void __launch_bounds__(PULL_THREADS, 1)
         if (threadIdx.x >= CNT_DEG0)
             a = sh_deg[threadIdx.x - CNT_DEG0];
         block_cnt[NCNT * blockIdx.x + threadIdx.x] = a;
-    }
-    if (APP == WEDGE_APP_PR && threadIdx.x == 0) {
-        double ps = 0.0;
-        for (int w = 0; w < WARPS; ++w)
-            ps = __dadd_rn(ps, sh_sum[w]);
-        s.block_part[blockIdx.x] = ps;
     }
 }
 
@@ -1566,13 +1557,27 @@ __global__ void init_root_kernel(DevGraph g, DevState s, uint32_t app, uint64_t 
 
 /* ------------------------------------------------------------- PageRank */
 
-// execution_initialize_pr (execution_pr.c:380-392)
-__global__ void pr_init_kernel(DevGraph g, DevState s)
+// 1 / outdegree' for every vertex (outdegree, or N for a dangling vertex;
+// execution_pr.c:384-390), once per PageRank state: the vertex phase then
+// multiplies where the reference divides (phase_vertex_pr.c:57-66), which this
+// GPU's FP64 units make the phase's cost; the results differ by at most an ulp
+// per step.
+__global__ void pr_inv_outdeg_kernel(DevGraph g, double* inv_od)
 {
     const double N = (double)g.V;
     for (uint64_t v = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; v < g.V; v += (uint64_t)gridDim.x * blockDim.x) {
         const uint32_t od = g.outdeg[v];
-        const double r = __ddiv_rn(__ddiv_rn(1.0, N), od ? (double)od : N);
+        inv_od[v] = __ddiv_rn(1.0, od ? (double)od : N);
+    }
+}
+
+// execution_initialize_pr (execution_pr.c:380-392); max_iter bounds the
+// captured iteration loop
+__global__ void pr_init_kernel(DevGraph g, DevState s, uint32_t max_iter)
+{
+    const double invN = __ddiv_rn(1.0, (double)g.V);
+    for (uint64_t v = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; v < g.V; v += (uint64_t)gridDim.x * blockDim.x) {
+        const double r = __dmul_rn(invN, s.inv_od[v]);
         s.acc[v] = 0.0;
         if (s.precision == WEDGE_PREC_FP32C)
             s.rank32[v] = (float)r;
@@ -1596,55 +1601,84 @@ __global__ void pr_init_kernel(DevGraph g, DevState s)
         c->error = 0;
         c->pr_total = 0.0;
         c->pr_sum = 0.0;
+        c->max_iter = max_iter;
     }
 }
 
-// Total rank (fixed-order reduction of the per-block tile sums; phases.c:37-46)
-// and the in-edge sums of destinations that span tiles (fixed tile order; the
-// GPU counterpart of the ordered merge of phases.c:71-114).
+// In-edge sums of the destinations whose in-edges span tiles: the partial sums
+// of the tiles a destination continues through (tail(t), t0 <= t < t1), then the
+// partial of the tile it ends in (head(t1)), in a fixed order (the GPU
+// counterpart of the ordered merge of phases.c:71-114).  A thread sums each of
+// the nshort splits at the front of the lists serially (most span one tile
+// boundary); a warp sums each of the nwide at the back (hubs).
+template <class Tail, class Head>
+__device__ __forceinline__ void merge_splits(const DevGraph& g, double* acc, const uint32_t* split_k,
+                                             const uint32_t* split_t0, const uint32_t* split_t1, uint32_t nshort,
+                                             uint32_t nwide, uint32_t cap, Tail tail, Head head)
+{
+    const uint32_t tid = blockIdx.x * blockDim.x + threadIdx.x;
+    const uint32_t nthreads = gridDim.x * blockDim.x;
+    for (uint32_t i = tid; i < nshort; i += nthreads) {
+        const uint32_t t0 = split_t0[i], t1 = split_t1[i], k = split_k[i];
+        double x = 0.0;
+        for (uint32_t t = t0; t < t1; ++t)
+            x = __dadd_rn(x, tail(t));
+        acc[g.dst_ident ? k : g.dst_id[k]] = __dadd_rn(x, head(t1));
+    }
+    const int lane = threadIdx.x & 31;
+    for (uint32_t j = tid >> 5; j < nwide; j += nthreads >> 5) {
+        const uint32_t i = cap - 1u - j;
+        const uint32_t a = split_t0[i], b = split_t1[i];
+        // four independent sums per lane, combined in a fixed order
+        double x0 = 0.0, x1 = 0.0, x2 = 0.0, x3 = 0.0;
+        uint32_t t = a + lane;
+        for (; t + 96u < b; t += 128u) {
+            x0 = __dadd_rn(x0, tail(t));
+            x1 = __dadd_rn(x1, tail(t + 32u));
+            x2 = __dadd_rn(x2, tail(t + 64u));
+            x3 = __dadd_rn(x3, tail(t + 96u));
+        }
+        for (; t < b; t += 32u)
+            x0 = __dadd_rn(x0, tail(t));
+        const double x = warp_sum_f64(__dadd_rn(__dadd_rn(x0, x1), __dadd_rn(x2, x3)));
+        if (lane == 0) {
+            const uint32_t k = split_k[i];
+            acc[g.dst_ident ? k : g.dst_id[k]] = __dadd_rn(x, head(b));
+        }
+    }
+}
+
+// The iteration's counters and log record, and the in-edge sums of the
+// destinations that span tiles (fixed tile order; the GPU counterpart of the
+// ordered merge of phases.c:71-114).
 __global__ void pr_finish_kernel(DevGraph g, DevState s, uint32_t nblocks, const unsigned long long* block_cnt)
 {
-    __shared__ double sh[AUX_THREADS / 32];
     Ctrl* c = s.ctrl;
-    const int lane = threadIdx.x & 31;
     if (blockIdx.x == 0) {
-        double x = 0.0;
-        for (uint32_t i = threadIdx.x; i < nblocks; i += blockDim.x)
-            x = __dadd_rn(x, s.block_part[i]);
-        x = warp_sum_f64(x);
-        if (lane == 0)
-            sh[threadIdx.x >> 5] = x;
         unsigned long long cnt[NCNT];
         reduce_counters(block_cnt, nblocks, cnt); /* contains __syncthreads */
         if (threadIdx.x == 0) {
-            double t = 0.0;
-            for (int w = 0; w < AUX_THREADS / 32; ++w)
-                t = __dadd_rn(t, sh[w]);
-            c->pr_total = t;
             c->last_mass = 0;
             log_iteration(s, c, cnt);
         }
     }
-    const uint32_t gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    const uint32_t nw = (gridDim.x * blockDim.x) >> 5;
-    const bool c32 = s.precision == WEDGE_PREC_FP32C;
-    for (uint32_t i = gw; i < g.nsplit; i += nw) {
-        const uint32_t t0 = g.split_t0[i], t1 = g.split_t1[i];
-        double x = 0.0;
-        for (uint32_t t = t0 + lane; t < t1; t += 32)
-            x = __dadd_rn(x, c32 ? __dadd_rn((double)s.tail_part32[2u * t], (double)s.tail_part32[2u * t + 1u])
-                                 : s.tail_part[t]);
-        x = warp_sum_f64(x);
-        if (lane == 0) {
-            const double h = c32 ? __dadd_rn((double)s.head_part32[2u * t1], (double)s.head_part32[2u * t1 + 1u])
-                                 : s.head_part[t1];
-            s.acc[g.dst_id[g.split_k[i]]] = __dadd_rn(x, h);
-        }
+    if (s.precision == WEDGE_PREC_FP32C) {
+        const float2* tp = (const float2*)s.tail_part32; /* (value, compensation) */
+        const float2* hp = (const float2*)s.head_part32;
+        merge_splits(
+            g, s.acc, g.split_k, g.split_t0, g.split_t1, g.nsplit, g.nwide, g.T,
+            [&](uint32_t t) { const float2 v = tp[t]; return __dadd_rn((double)v.x, (double)v.y); },
+            [&](uint32_t t) { const float2 v = hp[t]; return __dadd_rn((double)v.x, (double)v.y); });
+    } else {
+        merge_splits(g, s.acc, g.split_k, g.split_t0, g.split_t1, g.nsplit, g.nwide, g.T, [&](uint32_t t) { return s.tail_part[t]; },
+                     [&](uint32_t t) { return s.head_part[t]; });
     }
 }
 
 // perform_vertex_phase_pr (phase_vertex_pr.c:26-77):
 // rank' = ((acc + (1 - total)/N) * d + (1 - d)/N) / outdegree'
+// (a multiply by s.inv_od where the state holds it; the no-alloc entry point,
+// which has no state, divides)
 __global__ void pr_vertex_kernel(DevGraph g, DevState s)
 {
     const double N = (double)g.V;
@@ -1653,14 +1687,74 @@ __global__ void pr_vertex_kernel(DevGraph g, DevState s)
     const double corr = __ddiv_rn(__dsub_rn(1.0, s.ctrl->pr_total), N);
     const bool c32 = s.precision == WEDGE_PREC_FP32C;
     for (uint64_t v = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; v < g.V; v += (uint64_t)gridDim.x * blockDim.x) {
-        const uint32_t od = g.outdeg[v];
-        const double odd = od ? (double)od : N;
-        const double r = __ddiv_rn(__dadd_rn(__dmul_rn(__dadd_rn(s.acc[v], corr), d), omd), odd);
+        const double x = __dadd_rn(__dmul_rn(__dadd_rn(s.acc[v], corr), d), omd);
+        double r;
+        if (s.inv_od) {
+            r = __dmul_rn(x, s.inv_od[v]);
+        } else {
+            const uint32_t od = g.outdeg[v];
+            r = __ddiv_rn(x, od ? (double)od : N);
+        }
         if (c32)
             s.rank32[v] = (float)r;
         else
             s.rank[v] = r;
     }
+}
+
+// Total rank: the sum of all accumulators after the merge.  The reference
+// sums the gathered values per thread during the edge phase and combines the
+// per-thread sums (phases.c:37-46, phase_vertex_pr.c:43-46); this is the same
+// quantity summed in another fixed order, once per vertex instead of once per
+// edge (FP64 additions are scarce on this GPU).  Each block writes its sum to
+// part[]; the last block to finish combines them in block order.  grid <=
+// the length of part[].
+__global__ void pr_total_kernel(const double* acc, uint64_t V, double* part, Ctrl* c)
+{
+    __shared__ double sh[AUX_THREADS / 32];
+    __shared__ unsigned int ticket;
+    const int lane = threadIdx.x & 31;
+    const uint64_t n = (uint64_t)gridDim.x * blockDim.x;
+    uint64_t v = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
+    double x0 = 0.0, x1 = 0.0, x2 = 0.0, x3 = 0.0;
+    for (; v + 3u * n < V; v += 4u * n) {
+        x0 = __dadd_rn(x0, acc[v]);
+        x1 = __dadd_rn(x1, acc[v + n]);
+        x2 = __dadd_rn(x2, acc[v + 2u * n]);
+        x3 = __dadd_rn(x3, acc[v + 3u * n]);
+    }
+    for (; v < V; v += n)
+        x0 = __dadd_rn(x0, acc[v]);
+    double x = warp_sum_f64(__dadd_rn(__dadd_rn(x0, x1), __dadd_rn(x2, x3)));
+    if (lane == 0)
+        sh[threadIdx.x >> 5] = x;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double t = 0.0;
+        for (int w = 0; w < AUX_THREADS / 32; ++w)
+            t = __dadd_rn(t, sh[w]);
+        part[blockIdx.x] = t;
+        __threadfence();
+        ticket = atomicAdd(&c->pr_ticket, 1u);
+    }
+    __syncthreads();
+    if (ticket == gridDim.x - 1u && threadIdx.x < 32) { /* the last block: every part[] is visible */
+        __threadfence();
+        double y = 0.0;
+        for (uint32_t i = lane; i < gridDim.x; i += 32u)
+            y = __dadd_rn(y, __ldcg(part + i));
+        y = warp_sum_f64(y);
+        if (lane == 0) {
+            c->pr_total = y;
+            c->pr_ticket = 0u;
+        }
+    }
+}
+
+// condition of the captured PageRank iteration loop
+__global__ void pr_loop_cond_kernel(DevState s, cudaGraphConditionalHandle handle)
+{
+    cudaGraphSetConditional(handle, s.ctrl->iter < s.ctrl->max_iter ? 1u : 0u);
 }
 
 // PageRank Sum (execution_pr.c:63-71): sum of rank' * outdegree' over all vertices
@@ -1919,8 +2013,10 @@ static int ensure_state(wedge_graph* h, int app, int precision)
     WEDGE_CHECK(cudaMemset(bp, 0, sizeof(double) * (grid * (1 + 2 * NCNT))));
     s.app = (uint32_t)app;
     if (app == WEDGE_APP_PR) {
-        if ((rc = dalloc(h, &s.acc, V, true)))
+        if ((rc = dalloc(h, &s.acc, V, true)) || (rc = dalloc(h, &s.inv_od, V, true)))
             return rc;
+        pr_inv_outdeg_kernel<<<grid_for(V, AUX_THREADS, (uint32_t)h->num_sms * 8u), AUX_THREADS, 0, h->stream>>>(g, s.inv_od);
+        WEDGE_CHECK(cudaGetLastError());
         if (precision == WEDGE_PREC_FP32C) {
             if ((rc = dalloc(h, &s.rank32, V, true)) || (rc = dalloc(h, &s.head_part32, 2ull * g.T + 2, true)) ||
                 (rc = dalloc(h, &s.tail_part32, 2ull * g.T + 2, true)))
@@ -2005,6 +2101,20 @@ static uint64_t iteration_launches(int app) { return 6ull + (two_phase_app(app) 
 static uint32_t aux_grid(wedge_graph* h, uint64_t work)
 {
     return grid_for(work, AUX_THREADS, (uint32_t)h->num_sms * 8u);
+}
+
+// PageRank total rank into Ctrl::pr_total; its block sums use the PageRank-sum
+// partials (num_sms * 8 + 8 doubles after the counters)
+static void launch_pr_total(wedge_graph* h)
+{
+    pr_total_kernel<<<aux_grid(h, h->g.V), AUX_THREADS, 0, h->stream>>>(h->s.acc, h->g.V, pr_sums(h), h->s.ctrl);
+}
+
+// PageRank merge: a thread per short split, a warp per long one
+static uint32_t finish_grid(wedge_graph* h, const DevGraph& g)
+{
+    const uint64_t wide = (uint64_t)g.nwide * 32u;
+    return aux_grid(h, (g.nsplit > wide ? g.nsplit : wide) + 1);
 }
 
 // Wedge frontier -> tile list, with the tile size of the application's pull
@@ -2194,6 +2304,47 @@ static int run_traversal(wedge_graph* h, int app, const wedge_params_t* p, wedge
     return WEDGE_OK;
 }
 
+// Captures one PageRank iteration (pull, ordered merge, vertex phase) as the
+// body of a device-side while loop on Ctrl::iter < Ctrl::max_iter.  The
+// kernels hold the state by value, so the capture is keyed on the damping
+// factor (the precision is part of the state, whose rebuild drops it).
+static int build_pr_graph(wedge_graph* h)
+{
+    uint64_t key;
+    memcpy(&key, &h->s.damping, sizeof(key));
+    if (h->pr_exec && h->pr_key == key)
+        return WEDGE_OK;
+    if (h->pr_exec) {
+        cudaGraphExecDestroy(h->pr_exec);
+        h->pr_exec = nullptr;
+    }
+    const DevGraph& g = h->g;
+    cudaGraph_t graph;
+    WEDGE_CHECK(cudaGraphCreate(&graph, 0));
+    cudaGraphConditionalHandle handle;
+    WEDGE_CHECK(cudaGraphConditionalHandleCreate(&handle, graph, 1, cudaGraphCondAssignDefault));
+    cudaGraphNodeParams cparams = {};
+    cparams.type = cudaGraphNodeTypeConditional;
+    cparams.conditional.handle = handle;
+    cparams.conditional.type = cudaGraphCondTypeWhile;
+    cparams.conditional.size = 1;
+    cudaGraphNode_t cnode;
+    WEDGE_CHECK(cudaGraphAddNode(&cnode, graph, nullptr, nullptr, 0, &cparams));
+    cudaGraph_t body = cparams.conditional.phGraph_out[0];
+    WEDGE_CHECK(cudaStreamBeginCaptureToGraph(h->stream, body, nullptr, nullptr, 0, cudaStreamCaptureModeRelaxed));
+    launch_pull(h, WEDGE_APP_PR);
+    pr_finish_kernel<<<finish_grid(h, g), AUX_THREADS, 0, h->stream>>>(g, h->s, h->pull_grid, counters(h));
+    launch_pr_total(h);
+    pr_vertex_kernel<<<aux_grid(h, g.V), AUX_THREADS, 0, h->stream>>>(g, h->s);
+    pr_loop_cond_kernel<<<1, 1, 0, h->stream>>>(h->s, handle);
+    cudaGraph_t captured;
+    WEDGE_CHECK(cudaStreamEndCapture(h->stream, &captured));
+    WEDGE_CHECK(cudaGraphInstantiate(&h->pr_exec, graph, 0));
+    cudaGraphDestroy(graph);
+    h->pr_key = key;
+    return WEDGE_OK;
+}
+
 static int run_pr(wedge_graph* h, const wedge_params_t* p, wedge_stats_t* st)
 {
     const DevGraph& g = h->g;
@@ -2201,17 +2352,26 @@ static int run_pr(wedge_graph* h, const wedge_params_t* p, wedge_stats_t* st)
     h->s.damping = p->damping > 0.0 ? p->damping : 0.875;
     h->s.precision = (uint32_t)p->precision;
     const uint32_t vgrid = aux_grid(h, g.V);
-    const uint32_t fgrid = aux_grid(h, (uint64_t)g.nsplit * 32 + 1);
+    const uint32_t fgrid = finish_grid(h, g);
+    const bool use_graph = (p->flags & WEDGE_FLAG_GRAPH) != 0 && !timing && p->num_iterations > 0;
+    if (use_graph) {
+        int rc = build_pr_graph(h);
+        if (rc)
+            return rc;
+    }
     double t_pull = 0, t_vertex = 0;
     WEDGE_CHECK(cudaEventRecord(h->ev[0], h->stream));
-    pr_init_kernel<<<vgrid, AUX_THREADS, 0, h->stream>>>(g, h->s);
-    for (uint32_t it = 0; it < p->num_iterations; ++it) {
+    pr_init_kernel<<<vgrid, AUX_THREADS, 0, h->stream>>>(g, h->s, p->num_iterations);
+    if (use_graph)
+        WEDGE_CHECK(cudaGraphLaunch(h->pr_exec, h->stream));
+    for (uint32_t it = 0; !use_graph && it < p->num_iterations; ++it) {
         if (timing)
             WEDGE_CHECK(cudaEventRecord(h->ev[2], h->stream));
         launch_pull(h, WEDGE_APP_PR);
         if (timing)
             WEDGE_CHECK(cudaEventRecord(h->ev[3], h->stream));
         pr_finish_kernel<<<fgrid, AUX_THREADS, 0, h->stream>>>(g, h->s, h->pull_grid, counters(h));
+        launch_pr_total(h);
         pr_vertex_kernel<<<vgrid, AUX_THREADS, 0, h->stream>>>(g, h->s);
         if (timing) {
             WEDGE_CHECK(cudaEventRecord(h->ev[4], h->stream));
@@ -2250,7 +2410,7 @@ static int run_pr(wedge_graph* h, const wedge_params_t* p, wedge_stats_t* st)
         st->edges_scanned = c.edges_scanned;
         st->tiles_scanned = c.tiles_scanned;
         st->pull_launches = c.pull_launches;
-        st->kernel_launches = 3ull + 3ull * p->num_iterations;
+        st->kernel_launches = 3ull + (use_graph ? 5ull : 4ull) * p->num_iterations; /* + the loop condition */
         st->pr_sum = c.pr_sum;
     }
     if (c.error)
@@ -2334,7 +2494,7 @@ int wedge_cuda_run_phase(wedge_graph_t* g, int app, int phase, const wedge_param
     switch (phase) {
     case WEDGE_PHASE_INIT:
         if (app == WEDGE_APP_PR) {
-            pr_init_kernel<<<vgrid, AUX_THREADS, 0, g->stream>>>(dg, g->s);
+            pr_init_kernel<<<vgrid, AUX_THREADS, 0, g->stream>>>(dg, g->s, 0u);
         } else {
             const uint64_t root = params->root < dg.V ? params->root : 0;
             const unsigned long long thr =
@@ -2359,8 +2519,9 @@ int wedge_cuda_run_phase(wedge_graph_t* g, int app, int phase, const wedge_param
         }
         launch_pull(g, app);
         if (app == WEDGE_APP_PR) {
-            pr_finish_kernel<<<aux_grid(g, (uint64_t)dg.nsplit * 32 + 1), AUX_THREADS, 0, g->stream>>>(
+            pr_finish_kernel<<<finish_grid(g, dg), AUX_THREADS, 0, g->stream>>>(
                 dg, g->s, g->pull_grid, counters(g));
+            launch_pr_total(g);
         } else {
             decide_kernel<<<1, AUX_THREADS, 0, g->stream>>>(dg, g->s, counters(g), pull_slots(g, app), (uint32_t)app);
         }
@@ -2569,6 +2730,10 @@ int wedge_cuda_set_scheduler(wedge_graph_t* g, const float* blob, uint64_t count
         g->graph_exec = nullptr;
         g->graph_app = -1;
     }
+    if (g->pr_exec) {
+        cudaGraphExecDestroy(g->pr_exec);
+        g->pr_exec = nullptr;
+    }
     return WEDGE_OK;
 }
 
@@ -2599,7 +2764,7 @@ constexpr int NOALLOC_MAX_DEVICES = 64;
 struct NoAllocScratch {
     Ctrl ctrl;
     IterRec log[1];
-    unsigned int nsplit;
+    unsigned int nsplit[2];  // short splits at the front of the split lists, long ones at the back
     unsigned long long block_cnt[NCNT * NOALLOC_MAX_GRID];
     double block_part[NOALLOC_MAX_GRID];
     uint32_t tile_dst0[NOALLOC_MAX_TILES + 1];
@@ -2630,7 +2795,8 @@ __global__ void noalloc_prepare_kernel(const unsigned long long* dst_off, uint32
         memset(c, 0, sizeof(Ctrl));
         c->mode = MODE_DENSE;
         c->iter = LOG_CAP; /* no per-iteration log in this path */
-        sc->nsplit = 0u;
+        sc->nsplit[0] = 0u;
+        sc->nsplit[1] = 0u;
     }
     for (uint64_t i = tid; i < (uint64_t)T * TILE / 32 + 1; i += (uint64_t)gridDim.x * blockDim.x)
         sc->dst_start[i] = 0u; /* set by dst_start_kernel next */
@@ -2655,38 +2821,11 @@ __global__ void noalloc_prepare_kernel(const unsigned long long* dst_off, uint32
 
 // total rank and the destinations spanning tiles, as pr_finish_kernel, with the
 // split count read from the scratch
-__global__ void noalloc_finish_kernel(DevGraph g, DevState s, uint32_t nblocks)
+__global__ void noalloc_finish_kernel(DevGraph g, DevState s)
 {
-    __shared__ double sh[AUX_THREADS / 32];
     NoAllocScratch* sc = &g_noalloc_scratch;
-    const int lane = threadIdx.x & 31;
-    if (blockIdx.x == 0) {
-        double x = 0.0;
-        for (uint32_t i = threadIdx.x; i < nblocks; i += blockDim.x)
-            x = __dadd_rn(x, sc->block_part[i]);
-        x = warp_sum_f64(x);
-        if (lane == 0)
-            sh[threadIdx.x >> 5] = x;
-        __syncthreads();
-        if (threadIdx.x == 0) {
-            double t = 0.0;
-            for (int w = 0; w < AUX_THREADS / 32; ++w)
-                t = __dadd_rn(t, sh[w]);
-            sc->ctrl.pr_total = t;
-        }
-    }
-    const uint32_t nsplit = sc->nsplit;
-    const uint32_t gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    const uint32_t nw = (gridDim.x * blockDim.x) >> 5;
-    for (uint32_t i = gw; i < nsplit; i += nw) {
-        const uint32_t t0 = sc->split_t0[i], t1 = sc->split_t1[i];
-        double x = 0.0;
-        for (uint32_t t = t0 + lane; t < t1; t += 32)
-            x = __dadd_rn(x, sc->tail_part[t]);
-        x = warp_sum_f64(x);
-        if (lane == 0)
-            s.acc[g.dst_id[sc->split_k[i]]] = __dadd_rn(x, sc->head_part[t1]);
-    }
+    merge_splits(g, s.acc, sc->split_k, sc->split_t0, sc->split_t1, sc->nsplit[0], sc->nsplit[1], g.T,
+                 [&](uint32_t t) { return sc->tail_part[t]; }, [&](uint32_t t) { return sc->head_part[t]; });
 }
 
 static int noalloc_setup(int dev, NoAllocScratch** sc, uint32_t* grid)
@@ -2775,17 +2914,16 @@ extern "C" int wedge_cuda_pr_iteration_noalloc(uint64_t num_vertices, uint64_t n
                                                                                           sc->dst_start);
     if (num_dsts)
         split_kernel<<<grid_for(num_dsts, AUX_THREADS, grid * 2u), AUX_THREADS, 0, st>>>(
-            g.dst_off, g.Vne, sc->split_k, sc->split_t0, sc->split_t1, &sc->nsplit);
+            g.dst_off, g.Vne, T, sc->split_k, sc->split_t0, sc->split_t1, sc->nsplit);
     WEDGE_CHECK(cudaMemsetAsync(rank_out, 0, num_vertices * sizeof(double), st));
     DevState sp = s;
     sp.rank = (double*)rank_in; /* gathered by the pull */
     if (T)
         pull_kernel<WEDGE_APP_PR, PullEpl<WEDGE_APP_PR>::value><<<grid, PULL_THREADS, 0, st>>>(g, sp, sc->block_cnt,
                                                                                            PHASE_ALL); /* no hub cache */
-    else
-        WEDGE_CHECK(cudaMemsetAsync(sc->block_part, 0, sizeof(double), st));
-    noalloc_finish_kernel<<<grid_for((uint64_t)T * 32 + 1, AUX_THREADS, grid * 2u), AUX_THREADS, 0, st>>>(
-        g, s, T ? grid : 1u);
+    noalloc_finish_kernel<<<grid_for((uint64_t)T + 1, AUX_THREADS, grid * 2u), AUX_THREADS, 0, st>>>(g, s);
+    pr_total_kernel<<<grid_for(num_vertices, AUX_THREADS, NOALLOC_MAX_GRID < grid * 2u ? NOALLOC_MAX_GRID : grid * 2u),
+                      AUX_THREADS, 0, st>>>(s.acc, num_vertices, sc->block_part, &sc->ctrl);
     DevState sv = s;
     sv.rank = rank_out;
     pr_vertex_kernel<<<grid_for(num_vertices, AUX_THREADS, grid * 2u), AUX_THREADS, 0, st>>>(g, sv);

@@ -96,6 +96,7 @@ struct Ctrl {
     unsigned int probe_mode;
     unsigned int learned_iters;        // iterations whose mode the scheduler network chose
     unsigned int alist_n;              // vertices in the Wedge-build vertex list
+    unsigned int pr_ticket;            // blocks of pr_total_kernel done (the last one resets it)
     double pr_total;                   // sum of all accumulators (phase_vertex_pr.c:161)
     double pr_sum;                     // PageRank Sum statistic
 };
@@ -105,7 +106,7 @@ struct DevGraph {
     uint64_t V, E, Epad;
     uint32_t Vne, T, nsplit, weight_kind;
     uint32_t dst_ident;        // dst_id[k] == k for every k (the vertices with in-edges are [0, Vne))
-    uint32_t pad0;
+    uint32_t nwide;            // destinations spanning more than SPLIT_SERIAL tile boundaries (back of the split lists)
     const uint32_t* src;
     const unsigned long long* w;
     const uint32_t* dst_id;
@@ -115,7 +116,8 @@ struct DevGraph {
     const uint32_t* outdeg;
     const unsigned long long* csri_off;
     const uint32_t* csri;
-    const uint32_t* split_k;   // compressed destinations whose in-edges span tiles
+    const uint32_t* split_k;   // compressed destinations whose in-edges span tiles ([T]: nsplit short
+                               // ones from the front, nwide long ones from the back)
     const uint32_t* split_t0;  // their first tile
     const uint32_t* split_t1;  // their last tile
     const uint32_t* new2old;   // degree relabelling: engine id -> caller's id
@@ -129,6 +131,7 @@ struct DevState {
     double* rank;                  // PageRank FP64: rank / outdegree'
     float* rank32;                 // PageRank FP32C: rank / outdegree'
     double* acc;                   // PageRank accumulators (graph_vertex_accumulators)
+    double* inv_od;                // PageRank 1 / outdegree' (outdegree, or N for dangling vertices)
     double* head_part;             // [T] partial sum of a split destination ending in tile t
     double* tail_part;             // [T] partial sum of a split destination continuing past tile t
     float* head_part32;            // FP32C partial sums (value, compensation) interleaved
@@ -183,6 +186,8 @@ struct wedge_graph {
     double* iter_wedge_ms;
     int last_timing;
     cudaGraphExec_t graph_exec;        // captured traversal
+    cudaGraphExec_t pr_exec;           // captured PageRank iterations
+    uint64_t pr_key;                   // (iterations, precision) of pr_exec
     int graph_app;
     int graph_key;
 };
