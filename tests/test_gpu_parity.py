@@ -337,6 +337,43 @@ def test_phase_api_drives_the_reference_loop(W, O):
         check_bfs(g.read_results(), V, s, d, 0)
 
 
+def test_phase_api_cc_symmetric_reads_mid_traversal(W, O):
+    """CC over wedge_cuda_run_phase on a symmetric graph (engine-id labels): results read
+    between pulls are caller ids no lower than the final labels, and reading them does not
+    disturb the traversal, which ends on the reference's labels"""
+    V, s, d = graph_edges(O, "rmat", dict(scale=12, edge_factor=8, seed=7), True)
+    ref, _, _ = O.Graph.from_edges(V, s, d, O.CC).run(threads=4)
+    final = ref.view(np.float64)
+    p = W.Params()
+    with W.Graph.from_edges(V, s, d) as g:
+        g.run_phase(W.APP_CC, 0, p)
+        iters = 0
+        while True:
+            iters += 1
+            active = g.run_phase(W.APP_CC, 1, p)  # dense pull
+            mid = g.read_results().view(np.float64)
+            assert np.all(mid >= final) and np.all(mid < V) and np.all(mid == np.floor(mid))
+            if active == 0:
+                break
+            g.run_phase(W.APP_CC, 4, p)
+            g.run_phase(W.APP_CC, 5, p)
+            assert iters < 100
+        assert np.array_equal(g.read_results(), ref)
+
+
+def test_cc_label_space_symmetry_check(W, O):
+    """a symmetric graph propagates engine ids and converts them; one edge without its
+    reverse keeps the caller's ids; isolated vertices (V > E) change nothing: all exact"""
+    V, s, d = graph_edges(O, "rmat", dict(scale=11, edge_factor=8, seed=8), True)
+    i = int(np.flatnonzero(s != d)[len(s) // 2])
+    keep = ~((s == s[i]) & (d == d[i]))  # every copy of one edge, its reverse stays
+    for VV, ss, dd in ((V, s[keep], d[keep]), (V * 40, s, d)):
+        ref, _, _ = O.Graph.from_edges(VV, ss, dd, O.CC).run(threads=4)
+        for flags in (0, W.FLAG_GRAPH):
+            got, _, _ = run_engine(W, VV, ss, dd, W.APP_CC, flags=flags)
+            assert np.array_equal(got, ref)
+
+
 def test_iteration_cap_reports_not_converged(W, O):
     V, s, d = graph_edges(O, "grid", dict(side=32, frac=0.0, seed=3))
     with W.Graph.from_edges(V, s, d) as g:

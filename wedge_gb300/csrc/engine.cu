@@ -85,6 +85,7 @@ static void free_state(wedge_graph* h)
     memset(&h->s, 0, sizeof(h->s));
     h->s.net = h->net; /* the scheduler network outlives the state arrays */
     h->built_app = -1;
+    h->cc_pending = 0;
     if (h->graph_exec) {
         cudaGraphExecDestroy(h->graph_exec);
         h->graph_exec = nullptr;
@@ -227,6 +228,44 @@ __global__ void split_kernel(const unsigned long long* dst_off, uint32_t Vne, ui
             split_k[i] = k;
             split_t0[i] = t0;
             split_t1[i] = t1;
+        }
+    }
+}
+
+// vertex -> compressed destination index (preset to NONE32: no in-edges)
+__global__ void dst_index_kernel(const uint32_t* dst_id, uint32_t Vne, uint32_t* inv)
+{
+    for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < Vne; k += gridDim.x * blockDim.x)
+        inv[dst_id[k]] = k;
+}
+
+// Symmetry: the reverse of every edge s -> d is an edge, i.e. d is among the
+// in-neighbours of s (ascending within a destination: a binary search).  Sets
+// *asym at the first edge without its reverse; the others then stop early.
+__global__ void sym_check_kernel(const uint32_t* src, const uint32_t* dst, uint64_t E, const uint32_t* inv,
+                                 const unsigned long long* dst_off, unsigned int* asym)
+{
+    uint32_t n = 0;
+    for (uint64_t e = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; e < E; e += (uint64_t)gridDim.x * blockDim.x) {
+        if ((++n & 63u) == 0u && *(volatile unsigned int*)asym)
+            return;
+        const uint32_t sv = src[e], d = dst[e];
+        const uint32_t k = inv[sv];
+        bool found = false;
+        if (k != NONE32) {
+            unsigned long long lo = dst_off[k], hi = dst_off[k + 1]; /* first source >= d in [lo, hi) */
+            while (lo < hi) {
+                const unsigned long long mid = lo + (hi - lo) / 2u;
+                if (src[mid] < d)
+                    lo = mid + 1u;
+                else
+                    hi = mid;
+            }
+            found = lo < dst_off[k + 1] && src[lo] == d;
+        }
+        if (!found) {
+            atomicOr(asym, 1u);
+            return;
         }
     }
 }
@@ -422,6 +461,21 @@ int build_from_device_edges(wedge_graph* h, uint64_t V, uint64_t E, uint32_t* d_
     }
     tile_index_kernel<<<grid_for((uint64_t)g.T + 1, AUX_THREADS, cap), AUX_THREADS, 0, st>>>(kidx, E, g.T, Vne,
                                                                                                tile_dst0, dst_off);
+    // symmetry (CC's label space)
+    unsigned int h_asym = 1u;
+    if (E) {
+        uint32_t* inv = nullptr;
+        unsigned int* d_asym = nullptr;
+        WEDGE_CHECK(cudaMallocAsync((void**)&inv, V * sizeof(uint32_t), st));
+        WEDGE_CHECK(cudaMallocAsync((void**)&d_asym, sizeof(unsigned int), st));
+        WEDGE_CHECK(cudaMemsetAsync(d_asym, 0, sizeof(unsigned int), st));
+        WEDGE_CHECK(cudaMemsetAsync(inv, 0xFF, V * sizeof(uint32_t), st));
+        dst_index_kernel<<<grid_for(Vne, AUX_THREADS, cap), AUX_THREADS, 0, st>>>(dst_id, Vne, inv);
+        sym_check_kernel<<<grid_for(E, AUX_THREADS, cap), AUX_THREADS, 0, st>>>(d_src, d_dst, E, inv, dst_off, d_asym);
+        WEDGE_CHECK(cudaMemcpyAsync(&h_asym, d_asym, sizeof(unsigned int), cudaMemcpyDeviceToHost, st));
+        cudaFreeAsync(d_asym, st);
+        cudaFreeAsync(inv, st);
+    }
     cudaFreeAsync(kidx, st);
     cudaFreeAsync(d_dst, st);
 
@@ -474,6 +528,7 @@ int build_from_device_edges(wedge_graph* h, uint64_t V, uint64_t E, uint32_t* d_
     g.nsplit = nsplit[0];
     g.nwide = nsplit[1];
     g.dst_ident = (Vne && last_dst == Vne - 1) ? 1u : 0u;
+    g.sym = h_asym ? 0u : 1u;
     g.dst_id = dst_id;
     g.dst_off = dst_off;
     g.tile_dst0 = tile_dst0;
@@ -765,6 +820,12 @@ __global__ void __launch_bounds__(PULL_THREADS, 1)
     const uint64_t hub_fit = hub_have & ~15ull;
     const uint32_t hub_bytes = (uint64_t)s.hub_bytes < hub_fit ? s.hub_bytes : (uint32_t)hub_fit; /* within smem and the array */
     bool use_hub = hub_bytes != 0u && ((uintptr_t)hub_src & 15u) == 0u && (smem_u32(hub_smem) & 15u) == 0u;
+    // CC on a symmetric graph propagates engine ids: before the first pull every
+    // label is its vertex's own id, so that pull takes the ids of the sources
+    // outside the hub cache instead of gathering their labels (where another warp
+    // lowered one already, the old value only delays that progress by an
+    // iteration); hub sources come from the cache, which the hub launch updated
+    const bool ident0 = APP == WEDGE_APP_CC && g.sym != 0u && c->iter == 0u;
     if (APP == WEDGE_APP_BFS)
         use_hub = use_hub && (mode != MODE_WEDGE || c->tiles >= T / 16u);
     else if (two_phase_app(APP))
@@ -882,7 +943,11 @@ __global__ void __launch_bounds__(PULL_THREADS, 1)
             auto gather = [&](uint32_t x) -> uint32_t {
                 if (filtered && x != NONE32 && !((ld_ro_u32(cur + (x >> 5)) >> (x & 31u)) & 1u))
                     return NONE32; /* source unchanged by the previous pull */
-                return (x < hub_lim) ? hub32[x] : ((x != NONE32) ? s.prop32[x] : NONE32);
+                if (x < hub_lim)
+                    return hub32[x];
+                if (ident0)
+                    return x; /* first pull over engine-id labels: the source still holds its own id */
+                return (x != NONE32) ? s.prop32[x] : NONE32;
             };
             if (!in.anydone) {
 #pragma unroll
@@ -1450,8 +1515,13 @@ __global__ void init_kernel(DevGraph g, DevState s, uint32_t app, uint32_t topen
     for (uint64_t v = tid; v < g.V; v += stride) {
         if (app == WEDGE_APP_BFS)
             s.prop32[v] = NONE32; /* execution_bfs.c:106 */
-        else if (app == WEDGE_APP_CC)
-            s.prop32[v] = g.new2old[v]; /* execution_cc.c:77: labels are the caller's vertex ids */
+        else if (app == WEDGE_APP_CC) {
+            // execution_cc.c:77: labels are vertex ids -- the caller's, or on a
+            // symmetric graph the engine's, converted when the labels converge
+            s.prop32[v] = g.sym ? (uint32_t)v : g.new2old[v];
+            if (s.cc_best)
+                s.cc_best[v] = NONE32;
+        }
         else
             s.prop64[v] = (g.weight_kind == WEDGE_WEIGHTS_F64) ? 0x7FF0000000000000ull : NONE64; /* execution_sssp.c:78 */
     }
@@ -1489,8 +1559,8 @@ __global__ void init_root_kernel(DevGraph g, DevState s, uint32_t app, uint64_t 
     const uint32_t tid = blockIdx.x * blockDim.x + threadIdx.x;
     const uint64_t root = g.old2new[root_in]; /* the caller's id -> relabelled id */
     if (app == WEDGE_APP_BFS || app == WEDGE_APP_CC) {
-        // BFS: the root is visited; CC: the vertex the caller numbers 0 holds label 0 already
-        const uint32_t done = (app == WEDGE_APP_BFS) ? (uint32_t)root : g.old2new[0];
+        // BFS: the root is visited; CC: the vertex whose id is label 0 holds the least label already
+        const uint32_t done = (app == WEDGE_APP_BFS) ? (uint32_t)root : g.sym ? 0u : g.old2new[0];
         if (tid == 0 && g.Vne) { /* its compressed index: dst_id ascends */
             uint32_t lo = 0, hi = g.Vne;
             while (lo < hi) {
@@ -1553,6 +1623,45 @@ __global__ void init_root_kernel(DevGraph g, DevState s, uint32_t app, uint64_t 
             c->loop = 0;
         }
     }
+}
+
+/* -------------------------------------------- CC label space (symmetric) */
+
+// On a symmetric graph the labels converge to the least engine id of each
+// component (its representative r); the reference's label is the least caller
+// id of the component (execution_cc.c:77 and the min-pull of
+// phase_edge_pull_cc.c).  best[r] = min over the component of new2old[v], with
+// best preset to NONE32.  Label 0 (the component of engine vertex 0, the
+// highest-degree vertex: the giant component) is reduced per block first;
+// other components are small and take one global atomic per vertex.
+__global__ void cc_best_kernel(DevGraph g, const uint32_t* label, uint32_t* best)
+{
+    __shared__ uint32_t best0;
+    if (threadIdx.x == 0)
+        best0 = NONE32;
+    __syncthreads();
+    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+    uint32_t m0 = NONE32;
+    for (uint64_t v = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; v < g.V; v += stride) {
+        const uint32_t r = label[v], o = g.new2old[v];
+        if (r == 0u)
+            m0 = o < m0 ? o : m0;
+        else
+            atomicMin(&best[r], o);
+    }
+    m0 = __reduce_min_sync(FULL, m0);
+    if ((threadIdx.x & 31) == 0 && m0 != NONE32)
+        atomicMin(&best0, m0);
+    __syncthreads();
+    if (threadIdx.x == 0 && best0 != NONE32)
+        atomicMin(&best[0], best0);
+}
+
+// label[v] = best[label[v]]: the caller-id labels
+__global__ void cc_apply_kernel(DevGraph g, uint32_t* label, const uint32_t* best)
+{
+    for (uint64_t v = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; v < g.V; v += (uint64_t)gridDim.x * blockDim.x)
+        label[v] = best[label[v]];
 }
 
 /* ------------------------------------------------------------- PageRank */
@@ -1803,7 +1912,8 @@ __global__ void export_kernel(DevGraph g, DevState s, uint32_t app, unsigned lon
             const uint32_t p = s.prop32[v];
             x = (p == NONE32) ? NONE64 : (unsigned long long)g.new2old[p];
         } else if (app == WEDGE_APP_CC) {
-            x = (unsigned long long)__double_as_longlong((double)s.prop32[v]);
+            const uint32_t l = s.prop32[v];
+            x = (unsigned long long)__double_as_longlong((double)(s.cc_map ? s.cc_map[l] : l));
         } else if (app == WEDGE_APP_SSSP) {
             x = s.prop64[v];
         } else {
@@ -1827,7 +1937,8 @@ __device__ __forceinline__ void out_value(const DevGraph& g, const DevState& s, 
         neg = p == NONE32;
         x = neg ? 1ull : (unsigned long long)g.new2old[p];
     } else if (app == WEDGE_APP_CC) {
-        x = s.prop32[v];
+        const uint32_t l = s.prop32[v];
+        x = s.cc_map ? s.cc_map[l] : l;
     } else {
         const unsigned long long d = s.prop64[v];
         neg = (long long)d < 0;
@@ -2043,6 +2154,10 @@ static int ensure_state(wedge_graph* h, int app, int precision)
             if ((rc = dalloc(h, &s.vis_c, (uint64_t)g.Vne / 32 + 2, true)))
                 return rc;
         }
+        if (app == WEDGE_APP_CC && g.sym) {
+            if ((rc = dalloc(h, &s.cc_best, V, true)))
+                return rc;
+        }
         if (app == WEDGE_APP_BFS) {
             if ((rc = dalloc(h, &s.tile_open, (uint64_t)g.T / 32 + 2, true)))
                 return rc;
@@ -2155,8 +2270,32 @@ static void launch_init(wedge_graph* h, int app, uint64_t root, uint32_t sched, 
     init_kernel<<<aux_grid(h, work), AUX_THREADS, 0, h->stream>>>(h->g, h->s, (uint32_t)app, topen);
     init_root_kernel<<<1, 32, 0, h->stream>>>(h->g, h->s, (uint32_t)app, root, sched, thr,
                                                                            max_iter, probe_iter, probe_mode);
+    h->cc_pending = (app == WEDGE_APP_CC && h->s.cc_best) ? 1 : 0;
     launch_wedge_build(h, h->g, app);
     advance_kernel<<<aux_grid(h, (h->g.V + 31) / 32), AUX_THREADS, 0, h->stream>>>(h->g, h->s, (uint32_t)app);
+}
+
+// CC on a symmetric graph, once the labels converged: caller-id labels in
+// place (2 launches; best was preset by init_kernel)
+static void cc_finalize(wedge_graph* h)
+{
+    cc_best_kernel<<<aux_grid(h, h->g.V), AUX_THREADS, 0, h->stream>>>(h->g, h->s.prop32, h->s.cc_best);
+    cc_apply_kernel<<<aux_grid(h, h->g.V), AUX_THREADS, 0, h->stream>>>(h->g, h->s.prop32, h->s.cc_best);
+    h->cc_pending = 0;
+}
+
+// The state the results are read from: while CC labels are engine ids (a
+// traversal driven phase by phase), a lookup table of the caller-id labels is
+// built beside them, leaving the labels themselves for further pulls.
+static int result_state(wedge_graph* h, DevState* out)
+{
+    *out = h->s;
+    if (h->last_app == WEDGE_APP_CC && h->cc_pending) {
+        WEDGE_CHECK(cudaMemsetAsync(h->s.cc_best, 0xFF, h->g.V * sizeof(uint32_t), h->stream));
+        cc_best_kernel<<<aux_grid(h, h->g.V), AUX_THREADS, 0, h->stream>>>(h->g, h->s.prop32, h->s.cc_best);
+        out->cc_map = h->s.cc_best;
+    }
+    return WEDGE_OK;
 }
 
 static int read_ctrl(wedge_graph* h, Ctrl* out)
@@ -2272,6 +2411,10 @@ static int run_traversal(wedge_graph* h, int app, const wedge_params_t* p, wedge
             if (c.done)
                 break;
         }
+    }
+    if (app == WEDGE_APP_CC && h->cc_pending) {
+        cc_finalize(h);
+        launches += 2;
     }
     WEDGE_CHECK(cudaEventRecord(h->ev[1], h->stream));
     WEDGE_CHECK(cudaGetLastError());
@@ -2559,9 +2702,13 @@ int wedge_cuda_read_results(wedge_graph_t* g, void* host_props, uint64_t bytes)
     if (!g || !host_props || bytes < 8ull * g->g.V || g->last_app < 0)
         return WEDGE_ERR_ARG;
     WEDGE_CHECK(cudaSetDevice(g->device));
+    DevState rs;
+    int rc = result_state(g, &rs);
+    if (rc)
+        return rc;
     unsigned long long* tmp = nullptr;
     WEDGE_CHECK(cudaMallocAsync((void**)&tmp, 8ull * (g->g.V ? g->g.V : 1), g->stream));
-    export_kernel<<<aux_grid(g, g->g.V), AUX_THREADS, 0, g->stream>>>(g->g, g->s, (uint32_t)g->last_app, tmp);
+    export_kernel<<<aux_grid(g, g->g.V), AUX_THREADS, 0, g->stream>>>(g->g, rs, (uint32_t)g->last_app, tmp);
     cudaError_t e = cudaMemcpyAsync(host_props, tmp, 8ull * g->g.V, cudaMemcpyDeviceToHost, g->stream);
     cudaFreeAsync(tmp, g->stream);
     WEDGE_CHECK(e);
@@ -2578,10 +2725,13 @@ int wedge_cuda_write_output(wedge_graph_t* g, const char* path, int* gpu_formatt
     const int app = g->last_app;
     const bool on_gpu = app == WEDGE_APP_BFS || app == WEDGE_APP_CC ||
                         (app == WEDGE_APP_SSSP && g->g.weight_kind != WEDGE_WEIGHTS_F64);
+    DevState rs;
+    int rc = result_state(g, &rs);
+    if (rc)
+        return rc;
     FILE* f = fopen(path, "w");
     if (!f)
         return WEDGE_ERR_IO;
-    int rc = WEDGE_OK;
     float ms = 0.0f;
     if (on_gpu) {
         unsigned long long *len = nullptr, *off = nullptr;
@@ -2593,7 +2743,7 @@ int wedge_cuda_write_output(wedge_graph_t* g, const char* path, int* gpu_formatt
             rc = WEDGE_ERR_OOM;
         } else {
             cudaMemsetAsync(len + V, 0, 8, g->stream);
-            out_len_kernel<<<aux_grid(g, V), AUX_THREADS, 0, g->stream>>>(g->g, g->s, (uint32_t)app, len);
+            out_len_kernel<<<aux_grid(g, V), AUX_THREADS, 0, g->stream>>>(g->g, rs, (uint32_t)app, len);
             rc = device_scan(g, len, off, V + 1, false);
             if (!rc && (cudaMemcpyAsync(&total, off + V, 8, cudaMemcpyDeviceToHost, g->stream) != cudaSuccess ||
                         cudaStreamSynchronize(g->stream) != cudaSuccess))
@@ -2602,7 +2752,7 @@ int wedge_cuda_write_output(wedge_graph_t* g, const char* path, int* gpu_formatt
                         cudaMallocHost((void**)&hbuf, total ? total : 1) != cudaSuccess))
                 rc = WEDGE_ERR_OOM;
             if (!rc) {
-                out_write_kernel<<<aux_grid(g, V), AUX_THREADS, 0, g->stream>>>(g->g, g->s, (uint32_t)app, off, dbuf);
+                out_write_kernel<<<aux_grid(g, V), AUX_THREADS, 0, g->stream>>>(g->g, rs, (uint32_t)app, off, dbuf);
                 if (cudaMemcpyAsync(hbuf, dbuf, total, cudaMemcpyDeviceToHost, g->stream) != cudaSuccess ||
                     cudaEventRecord(g->ev[1], g->stream) != cudaSuccess || cudaStreamSynchronize(g->stream) != cudaSuccess)
                     rc = WEDGE_ERR_CUDA;

@@ -107,6 +107,8 @@ struct DevGraph {
     uint32_t Vne, T, nsplit, weight_kind;
     uint32_t dst_ident;        // dst_id[k] == k for every k (the vertices with in-edges are [0, Vne))
     uint32_t nwide;            // destinations spanning more than SPLIT_SERIAL tile boundaries (back of the split lists)
+    uint32_t sym;              // every edge's reverse is an edge too: CC propagates engine ids (see cc_best_kernel)
+    uint32_t pad1;
     const uint32_t* src;
     const unsigned long long* w;
     const uint32_t* dst_id;
@@ -146,6 +148,8 @@ struct DevState {
     unsigned long long* tile_list; // (tile << 32 | chunk mask) of the next Wedge pull
     uint2* items;                  // (vertex, piece) Wedge-build work items
     uint32_t* alist;               // vertices the last pull activated (Wedge build)
+    uint32_t* cc_best;             // CC on a symmetric graph: least caller id of the component a label represents
+    const uint32_t* cc_map;        // results only: CC labels are looked up here (engine ids not yet converted)
     Ctrl* ctrl;
     IterRec* log;                  // [LOG_CAP] per-iteration records
     double damping;
@@ -190,6 +194,7 @@ struct wedge_graph {
     uint64_t pr_key;                   // (iterations, precision) of pr_exec
     int graph_app;
     int graph_key;
+    int cc_pending;                    // CC labels are engine ids (symmetric graph, not yet converted)
 };
 
 namespace wedge {
