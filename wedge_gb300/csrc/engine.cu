@@ -826,6 +826,8 @@ __global__ void __launch_bounds__(PULL_THREADS, 1)
     // lowered one already, the old value only delays that progress by an
     // iteration); hub sources come from the cache, which the hub launch updated
     const bool ident0 = APP == WEDGE_APP_CC && g.sym != 0u && c->iter == 0u;
+    const bool first_by_dst = ident0 && mode == MODE_DENSE && phase != PHASE_ALL;
+    use_hub = use_hub && !first_by_dst;
     if (APP == WEDGE_APP_BFS)
         use_hub = use_hub && (mode != MODE_WEDGE || c->tiles >= T / 16u);
     else if (two_phase_app(APP))
@@ -847,13 +849,90 @@ __global__ void __launch_bounds__(PULL_THREADS, 1)
     }
     uint32_t hub_lim = 0; /* elements of the cache this warp reads: 0 until the copy completed */
 
+    if (APP == WEDGE_APP_CC && first_by_dst) {
+        // The first CC pull over engine-id labels, one destination per lane.  A
+        // source outside the hub range [0, hub_n) still holds its own id, and a
+        // destination's sources ascend, so past its hub sources only the first
+        // one can lower the minimum; the hub sources' labels are final once the
+        // hub launch (the destinations with ids < hub_n) is over.  The hub launch
+        // itself sees every label at its id: the first source decides.  This is
+        // the tile pull's result for the same labels without reading the other
+        // in-edges (Jacobi for the hubs, where the tile pull lets a block's
+        // warps see each other's hub updates).
+        const bool hubs = phase == PHASE_HUBS;
+        const uint32_t kb = hubs ? 0u : s.hub_k, ke = hubs ? s.hub_k : g.Vne;
+        const uint32_t hn = s.hub_n;
+        const uint32_t nthr = gridDim.x * blockDim.x;
+        for (uint32_t base = kb + gw * 32u; base < ke; base += nthr) {
+            const uint32_t k = base + (uint32_t)lane;
+            bool chg = false, zero = false;
+            uint32_t d = 0u, od = 0u;
+            if (k < ke) {
+                d = g.dst_ident ? k : g.dst_id[k];
+                const unsigned long long lo = g.dst_off[k], hi = g.dst_off[k + 1u];
+                uint32_t m = d;
+                unsigned long long e = lo;
+                while (e < hi) {
+                    const uint32_t x = g.src[e++];
+                    if (hubs || x >= hn) {
+                        m = x < m ? x : m;
+                        break;
+                    }
+                    const uint32_t l = s.prop32[x];
+                    m = l < m ? l : m;
+                    if (m == 0u)
+                        break;
+                }
+                edges += e - lo;
+                chg = m < d;
+                zero = chg && m == 0u;
+                if (chg) {
+                    s.prop32[d] = m; /* the destination's only writer */
+                    od = g.outdeg[d];
+                    mass += od;
+                    ++act;
+                }
+            }
+            dsts += (uint64_t)__popc(__ballot_sync(FULL, k < ke));
+#pragma unroll
+            for (uint32_t b = 0; b < 3u; ++b) {
+                const uint32_t nb = __popc(__ballot_sync(FULL, chg && degree_bucket(od) == b));
+                if (lane == 0 && nb)
+                    atomicAdd(&sh_deg[b], nb);
+            }
+            if (g.dst_ident) { /* d = k: the lanes' bits fall in two words at most */
+                const uint32_t w0 = base >> 5;
+                const bool in0 = (k >> 5) == w0;
+                const uint32_t bit = 1u << (k & 31u);
+                const uint32_t c0 = __reduce_or_sync(FULL, (chg && in0) ? bit : 0u);
+                const uint32_t c1 = __reduce_or_sync(FULL, (chg && !in0) ? bit : 0u);
+                const uint32_t z0 = __reduce_or_sync(FULL, (zero && in0) ? bit : 0u);
+                const uint32_t z1 = __reduce_or_sync(FULL, (zero && !in0) ? bit : 0u);
+                if (lane == 0) {
+                    if (c0)
+                        atomicOr(&nxt[w0], c0);
+                    if (c1)
+                        atomicOr(&nxt[w0 + 1u], c1);
+                    if (z0)
+                        atomicOr(&s.vis_c[w0], z0); /* label 0 is final */
+                    if (z1)
+                        atomicOr(&s.vis_c[w0 + 1u], z1);
+                }
+            } else {
+                if (chg)
+                    atomicOr(&nxt[d >> 5], 1u << (d & 31u));
+                if (zero)
+                    atomicOr(&s.vis_c[k >> 5], 1u << (k & 31u));
+            }
+        }
+    }
     TileIter it;
     it.i = t_begin + gw;
     it.step = nw;
     it.obits = it.obase = 0u;
     TileIn nextin;
     uint32_t tn, cn;
-    bool more = next_tile<EPL>(g, s, mode, t_end, it, lane, tn, cn);
+    bool more = !(APP == WEDGE_APP_CC && first_by_dst) && next_tile<EPL>(g, s, mode, t_end, it, lane, tn, cn);
     if (more)
         tile_prefetch<APP, EPL>(g, s, tn, cn, lane, nextin);
     while (more) {
@@ -2013,7 +2092,8 @@ __global__ void hub_split_kernel(DevGraph g, uint32_t hub_n, uint32_t tile_e, ui
             hi = mid;
     }
     const unsigned long long pos = g.dst_off[lo]; /* dst_off[Vne] = E */
-    *out = (uint32_t)((pos + tile_e - 1u) / tile_e);
+    out[0] = (uint32_t)((pos + tile_e - 1u) / tile_e);
+    out[1] = lo; /* compressed destinations with ids < hub_n */
 }
 
 /* ================================================================ host */
@@ -2085,6 +2165,7 @@ static int setup_hub(wedge_graph* h, int app, int precision)
     n &= ~3ull;
     h->s.hub_n = (uint32_t)n;
     h->s.hub_tile = 0;
+    h->s.hub_k = 0;
     h->hub_bytes = (uint32_t)(n * elem);
     h->s.hub_bytes = h->hub_bytes;
     WEDGE_CHECK(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)h->hub_bytes));
@@ -2092,10 +2173,11 @@ static int setup_hub(wedge_graph* h, int app, int precision)
         uint32_t* d = (uint32_t*)(h->s.block_part + h->pull_grid); /* counters: scratch until the first pull */
         hub_split_kernel<<<1, 1, 0, h->stream>>>(h->g, (uint32_t)n, pull_tile_e(app), d);
         WEDGE_CHECK(cudaGetLastError());
-        uint32_t t = 0;
-        WEDGE_CHECK(cudaMemcpyAsync(&t, d, sizeof(t), cudaMemcpyDeviceToHost, h->stream));
+        uint32_t t[2] = {0, 0};
+        WEDGE_CHECK(cudaMemcpyAsync(t, d, sizeof(t), cudaMemcpyDeviceToHost, h->stream));
         WEDGE_CHECK(cudaStreamSynchronize(h->stream));
-        h->s.hub_tile = t;
+        h->s.hub_tile = t[0];
+        h->s.hub_k = t[1];
     }
     return WEDGE_OK;
 }

@@ -159,6 +159,7 @@ struct DevState {
     uint32_t hub_n;                // elements of the gathered array cached in shared memory by dense pulls
     uint32_t hub_bytes;            // their bytes: the pulls' dynamic shared memory (a multiple of 16)
     uint32_t hub_tile;             // CC/SSSP: first tile whose destinations all have ids >= hub_n
+    uint32_t hub_k;                // CC/SSSP: compressed destinations with ids < hub_n
     const float* net;              // scheduler network blob (WEDGE_SCHED_LEARNED), or null
 };
 
