@@ -741,13 +741,23 @@ enum : uint32_t { ERR_HUB_TIMEOUT = 2u };
 
 // pull phases: 0 = all tiles; CC/SSSP dense pulls run as two launches,
 // 1 = tiles [0, hub_tile) (the hub destinations), 2 = tiles [hub_tile, T),
-// so the second launch caches hub values that no tile of it can change
-enum : uint32_t { PHASE_ALL = 0, PHASE_HUBS = 1, PHASE_REST = 2 };
+// so the second launch caches hub values that no tile of it can change;
+// BFS pulls run as 3 = the per-destination probe, then 0
+enum : uint32_t { PHASE_ALL = 0, PHASE_HUBS = 1, PHASE_REST = 2, PHASE_PROBE = 3 };
 
 __host__ __device__ constexpr bool two_phase_app(int app)
 {
     return app == WEDGE_APP_CC || app == WEDGE_APP_SSSP;
 }
+
+// launches of one pull (each fills its own NCNT * grid block counters)
+__host__ __device__ constexpr uint32_t pull_launches_of(int app)
+{
+    return app == WEDGE_APP_PR ? 1u : 2u;
+}
+
+// BFS probe: in-edges of an unvisited destination read before the tile pull
+constexpr uint32_t PROBE_EDGES = 16;
 
 // Edge pull over all tiles (dense) or over the tiles of the Wedge frontier.
 // block_cnt[NCNT*b + CNT_*] = changed mass, in-edges read, tiles visited,
@@ -774,8 +784,8 @@ __global__ void __launch_bounds__(PULL_THREADS, 1)
     if (c->done)
         return;
     const uint32_t mode = c->mode;
-    if (phase == PHASE_REST && mode == MODE_WEDGE) {
-        // a Wedge pull ran whole in the first launch: this one only reports zeros
+    if ((phase == PHASE_REST || phase == PHASE_PROBE) && mode == MODE_WEDGE) {
+        // a Wedge pull runs whole in one launch: this one only reports zeros
         if (threadIdx.x < NCNT)
             block_cnt[NCNT * blockIdx.x + threadIdx.x] = 0ull;
         return;
@@ -827,7 +837,8 @@ __global__ void __launch_bounds__(PULL_THREADS, 1)
     // iteration); hub sources come from the cache, which the hub launch updated
     const bool ident0 = APP == WEDGE_APP_CC && g.sym != 0u && c->iter == 0u;
     const bool first_by_dst = ident0 && mode == MODE_DENSE && phase != PHASE_ALL;
-    use_hub = use_hub && !first_by_dst;
+    const bool by_dst = (APP == WEDGE_APP_CC && first_by_dst) || (APP == WEDGE_APP_BFS && phase == PHASE_PROBE);
+    use_hub = use_hub && !by_dst;
     if (APP == WEDGE_APP_BFS)
         use_hub = use_hub && (mode != MODE_WEDGE || c->tiles >= T / 16u);
     else if (two_phase_app(APP))
@@ -926,13 +937,65 @@ __global__ void __launch_bounds__(PULL_THREADS, 1)
             }
         }
     }
+    if (APP == WEDGE_APP_BFS && phase == PHASE_PROBE) {
+        // Bottom-up probe, one unvisited destination per lane: its first
+        // PROBE_EDGES sources in ascending order, up to the first one in the
+        // frontier -- the least frontier source, the value the tile pull's min
+        // would give it.  Destinations it leaves unvisited go to the tile pull
+        // (the next launch), which reads all their in-edges.
+        const uint32_t nthr = gridDim.x * blockDim.x;
+        for (uint32_t base = gw * 32u; base < g.Vne; base += nthr) {
+            const uint32_t k = base + (uint32_t)lane; /* base is a multiple of 32: one vis_c word */
+            const uint32_t vw = s.vis_c[base >> 5];
+            const bool todo = k < g.Vne && !((vw >> lane) & 1u);
+            bool hit = false;
+            uint32_t od = 0u;
+            if (todo) {
+                const uint32_t d = g.dst_ident ? k : g.dst_id[k];
+                const unsigned long long lo = g.dst_off[k], hi = g.dst_off[k + 1u];
+                const unsigned long long lim = hi - lo > PROBE_EDGES ? lo + PROBE_EDGES : hi;
+                unsigned long long e = lo;
+                uint32_t par = NONE32;
+                while (e < lim) {
+                    const uint32_t x = g.src[e++];
+                    if ((ld_ro_u32(cur + (x >> 5)) >> (x & 31u)) & 1u) {
+                        par = x;
+                        break;
+                    }
+                }
+                edges += e - lo;
+                hit = par != NONE32;
+                if (hit) {
+                    s.prop32[d] = par; /* the destination's only writer in this launch */
+                    od = g.outdeg[d];
+                    mass += od;
+                    ++act;
+                    if (!g.dst_ident)
+                        atomicOr(&nxt[d >> 5], 1u << (d & 31u));
+                }
+            }
+            dsts += (uint64_t)__popc(__ballot_sync(FULL, todo));
+#pragma unroll
+            for (uint32_t b = 0; b < 3u; ++b) {
+                const uint32_t nb = __popc(__ballot_sync(FULL, hit && degree_bucket(od) == b));
+                if (lane == 0 && nb)
+                    atomicAdd(&sh_deg[b], nb);
+            }
+            const uint32_t hits = __ballot_sync(FULL, hit);
+            if (lane == 0 && hits) {
+                atomicOr(&s.vis_c[base >> 5], hits);
+                if (g.dst_ident)
+                    atomicOr(&nxt[base >> 5], hits); /* d = k */
+            }
+        }
+    }
     TileIter it;
     it.i = t_begin + gw;
     it.step = nw;
     it.obits = it.obase = 0u;
     TileIn nextin;
     uint32_t tn, cn;
-    bool more = !(APP == WEDGE_APP_CC && first_by_dst) && next_tile<EPL>(g, s, mode, t_end, it, lane, tn, cn);
+    bool more = !by_dst && next_tile<EPL>(g, s, mode, t_end, it, lane, tn, cn);
     if (more)
         tile_prefetch<APP, EPL>(g, s, tn, cn, lane, nextin);
     while (more) {
@@ -1295,7 +1358,7 @@ __device__ __forceinline__ void log_iteration(DevState& s, Ctrl* c, const unsign
     c->tiles_scanned += cnt[CNT_TILES];
     c->dsts_scanned += cnt[CNT_DSTS];
     c->activated += cnt[CNT_ACT];
-    c->pull_launches += two_phase_app((int)s.app) ? 2u : 1u;
+    c->pull_launches += pull_launches_of((int)s.app);
     if (c->iter < LOG_CAP) {
         IterRec& r = s.log[c->iter];
         r.mass_in = c->last_mass;
@@ -2255,7 +2318,7 @@ static int ensure_state(wedge_graph* h, int app, int precision)
 static unsigned long long* counters(wedge_graph* h) { return (unsigned long long*)(h->s.block_part + h->pull_grid); }
 
 // counter slots the pulls of one iteration fill (two launches for CC/SSSP)
-static uint32_t pull_slots(wedge_graph* h, int app) { return h->pull_grid * (two_phase_app(app) ? 2u : 1u); }
+static uint32_t pull_slots(wedge_graph* h, int app) { return h->pull_grid * pull_launches_of(app); }
 
 // PageRank-sum partials after the counters
 static double* pr_sums(wedge_graph* h) { return (double*)(counters(h) + 2ull * NCNT * h->pull_grid); }
@@ -2269,6 +2332,10 @@ static void launch_pull_app(wedge_graph* h)
         pull_kernel<APP, EPL><<<grid, PULL_THREADS, h->hub_bytes, h->stream>>>(h->g, h->s, counters(h), PHASE_HUBS);
         pull_kernel<APP, EPL><<<grid, PULL_THREADS, h->hub_bytes, h->stream>>>(h->g, h->s, counters(h) + NCNT * grid,
                                                                                PHASE_REST);
+    } else if (APP == WEDGE_APP_BFS) {
+        pull_kernel<APP, EPL><<<grid, PULL_THREADS, h->hub_bytes, h->stream>>>(h->g, h->s, counters(h), PHASE_PROBE);
+        pull_kernel<APP, EPL><<<grid, PULL_THREADS, h->hub_bytes, h->stream>>>(h->g, h->s, counters(h) + NCNT * grid,
+                                                                               PHASE_ALL);
     } else {
         pull_kernel<APP, EPL><<<grid, PULL_THREADS, h->hub_bytes, h->stream>>>(h->g, h->s, counters(h), PHASE_ALL);
     }
@@ -2293,7 +2360,7 @@ static void launch_pull(wedge_graph* h, int app)
 }
 
 // kernels one iteration launches: the pull(s) and the five of the tail
-static uint64_t iteration_launches(int app) { return 6ull + (two_phase_app(app) ? 2ull : 1ull); }
+static uint64_t iteration_launches(int app) { return 6ull + pull_launches_of(app); }
 
 static uint32_t aux_grid(wedge_graph* h, uint64_t work)
 {
