@@ -631,7 +631,7 @@ __device__ __forceinline__ void tile_prefetch(const DevGraph& g, const DevState&
         in.visw = visw;
         in.open = __any_sync(FULL, open);
         in.anydone = __any_sync(FULL, done);
-        if (APP == WEDGE_APP_BFS && !in.open && lane == 0)
+        if (s.tile_open && !in.open && lane == 0)
             atomicAnd(&s.tile_open[t >> 5], ~(1u << (t & 31u))); /* closed for good */
     }
 }
@@ -680,23 +680,29 @@ __device__ __forceinline__ void load_sources(const DevGraph& g, uint64_t base, u
 // of the Wedge frontier from the list compact_kernel built.  Warp-uniform.
 struct TileIter {
     uint32_t i, step;      // dense
-    uint32_t obits, obase; // BFS dense: open tiles left in the current unit, its first tile
+    uint32_t obits, obase; // BFS/CC dense: open tiles left in the current unit, its first tile
+    uint32_t ubeg, uend;   // the units [ubeg, uend) of OPEN_UNIT tiles this launch covers
+    unsigned int* grab;    // next unit a warp takes, counted from ubeg
 };
 
 constexpr uint32_t OPEN_UNIT = 8; /* tiles a warp takes per grab of the open-tile bitmap */
 
-template <int EPL>
+template <int APP, int EPL>
 __device__ __forceinline__ bool next_tile(const DevGraph& g, const DevState& s, uint32_t mode, uint32_t t_end,
                                           TileIter& it, int lane, uint32_t& t, uint32_t& cmask)
 {
     constexpr uint32_t MASK = (EPL >= 32) ? FULL : ((1u << EPL) - 1u);
-    if (mode != MODE_WEDGE && s.tile_open) {
+    // BFS dense pulls take the open tiles dynamically; CC's keep the static
+    // stride (their tiles close for the Wedge lists, compact_kernel)
+    if (APP == WEDGE_APP_BFS && mode != MODE_WEDGE && s.tile_open) {
+        // dynamic schedule over the open-tile bitmap, OPEN_UNIT tiles per grab
+        // (tiles close as the pulls find all their destinations finished)
         while (!it.obits) {
             uint32_t u = 0;
             if (lane == 0)
-                u = atomicAdd(&s.ctrl->region_next, 1u);
-            u = __shfl_sync(FULL, u, 0);
-            if (u >= (t_end + OPEN_UNIT - 1) / OPEN_UNIT)
+                u = atomicAdd(it.grab, 1u);
+            u = __shfl_sync(FULL, u, 0) + it.ubeg;
+            if (u >= it.uend)
                 return false;
             constexpr uint32_t PER_WORD = 32 / OPEN_UNIT;
             it.obits = (s.tile_open[u / PER_WORD] >> ((u % PER_WORD) * OPEN_UNIT)) & ((1u << OPEN_UNIT) - 1u);
@@ -993,14 +999,21 @@ __global__ void __launch_bounds__(PULL_THREADS, 1)
     it.i = t_begin + gw;
     it.step = nw;
     it.obits = it.obase = 0u;
+    {
+        // open-tile units: CC's hub launch takes [0, ceil(split / OPEN_UNIT)), the rest after
+        const uint32_t usplit = (t_begin + OPEN_UNIT - 1u) / OPEN_UNIT;
+        it.ubeg = (phase == PHASE_REST) ? usplit : 0u;
+        it.uend = (phase == PHASE_HUBS) ? (t_end + OPEN_UNIT - 1u) / OPEN_UNIT : (T + OPEN_UNIT - 1u) / OPEN_UNIT;
+        it.grab = (phase == PHASE_REST) ? &c->region_next2 : &c->region_next;
+    }
     TileIn nextin;
     uint32_t tn, cn;
-    bool more = !by_dst && next_tile<EPL>(g, s, mode, t_end, it, lane, tn, cn);
+    bool more = !by_dst && next_tile<APP, EPL>(g, s, mode, t_end, it, lane, tn, cn);
     if (more)
         tile_prefetch<APP, EPL>(g, s, tn, cn, lane, nextin);
     while (more) {
         const TileIn in = nextin;
-        more = next_tile<EPL>(g, s, mode, t_end, it, lane, tn, cn);
+        more = next_tile<APP, EPL>(g, s, mode, t_end, it, lane, tn, cn);
         if (more)
             tile_prefetch<APP, EPL>(g, s, tn, cn, lane, nextin);
         ++tiles;
@@ -1397,6 +1410,7 @@ __global__ void decide_kernel(DevGraph g, DevState s, const unsigned long long* 
         c->mass = m;
         c->parity ^= 1u;
         c->region_next = 0u;
+        c->region_next2 = 0u;
         c->tiles = 0u;
         c->items = 0u;
         c->alist_n = 0u;
@@ -1727,6 +1741,7 @@ __global__ void init_root_kernel(DevGraph g, DevState s, uint32_t app, uint64_t 
         c->items = 0;
         c->alist_n = 0;
         c->region_next = 0;
+        c->region_next2 = 0;
         c->tiles = 0;
         c->iter = 0;
         c->wedge_iters = 0;
@@ -1849,6 +1864,7 @@ __global__ void pr_init_kernel(DevGraph g, DevState s, uint32_t max_iter)
         c->mode = MODE_DENSE;
         c->parity = 0;
         c->region_next = 0;
+        c->region_next2 = 0;
         c->error = 0;
         c->pr_total = 0.0;
         c->pr_sum = 0.0;
@@ -2303,7 +2319,7 @@ static int ensure_state(wedge_graph* h, int app, int precision)
             if ((rc = dalloc(h, &s.cc_best, V, true)))
                 return rc;
         }
-        if (app == WEDGE_APP_BFS) {
+        if (app == WEDGE_APP_BFS || app == WEDGE_APP_CC) {
             if ((rc = dalloc(h, &s.tile_open, (uint64_t)g.T / 32 + 2, true)))
                 return rc;
         }
@@ -2415,7 +2431,8 @@ static void launch_init(wedge_graph* h, int app, uint64_t root, uint32_t sched, 
                         uint32_t probe_iter = 0xFFFFFFFFu, uint32_t probe_mode = MODE_DENSE)
 {
     const uint64_t work = h->g.V > h->g.T ? h->g.V : h->g.T;
-    const uint32_t topen = (uint32_t)((h->g.E + 32u * PullEpl<WEDGE_APP_BFS>::value - 1) / (32u * PullEpl<WEDGE_APP_BFS>::value));
+    const uint32_t tile_e = pull_tile_e(app);
+    const uint32_t topen = (uint32_t)((h->g.E + tile_e - 1) / tile_e); /* pull tiles holding in-edges */
     init_kernel<<<aux_grid(h, work), AUX_THREADS, 0, h->stream>>>(h->g, h->s, (uint32_t)app, topen);
     init_root_kernel<<<1, 32, 0, h->stream>>>(h->g, h->s, (uint32_t)app, root, sched, thr,
                                                                            max_iter, probe_iter, probe_mode);
