@@ -705,7 +705,8 @@ __device__ __forceinline__ bool next_tile(const DevGraph& g, const DevState& s, 
             if (u >= it.uend)
                 return false;
             constexpr uint32_t PER_WORD = 32 / OPEN_UNIT;
-            it.obits = (s.tile_open[u / PER_WORD] >> ((u % PER_WORD) * OPEN_UNIT)) & ((1u << OPEN_UNIT) - 1u);
+            const uint32_t* bm = s.tile_need ? s.tile_need : s.tile_open; /* BFS: the tiles its probe left work in */
+            it.obits = (bm[u / PER_WORD] >> ((u % PER_WORD) * OPEN_UNIT)) & ((1u << OPEN_UNIT) - 1u);
             it.obase = u * OPEN_UNIT;
         }
         t = it.obase + (uint32_t)(__ffs(it.obits) - 1);
@@ -944,11 +945,20 @@ __global__ void __launch_bounds__(PULL_THREADS, 1)
         }
     }
     if (APP == WEDGE_APP_BFS && phase == PHASE_PROBE) {
+        auto mark_tiles = [](uint32_t* bm, uint32_t ta, uint32_t tb) {
+            for (uint32_t w = ta >> 5; w <= (tb >> 5); ++w) {
+                const uint32_t a = (w == (ta >> 5)) ? (ta & 31u) : 0u;
+                const uint32_t z = (w == (tb >> 5)) ? (tb & 31u) : 31u;
+                atomicOr(&bm[w], (z == 31u ? FULL : ((2u << z) - 1u)) & ~((1u << a) - 1u));
+            }
+        };
         // Bottom-up probe, one unvisited destination per lane: its first
         // PROBE_EDGES sources in ascending order, up to the first one in the
         // frontier -- the least frontier source, the value the tile pull's min
-        // would give it.  Destinations it leaves unvisited go to the tile pull
-        // (the next launch), which reads all their in-edges.
+        // would give it.  A destination whose sources it read to the end
+        // without a hit has no parent this iteration (the frontier is fixed
+        // during a pull); one with sources left marks the tiles holding them in
+        // tile_need, the only tiles the tile pull (the next launch) walks.
         const uint32_t nthr = gridDim.x * blockDim.x;
         for (uint32_t base = gw * 32u; base < g.Vne; base += nthr) {
             const uint32_t k = base + (uint32_t)lane; /* base is a multiple of 32: one vis_c word */
@@ -956,6 +966,7 @@ __global__ void __launch_bounds__(PULL_THREADS, 1)
             const bool todo = k < g.Vne && !((vw >> lane) & 1u);
             bool hit = false;
             uint32_t od = 0u;
+            uint32_t ta = 1u, tb = 0u; /* tiles of a destination left unvisited (none: ta > tb) */
             if (todo) {
                 const uint32_t d = g.dst_ident ? k : g.dst_id[k];
                 const unsigned long long lo = g.dst_off[k], hi = g.dst_off[k + 1u];
@@ -971,6 +982,13 @@ __global__ void __launch_bounds__(PULL_THREADS, 1)
                 }
                 edges += e - lo;
                 hit = par != NONE32;
+                if (!hit) {
+                    ta = (uint32_t)(lo / TILE_E);
+                    tb = (uint32_t)((hi - 1u) / TILE_E);
+                    // sources past the window remain: the tile pull reads the tiles holding them
+                    if (lim < hi)
+                        mark_tiles(s.tile_need, (uint32_t)(lim / TILE_E), tb);
+                }
                 if (hit) {
                     s.prop32[d] = par; /* the destination's only writer in this launch */
                     od = g.outdeg[d];
@@ -978,6 +996,26 @@ __global__ void __launch_bounds__(PULL_THREADS, 1)
                     ++act;
                     if (!g.dst_ident)
                         atomicOr(&nxt[d >> 5], 1u << (d & 31u));
+                }
+            }
+            // An unvisited destination keeps its tiles open (the bitmap is rebuilt
+            // by every probe).  The lanes' destinations are consecutive, so most
+            // of their tiles share a word: one atomic per distinct word.
+            {
+                const bool one = ta <= tb && (ta >> 5) == (tb >> 5);
+                if (ta <= tb && !one)
+                    mark_tiles(s.tile_open, ta, tb);
+                const uint32_t bits = one ? ((tb & 31u) == 31u ? FULL : ((2u << (tb & 31u)) - 1u)) & ~((1u << (ta & 31u)) - 1u)
+                                          : 0u;
+                uint32_t pending = __ballot_sync(FULL, one);
+                while (pending) {
+                    const int leader = __ffs(pending) - 1;
+                    const uint32_t w = __shfl_sync(FULL, ta >> 5, leader);
+                    const bool mine = one && (ta >> 5) == w;
+                    const uint32_t all = __reduce_or_sync(FULL, mine ? bits : 0u);
+                    if (lane == leader)
+                        atomicOr(&s.tile_open[w], all);
+                    pending &= ~__ballot_sync(FULL, mine);
                 }
             }
             dsts += (uint64_t)__popc(__ballot_sync(FULL, todo));
@@ -1661,6 +1699,13 @@ __global__ void advance_kernel(DevGraph g, DevState s, uint32_t app)
     const uint64_t nwords = (g.V + 31) / 32;
     for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < nwords; i += (uint64_t)gridDim.x * blockDim.x)
         fb[i] = 0u;
+    if (s.tile_need && c->mode != MODE_WEDGE) { /* a dense BFS pull next: its probe marks both afresh */
+        const uint64_t twords = (uint64_t)g.T / 32 + 2;
+        for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < twords; i += (uint64_t)gridDim.x * blockDim.x) {
+            s.tile_need[i] = 0u;
+            s.tile_open[i] = 0u;
+        }
+    }
 }
 
 // execution_initialize_{bfs,cc,sssp} bulk part; topen = BFS pull tiles
@@ -2321,6 +2366,10 @@ static int ensure_state(wedge_graph* h, int app, int precision)
         }
         if (app == WEDGE_APP_BFS || app == WEDGE_APP_CC) {
             if ((rc = dalloc(h, &s.tile_open, (uint64_t)g.T / 32 + 2, true)))
+                return rc;
+        }
+        if (app == WEDGE_APP_BFS) {
+            if ((rc = dalloc(h, &s.tile_need, (uint64_t)g.T / 32 + 2, true)))
                 return rc;
         }
     }

@@ -143,7 +143,8 @@ struct DevState {
     uint32_t* front0;              // V-bit frontier bitmaps (active / snapshot)
     uint32_t* front1;
     uint32_t* vis_c;               // Vne-bit: destination finished (BFS visited; CC label 0, the least label)
-    uint32_t* tile_open;           // T-bit: tile still has an unvisited destination (BFS)
+    uint32_t* tile_open;           // T-bit: tile still has an unfinished destination (BFS, CC)
+    uint32_t* tile_need;           // T-bit: BFS tiles with in-edges the probe left to the tile pull
     uint32_t* chunk_bits;          // Wedge frontier: one bit per chunk
     uint32_t* summary;             // one bit per region of REGION_WORDS chunk words (any chunk marked)
     unsigned long long* tile_list; // (tile << 32 | chunk mask) of the next Wedge pull
