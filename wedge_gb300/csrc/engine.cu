@@ -692,9 +692,9 @@ __device__ __forceinline__ bool next_tile(const DevGraph& g, const DevState& s, 
                                           TileIter& it, int lane, uint32_t& t, uint32_t& cmask)
 {
     constexpr uint32_t MASK = (EPL >= 32) ? FULL : ((1u << EPL) - 1u);
-    // BFS dense pulls take the open tiles dynamically; CC's keep the static
-    // stride (their tiles close for the Wedge lists, compact_kernel)
-    if (APP == WEDGE_APP_BFS && mode != MODE_WEDGE && s.tile_open) {
+    // dense BFS/CC pulls take the tiles their probe left work in dynamically;
+    // CC's source-filtered pulls keep the static stride
+    if (mode == MODE_DENSE && s.tile_need) {
         // dynamic schedule over the open-tile bitmap, OPEN_UNIT tiles per grab
         // (tiles close as the pulls find all their destinations finished)
         while (!it.obits) {
@@ -705,8 +705,7 @@ __device__ __forceinline__ bool next_tile(const DevGraph& g, const DevState& s, 
             if (u >= it.uend)
                 return false;
             constexpr uint32_t PER_WORD = 32 / OPEN_UNIT;
-            const uint32_t* bm = s.tile_need ? s.tile_need : s.tile_open; /* BFS: the tiles its probe left work in */
-            it.obits = (bm[u / PER_WORD] >> ((u % PER_WORD) * OPEN_UNIT)) & ((1u << OPEN_UNIT) - 1u);
+            it.obits = (s.tile_need[u / PER_WORD] >> ((u % PER_WORD) * OPEN_UNIT)) & ((1u << OPEN_UNIT) - 1u);
             it.obase = u * OPEN_UNIT;
         }
         t = it.obase + (uint32_t)(__ffs(it.obits) - 1);
@@ -749,7 +748,7 @@ enum : uint32_t { ERR_HUB_TIMEOUT = 2u };
 // pull phases: 0 = all tiles; CC/SSSP dense pulls run as two launches,
 // 1 = tiles [0, hub_tile) (the hub destinations), 2 = tiles [hub_tile, T),
 // so the second launch caches hub values that no tile of it can change;
-// BFS pulls run as 3 = the per-destination probe, then 0
+// BFS pulls run as 3 = the per-destination probe, then 0; CC pulls as 3, 1, 2
 enum : uint32_t { PHASE_ALL = 0, PHASE_HUBS = 1, PHASE_REST = 2, PHASE_PROBE = 3 };
 
 __host__ __device__ constexpr bool two_phase_app(int app)
@@ -757,13 +756,16 @@ __host__ __device__ constexpr bool two_phase_app(int app)
     return app == WEDGE_APP_CC || app == WEDGE_APP_SSSP;
 }
 
-// launches of one pull (each fills its own NCNT * grid block counters)
+// launches of one pull (each fills its own NCNT * grid block counters):
+// PageRank 1; BFS probe + tiles; CC probe + hub tiles + other tiles; SSSP hub
+// tiles + other tiles
+constexpr uint32_t MAX_PULL_LAUNCHES = 3;
 __host__ __device__ constexpr uint32_t pull_launches_of(int app)
 {
-    return app == WEDGE_APP_PR ? 1u : 2u;
+    return app == WEDGE_APP_PR ? 1u : app == WEDGE_APP_CC ? 3u : 2u;
 }
 
-// BFS probe: in-edges of an unvisited destination read before the tile pull
+// BFS/CC probe: in-edges of an unfinished destination read before the tile pull
 constexpr uint32_t PROBE_EDGES = 16;
 
 // Edge pull over all tiles (dense) or over the tiles of the Wedge frontier.
@@ -791,8 +793,10 @@ __global__ void __launch_bounds__(PULL_THREADS, 1)
     if (c->done)
         return;
     const uint32_t mode = c->mode;
-    if ((phase == PHASE_REST || phase == PHASE_PROBE) && mode == MODE_WEDGE) {
-        // a Wedge pull runs whole in one launch: this one only reports zeros
+    if (((phase == PHASE_REST || phase == PHASE_PROBE) && mode == MODE_WEDGE) ||
+        (phase == PHASE_PROBE && (mode != MODE_DENSE || (APP == WEDGE_APP_CC && g.sym != 0u && c->iter == 0u)))) {
+        // a Wedge pull runs whole in one launch; a probe runs before dense pulls
+        // only (not the first CC pull over engine ids): this one only reports zeros
         if (threadIdx.x < NCNT)
             block_cnt[NCNT * blockIdx.x + threadIdx.x] = 0ull;
         return;
@@ -844,7 +848,7 @@ __global__ void __launch_bounds__(PULL_THREADS, 1)
     // iteration); hub sources come from the cache, which the hub launch updated
     const bool ident0 = APP == WEDGE_APP_CC && g.sym != 0u && c->iter == 0u;
     const bool first_by_dst = ident0 && mode == MODE_DENSE && phase != PHASE_ALL;
-    const bool by_dst = (APP == WEDGE_APP_CC && first_by_dst) || (APP == WEDGE_APP_BFS && phase == PHASE_PROBE);
+    const bool by_dst = (APP == WEDGE_APP_CC && first_by_dst) || phase == PHASE_PROBE;
     use_hub = use_hub && !by_dst;
     if (APP == WEDGE_APP_BFS)
         use_hub = use_hub && (mode != MODE_WEDGE || c->tiles >= T / 16u);
@@ -867,6 +871,35 @@ __global__ void __launch_bounds__(PULL_THREADS, 1)
     }
     uint32_t hub_lim = 0; /* elements of the cache this warp reads: 0 until the copy completed */
 
+    // bitmap marks of tiles [ta, tb] (one lane)
+    auto mark_tiles = [](uint32_t* bm, uint32_t ta, uint32_t tb) {
+        for (uint32_t w = ta >> 5; w <= (tb >> 5); ++w) {
+            const uint32_t a = (w == (ta >> 5)) ? (ta & 31u) : 0u;
+            const uint32_t z = (w == (tb >> 5)) ? (tb & 31u) : 31u;
+            atomicOr(&bm[w], (z == 31u ? FULL : ((2u << z) - 1u)) & ~((1u << a) - 1u));
+        }
+    };
+    // Open-tile marks of the warp's destinations left unfinished (tiles [ta, tb],
+    // none where ta > tb; the bitmap is rebuilt by every dense pull).  The lanes'
+    // destinations are consecutive, so most of their tiles share a word: one
+    // atomic per distinct word.  Called by all lanes.
+    auto mark_open = [&](uint32_t ta, uint32_t tb) {
+        const bool one = ta <= tb && (ta >> 5) == (tb >> 5);
+        if (ta <= tb && !one)
+            mark_tiles(s.tile_open, ta, tb);
+        const uint32_t bits = one ? ((tb & 31u) == 31u ? FULL : ((2u << (tb & 31u)) - 1u)) & ~((1u << (ta & 31u)) - 1u) : 0u;
+        uint32_t pending = __ballot_sync(FULL, one);
+        while (pending) {
+            const int leader = __ffs(pending) - 1;
+            const uint32_t w = __shfl_sync(FULL, ta >> 5, leader);
+            const bool mine = one && (ta >> 5) == w;
+            const uint32_t all = __reduce_or_sync(FULL, mine ? bits : 0u);
+            if (lane == leader)
+                atomicOr(&s.tile_open[w], all);
+            pending &= ~__ballot_sync(FULL, mine);
+        }
+    };
+
     if (APP == WEDGE_APP_CC && first_by_dst) {
         // The first CC pull over engine-id labels, one destination per lane.  A
         // source outside the hub range [0, hub_n) still holds its own id, and a
@@ -885,6 +918,7 @@ __global__ void __launch_bounds__(PULL_THREADS, 1)
             const uint32_t k = base + (uint32_t)lane;
             bool chg = false, zero = false;
             uint32_t d = 0u, od = 0u;
+            uint32_t ta = 1u, tb = 0u;
             if (k < ke) {
                 d = g.dst_ident ? k : g.dst_id[k];
                 const unsigned long long lo = g.dst_off[k], hi = g.dst_off[k + 1u];
@@ -904,6 +938,10 @@ __global__ void __launch_bounds__(PULL_THREADS, 1)
                 edges += e - lo;
                 chg = m < d;
                 zero = chg && m == 0u;
+                if (m != 0u) {
+                    ta = (uint32_t)(lo / TILE_E);
+                    tb = (uint32_t)((hi - 1u) / TILE_E);
+                }
                 if (chg) {
                     s.prop32[d] = m; /* the destination's only writer */
                     od = g.outdeg[d];
@@ -911,6 +949,7 @@ __global__ void __launch_bounds__(PULL_THREADS, 1)
                     ++act;
                 }
             }
+            mark_open(ta, tb);
             dsts += (uint64_t)__popc(__ballot_sync(FULL, k < ke));
 #pragma unroll
             for (uint32_t b = 0; b < 3u; ++b) {
@@ -945,13 +984,6 @@ __global__ void __launch_bounds__(PULL_THREADS, 1)
         }
     }
     if (APP == WEDGE_APP_BFS && phase == PHASE_PROBE) {
-        auto mark_tiles = [](uint32_t* bm, uint32_t ta, uint32_t tb) {
-            for (uint32_t w = ta >> 5; w <= (tb >> 5); ++w) {
-                const uint32_t a = (w == (ta >> 5)) ? (ta & 31u) : 0u;
-                const uint32_t z = (w == (tb >> 5)) ? (tb & 31u) : 31u;
-                atomicOr(&bm[w], (z == 31u ? FULL : ((2u << z) - 1u)) & ~((1u << a) - 1u));
-            }
-        };
         // Bottom-up probe, one unvisited destination per lane: its first
         // PROBE_EDGES sources in ascending order, up to the first one in the
         // frontier -- the least frontier source, the value the tile pull's min
@@ -998,26 +1030,7 @@ __global__ void __launch_bounds__(PULL_THREADS, 1)
                         atomicOr(&nxt[d >> 5], 1u << (d & 31u));
                 }
             }
-            // An unvisited destination keeps its tiles open (the bitmap is rebuilt
-            // by every probe).  The lanes' destinations are consecutive, so most
-            // of their tiles share a word: one atomic per distinct word.
-            {
-                const bool one = ta <= tb && (ta >> 5) == (tb >> 5);
-                if (ta <= tb && !one)
-                    mark_tiles(s.tile_open, ta, tb);
-                const uint32_t bits = one ? ((tb & 31u) == 31u ? FULL : ((2u << (tb & 31u)) - 1u)) & ~((1u << (ta & 31u)) - 1u)
-                                          : 0u;
-                uint32_t pending = __ballot_sync(FULL, one);
-                while (pending) {
-                    const int leader = __ffs(pending) - 1;
-                    const uint32_t w = __shfl_sync(FULL, ta >> 5, leader);
-                    const bool mine = one && (ta >> 5) == w;
-                    const uint32_t all = __reduce_or_sync(FULL, mine ? bits : 0u);
-                    if (lane == leader)
-                        atomicOr(&s.tile_open[w], all);
-                    pending &= ~__ballot_sync(FULL, mine);
-                }
-            }
+            mark_open(ta, tb);
             dsts += (uint64_t)__popc(__ballot_sync(FULL, todo));
 #pragma unroll
             for (uint32_t b = 0; b < 3u; ++b) {
@@ -1030,6 +1043,71 @@ __global__ void __launch_bounds__(PULL_THREADS, 1)
                 atomicOr(&s.vis_c[base >> 5], hits);
                 if (g.dst_ident)
                     atomicOr(&nxt[base >> 5], hits); /* d = k */
+            }
+        }
+    }
+    if (APP == WEDGE_APP_CC && phase == PHASE_PROBE && !ident0) {
+        // CC probe (dense pulls after the first), one unfinished destination
+        // (label not 0) per lane: the labels of its first PROBE_EDGES sources,
+        // hubs first, up to the first label 0, the least label there is.  Where
+        // that found 0 or read every source, the minimum is the whole pull's for
+        // the labels read and is applied here; a longer destination without a 0
+        // marks its tiles for the tile pull (the next two launches), which walks
+        // only those.
+        const uint32_t nthr = gridDim.x * blockDim.x;
+        for (uint32_t base = gw * 32u; base < g.Vne; base += nthr) {
+            const uint32_t k = base + (uint32_t)lane; /* base is a multiple of 32: one vis_c word */
+            const uint32_t vw = s.vis_c[base >> 5];
+            const bool todo = k < g.Vne && !((vw >> lane) & 1u);
+            bool chg = false, zero = false;
+            uint32_t d = 0u, od = 0u;
+            uint32_t ta = 1u, tb = 0u;
+            if (todo) {
+                d = g.dst_ident ? k : g.dst_id[k];
+                const unsigned long long lo = g.dst_off[k], hi = g.dst_off[k + 1u];
+                const unsigned long long lim = hi - lo > PROBE_EDGES ? lo + PROBE_EDGES : hi;
+                const uint32_t cv = s.prop32[d];
+                uint32_t m = cv;
+                unsigned long long e = lo;
+                while (e < lim) {
+                    const uint32_t l = s.prop32[g.src[e++]];
+                    m = l < m ? l : m;
+                    if (m == 0u)
+                        break;
+                }
+                edges += e - lo;
+                const bool whole = m == 0u || e == hi;
+                if (whole && m < cv) {
+                    s.prop32[d] = m; /* the destination's only writer in this launch */
+                    chg = true;
+                    zero = m == 0u;
+                    od = g.outdeg[d];
+                    mass += od;
+                    ++act;
+                    if (!g.dst_ident)
+                        atomicOr(&nxt[d >> 5], 1u << (d & 31u));
+                }
+                if (!whole)
+                    mark_tiles(s.tile_need, (uint32_t)(lo / TILE_E), (uint32_t)((hi - 1u) / TILE_E));
+                if (!zero) {
+                    ta = (uint32_t)(lo / TILE_E);
+                    tb = (uint32_t)((hi - 1u) / TILE_E);
+                }
+            }
+            mark_open(ta, tb);
+            dsts += (uint64_t)__popc(__ballot_sync(FULL, todo));
+#pragma unroll
+            for (uint32_t b = 0; b < 3u; ++b) {
+                const uint32_t nb = __popc(__ballot_sync(FULL, chg && degree_bucket(od) == b));
+                if (lane == 0 && nb)
+                    atomicAdd(&sh_deg[b], nb);
+            }
+            const uint32_t chgs = __ballot_sync(FULL, chg), zeros = __ballot_sync(FULL, zero);
+            if (lane == 0) {
+                if (zeros)
+                    atomicOr(&s.vis_c[base >> 5], zeros); /* label 0 is final */
+                if (chgs && g.dst_ident)
+                    atomicOr(&nxt[base >> 5], chgs); /* d = k */
             }
         }
     }
@@ -1180,11 +1258,11 @@ __global__ void __launch_bounds__(PULL_THREADS, 1)
                         atomicOr(&s.vis_c[k >> 5], 1u << (k & 31u)); /* label 0 is final */
                     const uint32_t b = 1u << (vtx & 31u);
                     if (kind == EMIT_COMPLETE) {
-                        // sole writer of vtx in this pull: cv is current and its
-                        // changed bit (cleared before the pull) is still clear
+                        // sole writer of vtx in this launch: cv is current; the
+                        // probe may have set its changed bit already
                         s.prop32[vtx] = val;
-                        atomicOr(&nxt[vtx >> 5], b);
-                        count_act(g.outdeg[vtx]);
+                        if (!(atomicOr(&nxt[vtx >> 5], b) & b))
+                            count_act(g.outdeg[vtx]);
                     } else if (val < atomicMin(&s.prop32[vtx], val)) {
                         if (!(atomicOr(&nxt[vtx >> 5], b) & b)) {
                             count_act(g.outdeg[vtx]);
@@ -1699,7 +1777,7 @@ __global__ void advance_kernel(DevGraph g, DevState s, uint32_t app)
     const uint64_t nwords = (g.V + 31) / 32;
     for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < nwords; i += (uint64_t)gridDim.x * blockDim.x)
         fb[i] = 0u;
-    if (s.tile_need && c->mode != MODE_WEDGE) { /* a dense BFS pull next: its probe marks both afresh */
+    if (s.tile_need && c->mode == MODE_DENSE) { /* a dense pull next: its probe (CC's first: its hub/rest launches) marks both afresh */
         const uint64_t twords = (uint64_t)g.T / 32 + 2;
         for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < twords; i += (uint64_t)gridDim.x * blockDim.x) {
             s.tile_need[i] = 0u;
@@ -1749,6 +1827,11 @@ __global__ void init_kernel(DevGraph g, DevState s, uint32_t app, uint32_t topen
             const uint64_t left = (uint64_t)topen - i * 32;
             s.tile_open[i] = left >= 32 ? FULL : ((1u << left) - 1u);
         }
+    }
+    if (s.tile_need) {
+        const uint64_t twords = (uint64_t)g.T / 32 + 2;
+        for (uint64_t i = tid; i < twords; i += stride)
+            s.tile_need[i] = 0u;
     }
 }
 
@@ -2320,14 +2403,15 @@ static int ensure_state(wedge_graph* h, int app, int precision)
     int rc;
     Ctrl* ctrl;
     double* bp;
-    // [grid] block sums | [2*NCNT*grid] block counters (two launches) | [aux grid] PageRank-sum partials
-    if ((rc = dalloc(h, &ctrl, 1, true)) || (rc = dalloc(h, &bp, grid * (1 + 2 * NCNT) + (uint64_t)h->num_sms * 8 + 8, true)) ||
+    // [grid] block sums | [MAX_PULL_LAUNCHES*NCNT*grid] block counters | [aux grid] PageRank-sum partials
+    if ((rc = dalloc(h, &ctrl, 1, true)) ||
+        (rc = dalloc(h, &bp, grid * (1 + MAX_PULL_LAUNCHES * NCNT) + (uint64_t)h->num_sms * 8 + 8, true)) ||
         (rc = dalloc(h, &s.log, LOG_CAP, true)))
         return rc;
     WEDGE_CHECK(cudaMemset(ctrl, 0, sizeof(Ctrl)));
     s.ctrl = ctrl;
     s.block_part = bp; /* [grid] doubles, then the counters */
-    WEDGE_CHECK(cudaMemset(bp, 0, sizeof(double) * (grid * (1 + 2 * NCNT))));
+    WEDGE_CHECK(cudaMemset(bp, 0, sizeof(double) * (grid * (1 + MAX_PULL_LAUNCHES * NCNT))));
     s.app = (uint32_t)app;
     if (app == WEDGE_APP_PR) {
         if ((rc = dalloc(h, &s.acc, V, true)) || (rc = dalloc(h, &s.inv_od, V, true)))
@@ -2368,7 +2452,7 @@ static int ensure_state(wedge_graph* h, int app, int precision)
             if ((rc = dalloc(h, &s.tile_open, (uint64_t)g.T / 32 + 2, true)))
                 return rc;
         }
-        if (app == WEDGE_APP_BFS) {
+        if (app == WEDGE_APP_BFS || app == WEDGE_APP_CC) {
             if ((rc = dalloc(h, &s.tile_need, (uint64_t)g.T / 32 + 2, true)))
                 return rc;
         }
@@ -2386,7 +2470,7 @@ static unsigned long long* counters(wedge_graph* h) { return (unsigned long long
 static uint32_t pull_slots(wedge_graph* h, int app) { return h->pull_grid * pull_launches_of(app); }
 
 // PageRank-sum partials after the counters
-static double* pr_sums(wedge_graph* h) { return (double*)(counters(h) + 2ull * NCNT * h->pull_grid); }
+static double* pr_sums(wedge_graph* h) { return (double*)(counters(h) + (uint64_t)MAX_PULL_LAUNCHES * NCNT * h->pull_grid); }
 
 template <int APP>
 static void launch_pull_app(wedge_graph* h)
@@ -2394,8 +2478,13 @@ static void launch_pull_app(wedge_graph* h)
     constexpr int EPL = PullEpl<APP>::value;
     const uint32_t grid = h->pull_grid;
     if (two_phase_app(APP)) {
-        pull_kernel<APP, EPL><<<grid, PULL_THREADS, h->hub_bytes, h->stream>>>(h->g, h->s, counters(h), PHASE_HUBS);
-        pull_kernel<APP, EPL><<<grid, PULL_THREADS, h->hub_bytes, h->stream>>>(h->g, h->s, counters(h) + NCNT * grid,
+        unsigned long long* cnt = counters(h);
+        if (APP == WEDGE_APP_CC) {
+            pull_kernel<APP, EPL><<<grid, PULL_THREADS, h->hub_bytes, h->stream>>>(h->g, h->s, cnt, PHASE_PROBE);
+            cnt += NCNT * grid;
+        }
+        pull_kernel<APP, EPL><<<grid, PULL_THREADS, h->hub_bytes, h->stream>>>(h->g, h->s, cnt, PHASE_HUBS);
+        pull_kernel<APP, EPL><<<grid, PULL_THREADS, h->hub_bytes, h->stream>>>(h->g, h->s, cnt + NCNT * grid,
                                                                                PHASE_REST);
     } else if (APP == WEDGE_APP_BFS) {
         pull_kernel<APP, EPL><<<grid, PULL_THREADS, h->hub_bytes, h->stream>>>(h->g, h->s, counters(h), PHASE_PROBE);
