@@ -374,6 +374,29 @@ def test_cc_label_space_symmetry_check(W, O):
             assert np.array_equal(got, ref)
 
 
+def test_read_results_into_page_locked_memory(W, O):
+    """page-locked caller buffers receive the export directly from the device:
+    the same words as a pageable buffer, for every application and for CC
+    labels read between phase-driven pulls (converted at read time)"""
+    torch = pytest.importorskip("torch")
+    V, s, d = graph_edges(O, "rmat", dict(scale=12, edge_factor=8, seed=9), True)
+    w = O.weights(s, d)
+    pinned = torch.empty(V, dtype=torch.int64, pin_memory=True).numpy().view(np.uint64)
+    with W.Graph.from_edges(V, s, d, w, W.WEIGHTS_U64) as g:
+        for app in (W.APP_BFS, W.APP_CC, W.APP_SSSP, W.APP_PR):
+            g.run(app, W.Params(root=3, num_iterations=5))
+            a = g.read_results()
+            pinned[:] = 0
+            g.read_results(pinned)
+            assert np.array_equal(a, pinned), app
+        g.run_phase(W.APP_CC, 0, W.Params())
+        g.run_phase(W.APP_CC, 1, W.Params())
+        a = g.read_results()
+        pinned[:] = 0
+        g.read_results(pinned)
+        assert np.array_equal(a, pinned)
+
+
 def test_iteration_cap_reports_not_converged(W, O):
     V, s, d = graph_edges(O, "grid", dict(side=32, frac=0.0, seed=3))
     with W.Graph.from_edges(V, s, d) as g:

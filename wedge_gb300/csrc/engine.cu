@@ -3010,6 +3010,18 @@ int wedge_cuda_read_results(wedge_graph_t* g, void* host_props, uint64_t bytes)
     int rc = result_state(g, &rs);
     if (rc)
         return rc;
+    // page-locked caller memory is mapped into the device's address space: the
+    // export writes the words there directly, with no device copy in between
+    cudaPointerAttributes pa;
+    if (cudaPointerGetAttributes(&pa, host_props) == cudaSuccess && pa.type == cudaMemoryTypeHost && pa.devicePointer &&
+        ((uintptr_t)pa.devicePointer & 7u) == 0u) {
+        export_kernel<<<aux_grid(g, g->g.V), AUX_THREADS, 0, g->stream>>>(g->g, rs, (uint32_t)g->last_app,
+                                                                         (unsigned long long*)pa.devicePointer);
+        WEDGE_CHECK(cudaGetLastError());
+        WEDGE_CHECK(cudaStreamSynchronize(g->stream));
+        return WEDGE_OK;
+    }
+    cudaGetLastError(); /* an unregistered pointer is not an error */
     unsigned long long* tmp = nullptr;
     WEDGE_CHECK(cudaMallocAsync((void**)&tmp, 8ull * (g->g.V ? g->g.V : 1), g->stream));
     export_kernel<<<aux_grid(g, g->g.V), AUX_THREADS, 0, g->stream>>>(g->g, rs, (uint32_t)g->last_app, tmp);
