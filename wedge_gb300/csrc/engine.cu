@@ -679,37 +679,27 @@ __device__ __forceinline__ void load_sources(const DevGraph& g, uint64_t base, u
 // tiles, 32 per dynamically grabbed word of the open-tile bitmap), or the tiles
 // of the Wedge frontier from the list compact_kernel built.  Warp-uniform.
 struct TileIter {
-    uint32_t i, step;      // dense
-    uint32_t obits, obase; // BFS/CC dense: open tiles left in the current unit, its first tile
-    uint32_t ubeg, uend;   // the units [ubeg, uend) of OPEN_UNIT tiles this launch covers
-    unsigned int* grab;    // next unit a warp takes, counted from ubeg
+    uint32_t i, step;      // dense (static stride), the probe's tile list, or the Wedge list
+    uint32_t tbeg, tend;   // the tiles [tbeg, tend) of this launch (CC's hub / other split)
 };
-
-constexpr uint32_t OPEN_UNIT = 8; /* tiles a warp takes per grab of the open-tile bitmap */
 
 template <int APP, int EPL>
 __device__ __forceinline__ bool next_tile(const DevGraph& g, const DevState& s, uint32_t mode, uint32_t t_end,
                                           TileIter& it, int lane, uint32_t& t, uint32_t& cmask)
 {
     constexpr uint32_t MASK = (EPL >= 32) ? FULL : ((1u << EPL) - 1u);
-    // dense BFS/CC pulls take the tiles their probe left work in dynamically;
-    // CC's source-filtered pulls keep the static stride
+    // dense BFS/CC pulls walk the list of tiles their probe left work in
+    // (tile_list, each tile once); a CC launch takes the ones of its range
     if (mode == MODE_DENSE && s.tile_need) {
-        // dynamic schedule over the open-tile bitmap, OPEN_UNIT tiles per grab
-        // (tiles close as the pulls find all their destinations finished)
-        while (!it.obits) {
-            uint32_t u = 0;
-            if (lane == 0)
-                u = atomicAdd(it.grab, 1u);
-            u = __shfl_sync(FULL, u, 0) + it.ubeg;
-            if (u >= it.uend)
+        const uint32_t n = s.ctrl->need_n;
+        for (;;) {
+            if (it.i >= n)
                 return false;
-            constexpr uint32_t PER_WORD = 32 / OPEN_UNIT;
-            it.obits = (s.tile_need[u / PER_WORD] >> ((u % PER_WORD) * OPEN_UNIT)) & ((1u << OPEN_UNIT) - 1u);
-            it.obase = u * OPEN_UNIT;
+            t = (uint32_t)(s.tile_list[it.i] >> 32);
+            it.i += it.step;
+            if (t >= it.tbeg && t < it.tend)
+                break;
         }
-        t = it.obase + (uint32_t)(__ffs(it.obits) - 1);
-        it.obits &= it.obits - 1u;
         cmask = MASK;
         return true;
     }
@@ -879,6 +869,21 @@ __global__ void __launch_bounds__(PULL_THREADS, 1)
             atomicOr(&bm[w], (z == 31u ? FULL : ((2u << z) - 1u)) & ~((1u << a) - 1u));
         }
     };
+    // tiles [ta, tb] into the tile pull's work: the lane that sets a tile's
+    // tile_need bit appends the tile to tile_list, so each is listed once
+    auto need_tiles = [&](uint32_t ta, uint32_t tb) {
+        for (uint32_t w = ta >> 5; w <= (tb >> 5); ++w) {
+            const uint32_t a = (w == (ta >> 5)) ? (ta & 31u) : 0u;
+            const uint32_t z = (w == (tb >> 5)) ? (tb & 31u) : 31u;
+            const uint32_t m = (z == 31u ? FULL : ((2u << z) - 1u)) & ~((1u << a) - 1u);
+            uint32_t fresh = m & ~atomicOr(&s.tile_need[w], m);
+            if (fresh) {
+                uint32_t pos = atomicAdd(&c->need_n, (uint32_t)__popc(fresh));
+                for (; fresh; fresh &= fresh - 1u)
+                    s.tile_list[pos++] = (unsigned long long)(w * 32u + (uint32_t)(__ffs(fresh) - 1)) << 32;
+            }
+        }
+    };
     // Open-tile marks of the warp's destinations left unfinished (tiles [ta, tb],
     // none where ta > tb; the bitmap is rebuilt by every dense pull).  The lanes'
     // destinations are consecutive, so most of their tiles share a word: one
@@ -1019,7 +1024,7 @@ __global__ void __launch_bounds__(PULL_THREADS, 1)
                     tb = (uint32_t)((hi - 1u) / TILE_E);
                     // sources past the window remain: the tile pull reads the tiles holding them
                     if (lim < hi)
-                        mark_tiles(s.tile_need, (uint32_t)(lim / TILE_E), tb);
+                        need_tiles((uint32_t)(lim / TILE_E), tb);
                 }
                 if (hit) {
                     s.prop32[d] = par; /* the destination's only writer in this launch */
@@ -1088,7 +1093,7 @@ __global__ void __launch_bounds__(PULL_THREADS, 1)
                         atomicOr(&nxt[d >> 5], 1u << (d & 31u));
                 }
                 if (!whole)
-                    mark_tiles(s.tile_need, (uint32_t)(lo / TILE_E), (uint32_t)((hi - 1u) / TILE_E));
+                    need_tiles((uint32_t)(lo / TILE_E), (uint32_t)((hi - 1u) / TILE_E));
                 if (!zero) {
                     ta = (uint32_t)(lo / TILE_E);
                     tb = (uint32_t)((hi - 1u) / TILE_E);
@@ -1112,16 +1117,10 @@ __global__ void __launch_bounds__(PULL_THREADS, 1)
         }
     }
     TileIter it;
-    it.i = t_begin + gw;
+    it.i = (mode == MODE_DENSE && s.tile_need) ? gw : t_begin + gw; /* the probe's list starts at 0 */
     it.step = nw;
-    it.obits = it.obase = 0u;
-    {
-        // open-tile units: CC's hub launch takes [0, ceil(split / OPEN_UNIT)), the rest after
-        const uint32_t usplit = (t_begin + OPEN_UNIT - 1u) / OPEN_UNIT;
-        it.ubeg = (phase == PHASE_REST) ? usplit : 0u;
-        it.uend = (phase == PHASE_HUBS) ? (t_end + OPEN_UNIT - 1u) / OPEN_UNIT : (T + OPEN_UNIT - 1u) / OPEN_UNIT;
-        it.grab = (phase == PHASE_REST) ? &c->region_next2 : &c->region_next;
-    }
+    it.tbeg = t_begin;
+    it.tend = t_end;
     TileIn nextin;
     uint32_t tn, cn;
     bool more = !by_dst && next_tile<APP, EPL>(g, s, mode, t_end, it, lane, tn, cn);
@@ -1525,8 +1524,7 @@ __global__ void decide_kernel(DevGraph g, DevState s, const unsigned long long* 
         c->last_mass = m;
         c->mass = m;
         c->parity ^= 1u;
-        c->region_next = 0u;
-        c->region_next2 = 0u;
+        c->need_n = 0u;
         c->tiles = 0u;
         c->items = 0u;
         c->alist_n = 0u;
@@ -1868,8 +1866,7 @@ __global__ void init_root_kernel(DevGraph g, DevState s, uint32_t app, uint64_t 
         c->threshold = thr;
         c->items = 0;
         c->alist_n = 0;
-        c->region_next = 0;
-        c->region_next2 = 0;
+        c->need_n = 0;
         c->tiles = 0;
         c->iter = 0;
         c->wedge_iters = 0;
@@ -1991,8 +1988,7 @@ __global__ void pr_init_kernel(DevGraph g, DevState s, uint32_t max_iter)
         c->done = 0;
         c->mode = MODE_DENSE;
         c->parity = 0;
-        c->region_next = 0;
-        c->region_next2 = 0;
+        c->need_n = 0;
         c->error = 0;
         c->pr_total = 0.0;
         c->pr_sum = 0.0;
@@ -2960,6 +2956,8 @@ int wedge_cuda_run_phase(wedge_graph_t* g, int app, int phase, const wedge_param
                 if (want == MODE_WEDGE)
                     return WEDGE_ERR_ARG; /* no Wedge frontier was built for this pull */
                 WEDGE_CHECK(cudaMemcpyAsync(&g->s.ctrl->mode, &want, sizeof(want), cudaMemcpyHostToDevice, g->stream));
+                if (g->s.tile_need) /* its probe lists the tiles whose need bit it sets first */
+                    WEDGE_CHECK(cudaMemsetAsync(g->s.tile_need, 0, ((uint64_t)dg.T / 32 + 2) * sizeof(uint32_t), g->stream));
             }
         } else if (phase == WEDGE_PHASE_PULL_WEDGE) {
             return WEDGE_ERR_UNSUPPORTED; /* PageRank has no Wedge pull (application.c:154) */

@@ -79,8 +79,7 @@ struct Ctrl {
     unsigned long long dsts_scanned;   // destinations in visited tiles
     unsigned long long activated;      // vertices activated by pulls
     unsigned int items;                // Wedge-build work items appended by the last pull
-    unsigned int region_next;          // next open-tile word a warp takes (BFS/CC dense, dynamic schedule)
-    unsigned int region_next2;         // the same for the second launch of a CC pull
+    unsigned int need_n;               // tiles the probe listed for the dense tile pull (tile_list)
     unsigned int tiles;                // length of the Wedge tile list
     unsigned int mode;                 // MODE_DENSE / MODE_WEDGE for the next pull
     unsigned int iter;                 // completed pulls
