@@ -1579,10 +1579,24 @@ __global__ void decide_kernel(DevGraph g, DevState s, const unsigned long long* 
 // of its region.  Fire-and-forget atomics behind plain-load checks: bits are
 // only set while the frontier is built, so a stale read can only cost a
 // redundant atomic, and no thread waits for an atomic's return.
+// chunks per pull tile of an application, as a shift (tile = 32 * EPL in-edges)
+__device__ __forceinline__ uint32_t chunk_tile_shift(uint32_t app)
+{
+    const uint32_t epl = app == WEDGE_APP_CC ? (uint32_t)WEDGE_EPL_CC : 8u;
+    return 31u - (uint32_t)__clz(epl);
+}
+
+// A chunk of the Wedge frontier.  Chunks of closed tiles (every destination
+// finished) are left out: compact_kernel would drop them from the tile list.
 __device__ __forceinline__ void mark_chunk(const DevState& s, uint32_t ch, bool valid)
 {
     if (!valid)
         return;
+    if (s.tile_open) {
+        const uint32_t t = ch >> chunk_tile_shift(s.app);
+        if (!((s.tile_open[t >> 5] >> (t & 31u)) & 1u))
+            return;
+    }
     const uint32_t word = ch >> 5, bit = 1u << (ch & 31u);
     if (!(s.chunk_bits[word] & bit)) {
         atomicOr(&s.chunk_bits[word], bit);
@@ -1661,8 +1675,14 @@ __global__ void expand_kernel(DevGraph g, DevState s)
                 len = 0;
             }
         }
-        for (unsigned long long j = 0; j < len; ++j)
-            mark_chunk(s, g.csri[start + j], true);
+        // a short list's chunk indices are loaded together, then marked
+        uint32_t ch[BIG_LIST];
+#pragma unroll
+        for (uint32_t j = 0; j < BIG_LIST; ++j)
+            ch[j] = (j < len) ? g.csri[start + j] : 0u;
+#pragma unroll
+        for (uint32_t j = 0; j < BIG_LIST; ++j)
+            mark_chunk(s, ch[j], j < len);
         uint32_t incl = np;
 #pragma unroll
         for (int d = 1; d < 32; d <<= 1) {

@@ -34,7 +34,7 @@ constexpr uint32_t TILES_PER_WORD = 32 / CHUNKS_PER_TILE;  // 8 tiles per 32-bit
 constexpr uint32_t REGION_WORDS = 32;                      // chunk-bitmap words per summary bit
 constexpr uint32_t TILES_PER_REGION = REGION_WORDS * TILES_PER_WORD;  // 256 tiles = 32768 in-edges
 constexpr uint32_t PIECE = 256;                            // CSRI entries per Wedge-build work item
-constexpr uint32_t BIG_LIST = 64;                          // longer CSRI lists are split into work items
+constexpr uint32_t BIG_LIST = 8;                           // longer CSRI lists go to warp-wide work items
 constexpr uint32_t NONE32 = 0xFFFFFFFFu;
 constexpr unsigned long long NONE64 = ~0ull;
 constexpr uint32_t FULL = 0xFFFFFFFFu;
