@@ -737,22 +737,28 @@ enum : uint32_t { ERR_HUB_TIMEOUT = 2u };
 
 // pull phases: 0 = all tiles; CC/SSSP dense pulls run as two launches,
 // 1 = tiles [0, hub_tile) (the hub destinations), 2 = tiles [hub_tile, T),
-// so the second launch caches hub values that no tile of it can change;
-// BFS pulls run as 3 = the per-destination probe, then 0; CC pulls as 3, 1, 2
-enum : uint32_t { PHASE_ALL = 0, PHASE_HUBS = 1, PHASE_REST = 2, PHASE_PROBE = 3 };
+// so the second launch caches hub values that no tile of it can change.
+// dst_kernel phases before a dense pull: A = the BFS or CC probe, or the hub
+// destinations of CC's first pull over engine ids; B = the other destinations
+// of that first pull (CC)
+enum : uint32_t { PHASE_ALL = 0, PHASE_HUBS = 1, PHASE_REST = 2, PHASE_DST_A = 3, PHASE_DST_B = 4 };
 
 __host__ __device__ constexpr bool two_phase_app(int app)
 {
     return app == WEDGE_APP_CC || app == WEDGE_APP_SSSP;
 }
 
-// launches of one pull (each fills its own NCNT * grid block counters):
-// PageRank 1; BFS probe + tiles; CC probe + hub tiles + other tiles; SSSP hub
-// tiles + other tiles
-constexpr uint32_t MAX_PULL_LAUNCHES = 3;
+// launches of one pull (each fills its own NCNT block counters per block):
+// PageRank: tiles; BFS: dst_kernel A + tiles; CC: dst_kernel A and B + hub
+// tiles + other tiles; SSSP: hub tiles + other tiles
 __host__ __device__ constexpr uint32_t pull_launches_of(int app)
 {
-    return app == WEDGE_APP_PR ? 1u : app == WEDGE_APP_CC ? 3u : 2u;
+    return app == WEDGE_APP_PR ? 1u : app == WEDGE_APP_CC ? 4u : 2u;
+}
+// dst_kernel launches of one pull
+__host__ __device__ constexpr uint32_t dst_launches_of(int app)
+{
+    return app == WEDGE_APP_BFS ? 1u : app == WEDGE_APP_CC ? 2u : 0u;
 }
 
 // BFS/CC probe: in-edges of an unfinished destination read before the tile pull
@@ -783,10 +789,8 @@ __global__ void __launch_bounds__(PULL_THREADS, 1)
     if (c->done)
         return;
     const uint32_t mode = c->mode;
-    if (((phase == PHASE_REST || phase == PHASE_PROBE) && mode == MODE_WEDGE) ||
-        (phase == PHASE_PROBE && (mode != MODE_DENSE || (APP == WEDGE_APP_CC && g.sym != 0u && c->iter == 0u)))) {
-        // a Wedge pull runs whole in one launch; a probe runs before dense pulls
-        // only (not the first CC pull over engine ids): this one only reports zeros
+    if (phase == PHASE_REST && mode == MODE_WEDGE) {
+        // a Wedge pull runs whole in the first launch: this one only reports zeros
         if (threadIdx.x < NCNT)
             block_cnt[NCNT * blockIdx.x + threadIdx.x] = 0ull;
         return;
@@ -831,15 +835,6 @@ __global__ void __launch_bounds__(PULL_THREADS, 1)
     const uint64_t hub_fit = hub_have & ~15ull;
     const uint32_t hub_bytes = (uint64_t)s.hub_bytes < hub_fit ? s.hub_bytes : (uint32_t)hub_fit; /* within smem and the array */
     bool use_hub = hub_bytes != 0u && ((uintptr_t)hub_src & 15u) == 0u && (smem_u32(hub_smem) & 15u) == 0u;
-    // CC on a symmetric graph propagates engine ids: before the first pull every
-    // label is its vertex's own id, so that pull takes the ids of the sources
-    // outside the hub cache instead of gathering their labels (where another warp
-    // lowered one already, the old value only delays that progress by an
-    // iteration); hub sources come from the cache, which the hub launch updated
-    const bool ident0 = APP == WEDGE_APP_CC && g.sym != 0u && c->iter == 0u;
-    const bool first_by_dst = ident0 && mode == MODE_DENSE && phase != PHASE_ALL;
-    const bool by_dst = (APP == WEDGE_APP_CC && first_by_dst) || phase == PHASE_PROBE;
-    use_hub = use_hub && !by_dst;
     if (APP == WEDGE_APP_BFS)
         use_hub = use_hub && (mode != MODE_WEDGE || c->tiles >= T / 16u);
     else if (two_phase_app(APP))
@@ -861,261 +856,6 @@ __global__ void __launch_bounds__(PULL_THREADS, 1)
     }
     uint32_t hub_lim = 0; /* elements of the cache this warp reads: 0 until the copy completed */
 
-    // bitmap marks of tiles [ta, tb] (one lane)
-    auto mark_tiles = [](uint32_t* bm, uint32_t ta, uint32_t tb) {
-        for (uint32_t w = ta >> 5; w <= (tb >> 5); ++w) {
-            const uint32_t a = (w == (ta >> 5)) ? (ta & 31u) : 0u;
-            const uint32_t z = (w == (tb >> 5)) ? (tb & 31u) : 31u;
-            atomicOr(&bm[w], (z == 31u ? FULL : ((2u << z) - 1u)) & ~((1u << a) - 1u));
-        }
-    };
-    // tiles [ta, tb] into the tile pull's work: the lane that sets a tile's
-    // tile_need bit appends the tile to tile_list, so each is listed once
-    auto need_tiles = [&](uint32_t ta, uint32_t tb) {
-        for (uint32_t w = ta >> 5; w <= (tb >> 5); ++w) {
-            const uint32_t a = (w == (ta >> 5)) ? (ta & 31u) : 0u;
-            const uint32_t z = (w == (tb >> 5)) ? (tb & 31u) : 31u;
-            const uint32_t m = (z == 31u ? FULL : ((2u << z) - 1u)) & ~((1u << a) - 1u);
-            uint32_t fresh = m & ~atomicOr(&s.tile_need[w], m);
-            if (fresh) {
-                uint32_t pos = atomicAdd(&c->need_n, (uint32_t)__popc(fresh));
-                for (; fresh; fresh &= fresh - 1u)
-                    s.tile_list[pos++] = (unsigned long long)(w * 32u + (uint32_t)(__ffs(fresh) - 1)) << 32;
-            }
-        }
-    };
-    // Open-tile marks of the warp's destinations left unfinished (tiles [ta, tb],
-    // none where ta > tb; the bitmap is rebuilt by every dense pull).  The lanes'
-    // destinations are consecutive, so most of their tiles share a word: one
-    // atomic per distinct word.  Called by all lanes.
-    auto mark_open = [&](uint32_t ta, uint32_t tb) {
-        const bool one = ta <= tb && (ta >> 5) == (tb >> 5);
-        if (ta <= tb && !one)
-            mark_tiles(s.tile_open, ta, tb);
-        const uint32_t bits = one ? ((tb & 31u) == 31u ? FULL : ((2u << (tb & 31u)) - 1u)) & ~((1u << (ta & 31u)) - 1u) : 0u;
-        uint32_t pending = __ballot_sync(FULL, one);
-        while (pending) {
-            const int leader = __ffs(pending) - 1;
-            const uint32_t w = __shfl_sync(FULL, ta >> 5, leader);
-            const bool mine = one && (ta >> 5) == w;
-            const uint32_t all = __reduce_or_sync(FULL, mine ? bits : 0u);
-            if (lane == leader)
-                atomicOr(&s.tile_open[w], all);
-            pending &= ~__ballot_sync(FULL, mine);
-        }
-    };
-
-    if (APP == WEDGE_APP_CC && first_by_dst) {
-        // The first CC pull over engine-id labels, one destination per lane.  A
-        // source outside the hub range [0, hub_n) still holds its own id, and a
-        // destination's sources ascend, so past its hub sources only the first
-        // one can lower the minimum; the hub sources' labels are final once the
-        // hub launch (the destinations with ids < hub_n) is over.  The hub launch
-        // itself sees every label at its id: the first source decides.  This is
-        // the tile pull's result for the same labels without reading the other
-        // in-edges (Jacobi for the hubs, where the tile pull lets a block's
-        // warps see each other's hub updates).
-        const bool hubs = phase == PHASE_HUBS;
-        const uint32_t kb = hubs ? 0u : s.hub_k, ke = hubs ? s.hub_k : g.Vne;
-        const uint32_t hn = s.hub_n;
-        const uint32_t nthr = gridDim.x * blockDim.x;
-        for (uint32_t base = kb + gw * 32u; base < ke; base += nthr) {
-            const uint32_t k = base + (uint32_t)lane;
-            bool chg = false, zero = false;
-            uint32_t d = 0u, od = 0u;
-            uint32_t ta = 1u, tb = 0u;
-            if (k < ke) {
-                d = g.dst_ident ? k : g.dst_id[k];
-                const unsigned long long lo = g.dst_off[k], hi = g.dst_off[k + 1u];
-                uint32_t m = d;
-                unsigned long long e = lo;
-                while (e < hi) {
-                    const uint32_t x = g.src[e++];
-                    if (hubs || x >= hn) {
-                        m = x < m ? x : m;
-                        break;
-                    }
-                    const uint32_t l = s.prop32[x];
-                    m = l < m ? l : m;
-                    if (m == 0u)
-                        break;
-                }
-                edges += e - lo;
-                chg = m < d;
-                zero = chg && m == 0u;
-                if (m != 0u) {
-                    ta = (uint32_t)(lo / TILE_E);
-                    tb = (uint32_t)((hi - 1u) / TILE_E);
-                }
-                if (chg) {
-                    s.prop32[d] = m; /* the destination's only writer */
-                    od = g.outdeg[d];
-                    mass += od;
-                    ++act;
-                }
-            }
-            mark_open(ta, tb);
-            dsts += (uint64_t)__popc(__ballot_sync(FULL, k < ke));
-#pragma unroll
-            for (uint32_t b = 0; b < 3u; ++b) {
-                const uint32_t nb = __popc(__ballot_sync(FULL, chg && degree_bucket(od) == b));
-                if (lane == 0 && nb)
-                    atomicAdd(&sh_deg[b], nb);
-            }
-            if (g.dst_ident) { /* d = k: the lanes' bits fall in two words at most */
-                const uint32_t w0 = base >> 5;
-                const bool in0 = (k >> 5) == w0;
-                const uint32_t bit = 1u << (k & 31u);
-                const uint32_t c0 = __reduce_or_sync(FULL, (chg && in0) ? bit : 0u);
-                const uint32_t c1 = __reduce_or_sync(FULL, (chg && !in0) ? bit : 0u);
-                const uint32_t z0 = __reduce_or_sync(FULL, (zero && in0) ? bit : 0u);
-                const uint32_t z1 = __reduce_or_sync(FULL, (zero && !in0) ? bit : 0u);
-                if (lane == 0) {
-                    if (c0)
-                        atomicOr(&nxt[w0], c0);
-                    if (c1)
-                        atomicOr(&nxt[w0 + 1u], c1);
-                    if (z0)
-                        atomicOr(&s.vis_c[w0], z0); /* label 0 is final */
-                    if (z1)
-                        atomicOr(&s.vis_c[w0 + 1u], z1);
-                }
-            } else {
-                if (chg)
-                    atomicOr(&nxt[d >> 5], 1u << (d & 31u));
-                if (zero)
-                    atomicOr(&s.vis_c[k >> 5], 1u << (k & 31u));
-            }
-        }
-    }
-    if (APP == WEDGE_APP_BFS && phase == PHASE_PROBE) {
-        // Bottom-up probe, one unvisited destination per lane: its first
-        // PROBE_EDGES sources in ascending order, up to the first one in the
-        // frontier -- the least frontier source, the value the tile pull's min
-        // would give it.  A destination whose sources it read to the end
-        // without a hit has no parent this iteration (the frontier is fixed
-        // during a pull); one with sources left marks the tiles holding them in
-        // tile_need, the only tiles the tile pull (the next launch) walks.
-        const uint32_t nthr = gridDim.x * blockDim.x;
-        for (uint32_t base = gw * 32u; base < g.Vne; base += nthr) {
-            const uint32_t k = base + (uint32_t)lane; /* base is a multiple of 32: one vis_c word */
-            const uint32_t vw = s.vis_c[base >> 5];
-            const bool todo = k < g.Vne && !((vw >> lane) & 1u);
-            bool hit = false;
-            uint32_t od = 0u;
-            uint32_t ta = 1u, tb = 0u; /* tiles of a destination left unvisited (none: ta > tb) */
-            if (todo) {
-                const uint32_t d = g.dst_ident ? k : g.dst_id[k];
-                const unsigned long long lo = g.dst_off[k], hi = g.dst_off[k + 1u];
-                const unsigned long long lim = hi - lo > PROBE_EDGES ? lo + PROBE_EDGES : hi;
-                unsigned long long e = lo;
-                uint32_t par = NONE32;
-                while (e < lim) {
-                    const uint32_t x = g.src[e++];
-                    if ((ld_ro_u32(cur + (x >> 5)) >> (x & 31u)) & 1u) {
-                        par = x;
-                        break;
-                    }
-                }
-                edges += e - lo;
-                hit = par != NONE32;
-                if (!hit) {
-                    ta = (uint32_t)(lo / TILE_E);
-                    tb = (uint32_t)((hi - 1u) / TILE_E);
-                    // sources past the window remain: the tile pull reads the tiles holding them
-                    if (lim < hi)
-                        need_tiles((uint32_t)(lim / TILE_E), tb);
-                }
-                if (hit) {
-                    s.prop32[d] = par; /* the destination's only writer in this launch */
-                    od = g.outdeg[d];
-                    mass += od;
-                    ++act;
-                    if (!g.dst_ident)
-                        atomicOr(&nxt[d >> 5], 1u << (d & 31u));
-                }
-            }
-            mark_open(ta, tb);
-            dsts += (uint64_t)__popc(__ballot_sync(FULL, todo));
-#pragma unroll
-            for (uint32_t b = 0; b < 3u; ++b) {
-                const uint32_t nb = __popc(__ballot_sync(FULL, hit && degree_bucket(od) == b));
-                if (lane == 0 && nb)
-                    atomicAdd(&sh_deg[b], nb);
-            }
-            const uint32_t hits = __ballot_sync(FULL, hit);
-            if (lane == 0 && hits) {
-                atomicOr(&s.vis_c[base >> 5], hits);
-                if (g.dst_ident)
-                    atomicOr(&nxt[base >> 5], hits); /* d = k */
-            }
-        }
-    }
-    if (APP == WEDGE_APP_CC && phase == PHASE_PROBE && !ident0) {
-        // CC probe (dense pulls after the first), one unfinished destination
-        // (label not 0) per lane: the labels of its first PROBE_EDGES sources,
-        // hubs first, up to the first label 0, the least label there is.  Where
-        // that found 0 or read every source, the minimum is the whole pull's for
-        // the labels read and is applied here; a longer destination without a 0
-        // marks its tiles for the tile pull (the next two launches), which walks
-        // only those.
-        const uint32_t nthr = gridDim.x * blockDim.x;
-        for (uint32_t base = gw * 32u; base < g.Vne; base += nthr) {
-            const uint32_t k = base + (uint32_t)lane; /* base is a multiple of 32: one vis_c word */
-            const uint32_t vw = s.vis_c[base >> 5];
-            const bool todo = k < g.Vne && !((vw >> lane) & 1u);
-            bool chg = false, zero = false;
-            uint32_t d = 0u, od = 0u;
-            uint32_t ta = 1u, tb = 0u;
-            if (todo) {
-                d = g.dst_ident ? k : g.dst_id[k];
-                const unsigned long long lo = g.dst_off[k], hi = g.dst_off[k + 1u];
-                const unsigned long long lim = hi - lo > PROBE_EDGES ? lo + PROBE_EDGES : hi;
-                const uint32_t cv = s.prop32[d];
-                uint32_t m = cv;
-                unsigned long long e = lo;
-                while (e < lim) {
-                    const uint32_t l = s.prop32[g.src[e++]];
-                    m = l < m ? l : m;
-                    if (m == 0u)
-                        break;
-                }
-                edges += e - lo;
-                const bool whole = m == 0u || e == hi;
-                if (whole && m < cv) {
-                    s.prop32[d] = m; /* the destination's only writer in this launch */
-                    chg = true;
-                    zero = m == 0u;
-                    od = g.outdeg[d];
-                    mass += od;
-                    ++act;
-                    if (!g.dst_ident)
-                        atomicOr(&nxt[d >> 5], 1u << (d & 31u));
-                }
-                if (!whole)
-                    need_tiles((uint32_t)(lo / TILE_E), (uint32_t)((hi - 1u) / TILE_E));
-                if (!zero) {
-                    ta = (uint32_t)(lo / TILE_E);
-                    tb = (uint32_t)((hi - 1u) / TILE_E);
-                }
-            }
-            mark_open(ta, tb);
-            dsts += (uint64_t)__popc(__ballot_sync(FULL, todo));
-#pragma unroll
-            for (uint32_t b = 0; b < 3u; ++b) {
-                const uint32_t nb = __popc(__ballot_sync(FULL, chg && degree_bucket(od) == b));
-                if (lane == 0 && nb)
-                    atomicAdd(&sh_deg[b], nb);
-            }
-            const uint32_t chgs = __ballot_sync(FULL, chg), zeros = __ballot_sync(FULL, zero);
-            if (lane == 0) {
-                if (zeros)
-                    atomicOr(&s.vis_c[base >> 5], zeros); /* label 0 is final */
-                if (chgs && g.dst_ident)
-                    atomicOr(&nxt[base >> 5], chgs); /* d = k */
-            }
-        }
-    }
     TileIter it;
     it.i = (mode == MODE_DENSE && s.tile_need) ? gw : t_begin + gw; /* the probe's list starts at 0 */
     it.step = nw;
@@ -1123,7 +863,7 @@ __global__ void __launch_bounds__(PULL_THREADS, 1)
     it.tend = t_end;
     TileIn nextin;
     uint32_t tn, cn;
-    bool more = !by_dst && next_tile<APP, EPL>(g, s, mode, t_end, it, lane, tn, cn);
+    bool more = next_tile<APP, EPL>(g, s, mode, t_end, it, lane, tn, cn);
     if (more)
         tile_prefetch<APP, EPL>(g, s, tn, cn, lane, nextin);
     while (more) {
@@ -1213,11 +953,7 @@ __global__ void __launch_bounds__(PULL_THREADS, 1)
             auto gather = [&](uint32_t x) -> uint32_t {
                 if (filtered && x != NONE32 && !((ld_ro_u32(cur + (x >> 5)) >> (x & 31u)) & 1u))
                     return NONE32; /* source unchanged by the previous pull */
-                if (x < hub_lim)
-                    return hub32[x];
-                if (ident0)
-                    return x; /* first pull over engine-id labels: the source still holds its own id */
-                return (x != NONE32) ? s.prop32[x] : NONE32;
+                return (x < hub_lim) ? hub32[x] : ((x != NONE32) ? s.prop32[x] : NONE32);
             };
             if (!in.anydone) {
 #pragma unroll
@@ -1387,6 +1123,322 @@ __global__ void __launch_bounds__(PULL_THREADS, 1)
         sh_cnt[wib][CNT_EDGES] = edges;
         sh_cnt[wib][CNT_TILES] = tiles;  // warp-uniform
         sh_cnt[wib][CNT_DSTS] = dsts;    // warp-uniform
+        sh_cnt[wib][CNT_ACT] = act;
+        sh_cnt[wib][CNT_DEG0] = 0ull;
+        sh_cnt[wib][CNT_DEG1] = 0ull;
+        sh_cnt[wib][CNT_DEG2] = 0ull;
+    }
+    __syncthreads();
+    if (threadIdx.x < NCNT) {
+        unsigned long long a = 0;
+        for (int w = 0; w < WARPS; ++w)
+            a += sh_cnt[w][threadIdx.x];
+        if (threadIdx.x >= CNT_DEG0)
+            a = sh_deg[threadIdx.x - CNT_DEG0];
+        block_cnt[NCNT * blockIdx.x + threadIdx.x] = a;
+    }
+}
+
+// The per-destination work of a dense pull, one destination per lane, launched
+// before the tile pull (pull_kernel): the BFS probe; the CC probe; CC's first
+// pull over engine-id labels (launch A: the hub destinations, launch B: the
+// rest).  Latency-bound chains of a few dependent loads: 32 registers, two
+// 1024-thread blocks per SM, so twice the warps of the tile pull are in
+// flight.  block_cnt as pull_kernel's.
+template <int APP, int EPL>
+__global__ void __launch_bounds__(PULL_THREADS, 2)
+    dst_kernel(DevGraph g, DevState s, unsigned long long* block_cnt, uint32_t phase)
+{
+    constexpr int WARPS = PULL_THREADS / 32;
+    constexpr uint32_t TILE_E = 32u * EPL;
+    __shared__ unsigned long long sh_cnt[WARPS][NCNT];
+    __shared__ unsigned int sh_deg[3];
+    Ctrl* c = s.ctrl;
+    if (c->done)
+        return;
+    const uint32_t mode = c->mode;
+    // CC on a symmetric graph propagates engine ids; before its first pull every
+    // label is its vertex's own id
+    const bool ident0 = APP == WEDGE_APP_CC && g.sym != 0u && c->iter == 0u;
+    if (mode != MODE_DENSE || (phase == PHASE_DST_B && !ident0)) {
+        // nothing to do before this pull: report zeros
+        if (threadIdx.x < NCNT)
+            block_cnt[NCNT * blockIdx.x + threadIdx.x] = 0ull;
+        return;
+    }
+    const int lane = threadIdx.x & 31;
+    const int wib = threadIdx.x >> 5;
+    const uint32_t gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const uint32_t* cur = cur_front(s, c->parity);
+    uint32_t* nxt = next_front(s, c->parity);
+    unsigned long long mass = 0, edges = 0, dsts = 0, act = 0;
+    if (threadIdx.x < 3)
+        sh_deg[threadIdx.x] = 0u;
+    __syncthreads();
+
+    // bitmap marks of tiles [ta, tb] (one lane)
+    auto mark_tiles = [](uint32_t* bm, uint32_t ta, uint32_t tb) {
+        for (uint32_t w = ta >> 5; w <= (tb >> 5); ++w) {
+            const uint32_t a = (w == (ta >> 5)) ? (ta & 31u) : 0u;
+            const uint32_t z = (w == (tb >> 5)) ? (tb & 31u) : 31u;
+            atomicOr(&bm[w], (z == 31u ? FULL : ((2u << z) - 1u)) & ~((1u << a) - 1u));
+        }
+    };
+    // tiles [ta, tb] into the tile pull's work: the lane that sets a tile's
+    // tile_need bit appends the tile to tile_list, so each is listed once
+    auto need_tiles = [&](uint32_t ta, uint32_t tb) {
+        for (uint32_t w = ta >> 5; w <= (tb >> 5); ++w) {
+            const uint32_t a = (w == (ta >> 5)) ? (ta & 31u) : 0u;
+            const uint32_t z = (w == (tb >> 5)) ? (tb & 31u) : 31u;
+            const uint32_t m = (z == 31u ? FULL : ((2u << z) - 1u)) & ~((1u << a) - 1u);
+            uint32_t fresh = m & ~atomicOr(&s.tile_need[w], m);
+            if (fresh) {
+                uint32_t pos = atomicAdd(&c->need_n, (uint32_t)__popc(fresh));
+                for (; fresh; fresh &= fresh - 1u)
+                    s.tile_list[pos++] = (unsigned long long)(w * 32u + (uint32_t)(__ffs(fresh) - 1)) << 32;
+            }
+        }
+    };
+    // Open-tile marks of the warp's destinations left unfinished (tiles [ta, tb],
+    // none where ta > tb; the bitmap is rebuilt by every dense pull).  The lanes'
+    // destinations are consecutive, so most of their tiles share a word: one
+    // atomic per distinct word.  Called by all lanes.
+    auto mark_open = [&](uint32_t ta, uint32_t tb) {
+        const bool one = ta <= tb && (ta >> 5) == (tb >> 5);
+        if (ta <= tb && !one)
+            mark_tiles(s.tile_open, ta, tb);
+        const uint32_t bits = one ? ((tb & 31u) == 31u ? FULL : ((2u << (tb & 31u)) - 1u)) & ~((1u << (ta & 31u)) - 1u) : 0u;
+        uint32_t pending = __ballot_sync(FULL, one);
+        while (pending) {
+            const int leader = __ffs(pending) - 1;
+            const uint32_t w = __shfl_sync(FULL, ta >> 5, leader);
+            const bool mine = one && (ta >> 5) == w;
+            const uint32_t all = __reduce_or_sync(FULL, mine ? bits : 0u);
+            if (lane == leader)
+                atomicOr(&s.tile_open[w], all);
+            pending &= ~__ballot_sync(FULL, mine);
+        }
+    };
+
+    if (APP == WEDGE_APP_CC && ident0) {
+        // The first CC pull over engine-id labels, one destination per lane.  A
+        // source outside the hub range [0, hub_n) still holds its own id, and a
+        // destination's sources ascend, so past its hub sources only the first
+        // one can lower the minimum; the hub sources' labels are final once the
+        // hub launch (the destinations with ids < hub_n) is over.  The hub launch
+        // itself sees every label at its id: the first source decides.  This is
+        // the tile pull's result for the same labels without reading the other
+        // in-edges (Jacobi for the hubs, where the tile pull lets a block's
+        // warps see each other's hub updates).
+        const bool hubs = phase == PHASE_DST_A;
+        const uint32_t kb = hubs ? 0u : s.hub_k, ke = hubs ? s.hub_k : g.Vne;
+        const uint32_t hn = s.hub_n;
+        const uint32_t nthr = gridDim.x * blockDim.x;
+        for (uint32_t base = kb + gw * 32u; base < ke; base += nthr) {
+            const uint32_t k = base + (uint32_t)lane;
+            bool chg = false, zero = false;
+            uint32_t d = 0u, od = 0u;
+            uint32_t ta = 1u, tb = 0u;
+            if (k < ke) {
+                d = g.dst_ident ? k : g.dst_id[k];
+                const unsigned long long lo = g.dst_off[k], hi = g.dst_off[k + 1u];
+                uint32_t m = d;
+                unsigned long long e = lo;
+                while (e < hi) {
+                    const uint32_t x = g.src[e++];
+                    if (hubs || x >= hn) {
+                        m = x < m ? x : m;
+                        break;
+                    }
+                    const uint32_t l = s.prop32[x];
+                    m = l < m ? l : m;
+                    if (m == 0u)
+                        break;
+                }
+                edges += e - lo;
+                chg = m < d;
+                zero = chg && m == 0u;
+                if (m != 0u) {
+                    ta = (uint32_t)(lo / TILE_E);
+                    tb = (uint32_t)((hi - 1u) / TILE_E);
+                }
+                if (chg) {
+                    s.prop32[d] = m; /* the destination's only writer */
+                    od = g.outdeg[d];
+                    mass += od;
+                    ++act;
+                }
+            }
+            mark_open(ta, tb);
+            dsts += (uint64_t)__popc(__ballot_sync(FULL, k < ke));
+#pragma unroll
+            for (uint32_t b = 0; b < 3u; ++b) {
+                const uint32_t nb = __popc(__ballot_sync(FULL, chg && degree_bucket(od) == b));
+                if (lane == 0 && nb)
+                    atomicAdd(&sh_deg[b], nb);
+            }
+            if (g.dst_ident) { /* d = k: the lanes' bits fall in two words at most */
+                const uint32_t w0 = base >> 5;
+                const bool in0 = (k >> 5) == w0;
+                const uint32_t bit = 1u << (k & 31u);
+                const uint32_t c0 = __reduce_or_sync(FULL, (chg && in0) ? bit : 0u);
+                const uint32_t c1 = __reduce_or_sync(FULL, (chg && !in0) ? bit : 0u);
+                const uint32_t z0 = __reduce_or_sync(FULL, (zero && in0) ? bit : 0u);
+                const uint32_t z1 = __reduce_or_sync(FULL, (zero && !in0) ? bit : 0u);
+                if (lane == 0) {
+                    if (c0)
+                        atomicOr(&nxt[w0], c0);
+                    if (c1)
+                        atomicOr(&nxt[w0 + 1u], c1);
+                    if (z0)
+                        atomicOr(&s.vis_c[w0], z0); /* label 0 is final */
+                    if (z1)
+                        atomicOr(&s.vis_c[w0 + 1u], z1);
+                }
+            } else {
+                if (chg)
+                    atomicOr(&nxt[d >> 5], 1u << (d & 31u));
+                if (zero)
+                    atomicOr(&s.vis_c[k >> 5], 1u << (k & 31u));
+            }
+        }
+    }
+    if (APP == WEDGE_APP_BFS) {
+        // Bottom-up probe, one unvisited destination per lane: its first
+        // PROBE_EDGES sources in ascending order, up to the first one in the
+        // frontier -- the least frontier source, the value the tile pull's min
+        // would give it.  A destination whose sources it read to the end
+        // without a hit has no parent this iteration (the frontier is fixed
+        // during a pull); one with sources left marks the tiles holding them in
+        // tile_need, the only tiles the tile pull (the next launch) walks.
+        const uint32_t nthr = gridDim.x * blockDim.x;
+        for (uint32_t base = gw * 32u; base < g.Vne; base += nthr) {
+            const uint32_t k = base + (uint32_t)lane; /* base is a multiple of 32: one vis_c word */
+            const uint32_t vw = s.vis_c[base >> 5];
+            const bool todo = k < g.Vne && !((vw >> lane) & 1u);
+            bool hit = false;
+            uint32_t od = 0u;
+            uint32_t ta = 1u, tb = 0u; /* tiles of a destination left unvisited (none: ta > tb) */
+            if (todo) {
+                const uint32_t d = g.dst_ident ? k : g.dst_id[k];
+                const unsigned long long lo = g.dst_off[k], hi = g.dst_off[k + 1u];
+                const unsigned long long lim = hi - lo > PROBE_EDGES ? lo + PROBE_EDGES : hi;
+                unsigned long long e = lo;
+                uint32_t par = NONE32;
+                while (e < lim) {
+                    const uint32_t x = g.src[e++];
+                    if ((ld_ro_u32(cur + (x >> 5)) >> (x & 31u)) & 1u) {
+                        par = x;
+                        break;
+                    }
+                }
+                edges += e - lo;
+                hit = par != NONE32;
+                if (!hit) {
+                    ta = (uint32_t)(lo / TILE_E);
+                    tb = (uint32_t)((hi - 1u) / TILE_E);
+                    // sources past the window remain: the tile pull reads the tiles holding them
+                    if (lim < hi)
+                        need_tiles((uint32_t)(lim / TILE_E), tb);
+                }
+                if (hit) {
+                    s.prop32[d] = par; /* the destination's only writer in this launch */
+                    od = g.outdeg[d];
+                    mass += od;
+                    ++act;
+                    if (!g.dst_ident)
+                        atomicOr(&nxt[d >> 5], 1u << (d & 31u));
+                }
+            }
+            mark_open(ta, tb);
+            dsts += (uint64_t)__popc(__ballot_sync(FULL, todo));
+#pragma unroll
+            for (uint32_t b = 0; b < 3u; ++b) {
+                const uint32_t nb = __popc(__ballot_sync(FULL, hit && degree_bucket(od) == b));
+                if (lane == 0 && nb)
+                    atomicAdd(&sh_deg[b], nb);
+            }
+            const uint32_t hits = __ballot_sync(FULL, hit);
+            if (lane == 0 && hits) {
+                atomicOr(&s.vis_c[base >> 5], hits);
+                if (g.dst_ident)
+                    atomicOr(&nxt[base >> 5], hits); /* d = k */
+            }
+        }
+    }
+    if (APP == WEDGE_APP_CC && !ident0) {
+        // CC probe (dense pulls after the first), one unfinished destination
+        // (label not 0) per lane: the labels of its first PROBE_EDGES sources,
+        // hubs first, up to the first label 0, the least label there is.  Where
+        // that found 0 or read every source, the minimum is the whole pull's for
+        // the labels read and is applied here; a longer destination without a 0
+        // marks its tiles for the tile pull (the next two launches), which walks
+        // only those.
+        const uint32_t nthr = gridDim.x * blockDim.x;
+        for (uint32_t base = gw * 32u; base < g.Vne; base += nthr) {
+            const uint32_t k = base + (uint32_t)lane; /* base is a multiple of 32: one vis_c word */
+            const uint32_t vw = s.vis_c[base >> 5];
+            const bool todo = k < g.Vne && !((vw >> lane) & 1u);
+            bool chg = false, zero = false;
+            uint32_t d = 0u, od = 0u;
+            uint32_t ta = 1u, tb = 0u;
+            if (todo) {
+                d = g.dst_ident ? k : g.dst_id[k];
+                const unsigned long long lo = g.dst_off[k], hi = g.dst_off[k + 1u];
+                const unsigned long long lim = hi - lo > PROBE_EDGES ? lo + PROBE_EDGES : hi;
+                const uint32_t cv = s.prop32[d];
+                uint32_t m = cv;
+                unsigned long long e = lo;
+                while (e < lim) {
+                    const uint32_t l = s.prop32[g.src[e++]];
+                    m = l < m ? l : m;
+                    if (m == 0u)
+                        break;
+                }
+                edges += e - lo;
+                const bool whole = m == 0u || e == hi;
+                if (whole && m < cv) {
+                    s.prop32[d] = m; /* the destination's only writer in this launch */
+                    chg = true;
+                    zero = m == 0u;
+                    od = g.outdeg[d];
+                    mass += od;
+                    ++act;
+                    if (!g.dst_ident)
+                        atomicOr(&nxt[d >> 5], 1u << (d & 31u));
+                }
+                if (!whole)
+                    need_tiles((uint32_t)(lo / TILE_E), (uint32_t)((hi - 1u) / TILE_E));
+                if (!zero) {
+                    ta = (uint32_t)(lo / TILE_E);
+                    tb = (uint32_t)((hi - 1u) / TILE_E);
+                }
+            }
+            mark_open(ta, tb);
+            dsts += (uint64_t)__popc(__ballot_sync(FULL, todo));
+#pragma unroll
+            for (uint32_t b = 0; b < 3u; ++b) {
+                const uint32_t nb = __popc(__ballot_sync(FULL, chg && degree_bucket(od) == b));
+                if (lane == 0 && nb)
+                    atomicAdd(&sh_deg[b], nb);
+            }
+            const uint32_t chgs = __ballot_sync(FULL, chg), zeros = __ballot_sync(FULL, zero);
+            if (lane == 0) {
+                if (zeros)
+                    atomicOr(&s.vis_c[base >> 5], zeros); /* label 0 is final */
+                if (chgs && g.dst_ident)
+                    atomicOr(&nxt[base >> 5], chgs); /* d = k */
+            }
+        }
+    }
+    mass = warp_sum_u64(mass);
+    edges = warp_sum_u64(edges);
+    act = warp_sum_u64(act);
+    if (lane == 0) {
+        sh_cnt[wib][CNT_MASS] = mass;
+        sh_cnt[wib][CNT_EDGES] = edges;
+        sh_cnt[wib][CNT_TILES] = 0ull;
+        sh_cnt[wib][CNT_DSTS] = dsts; // warp-uniform
         sh_cnt[wib][CNT_ACT] = act;
         sh_cnt[wib][CNT_DEG0] = 0ull;
         sh_cnt[wib][CNT_DEG1] = 0ull;
@@ -2329,8 +2381,16 @@ int compute_grids(wedge_graph* h)
         return WEDGE_ERR_CUDA;
     h->pull_grid = (uint32_t)h->num_sms; /* one block per SM: the hub cache takes the SM's shared memory */
     h->build_grid = (uint32_t)h->num_sms * 8u;
+    int dblocks = 0;
+    WEDGE_CHECK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&dblocks, dst_kernel<WEDGE_APP_CC, PullEpl<WEDGE_APP_CC>::value>,
+                                                              PULL_THREADS, 0));
+    h->dst_grid = (uint32_t)h->num_sms * (uint32_t)(dblocks < 1 ? 1 : dblocks > 2 ? 2 : dblocks);
     return WEDGE_OK;
 }
+
+// block-counter slots: the launches of the largest pull (CC: two dst_kernel
+// launches + two tile launches)
+static uint64_t counter_slots(const wedge_graph* h) { return 2ull * h->dst_grid + 2ull * h->pull_grid; }
 
 static const void* pull_fn(int app)
 {
@@ -2419,15 +2479,16 @@ static int ensure_state(wedge_graph* h, int app, int precision)
     int rc;
     Ctrl* ctrl;
     double* bp;
-    // [grid] block sums | [MAX_PULL_LAUNCHES*NCNT*grid] block counters | [aux grid] PageRank-sum partials
+    // [grid] block sums | [counter_slots * NCNT] block counters | [aux grid] PageRank-sum partials
+    const uint64_t slots = counter_slots(h);
     if ((rc = dalloc(h, &ctrl, 1, true)) ||
-        (rc = dalloc(h, &bp, grid * (1 + MAX_PULL_LAUNCHES * NCNT) + (uint64_t)h->num_sms * 8 + 8, true)) ||
+        (rc = dalloc(h, &bp, grid + slots * NCNT + (uint64_t)h->num_sms * 8 + 8, true)) ||
         (rc = dalloc(h, &s.log, LOG_CAP, true)))
         return rc;
     WEDGE_CHECK(cudaMemset(ctrl, 0, sizeof(Ctrl)));
     s.ctrl = ctrl;
     s.block_part = bp; /* [grid] doubles, then the counters */
-    WEDGE_CHECK(cudaMemset(bp, 0, sizeof(double) * (grid * (1 + MAX_PULL_LAUNCHES * NCNT))));
+    WEDGE_CHECK(cudaMemset(bp, 0, sizeof(double) * (grid + slots * NCNT)));
     s.app = (uint32_t)app;
     if (app == WEDGE_APP_PR) {
         if ((rc = dalloc(h, &s.acc, V, true)) || (rc = dalloc(h, &s.inv_od, V, true)))
@@ -2483,31 +2544,35 @@ static int ensure_state(wedge_graph* h, int app, int precision)
 static unsigned long long* counters(wedge_graph* h) { return (unsigned long long*)(h->s.block_part + h->pull_grid); }
 
 // counter slots the pulls of one iteration fill (two launches for CC/SSSP)
-static uint32_t pull_slots(wedge_graph* h, int app) { return h->pull_grid * pull_launches_of(app); }
+static uint32_t pull_slots(wedge_graph* h, int app)
+{
+    return h->dst_grid * dst_launches_of(app) + h->pull_grid * (pull_launches_of(app) - dst_launches_of(app));
+}
 
 // PageRank-sum partials after the counters
-static double* pr_sums(wedge_graph* h) { return (double*)(counters(h) + (uint64_t)MAX_PULL_LAUNCHES * NCNT * h->pull_grid); }
+static double* pr_sums(wedge_graph* h) { return (double*)(counters(h) + counter_slots(h) * NCNT); }
 
 template <int APP>
 static void launch_pull_app(wedge_graph* h)
 {
     constexpr int EPL = PullEpl<APP>::value;
     const uint32_t grid = h->pull_grid;
-    if (two_phase_app(APP)) {
-        unsigned long long* cnt = counters(h);
+    unsigned long long* cnt = counters(h);
+    if constexpr (APP == WEDGE_APP_BFS || APP == WEDGE_APP_CC) {
+        const uint32_t dgrid = h->dst_grid;
+        dst_kernel<APP, EPL><<<dgrid, PULL_THREADS, 0, h->stream>>>(h->g, h->s, cnt, PHASE_DST_A);
+        cnt += (uint64_t)NCNT * dgrid;
         if (APP == WEDGE_APP_CC) {
-            pull_kernel<APP, EPL><<<grid, PULL_THREADS, h->hub_bytes, h->stream>>>(h->g, h->s, cnt, PHASE_PROBE);
-            cnt += NCNT * grid;
+            dst_kernel<APP, EPL><<<dgrid, PULL_THREADS, 0, h->stream>>>(h->g, h->s, cnt, PHASE_DST_B);
+            cnt += (uint64_t)NCNT * dgrid;
         }
+    }
+    if (two_phase_app(APP)) {
         pull_kernel<APP, EPL><<<grid, PULL_THREADS, h->hub_bytes, h->stream>>>(h->g, h->s, cnt, PHASE_HUBS);
         pull_kernel<APP, EPL><<<grid, PULL_THREADS, h->hub_bytes, h->stream>>>(h->g, h->s, cnt + NCNT * grid,
                                                                                PHASE_REST);
-    } else if (APP == WEDGE_APP_BFS) {
-        pull_kernel<APP, EPL><<<grid, PULL_THREADS, h->hub_bytes, h->stream>>>(h->g, h->s, counters(h), PHASE_PROBE);
-        pull_kernel<APP, EPL><<<grid, PULL_THREADS, h->hub_bytes, h->stream>>>(h->g, h->s, counters(h) + NCNT * grid,
-                                                                               PHASE_ALL);
     } else {
-        pull_kernel<APP, EPL><<<grid, PULL_THREADS, h->hub_bytes, h->stream>>>(h->g, h->s, counters(h), PHASE_ALL);
+        pull_kernel<APP, EPL><<<grid, PULL_THREADS, h->hub_bytes, h->stream>>>(h->g, h->s, cnt, PHASE_ALL);
     }
 }
 

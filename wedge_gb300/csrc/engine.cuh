@@ -179,6 +179,7 @@ struct wedge_graph {
     int last_precision;
     uint32_t pull_grid;                // persistent grid of the pull kernels (one 1024-thread block per SM)
     uint32_t build_grid;
+    uint32_t dst_grid;                 // dst_kernel grid (two 1024-thread blocks per SM)
     uint32_t hub_bytes;                // dynamic shared memory of the pull kernels (the hub cache)
     float* net;                        // device copy of the scheduler network (wedge_cuda_set_scheduler)
     // allocations owned by the handle
