@@ -1627,10 +1627,6 @@ __global__ void decide_kernel(DevGraph g, DevState s, const unsigned long long* 
     }
 }
 
-// set the Wedge-frontier bit of chunk ch (wedge.c:22-31) and the summary bit
-// of its region.  Fire-and-forget atomics behind plain-load checks: bits are
-// only set while the frontier is built, so a stale read can only cost a
-// redundant atomic, and no thread waits for an atomic's return.
 // chunks per pull tile of an application, as a shift (tile = 32 * EPL in-edges)
 __device__ __forceinline__ uint32_t chunk_tile_shift(uint32_t app)
 {
@@ -1638,8 +1634,12 @@ __device__ __forceinline__ uint32_t chunk_tile_shift(uint32_t app)
     return 31u - (uint32_t)__clz(epl);
 }
 
-// A chunk of the Wedge frontier.  Chunks of closed tiles (every destination
-// finished) are left out: compact_kernel would drop them from the tile list.
+// set the Wedge-frontier bit of chunk ch (wedge.c:22-31) and the summary bit
+// of its region.  Fire-and-forget atomics behind plain-load checks: bits are
+// only set while the frontier is built, so a stale read can only cost a
+// redundant atomic, and no thread waits for an atomic's return.
+// Chunks of closed tiles (every destination finished) are left out:
+// compact_kernel would drop them from the tile list.
 __device__ __forceinline__ void mark_chunk(const DevState& s, uint32_t ch, bool valid)
 {
     if (!valid)
