@@ -41,6 +41,7 @@ struct BGraph {
     const uint32_t* outdeg;
     const unsigned long long* csri_off;
     const uint32_t* csri;
+    uint32_t csri_shift;  // chunk of a CSRI entry: entry >> csri_shift (5: positions, 0: chunk ids)
     const uint32_t* new2old;
     const uint32_t* old2new;
     uint64_t V, E;
@@ -169,7 +170,7 @@ __device__ void phase_build(const BArgs& a)
         if (valid && len <= a.split) {
             const BGraph& G = a.graphs[a.q[q].graph];
             for (unsigned long long j = 0; j < len; ++j)
-                mark_batch_chunk(a.q[q], a.ctl[q], G.csri[start + j]);
+                mark_batch_chunk(a.q[q], a.ctl[q], G.csri[start + j] >> G.csri_shift);
         }
         // long lists: the whole warp, one list at a time
         uint32_t longs = __ballot_sync(FULL, valid && len > a.split);
@@ -180,7 +181,7 @@ __device__ void phase_build(const BArgs& a)
             const unsigned long long ls = __shfl_sync(FULL, start, l), ll = __shfl_sync(FULL, len, l);
             const BGraph& G = a.graphs[a.q[lq].graph];
             for (unsigned long long j = lane; j < ll; j += 32)
-                mark_batch_chunk(a.q[lq], a.ctl[lq], G.csri[ls + j]);
+                mark_batch_chunk(a.q[lq], a.ctl[lq], G.csri[ls + j] >> G.csri_shift);
         }
     }
     // clear the previous frontier bits (their list is exact)
@@ -600,6 +601,7 @@ extern "C" int wedge_cuda_batch_create(wedge_graph_t* const* graphs, uint32_t nu
         G.outdeg = g.outdeg;
         G.csri_off = g.csri_off;
         G.csri = g.csri;
+        G.csri_shift = g.csri_pos ? 5u : 0u;
         G.new2old = g.new2old;
         G.old2new = g.old2new;
         G.V = g.V;

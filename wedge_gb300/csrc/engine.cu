@@ -194,12 +194,15 @@ __global__ void widen_kernel(const uint32_t* in, unsigned long long* out, uint64
         out[i] = in[i];
 }
 
-// CSRI fill (graphdata.c:535-569): chunk id of every out-edge, grouped by source
-__global__ void csri_fill_kernel(const uint32_t* src, uint64_t E, unsigned long long* cursor, uint32_t* csri)
+// CSRI fill (graphdata.c:535-569), grouped by source: the in-edge position of
+// every out-edge (its chunk is position / 32), or, on graphs whose padded
+// in-edges do not fit 32 bits, its chunk id
+__global__ void csri_fill_kernel(const uint32_t* src, uint64_t E, unsigned long long* cursor, uint32_t* csri,
+                                 uint32_t positions)
 {
     for (uint64_t e = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; e < E; e += (uint64_t)gridDim.x * blockDim.x) {
         const unsigned long long pos = atomicAdd(&cursor[src[e]], 1ull);
-        csri[pos] = (uint32_t)(e / CHUNK);
+        csri[pos] = (uint32_t)(positions ? e : e / CHUNK);
     }
 }
 
@@ -491,7 +494,8 @@ int build_from_device_edges(wedge_graph* h, uint64_t V, uint64_t E, uint32_t* d_
         return rc;
     WEDGE_CHECK(cudaMemcpyAsync(wide, csri_off, (V + 1) * sizeof(unsigned long long), cudaMemcpyDeviceToDevice, st));
     if (E)
-        csri_fill_kernel<<<grid_for(E, AUX_THREADS, cap), AUX_THREADS, 0, st>>>(d_src, E, wide, csri);
+        csri_fill_kernel<<<grid_for(E, AUX_THREADS, cap), AUX_THREADS, 0, st>>>(d_src, E, wide, csri,
+                                                                              g.Epad < (1ull << 32) ? 1u : 0u);
     cudaFreeAsync(wide, st);
 
     // destination starts, one bit per in-edge (the pulls' tile geometry)
@@ -536,6 +540,7 @@ int build_from_device_edges(wedge_graph* h, uint64_t V, uint64_t E, uint32_t* d_
     g.outdeg = outdeg;
     g.csri_off = csri_off;
     g.csri = csri;
+    g.csri_pos = g.Epad < (1ull << 32) ? 1u : 0u;
     g.split_k = split_k;
     g.split_t0 = split_t0;
     g.split_t1 = split_t1;
@@ -681,6 +686,7 @@ __device__ __forceinline__ void load_sources(const DevGraph& g, uint64_t base, u
 struct TileIter {
     uint32_t i, step;      // dense (static stride), the probe's tile list, or the Wedge list
     uint32_t tbeg, tend;   // the tiles [tbeg, tend) of this launch (CC's hub / other split)
+    bool need;             // walk the tiles the probe listed (dense BFS/CC pulls, BFS candidate pulls)
 };
 
 template <int APP, int EPL>
@@ -688,9 +694,10 @@ __device__ __forceinline__ bool next_tile(const DevGraph& g, const DevState& s, 
                                           TileIter& it, int lane, uint32_t& t, uint32_t& cmask)
 {
     constexpr uint32_t MASK = (EPL >= 32) ? FULL : ((1u << EPL) - 1u);
-    // dense BFS/CC pulls walk the list of tiles their probe left work in
-    // (tile_list, each tile once); a CC launch takes the ones of its range
-    if (mode == MODE_DENSE && s.tile_need) {
+    // dense BFS/CC pulls (and BFS candidate pulls) walk the list of tiles their
+    // probe left work in (tile_list, each tile once); a CC launch takes the
+    // ones of its range
+    if (it.need) {
         const uint32_t n = s.ctrl->need_n;
         for (;;) {
             if (it.i >= n)
@@ -857,7 +864,8 @@ __global__ void __launch_bounds__(PULL_THREADS, 1)
     uint32_t hub_lim = 0; /* elements of the cache this warp reads: 0 until the copy completed */
 
     TileIter it;
-    it.i = (mode == MODE_DENSE && s.tile_need) ? gw : t_begin + gw; /* the probe's list starts at 0 */
+    it.need = s.tile_need && (mode == MODE_DENSE || (APP == WEDGE_APP_BFS && mode == MODE_WEDGE && s.cand));
+    it.i = it.need ? gw : t_begin + gw; /* the probe's list starts at 0 */
     it.step = nw;
     it.tbeg = t_begin;
     it.tend = t_end;
@@ -1160,7 +1168,8 @@ __global__ void __launch_bounds__(PULL_THREADS, 2)
     // CC on a symmetric graph propagates engine ids; before its first pull every
     // label is its vertex's own id
     const bool ident0 = APP == WEDGE_APP_CC && g.sym != 0u && c->iter == 0u;
-    if (mode != MODE_DENSE || (phase == PHASE_DST_B && !ident0)) {
+    const bool cand = APP == WEDGE_APP_BFS && mode == MODE_WEDGE && s.cand != nullptr;
+    if ((mode != MODE_DENSE && !cand) || (phase == PHASE_DST_B && !ident0)) {
         // nothing to do before this pull: report zeros
         if (threadIdx.x < NCNT)
             block_cnt[NCNT * blockIdx.x + threadIdx.x] = 0ull;
@@ -1303,7 +1312,54 @@ __global__ void __launch_bounds__(PULL_THREADS, 2)
             }
         }
     }
-    if (APP == WEDGE_APP_BFS) {
+    if (APP == WEDGE_APP_BFS && cand) {
+        // A Wedge pull over the candidates the last build listed (unvisited
+        // destinations with an in-edge from the frontier): the probe below for
+        // each, one per lane, in list order.  The lanes clear the candidates'
+        // bitmap words for the next build (every bit set there is in the list).
+        const uint32_t n = c->cand_n;
+        const uint32_t nthr = gridDim.x * blockDim.x;
+        for (uint32_t base = gw * 32u; base < n; base += nthr) {
+            const uint32_t i = base + (uint32_t)lane;
+            bool hit = false;
+            uint32_t od = 0u;
+            if (i < n) {
+                const uint32_t k = s.cand_list[i];
+                s.cand[k >> 5] = 0u;
+                const uint32_t d = g.dst_ident ? k : g.dst_id[k];
+                const unsigned long long lo = g.dst_off[k], hi = g.dst_off[k + 1u];
+                const unsigned long long lim = hi - lo > PROBE_EDGES ? lo + PROBE_EDGES : hi;
+                unsigned long long e = lo;
+                uint32_t par = NONE32;
+                while (e < lim) {
+                    const uint32_t x = g.src[e++];
+                    if ((ld_ro_u32(cur + (x >> 5)) >> (x & 31u)) & 1u) {
+                        par = x;
+                        break;
+                    }
+                }
+                edges += e - lo;
+                hit = par != NONE32;
+                if (!hit && lim < hi)
+                    need_tiles((uint32_t)(lim / TILE_E), (uint32_t)((hi - 1u) / TILE_E));
+                if (hit) {
+                    s.prop32[d] = par; /* the destination's only writer in this launch */
+                    atomicOr(&s.vis_c[k >> 5], 1u << (k & 31u));
+                    atomicOr(&nxt[d >> 5], 1u << (d & 31u));
+                    od = g.outdeg[d];
+                    mass += od;
+                    ++act;
+                }
+            }
+            dsts += (uint64_t)__popc(__ballot_sync(FULL, i < n));
+#pragma unroll
+            for (uint32_t b = 0; b < 3u; ++b) {
+                const uint32_t nb = __popc(__ballot_sync(FULL, hit && degree_bucket(od) == b));
+                if (lane == 0 && nb)
+                    atomicAdd(&sh_deg[b], nb);
+            }
+        }
+    } else if (APP == WEDGE_APP_BFS) {
         // Bottom-up probe, one unvisited destination per lane: its first
         // PROBE_EDGES sources in ascending order, up to the first one in the
         // frontier -- the least frontier source, the value the tile pull's min
@@ -1577,6 +1633,7 @@ __global__ void decide_kernel(DevGraph g, DevState s, const unsigned long long* 
         c->mass = m;
         c->parity ^= 1u;
         c->need_n = 0u;
+        c->cand_n = 0u;
         c->tiles = 0u;
         c->items = 0u;
         c->alist_n = 0u;
@@ -1627,6 +1684,46 @@ __global__ void decide_kernel(DevGraph g, DevState s, const unsigned long long* 
     }
 }
 
+// chunk of a CSRI entry (an in-edge position, or a chunk id on graphs too large for 32-bit positions)
+__device__ __forceinline__ uint32_t csri_chunk(const DevGraph& g, uint32_t x) { return g.csri_pos ? x / CHUNK : x; }
+
+// compressed destination owning in-edge position pos: the owner of the
+// 128-edge index tile's first edge plus the destination starts after it
+__device__ __forceinline__ uint32_t dst_of_pos(const DevGraph& g, uint32_t pos)
+{
+    const uint32_t t = pos >> 7, w0 = t << 2, wp = pos >> 5;
+    uint32_t n = 0;
+    for (uint32_t w = w0; w < wp; ++w)
+        n += __popc(g.dst_start[w]);
+    n += __popc(g.dst_start[wp] & ((pos & 31u) == 31u ? FULL : ((2u << (pos & 31u)) - 1u)));
+    return g.tile_dst0[t] + n - (g.dst_start[w0] & 1u); /* a start at the index tile's first edge is the owner's */
+}
+
+// BFS Wedge build over in-edge positions: the destination of in-edge pos, if
+// unvisited, becomes a candidate of the next pull, listed once (its cand bit).
+// Warp-collective: every lane calls it, with valid false where it has no edge.
+__device__ __forceinline__ void add_candidate(const DevGraph& g, const DevState& s, uint32_t pos, bool valid)
+{
+    uint32_t k = 0;
+    bool add = false;
+    if (valid) {
+        k = dst_of_pos(g, pos);
+        const uint32_t b = 1u << (k & 31u);
+        if (!(s.vis_c[k >> 5] & b) && !(s.cand[k >> 5] & b))
+            add = !(atomicOr(&s.cand[k >> 5], b) & b);
+    }
+    const uint32_t m = __ballot_sync(FULL, add);
+    if (m) {
+        const int lane = threadIdx.x & 31, first = __ffs(m) - 1;
+        uint32_t base = 0;
+        if (lane == first)
+            base = atomicAdd(&s.ctrl->cand_n, (uint32_t)__popc(m));
+        base = __shfl_sync(FULL, base, first);
+        if (add)
+            s.cand_list[base + (uint32_t)__popc(m & ((1u << lane) - 1u))] = k;
+    }
+}
+
 // chunks per pull tile of an application, as a shift (tile = 32 * EPL in-edges)
 __device__ __forceinline__ uint32_t chunk_tile_shift(uint32_t app)
 {
@@ -1658,6 +1755,27 @@ __device__ __forceinline__ void mark_chunk(const DevState& s, uint32_t ch, bool 
     }
 }
 
+// Clears the bitmap the next pull writes and, before a dense pull, the tile
+// bitmaps its probe rebuilds (every thread of the grid takes part)
+__device__ __forceinline__ void advance_body(const DevGraph& g, const DevState& s, const Ctrl* c)
+{
+    uint32_t* fb = next_front(s, c->parity);
+    const uint64_t nwords = (g.V + 31) / 32;
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < nwords; i += (uint64_t)gridDim.x * blockDim.x)
+        fb[i] = 0u;
+    // a dense pull next: its probe (CC's first: its hub/rest launches) marks
+    // both afresh; a BFS candidate pull's probe marks the needed tiles
+    const bool dense = c->mode == MODE_DENSE;
+    if (s.tile_need && (dense || s.cand)) {
+        const uint64_t twords = (uint64_t)g.T / 32 + 2;
+        for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < twords; i += (uint64_t)gridDim.x * blockDim.x) {
+            s.tile_need[i] = 0u;
+            if (dense)
+                s.tile_open[i] = 0u;
+        }
+    }
+}
+
 // Wedge frontier generation (wedge.c:63-155), in three launches:
 //   collect_kernel  the bitmap of vertices the last pull activated -> a vertex
 //                   list (one warp per 32 words, one atomic per warp)
@@ -1671,7 +1789,10 @@ __device__ __forceinline__ void mark_chunk(const DevState& s, uint32_t ch, bool 
 __global__ void collect_kernel(DevGraph g, DevState s, uint32_t app)
 {
     Ctrl* c = s.ctrl;
-    if (c->done || c->mode != MODE_WEDGE)
+    if (c->done)
+        return;
+    advance_body(g, s, c); /* a different bitmap from the one collected here */
+    if (c->mode != MODE_WEDGE)
         return;
     const uint32_t* fb = cur_front(s, c->parity);
     const uint64_t nwords = (g.V + 31) / 32;
@@ -1727,14 +1848,20 @@ __global__ void expand_kernel(DevGraph g, DevState s)
                 len = 0;
             }
         }
-        // a short list's chunk indices are loaded together, then marked
+        // a short list's entries are loaded together, then marked
         uint32_t ch[BIG_LIST];
 #pragma unroll
         for (uint32_t j = 0; j < BIG_LIST; ++j)
             ch[j] = (j < len) ? g.csri[start + j] : 0u;
+        if (s.cand) {
 #pragma unroll
-        for (uint32_t j = 0; j < BIG_LIST; ++j)
-            mark_chunk(s, ch[j], j < len);
+            for (uint32_t j = 0; j < BIG_LIST; ++j)
+                add_candidate(g, s, ch[j], j < len);
+        } else {
+#pragma unroll
+            for (uint32_t j = 0; j < BIG_LIST; ++j)
+                mark_chunk(s, csri_chunk(g, ch[j]), j < len);
+        }
         uint32_t incl = np;
 #pragma unroll
         for (int d = 1; d < 32; d <<= 1) {
@@ -1771,7 +1898,11 @@ __global__ void wedge_build_kernel(DevGraph g, DevState s)
         for (unsigned long long j0 = lo; j0 < hi; j0 += 32) {
             const unsigned long long j = j0 + lane;
             const bool valid = j < hi;
-            mark_chunk(s, valid ? g.csri[j] : 0u, valid);
+            const uint32_t x = valid ? g.csri[j] : 0u;
+            if (s.cand)
+                add_candidate(g, s, x, valid);
+            else
+                mark_chunk(s, csri_chunk(g, x), valid);
         }
     }
 }
@@ -1788,7 +1919,7 @@ __global__ void compact_kernel(DevGraph g, DevState s)
     constexpr uint32_t TPW = 32 / EPL;
     constexpr uint32_t MASK = (EPL >= 32) ? FULL : ((1u << EPL) - 1u);
     Ctrl* c = s.ctrl;
-    if (c->done || c->mode != MODE_WEDGE)
+    if (c->done || c->mode != MODE_WEDGE || s.cand) /* BFS over in-edge positions: a candidate list, no tiles */
         return;
     const int lane = threadIdx.x & 31;
     const uint32_t gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
@@ -1838,22 +1969,14 @@ __global__ void compact_kernel(DevGraph g, DevState s)
 
 // Clear the bitmap the next pull writes (execution_bfs.c:320-338: swap + memset;
 // execution_cc.c:243-277: clear of the active bitmap).
+// the iteration's last step (the phase API's WEDGE_PHASE_ADVANCE; the traversal
+// loops do it inside collect_kernel)
 __global__ void advance_kernel(DevGraph g, DevState s, uint32_t app)
 {
     Ctrl* c = s.ctrl;
     if (c->done)
         return;
-    uint32_t* fb = next_front(s, c->parity);
-    const uint64_t nwords = (g.V + 31) / 32;
-    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < nwords; i += (uint64_t)gridDim.x * blockDim.x)
-        fb[i] = 0u;
-    if (s.tile_need && c->mode == MODE_DENSE) { /* a dense pull next: its probe (CC's first: its hub/rest launches) marks both afresh */
-        const uint64_t twords = (uint64_t)g.T / 32 + 2;
-        for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < twords; i += (uint64_t)gridDim.x * blockDim.x) {
-            s.tile_need[i] = 0u;
-            s.tile_open[i] = 0u;
-        }
-    }
+    advance_body(g, s, c);
 }
 
 // execution_initialize_{bfs,cc,sssp} bulk part; topen = BFS pull tiles
@@ -1903,6 +2026,11 @@ __global__ void init_kernel(DevGraph g, DevState s, uint32_t app, uint32_t topen
         for (uint64_t i = tid; i < twords; i += stride)
             s.tile_need[i] = 0u;
     }
+    if (s.cand) {
+        const uint64_t cwords = (uint64_t)g.Vne / 32 + 2;
+        for (uint64_t i = tid; i < cwords; i += stride)
+            s.cand[i] = 0u;
+    }
 }
 
 // root activation (execution_bfs.c:110-117, execution_sssp.c:83-88) and the
@@ -1938,6 +2066,7 @@ __global__ void init_root_kernel(DevGraph g, DevState s, uint32_t app, uint64_t 
         c->threshold = thr;
         c->items = 0;
         c->alist_n = 0;
+        c->cand_n = 0;
         c->need_n = 0;
         c->tiles = 0;
         c->iter = 0;
@@ -2533,6 +2662,11 @@ static int ensure_state(wedge_graph* h, int app, int precision)
             if ((rc = dalloc(h, &s.tile_need, (uint64_t)g.T / 32 + 2, true)))
                 return rc;
         }
+        if (app == WEDGE_APP_BFS && g.csri_pos) { /* Wedge pulls over candidate destinations */
+            if ((rc = dalloc(h, &s.cand, (uint64_t)g.Vne / 32 + 2, true)) ||
+                (rc = dalloc(h, &s.cand_list, (uint64_t)g.Vne + 1, true)))
+                return rc;
+        }
     }
     if ((rc = setup_hub(h, app, precision)))
         return rc;
@@ -2595,7 +2729,7 @@ static void launch_pull(wedge_graph* h, int app)
 }
 
 // kernels one iteration launches: the pull(s) and the five of the tail
-static uint64_t iteration_launches(int app) { return 6ull + pull_launches_of(app); }
+static uint64_t iteration_launches(int app) { return 5ull + pull_launches_of(app); }
 
 static uint32_t aux_grid(wedge_graph* h, uint64_t work)
 {
@@ -2642,8 +2776,7 @@ static void launch_wedge_build(wedge_graph* h, const DevGraph& g, int app)
 static void launch_tail(wedge_graph* h, int app)
 {
     decide_kernel<<<1, AUX_THREADS, 0, h->stream>>>(h->g, h->s, counters(h), pull_slots(h, app), (uint32_t)app);
-    launch_wedge_build(h, h->g, app);
-    advance_kernel<<<aux_grid(h, (h->g.V + 31) / 32), AUX_THREADS, 0, h->stream>>>(h->g, h->s, (uint32_t)app);
+    launch_wedge_build(h, h->g, app); /* collect_kernel clears the bitmaps for the next pull */
 }
 
 static void launch_init(wedge_graph* h, int app, uint64_t root, uint32_t sched, unsigned long long thr, uint32_t max_iter,
@@ -2656,8 +2789,7 @@ static void launch_init(wedge_graph* h, int app, uint64_t root, uint32_t sched, 
     init_root_kernel<<<1, 32, 0, h->stream>>>(h->g, h->s, (uint32_t)app, root, sched, thr,
                                                                            max_iter, probe_iter, probe_mode);
     h->cc_pending = (app == WEDGE_APP_CC && h->s.cc_best) ? 1 : 0;
-    launch_wedge_build(h, h->g, app);
-    advance_kernel<<<aux_grid(h, (h->g.V + 31) / 32), AUX_THREADS, 0, h->stream>>>(h->g, h->s, (uint32_t)app);
+    launch_wedge_build(h, h->g, app); /* collect_kernel clears the bitmaps for the first pull */
 }
 
 // CC on a symmetric graph, once the labels converged: caller-id labels in
@@ -2823,7 +2955,8 @@ static int run_traversal(wedge_graph* h, int app, const wedge_params_t* p, wedge
         st->edges_scanned = c.edges_scanned;
         st->tiles_scanned = c.tiles_scanned;
         st->pull_launches = c.pull_launches;
-        st->kernel_launches = use_graph ? (uint64_t)6 + (iteration_launches(app) + 1ull) * c.iter : launches;
+        // graph loop: `launches` holds the init (and the CC label conversion); + the loop condition per iteration
+        st->kernel_launches = use_graph ? launches + (iteration_launches(app) + 1ull) * c.iter : launches;
     }
     if (c.error)
         return WEDGE_ERR_CUDA;
@@ -3043,6 +3176,8 @@ int wedge_cuda_run_phase(wedge_graph_t* g, int app, int phase, const wedge_param
                 WEDGE_CHECK(cudaMemcpyAsync(&g->s.ctrl->mode, &want, sizeof(want), cudaMemcpyHostToDevice, g->stream));
                 if (g->s.tile_need) /* its probe lists the tiles whose need bit it sets first */
                     WEDGE_CHECK(cudaMemsetAsync(g->s.tile_need, 0, ((uint64_t)dg.T / 32 + 2) * sizeof(uint32_t), g->stream));
+                if (g->s.cand) /* candidates built for a Wedge pull that is not run */
+                    WEDGE_CHECK(cudaMemsetAsync(g->s.cand, 0, ((uint64_t)dg.Vne / 32 + 2) * sizeof(uint32_t), g->stream));
             }
         } else if (phase == WEDGE_PHASE_PULL_WEDGE) {
             return WEDGE_ERR_UNSUPPORTED; /* PageRank has no Wedge pull (application.c:154) */

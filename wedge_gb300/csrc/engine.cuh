@@ -11,8 +11,9 @@
 //   tile_dst0[T+1] compressed destination owning edge 128*t (Vne where that
 //                  edge is padding); pull tiles of 32*EPL edges index it with a stride
 //   outdeg[V]      out-degree (graphdata.c:430-490)
-//   csri_off[V+1], csri[E]  for every source, the Wedge chunk (32 in-edges)
-//                  holding each of its out-edges (the CSRI of graphdata.c:493-585)
+//   csri_off[V+1], csri[E]  for every source, the in-edge position of each of
+//                  its out-edges (its Wedge chunk of 32 in-edges = position / 32;
+//                  chunk ids where Epad >= 2^32): the CSRI of graphdata.c:493-585
 // A tile (128 consecutive in-edges) is the unit of work of one warp; a chunk
 // (32 in-edges, one 128-byte line of sources) is the unit the Wedge frontier
 // marks, i.e. the GPU form of the reference's frontier element of 4 edge
@@ -80,6 +81,7 @@ struct Ctrl {
     unsigned long long activated;      // vertices activated by pulls
     unsigned int items;                // Wedge-build work items appended by the last pull
     unsigned int need_n;               // tiles the probe listed for the dense tile pull (tile_list)
+    unsigned int cand_n;               // BFS: candidate destinations the last Wedge build listed
     unsigned int tiles;                // length of the Wedge tile list
     unsigned int mode;                 // MODE_DENSE / MODE_WEDGE for the next pull
     unsigned int iter;                 // completed pulls
@@ -108,7 +110,7 @@ struct DevGraph {
     uint32_t dst_ident;        // dst_id[k] == k for every k (the vertices with in-edges are [0, Vne))
     uint32_t nwide;            // destinations spanning more than SPLIT_SERIAL tile boundaries (back of the split lists)
     uint32_t sym;              // every edge's reverse is an edge too: CC propagates engine ids (see cc_best_kernel)
-    uint32_t pad1;
+    uint32_t csri_pos;         // csri holds in-edge positions (Epad < 2^32), else chunk ids
     const uint32_t* src;
     const unsigned long long* w;
     const uint32_t* dst_id;
@@ -144,6 +146,8 @@ struct DevState {
     uint32_t* vis_c;               // Vne-bit: destination finished (BFS visited; CC label 0, the least label)
     uint32_t* tile_open;           // T-bit: tile still has an unfinished destination (BFS, CC)
     uint32_t* tile_need;           // T-bit: BFS tiles with in-edges the probe left to the tile pull
+    uint32_t* cand;                // Vne-bit: BFS candidate destinations of the next Wedge pull (listed once)
+    uint32_t* cand_list;           // [Vne] those candidates
     uint32_t* chunk_bits;          // Wedge frontier: one bit per chunk
     uint32_t* summary;             // one bit per region of REGION_WORDS chunk words (any chunk marked)
     unsigned long long* tile_list; // (tile << 32 | chunk mask) of the next Wedge pull
