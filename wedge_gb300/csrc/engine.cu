@@ -1687,6 +1687,13 @@ __global__ void decide_kernel(DevGraph g, DevState s, const unsigned long long* 
 // chunk of a CSRI entry (an in-edge position, or a chunk id on graphs too large for 32-bit positions)
 __device__ __forceinline__ uint32_t csri_chunk(const DevGraph& g, uint32_t x) { return g.csri_pos ? x / CHUNK : x; }
 
+// chunks per pull tile of an application, as a shift (tile = 32 * EPL in-edges)
+__device__ __forceinline__ uint32_t chunk_tile_shift(uint32_t app)
+{
+    const uint32_t epl = app == WEDGE_APP_CC ? (uint32_t)WEDGE_EPL_CC : 8u;
+    return 31u - (uint32_t)__clz(epl);
+}
+
 // compressed destination owning in-edge position pos: the owner of the
 // 128-edge index tile's first edge plus the destination starts after it
 __device__ __forceinline__ uint32_t dst_of_pos(const DevGraph& g, uint32_t pos)
@@ -1706,6 +1713,10 @@ __device__ __forceinline__ void add_candidate(const DevGraph& g, const DevState&
 {
     uint32_t k = 0;
     bool add = false;
+    if (valid && s.tile_open) { /* a closed tile has no unvisited destination (BFS tiles: 256 in-edges) */
+        const uint32_t t = pos >> (5u + chunk_tile_shift(WEDGE_APP_BFS));
+        valid = (s.tile_open[t >> 5] >> (t & 31u)) & 1u;
+    }
     if (valid) {
         k = dst_of_pos(g, pos);
         const uint32_t b = 1u << (k & 31u);
@@ -1722,13 +1733,6 @@ __device__ __forceinline__ void add_candidate(const DevGraph& g, const DevState&
         if (add)
             s.cand_list[base + (uint32_t)__popc(m & ((1u << lane) - 1u))] = k;
     }
-}
-
-// chunks per pull tile of an application, as a shift (tile = 32 * EPL in-edges)
-__device__ __forceinline__ uint32_t chunk_tile_shift(uint32_t app)
-{
-    const uint32_t epl = app == WEDGE_APP_CC ? (uint32_t)WEDGE_EPL_CC : 8u;
-    return 31u - (uint32_t)__clz(epl);
 }
 
 // set the Wedge-frontier bit of chunk ch (wedge.c:22-31) and the summary bit
@@ -2729,7 +2733,10 @@ static void launch_pull(wedge_graph* h, int app)
 }
 
 // kernels one iteration launches: the pull(s) and the five of the tail
-static uint64_t iteration_launches(int app) { return 5ull + pull_launches_of(app); }
+static uint64_t iteration_launches(const wedge_graph* h, int app)
+{
+    return (h->s.cand ? 4ull : 5ull) + pull_launches_of(app); /* no compact_kernel for BFS candidates */
+}
 
 static uint32_t aux_grid(wedge_graph* h, uint64_t work)
 {
@@ -2769,7 +2776,8 @@ static void launch_wedge_build(wedge_graph* h, const DevGraph& g, int app)
     collect_kernel<<<aux_grid(h, (g.V + 31) / 32), AUX_THREADS, 0, h->stream>>>(g, h->s, (uint32_t)app);
     expand_kernel<<<h->build_grid, AUX_THREADS, 0, h->stream>>>(g, h->s);
     wedge_build_kernel<<<h->build_grid, AUX_THREADS, 0, h->stream>>>(g, h->s);
-    launch_compact(h, app);
+    if (!h->s.cand) /* BFS over in-edge positions lists candidates, not tiles */
+        launch_compact(h, app);
 }
 
 // iteration tail after a pull: mass/convergence, Wedge frontier, bitmap reset
@@ -2882,7 +2890,7 @@ static int run_traversal(wedge_graph* h, int app, const wedge_params_t* p, wedge
     }
     WEDGE_CHECK(cudaEventRecord(h->ev[0], h->stream));
     launch_init(h, app, root, (uint32_t)p->sched, thr, (uint32_t)cap, p->probe_iter, (uint32_t)p->probe_mode);
-    launches += 6;
+    launches += h->s.cand ? 5 : 6; /* init, root, the Wedge build */
     Ctrl c;
     if (use_graph) {
         WEDGE_CHECK(cudaGraphLaunch(h->graph_exec, h->stream));
@@ -2899,7 +2907,7 @@ static int run_traversal(wedge_graph* h, int app, const wedge_params_t* p, wedge
             WEDGE_CHECK(cudaEventRecord(h->ev[3], h->stream));
             launch_tail(h, app);
             WEDGE_CHECK(cudaEventRecord(h->ev[4], h->stream));
-            launches += iteration_launches(app);
+            launches += iteration_launches(h, app);
             WEDGE_CHECK(cudaEventSynchronize(h->ev[4]));
             float a = 0, b = 0;
             cudaEventElapsedTime(&a, h->ev[2], h->ev[3]);
@@ -2920,7 +2928,7 @@ static int run_traversal(wedge_graph* h, int app, const wedge_params_t* p, wedge
             for (int b = 0; b < 3; ++b) {
                 launch_pull(h, app);
                 launch_tail(h, app);
-                launches += iteration_launches(app);
+                launches += iteration_launches(h, app);
             }
             int rc = read_ctrl(h, &c);
             if (rc)
@@ -2956,7 +2964,7 @@ static int run_traversal(wedge_graph* h, int app, const wedge_params_t* p, wedge
         st->tiles_scanned = c.tiles_scanned;
         st->pull_launches = c.pull_launches;
         // graph loop: `launches` holds the init (and the CC label conversion); + the loop condition per iteration
-        st->kernel_launches = use_graph ? launches + (iteration_launches(app) + 1ull) * c.iter : launches;
+        st->kernel_launches = use_graph ? launches + (iteration_launches(h, app) + 1ull) * c.iter : launches;
     }
     if (c.error)
         return WEDGE_ERR_CUDA;
