@@ -1247,7 +1247,6 @@ __global__ void __launch_bounds__(PULL_THREADS, 2)
             const uint32_t k = base + (uint32_t)lane;
             bool chg = false, zero = false;
             uint32_t d = 0u, od = 0u;
-            uint32_t ta = 1u, tb = 0u;
             if (k < ke) {
                 d = g.dst_ident ? k : g.dst_id[k];
                 const unsigned long long lo = g.dst_off[k], hi = g.dst_off[k + 1u];
@@ -1267,10 +1266,6 @@ __global__ void __launch_bounds__(PULL_THREADS, 2)
                 edges += e - lo;
                 chg = m < d;
                 zero = chg && m == 0u;
-                if (m != 0u) {
-                    ta = (uint32_t)(lo / TILE_E);
-                    tb = (uint32_t)((hi - 1u) / TILE_E);
-                }
                 if (chg) {
                     s.prop32[d] = m; /* the destination's only writer */
                     od = g.outdeg[d];
@@ -1278,7 +1273,6 @@ __global__ void __launch_bounds__(PULL_THREADS, 2)
                     ++act;
                 }
             }
-            mark_open(ta, tb);
             dsts += (uint64_t)__popc(__ballot_sync(FULL, k < ke));
 #pragma unroll
             for (uint32_t b = 0; b < 3u; ++b) {
@@ -1769,7 +1763,9 @@ __device__ __forceinline__ void advance_body(const DevGraph& g, const DevState& 
         fb[i] = 0u;
     // a dense pull next: its probe (CC's first: its hub/rest launches) marks
     // both afresh; a BFS candidate pull's probe marks the needed tiles
-    const bool dense = c->mode == MODE_DENSE;
+    // (CC's first pull over engine ids rebuilds nothing: the bitmap keeps
+    // init's every-tile-open until the next dense probe)
+    const bool dense = c->mode == MODE_DENSE && !(s.app == WEDGE_APP_CC && g.sym && c->iter == 0u);
     if (s.tile_need && (dense || s.cand)) {
         const uint64_t twords = (uint64_t)g.T / 32 + 2;
         for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < twords; i += (uint64_t)gridDim.x * blockDim.x) {
