@@ -1243,13 +1243,24 @@ __global__ void __launch_bounds__(PULL_THREADS, 2)
         const uint32_t kb = hubs ? 0u : s.hub_k, ke = hubs ? s.hub_k : g.Vne;
         const uint32_t hn = s.hub_n;
         const uint32_t nthr = gridDim.x * blockDim.x;
+        // the next group's offsets are loaded while this one is processed
+        unsigned long long plo = 0ull, phi = 0ull;
+        auto prefetch = [&](uint32_t b) {
+            const uint32_t kk = b + (uint32_t)lane;
+            if (kk < ke) {
+                plo = g.dst_off[kk];
+                phi = g.dst_off[kk + 1u];
+            }
+        };
+        prefetch(kb + gw * 32u);
         for (uint32_t base = kb + gw * 32u; base < ke; base += nthr) {
             const uint32_t k = base + (uint32_t)lane;
+            const unsigned long long lo = plo, hi = phi;
+            prefetch(base + nthr);
             bool chg = false, zero = false;
             uint32_t d = 0u, od = 0u;
             if (k < ke) {
                 d = g.dst_ident ? k : g.dst_id[k];
-                const unsigned long long lo = g.dst_off[k], hi = g.dst_off[k + 1u];
                 uint32_t m = d;
                 unsigned long long e = lo;
                 while (e < hi) {
@@ -1362,16 +1373,31 @@ __global__ void __launch_bounds__(PULL_THREADS, 2)
         // during a pull); one with sources left marks the tiles holding them in
         // tile_need, the only tiles the tile pull (the next launch) walks.
         const uint32_t nthr = gridDim.x * blockDim.x;
+        // the next group's visited word and offsets are loaded while this one is
+        // probed (each group's vis_c word belongs to its warp alone)
+        uint32_t pv = 0u;
+        unsigned long long plo = 0ull, phi = 0ull;
+        auto prefetch = [&](uint32_t b) {
+            const uint32_t kk = b + (uint32_t)lane;
+            if (b < g.Vne)
+                pv = s.vis_c[b >> 5];
+            if (kk < g.Vne) {
+                plo = g.dst_off[kk];
+                phi = g.dst_off[kk + 1u];
+            }
+        };
+        prefetch(gw * 32u);
         for (uint32_t base = gw * 32u; base < g.Vne; base += nthr) {
             const uint32_t k = base + (uint32_t)lane; /* base is a multiple of 32: one vis_c word */
-            const uint32_t vw = s.vis_c[base >> 5];
+            const uint32_t vw = pv;
+            const unsigned long long lo = plo, hi = phi;
+            prefetch(base + nthr);
             const bool todo = k < g.Vne && !((vw >> lane) & 1u);
             bool hit = false;
             uint32_t od = 0u;
             uint32_t ta = 1u, tb = 0u; /* tiles of a destination left unvisited (none: ta > tb) */
             if (todo) {
                 const uint32_t d = g.dst_ident ? k : g.dst_id[k];
-                const unsigned long long lo = g.dst_off[k], hi = g.dst_off[k + 1u];
                 const unsigned long long lim = hi - lo > PROBE_EDGES ? lo + PROBE_EDGES : hi;
                 unsigned long long e = lo;
                 uint32_t par = NONE32;
@@ -1425,16 +1451,31 @@ __global__ void __launch_bounds__(PULL_THREADS, 2)
         // marks its tiles for the tile pull (the next two launches), which walks
         // only those.
         const uint32_t nthr = gridDim.x * blockDim.x;
+        // the next group's finished word and offsets are loaded while this one
+        // is probed (each group's vis_c word belongs to its warp alone)
+        uint32_t pv = 0u;
+        unsigned long long plo = 0ull, phi = 0ull;
+        auto prefetch = [&](uint32_t b) {
+            const uint32_t kk = b + (uint32_t)lane;
+            if (b < g.Vne)
+                pv = s.vis_c[b >> 5];
+            if (kk < g.Vne) {
+                plo = g.dst_off[kk];
+                phi = g.dst_off[kk + 1u];
+            }
+        };
+        prefetch(gw * 32u);
         for (uint32_t base = gw * 32u; base < g.Vne; base += nthr) {
             const uint32_t k = base + (uint32_t)lane; /* base is a multiple of 32: one vis_c word */
-            const uint32_t vw = s.vis_c[base >> 5];
+            const uint32_t vw = pv;
+            const unsigned long long lo = plo, hi = phi;
+            prefetch(base + nthr);
             const bool todo = k < g.Vne && !((vw >> lane) & 1u);
             bool chg = false, zero = false;
             uint32_t d = 0u, od = 0u;
             uint32_t ta = 1u, tb = 0u;
             if (todo) {
                 d = g.dst_ident ? k : g.dst_id[k];
-                const unsigned long long lo = g.dst_off[k], hi = g.dst_off[k + 1u];
                 const unsigned long long lim = hi - lo > PROBE_EDGES ? lo + PROBE_EDGES : hi;
                 const uint32_t cv = s.prop32[d];
                 uint32_t m = cv;
