@@ -686,7 +686,7 @@ __device__ __forceinline__ void load_sources(const DevGraph& g, uint64_t base, u
 struct TileIter {
     uint32_t i, step;      // dense (static stride), the probe's tile list, or the Wedge list
     uint32_t tbeg, tend;   // the tiles [tbeg, tend) of this launch (CC's hub / other split)
-    bool need;             // walk the tiles the probe listed (dense BFS/CC pulls, BFS candidate pulls)
+    bool need;             // walk the tiles the probe listed (dense BFS/CC pulls, candidate pulls)
 };
 
 template <int APP, int EPL>
@@ -694,7 +694,7 @@ __device__ __forceinline__ bool next_tile(const DevGraph& g, const DevState& s, 
                                           TileIter& it, int lane, uint32_t& t, uint32_t& cmask)
 {
     constexpr uint32_t MASK = (EPL >= 32) ? FULL : ((1u << EPL) - 1u);
-    // dense BFS/CC pulls (and BFS candidate pulls) walk the list of tiles their
+    // dense BFS/CC pulls (and candidate Wedge pulls) walk the list of tiles their
     // probe left work in (tile_list, each tile once); a CC launch takes the
     // ones of its range
     if (it.need) {
@@ -864,7 +864,7 @@ __global__ void __launch_bounds__(PULL_THREADS, 1)
     uint32_t hub_lim = 0; /* elements of the cache this warp reads: 0 until the copy completed */
 
     TileIter it;
-    it.need = s.tile_need && (mode == MODE_DENSE || (APP == WEDGE_APP_BFS && mode == MODE_WEDGE && s.cand));
+    it.need = s.tile_need && (mode == MODE_DENSE || (mode == MODE_WEDGE && s.cand));
     it.i = it.need ? gw : t_begin + gw; /* the probe's list starts at 0 */
     it.step = nw;
     it.tbeg = t_begin;
@@ -1168,7 +1168,7 @@ __global__ void __launch_bounds__(PULL_THREADS, 2)
     // CC on a symmetric graph propagates engine ids; before its first pull every
     // label is its vertex's own id
     const bool ident0 = APP == WEDGE_APP_CC && g.sym != 0u && c->iter == 0u;
-    const bool cand = APP == WEDGE_APP_BFS && mode == MODE_WEDGE && s.cand != nullptr;
+    const bool cand = (APP == WEDGE_APP_BFS || APP == WEDGE_APP_CC) && mode == MODE_WEDGE && s.cand != nullptr;
     if ((mode != MODE_DENSE && !cand) || (phase == PHASE_DST_B && !ident0)) {
         // nothing to do before this pull: report zeros
         if (threadIdx.x < NCNT)
@@ -1442,7 +1442,56 @@ __global__ void __launch_bounds__(PULL_THREADS, 2)
             }
         }
     }
-    if (APP == WEDGE_APP_CC && !ident0) {
+    if (APP == WEDGE_APP_CC && cand && phase == PHASE_DST_A) {
+        // A Wedge pull over the candidates the last build listed (unfinished
+        // destinations with an in-edge from a vertex the last pull changed): the
+        // CC probe below for each, one per lane, in list order; the lanes clear
+        // the candidates' bitmap words for the next build.
+        const uint32_t n = c->cand_n;
+        const uint32_t nthr = gridDim.x * blockDim.x;
+        for (uint32_t base = gw * 32u; base < n; base += nthr) {
+            const uint32_t i = base + (uint32_t)lane;
+            bool chg = false;
+            uint32_t od = 0u;
+            if (i < n) {
+                const uint32_t k = s.cand_list[i];
+                s.cand[k >> 5] = 0u;
+                const uint32_t d = g.dst_ident ? k : g.dst_id[k];
+                const unsigned long long lo = g.dst_off[k], hi = g.dst_off[k + 1u];
+                const unsigned long long lim = hi - lo > PROBE_EDGES ? lo + PROBE_EDGES : hi;
+                const uint32_t cv = s.prop32[d];
+                uint32_t m = cv;
+                unsigned long long e = lo;
+                while (e < lim) {
+                    const uint32_t l = s.prop32[g.src[e++]];
+                    m = l < m ? l : m;
+                    if (m == 0u)
+                        break;
+                }
+                edges += e - lo;
+                const bool whole = m == 0u || e == hi;
+                if (whole && m < cv) {
+                    s.prop32[d] = m; /* the destination's only writer in this launch */
+                    chg = true;
+                    if (m == 0u)
+                        atomicOr(&s.vis_c[k >> 5], 1u << (k & 31u)); /* label 0 is final */
+                    atomicOr(&nxt[d >> 5], 1u << (d & 31u));
+                    od = g.outdeg[d];
+                    mass += od;
+                    ++act;
+                }
+                if (!whole)
+                    need_tiles((uint32_t)(lo / TILE_E), (uint32_t)((hi - 1u) / TILE_E));
+            }
+            dsts += (uint64_t)__popc(__ballot_sync(FULL, i < n));
+#pragma unroll
+            for (uint32_t b = 0; b < 3u; ++b) {
+                const uint32_t nb = __popc(__ballot_sync(FULL, chg && degree_bucket(od) == b));
+                if (lane == 0 && nb)
+                    atomicAdd(&sh_deg[b], nb);
+            }
+        }
+    } else if (APP == WEDGE_APP_CC && !ident0 && !cand) {
         // CC probe (dense pulls after the first), one unfinished destination
         // (label not 0) per lane: the labels of its first PROBE_EDGES sources,
         // hubs first, up to the first label 0, the least label there is.  Where
@@ -1741,15 +1790,16 @@ __device__ __forceinline__ uint32_t dst_of_pos(const DevGraph& g, uint32_t pos)
     return g.tile_dst0[t] + n - (g.dst_start[w0] & 1u); /* a start at the index tile's first edge is the owner's */
 }
 
-// BFS Wedge build over in-edge positions: the destination of in-edge pos, if
-// unvisited, becomes a candidate of the next pull, listed once (its cand bit).
+// Wedge build over in-edge positions (BFS, CC): the destination of in-edge
+// pos, if unfinished (BFS unvisited, CC label not 0), becomes a candidate of
+// the next pull, listed once (its cand bit).
 // Warp-collective: every lane calls it, with valid false where it has no edge.
 __device__ __forceinline__ void add_candidate(const DevGraph& g, const DevState& s, uint32_t pos, bool valid)
 {
     uint32_t k = 0;
     bool add = false;
-    if (valid && s.tile_open) { /* a closed tile has no unvisited destination (BFS tiles: 256 in-edges) */
-        const uint32_t t = pos >> (5u + chunk_tile_shift(WEDGE_APP_BFS));
+    if (valid && s.tile_open) { /* a closed tile has no unfinished destination */
+        const uint32_t t = pos >> (5u + chunk_tile_shift(s.app));
         valid = (s.tile_open[t >> 5] >> (t & 31u)) & 1u;
     }
     if (valid) {
@@ -1803,7 +1853,7 @@ __device__ __forceinline__ void advance_body(const DevGraph& g, const DevState& 
     for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < nwords; i += (uint64_t)gridDim.x * blockDim.x)
         fb[i] = 0u;
     // a dense pull next: its probe (CC's first: its hub/rest launches) marks
-    // both afresh; a BFS candidate pull's probe marks the needed tiles
+    // both afresh; a candidate Wedge pull's probe marks the needed tiles
     // (CC's first pull over engine ids rebuilds nothing: the bitmap keeps
     // init's every-tile-open until the next dense probe)
     const bool dense = c->mode == MODE_DENSE && !(s.app == WEDGE_APP_CC && g.sym && c->iter == 0u);
@@ -1960,7 +2010,7 @@ __global__ void compact_kernel(DevGraph g, DevState s)
     constexpr uint32_t TPW = 32 / EPL;
     constexpr uint32_t MASK = (EPL >= 32) ? FULL : ((1u << EPL) - 1u);
     Ctrl* c = s.ctrl;
-    if (c->done || c->mode != MODE_WEDGE || s.cand) /* BFS over in-edge positions: a candidate list, no tiles */
+    if (c->done || c->mode != MODE_WEDGE || s.cand) /* over in-edge positions: a candidate list, no tiles */
         return;
     const int lane = threadIdx.x & 31;
     const uint32_t gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
@@ -2703,7 +2753,7 @@ static int ensure_state(wedge_graph* h, int app, int precision)
             if ((rc = dalloc(h, &s.tile_need, (uint64_t)g.T / 32 + 2, true)))
                 return rc;
         }
-        if (app == WEDGE_APP_BFS && g.csri_pos) { /* Wedge pulls over candidate destinations */
+        if ((app == WEDGE_APP_BFS || app == WEDGE_APP_CC) && g.csri_pos) { /* Wedge pulls over candidate destinations */
             if ((rc = dalloc(h, &s.cand, (uint64_t)g.Vne / 32 + 2, true)) ||
                 (rc = dalloc(h, &s.cand_list, (uint64_t)g.Vne + 1, true)))
                 return rc;
@@ -2772,7 +2822,7 @@ static void launch_pull(wedge_graph* h, int app)
 // kernels one iteration launches: the pull(s) and the five of the tail
 static uint64_t iteration_launches(const wedge_graph* h, int app)
 {
-    return (h->s.cand ? 4ull : 5ull) + pull_launches_of(app); /* no compact_kernel for BFS candidates */
+    return (h->s.cand ? 4ull : 5ull) + pull_launches_of(app); /* no compact_kernel for candidate lists */
 }
 
 static uint32_t aux_grid(wedge_graph* h, uint64_t work)
@@ -2813,7 +2863,7 @@ static void launch_wedge_build(wedge_graph* h, const DevGraph& g, int app)
     collect_kernel<<<aux_grid(h, (g.V + 31) / 32), AUX_THREADS, 0, h->stream>>>(g, h->s, (uint32_t)app);
     expand_kernel<<<h->build_grid, AUX_THREADS, 0, h->stream>>>(g, h->s);
     wedge_build_kernel<<<h->build_grid, AUX_THREADS, 0, h->stream>>>(g, h->s);
-    if (!h->s.cand) /* BFS over in-edge positions lists candidates, not tiles */
+    if (!h->s.cand) /* over in-edge positions the build lists candidates, not tiles */
         launch_compact(h, app);
 }
 
