@@ -285,7 +285,7 @@ def run_ours(args, dist: Dist):
                 "d2h_bytes_per_step": 2 * 8 * V, "steps": e2e_steps,
                 "what": "wedge_cuda_run + wedge_cuda_read_results per app into pinned host memory; "
                         "graph resident (loaded once, as the reference excludes load from Running Time)"},
-        "roofline": {"bound": "hbm", "kernel": "pull_kernel (BFS + CC, all iterations)",
+        "roofline": {"bound": "hbm", "kernel": "edge pull: dst_kernel + pull_kernel (BFS + CC, all iterations)",
                      "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
                      "frac": round(achieved / peak, 4), "peak_source": peak_kind,
                      "traffic": traffic,
