@@ -17,15 +17,6 @@
 
 namespace wedge {
 
-__device__ __forceinline__ uint4 ld_stream_v4(const uint32_t* p)
-{
-    uint4 r;
-    asm volatile("ld.global.nc.L1::no_allocate.v4.u32 {%0,%1,%2,%3}, [%4];"
-                 : "=r"(r.x), "=r"(r.y), "=r"(r.z), "=r"(r.w)
-                 : "l"(p));
-    return r;
-}
-
 // 256-bit streaming loads (sm_100+): one lane reads a whole 32-byte sector, so
 // a warp's strided per-lane runs cost one L2 request per sector and need no
 // L1 reuse (the L1 is mostly given to the hub cache)
@@ -41,18 +32,6 @@ __device__ __forceinline__ void ld_stream_v4u64(const unsigned long long* p, uns
     asm volatile("ld.global.nc.L1::no_allocate.v4.u64 {%0,%1,%2,%3}, [%4];"
                  : "=l"(r[0]), "=l"(r[1]), "=l"(r[2]), "=l"(r[3])
                  : "l"(p));
-}
-
-__device__ __forceinline__ ulonglong2 ld_stream_v2u64(const unsigned long long* p)
-{
-    ulonglong2 r;
-    asm volatile("ld.global.nc.L1::no_allocate.v2.u64 {%0,%1}, [%2];" : "=l"(r.x), "=l"(r.y) : "l"(p));
-    return r;
-}
-
-__device__ __forceinline__ bool test_bit32(const uint32_t* bm, uint64_t i)
-{
-    return (bm[i >> 5] >> (i & 31)) & 1u;
 }
 
 /* ---- hub cache: a bulk (TMA) copy of the low-id end of the gathered array
@@ -147,8 +126,9 @@ struct TileGeo {
     bool tail_cont;      // the tile's last destination continues into the next tile
 };
 
-// Destination ranks inside a tile: position p belongs to compressed destination
-// k0 + (number of destination starts in [1, p]).  k0 / kend are the compressed
+// Destination ranks inside a tile from dst_off (the batched kernel's form):
+// position p belongs to compressed destination k0 + (number of destination
+// starts in [1, p]).  k0 / kend are the compressed
 // destinations owning the tile's first edge and the next tile's first edge.
 // The starts are collected in the warp's shared `heads` words (EPL words) and
 // prefix-counted with a shuffle scan.  fill(slot, k) is called once for every
@@ -200,10 +180,13 @@ __device__ __forceinline__ void tile_geometry(const DevGraph& g, uint64_t base, 
     __syncwarp();
 }
 
-// The same geometry from the destination-start bitmap (bit p of g.dst_start:
-// in-edge p is the first in-edge of its destination): lane l < EPL loads word
-// l of the tile, no loads of dst_off and no shared memory.  base is a multiple
-// of 32*EPL.
+// Destination ranks inside a tile, from the destination-start bitmap (bit p
+// of g.dst_start: in-edge p is the first in-edge of its destination): position
+// p belongs to compressed destination k0 + (number of starts in [1, p]).  Lane
+// l < EPL loads word l of the tile and the words are prefix-counted with a
+// shuffle scan: no loads of dst_off and no shared memory.  k0 / kend are the
+// compressed destinations owning the tile's first edge and the next tile's
+// first edge; base is a multiple of 32*EPL.
 template <int EPL>
 __device__ __forceinline__ void tile_geometry_bits(const DevGraph& g, uint64_t base, bool last_tile, uint32_t k0,
                                                    uint32_t kend, int lane, TileGeo<EPL>& tg)
