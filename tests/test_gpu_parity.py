@@ -397,6 +397,23 @@ def test_read_results_into_page_locked_memory(W, O):
         assert np.array_equal(a, pinned)
 
 
+def test_wedge_pulls_over_chunk_ids(W, O, monkeypatch):
+    """the chunk form of the Wedge frontier (CSRI chunk ids, the encoding of graphs
+    beyond 2^32 padded in-edges, selected here by WEDGE_CSRI_CHUNKS) gives the
+    same results as the candidate form"""
+    monkeypatch.setenv("WEDGE_CSRI_CHUNKS", "1")
+    V, s, d = graph_edges(O, "rmat", dict(scale=13, edge_factor=16, seed=11))
+    Vs, ss, ds = graph_edges(O, "rmat", dict(scale=13, edge_factor=16, seed=11), True)
+    lv = bfs_levels(V, s, d, 0)
+    cc_ref, _, _ = O.Graph.from_edges(Vs, ss, ds, O.CC).run(threads=4)
+    for sched in (W.SCHED_PLAIN, W.SCHED_WEDGE):
+        got, _, st = run_engine(W, V, s, d, W.APP_BFS, root=0, sched=sched)
+        check_bfs(got, V, s, d, 0, lv)
+        assert st["wedge_iterations"] >= 1
+        got, _, _ = run_engine(W, Vs, ss, ds, W.APP_CC, sched=sched)
+        assert np.array_equal(got, cc_ref)
+
+
 def test_iteration_cap_reports_not_converged(W, O):
     V, s, d = graph_edges(O, "grid", dict(side=32, frac=0.0, seed=3))
     with W.Graph.from_edges(V, s, d) as g:

@@ -482,7 +482,11 @@ int build_from_device_edges(wedge_graph* h, uint64_t V, uint64_t E, uint32_t* d_
     cudaFreeAsync(kidx, st);
     cudaFreeAsync(d_dst, st);
 
-    // out-degrees and CSRI
+    // out-degrees and CSRI: in-edge positions where they fit 32 bits
+    // (WEDGE_CSRI_CHUNKS=1 selects chunk ids on any graph: the encoding, and
+    // the chunk Wedge pulls, of graphs beyond 2^32 padded in-edges)
+    const char* force_chunks = getenv("WEDGE_CSRI_CHUNKS");
+    const uint32_t csri_pos = (g.Epad < (1ull << 32) && !(force_chunks && force_chunks[0] == '1')) ? 1u : 0u;
     WEDGE_CHECK(cudaMemsetAsync(outdeg, 0, V * sizeof(uint32_t), st));
     if (E)
         outdeg_kernel<<<grid_for(E, AUX_THREADS, cap), AUX_THREADS, 0, st>>>(d_src, E, outdeg);
@@ -494,8 +498,7 @@ int build_from_device_edges(wedge_graph* h, uint64_t V, uint64_t E, uint32_t* d_
         return rc;
     WEDGE_CHECK(cudaMemcpyAsync(wide, csri_off, (V + 1) * sizeof(unsigned long long), cudaMemcpyDeviceToDevice, st));
     if (E)
-        csri_fill_kernel<<<grid_for(E, AUX_THREADS, cap), AUX_THREADS, 0, st>>>(d_src, E, wide, csri,
-                                                                              g.Epad < (1ull << 32) ? 1u : 0u);
+        csri_fill_kernel<<<grid_for(E, AUX_THREADS, cap), AUX_THREADS, 0, st>>>(d_src, E, wide, csri, csri_pos);
     cudaFreeAsync(wide, st);
 
     // destination starts, one bit per in-edge (the pulls' tile geometry)
@@ -540,7 +543,7 @@ int build_from_device_edges(wedge_graph* h, uint64_t V, uint64_t E, uint32_t* d_
     g.outdeg = outdeg;
     g.csri_off = csri_off;
     g.csri = csri;
-    g.csri_pos = g.Epad < (1ull << 32) ? 1u : 0u;
+    g.csri_pos = csri_pos;
     g.split_k = split_k;
     g.split_t0 = split_t0;
     g.split_t1 = split_t1;
