@@ -35,6 +35,13 @@ RMAT_ABC = (0.57, 0.19, 0.19)
 WORKLOAD = dict(workload="rmat24_bfs_cc", scale=24, edge_factor=16, seed=2, bfs_root=0, threshold_pct=20)
 
 
+def workload_name(scale: int, ef: int) -> str:
+    """the workload as run: the default is rmat24_bfs_cc (R-MAT scale 24, edge factor 16)"""
+    if (scale, ef) == (WORKLOAD["scale"], WORKLOAD["edge_factor"]):
+        return WORKLOAD["workload"]
+    return f"rmat{scale}_ef{ef}_bfs_cc"
+
+
 def parse():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -272,7 +279,7 @@ def run_ours(args, dist: Dist):
         "vs_baseline": None,
         "dtype": "u32",
         "data": "synthetic (device R-MAT, counter-based generator; no dataset)",
-        "config": {"workload": WORKLOAD["workload"], "scale": scale, "edge_factor": ef, "seed": WORKLOAD["seed"],
+        "config": {"workload": workload_name(scale, ef), "scale": scale, "edge_factor": ef, "seed": WORKLOAD["seed"],
                    "vertices": V, "edges_bfs": E_bfs, "edges_cc": E_cc, "bfs_root": WORKLOAD["bfs_root"],
                    "threshold_pct": WORKLOAD["threshold_pct"], "loop": args.mode,
                    "l2": "inputs larger than L2 (sources 1 GiB / 2 GiB vs 126 MB L2); no flush",
@@ -430,7 +437,7 @@ def run_reference(args, dist: Dist):
         "value": round(value, 4), "unit": "GTEPS", "n_gpus": args.gpus, "steps": steps, "warmup": warmup,
         "ms_per_step": round(t * 1e3 / steps, 3), "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "u32", "data": "synthetic (CPU R-MAT, same generator as the GPU arm)",
-        "config": {"workload": WORKLOAD["workload"], "scale": scale, "edge_factor": ef, "seed": WORKLOAD["seed"],
+        "config": {"workload": workload_name(scale, ef), "scale": scale, "edge_factor": ef, "seed": WORKLOAD["seed"],
                    "vertices": V, "edges_bfs": E_b, "edges_cc": E_c, "threads": threads},
         "cpu_baseline": {"value": round(value, 4), "unit": "GTEPS", "cores": threads, "kind": "port",
                          "sample": f"{steps} steps of one BFS + one CC on the full scale-{scale} graphs "
