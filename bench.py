@@ -1,12 +1,19 @@
-"""Benchmark of the edge-pull engine: GTEPS of BFS + CC on R-MAT scale 24.
+"""Benchmark of the edge-pull engine: GTEPS per application on R-MAT scale 26.
 
-Workload (one "step"): BFS from vertex 0 on the directed R-MAT graph (scale 24,
-edge factor 16, a/b/c/d = 0.57/0.19/0.19/0.05, seed 2: 16,777,216 vertices,
-268,435,456 edges) and Connected Components on its symmetrised copy
-(536,870,912 edges), plain fixed-threshold scheduling (t = 20%).  Synthetic
-graphs are generated on the device with the same counter-based generator the
-CPU side uses.  GTEPS counts every input edge once per traversal:
-    value = steps * (|E_bfs| + |E_cc|) / time.
+Workload (one "step", the configuration the metric is quoted on): on the R-MAT
+graph of scale 26 (edge factor 16, a/b/c/d = 0.57/0.19/0.19/0.05, seed 5:
+67,108,864 vertices, 1,073,741,824 edges), BFS from vertex 0, SSSP from vertex
+0 (uint64 hash weights in [1, 255]) and 30 iterations of compensated-FP32
+PageRank (damping 0.85) on the directed graph, and Connected Components on its
+symmetrised copy (2,147,483,648 edges); plain fixed-threshold scheduling (t =
+20%).  Synthetic graphs are generated on the device with the same
+counter-based generator the CPU side uses.  GTEPS counts every input edge once
+per traversal (BFS, CC, SSSP) and once per iteration (PageRank):
+    value = steps * (|E| + |E_sym| + |E| + 30 |E|) / time.
+The same steps under the learned scheduler, per application, and sub-records
+for the other configurations (PageRank R-MAT 16 FP64; BFS + CC R-MAT 24; SSSP
+on the 4096^2 grid, uint64 and FP64 weights; 256 BFS + 256 SSSP queries over
+64 graphs in one persistent kernel) follow in the same JSON line.
 
 Arms
   (default)          the CUDA engine through its C ABI; graphs resident in HBM
@@ -25,32 +32,34 @@ import os
 import subprocess
 import sys
 import tempfile
-import threading
 import time
 
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 RMAT_ABC = (0.57, 0.19, 0.19)
-WORKLOAD = dict(workload="rmat24_bfs_cc", scale=24, edge_factor=16, seed=2, bfs_root=0, threshold_pct=20)
+WORKLOAD = dict(workload="rmat26_bfs_cc_sssp_pr", scale=26, edge_factor=16, seed=5, root=0, threshold_pct=20,
+                pr_iterations=30, damping=0.85)
+APPS = ("bfs", "cc", "sssp", "pr")
 
 
 def workload_name(scale: int, ef: int) -> str:
-    """the workload as run: the default is rmat24_bfs_cc (R-MAT scale 24, edge factor 16)"""
+    """the workload as run: the default is rmat26_bfs_cc_sssp_pr (R-MAT scale 26, edge factor 16)"""
     if (scale, ef) == (WORKLOAD["scale"], WORKLOAD["edge_factor"]):
         return WORKLOAD["workload"]
-    return f"rmat{scale}_ef{ef}_bfs_cc"
+    return f"rmat{scale}_ef{ef}_bfs_cc_sssp_pr"
 
 
 def parse():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=100)
+    ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--scale", type=int, default=WORKLOAD["scale"])
     ap.add_argument("--edge-factor", type=int, default=WORKLOAD["edge_factor"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-sub", action="store_true", help="skip the other configurations' sub-records")
     ap.add_argument("--mode", default="graph", choices=["graph", "host"], help="traversal loop: CUDA graph or host")
     return ap.parse_args()
 
@@ -149,125 +158,231 @@ def measured_peaks():
         return 6800.0, "fallback"
 
 
-# ---------------------------------------------------------------- algorithmic bytes per pull launch
-def pull_bytes(app: str, rec: dict, V: int, Vne: int) -> float:
-    """Compulsory bytes of one pull launch, counting each touched array once:
-    sources 4*E_s, destination offsets 8*V_s (+ ids 4*V_s), the property array
-    read once, the frontier bitmaps, and the writes of changed properties."""
+# ---------------------------------------------------------------- algorithmic bytes per pull
+def pull_bytes(app: str, rec: dict, V: int, wbytes: int = 1) -> float:
+    """Compulsory bytes of one iteration's pull, each touched array counted once
+    (E_s = in-edges read, V_s = destinations examined, act = vertices activated):
+      BFS   4 E_s + 12 V_s + 3 V/8 + 4 act  (sources, offsets + ids, frontier / next / visited bits, parents)
+      CC    4 E_s + 12 V_s + 4 V + 4 act + V/8  (labels read once, changed labels, changed bitmap)
+      SSSP  (4 + w) E_s + 12 V_s + 8 V + 8 act + 2 V/8  (w = stored weight bytes per in-edge)"""
     Es, Vs, act = rec["edges_scanned"], rec["dsts_scanned"], rec["vertices_activated"]
     bitmap = V / 8.0
     if app == "bfs":
-        # sources, offsets+ids, current frontier + next frontier + visited bits, parent writes
-        return 4.0 * Es + 12.0 * Vs + 2 * bitmap + Vne / 8.0 + 4.0 * act
+        return 4.0 * Es + 12.0 * Vs + 3 * bitmap + 4.0 * act
     if app == "cc":
-        # sources, offsets+ids, labels read once, label writes, changed bitmap
         return 4.0 * Es + 12.0 * Vs + 4.0 * V + 4.0 * act + bitmap
+    if app == "sssp":
+        return (4.0 + wbytes) * Es + 12.0 * Vs + 8.0 * V + 8.0 * act + 2 * bitmap
     raise ValueError(app)
 
 
+def pr_iteration_bytes(V: int, E: int) -> float:
+    """compensated-FP32 PageRank, one iteration: 4 E (sources) + 20 V (destination
+    offsets 8, rank read 4, 1/outdegree' 4, rank write 4)"""
+    return 4.0 * E + 20.0 * V
+
+
 # ---------------------------------------------------------------- our arm
+class Suite:
+    """the four applications on the scale-26 graphs, one handle per application"""
+
+    def __init__(self, W, scale, ef, seed, mode):
+        self.W = W
+        flags = W.FLAG_GRAPH if mode == "graph" else 0
+        self.g = {
+            "bfs": W.Graph.rmat(scale, ef, seed),
+            "cc": W.Graph.rmat(scale, ef, seed, symmetrise=True),
+            "sssp": W.Graph.rmat(scale, ef, seed, weight_kind=W.WEIGHTS_U64),
+            "pr": W.Graph.rmat(scale, ef, seed),
+        }
+        self.V = self.g["bfs"].V
+        self.E = {a: self.g[a].E for a in APPS}
+        self.app = {"bfs": W.APP_BFS, "cc": W.APP_CC, "sssp": W.APP_SSSP, "pr": W.APP_PR}
+        t = WORKLOAD["threshold_pct"]
+        self.params = {}
+        for sched_name, sched in (("plain", W.SCHED_PLAIN), ("learned", W.SCHED_LEARNED)):
+            self.params[sched_name] = {
+                "bfs": W.Params(root=WORKLOAD["root"], threshold_pct=t, flags=flags, sched=sched),
+                "cc": W.Params(threshold_pct=t, flags=flags, sched=sched),
+                "sssp": W.Params(root=WORKLOAD["root"], threshold_pct=t, flags=flags, sched=sched),
+                "pr": W.Params(num_iterations=WORKLOAD["pr_iterations"], damping=WORKLOAD["damping"],
+                               precision=W.PREC_FP32C, flags=flags),
+            }
+
+    def edges(self, a):
+        """edges one run of application a processes (PageRank: per iteration)"""
+        return self.E[a] * (WORKLOAD["pr_iterations"] if a == "pr" else 1)
+
+    def step_edges(self):
+        return sum(self.edges(a) for a in APPS)
+
+    def run(self, a, sched="plain"):
+        return self.g[a].run(self.app[a], self.params[sched][a])
+
+    def close(self):
+        for g in self.g.values():
+            g.close()
+
+
+def _timed_steps(W, suite, sched, steps, warmup, dist):
+    """device time of `steps` four-application steps (CUDA events on the first and
+    last handles' streams; each run returns after its stream drained) and the
+    per-application device times from the runs' own events"""
+    import torch
+
+    for _ in range(warmup):
+        for a in APPS:
+            suite.run(a, sched)
+    torch.cuda.synchronize()
+    streams = {a: torch.cuda.ExternalStream(suite.g[a].stream) for a in APPS}
+    per_app = {a: 0.0 for a in APPS}
+    info = {a: {} for a in APPS}
+    launches = 0
+    dist.barrier()
+    torch.cuda.synchronize()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(streams[APPS[0]])
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        for a in APPS:
+            st = suite.run(a, sched)
+            per_app[a] += st["running_ms"]
+            launches += st["kernel_launches"]
+            info[a] = {"iterations": st["iterations"], "wedge_iterations": st["wedge_iterations"]}
+    e1.record(streams[APPS[-1]])
+    e1.synchronize()
+    torch.cuda.synchronize()
+    wall = time.perf_counter() - t0
+    dist.barrier()
+    return e0.elapsed_time(e1), per_app, info, launches, wall
+
+
+def _timed_records(W, suite, a):
+    """the per-iteration records of one run with per-pull CUDA events (WEDGE_FLAG_TIMING)"""
+    p = suite.params["plain"][a]
+    q = W.Params(root=p.root, threshold_pct=p.threshold_pct, num_iterations=p.num_iterations, damping=p.damping,
+                 precision=p.precision, flags=W.FLAG_TIMING)
+    st = suite.g[a].run(suite.app[a], q)
+    return st, suite.g[a].iteration_log()
+
+
+def _roofline(W, suite, peak):
+    """per application: algorithmic bytes of its pulls over their CUDA-event time"""
+    out = {}
+    V = suite.V
+    for a in APPS:
+        st, log = _timed_records(W, suite, a)
+        if a == "pr":
+            n = len(log)
+            ms = sum(r["pull_ms"] for r in log)
+            byts = pr_iteration_bytes(V, suite.E[a]) * n
+            out[a] = {"kernel": "pr32_pull_kernel (the pull with the fused vertex phase), per iteration",
+                      "iterations": n, "pull_ms": round(ms, 4), "vertex_ms": round(st["vertex_ms"], 4),
+                      "algorithmic_bytes": int(byts)}
+        else:
+            ms = sum(r["pull_ms"] for r in log)
+            byts = sum(pull_bytes(a, r, V) for r in log)
+            out[a] = {"kernel": "dst_kernel + pull_kernel" if a in ("bfs", "cc") else "pull_kernel",
+                      "iterations": len(log), "pull_ms": round(ms, 4), "algorithmic_bytes": int(byts),
+                      "modes": [r["mode"] for r in log], "edges_scanned": int(sum(r["edges_scanned"] for r in log))}
+        ach = byts / (ms / 1e3) / 1e9 if ms > 0 else 0.0
+        out[a].update({"achieved": round(ach, 1), "frac": round(ach / peak, 4)})
+    return out
+
+
+def _ncu_traffic(default_workload: bool):
+    """DRAM bytes per launch of the PageRank pull at this workload, scaled from the
+    committed ncu capture of a smaller case (profiles/), or None elsewhere"""
+    if not default_workload:
+        return None
+    try:
+        with open(os.path.join(ROOT, "profiles", "pr32_pull_traffic.json")) as f:
+            return json.load(f).get("traffic_bytes_per_launch_rmat26")
+    except Exception:
+        return None
+
+
 def run_ours(args, dist: Dist):
     if dist.world > 1:
         # one GPU per process, chosen before any CUDA call: the engine binds to the current device
         ids = [x for x in os.environ.get("CUDA_VISIBLE_DEVICES", "").split(",") if x.strip()]
         os.environ["CUDA_VISIBLE_DEVICES"] = ids[dist.local] if len(ids) > dist.local else str(dist.local)
     import ctypes
+
     import numpy as np
     import torch
 
     dist.init("nccl")
     torch.cuda.set_device(0)
     import wedge_gb300 as W
+    from wedge_gb300 import scheduler as S
 
     steps, warmup = args.steps, max(3, args.warmup)
     scale, ef = args.scale, args.edge_factor
-    gb = W.Graph.rmat(scale, ef, WORKLOAD["seed"], symmetrise=False)
-    gc = W.Graph.rmat(scale, ef, WORKLOAD["seed"], symmetrise=True)
-    V, E_bfs, E_cc = gb.V, gb.E, gc.E
-    flags = W.FLAG_GRAPH if args.mode == "graph" else 0
-    p_bfs = W.Params(root=WORKLOAD["bfs_root"], threshold_pct=WORKLOAD["threshold_pct"], flags=flags)
-    p_cc = W.Params(threshold_pct=WORKLOAD["threshold_pct"], flags=flags)
-    try:  # events on the engine's own streams; each run returns after its stream drained
-        s_bfs = torch.cuda.ExternalStream(gb.stream)
-        s_cc = torch.cuda.ExternalStream(gc.stream)
-    except Exception:
-        s_bfs = s_cc = torch.cuda.current_stream()
+    default_workload = (scale, ef) == (WORKLOAD["scale"], WORKLOAD["edge_factor"])
+    suite = Suite(W, scale, ef, WORKLOAD["seed"], args.mode)
+    V = suite.V
+    try:
+        blob = S.load()
+        for a in ("bfs", "cc", "sssp"):
+            suite.g[a].set_scheduler(blob)
+    except Exception as e:  # no trained network: the learned arm reports it
+        blob = None
+        blob_err = str(e)
 
-    def step(counts):
-        a = gb.run(W.APP_BFS, p_bfs)
-        b = gc.run(W.APP_CC, p_cc)
-        counts["launches"] += a["kernel_launches"] + b["kernel_launches"]
-        counts["iters_bfs"] = a["iterations"]
-        counts["iters_cc"] = b["iterations"]
-        counts["wedge_bfs"] = a["wedge_iterations"]
-        counts["wedge_cc"] = b["wedge_iterations"]
-
-    counts = {"launches": 0}
-    for _ in range(warmup):
-        step(counts)
-    torch.cuda.synchronize()
-
-    # ---- device-timed region: inputs resident in HBM
+    # ---- device-timed region: graphs resident in HBM
     sampler = ClockSampler(visible_index(dist.local))
     sampler.start()
-    counts = {"launches": 0}
-    dist.barrier()
-    torch.cuda.synchronize()
-    e0 = torch.cuda.Event(enable_timing=True)
-    e1 = torch.cuda.Event(enable_timing=True)
-    e0.record(s_bfs)
-    t0 = time.perf_counter()
-    for _ in range(steps):
-        step(counts)
-    e1.record(s_cc)
-    e1.synchronize()
-    torch.cuda.synchronize()
-    wall = time.perf_counter() - t0
-    dist.barrier()
+    dev_ms, per_app_ms, info, launches, wall = _timed_steps(W, suite, "plain", steps, warmup, dist)
     clocks = sampler.stop()
-    dev_ms = e0.elapsed_time(e1)
     t_max = dist.max(dev_ms / 1e3)
-    edges_step = E_bfs + E_cc
-    value = dist.world * steps * edges_step / t_max / 1e9
+    value = dist.world * steps * suite.step_edges() / t_max / 1e9
+    per_app = {}
+    for a in APPS:
+        gteps = steps * suite.edges(a) / (per_app_ms[a] / 1e3) / 1e9 if per_app_ms[a] > 0 else None
+        per_app[a] = {"gteps": round(gteps, 2), "ms_per_run": round(per_app_ms[a] / steps, 4),
+                      "edges": suite.E[a], **info[a]}
+    per_app["pr"].update({"precision": "fp32 compensated (two-sum), fp64 total rank",
+                          "iterations": WORKLOAD["pr_iterations"], "damping": WORKLOAD["damping"]})
 
     # ---- the same steps under the learned scheduler (on-device network, plain-rule fallback)
-    learned = _learned_arm(W, gb, gc, p_bfs, p_cc, steps, warmup, s_bfs, s_cc, edges_step, dist, value)
+    if blob is not None:
+        l_ms, l_app_ms, l_info, _, _ = _timed_steps(W, suite, "learned", steps, warmup, dist)
+        l_value = dist.world * steps * suite.step_edges() / dist.max(l_ms / 1e3) / 1e9
+        learned = {"value": round(l_value, 4), "unit": "GTEPS", "ms_per_step": round(l_ms / steps, 4),
+                   "ratio_vs_plain": round(l_value / value, 4), "network": "wedge_gb300/data/sched_net.f32",
+                   "per_app": {}}
+        for a in APPS:
+            lg = steps * suite.edges(a) / (l_app_ms[a] / 1e3) / 1e9
+            learned["per_app"][a] = {"gteps": round(lg, 2), "ratio_vs_plain": round(lg / per_app[a]["gteps"], 4),
+                                     **l_info[a]}
+        learned["per_app"]["pr"]["note"] = "no schedule choice: every PageRank iteration is a dense pull"
+    else:
+        learned = {"unavailable": f"no scheduler network: {blob_err}"}
 
     # ---- end to end through the C ABI with host buffers: query parameters in,
     # full property arrays (8 bytes per vertex, graph_vertex_props) out, every step
-    host_bfs = torch.empty(V, dtype=torch.int64, pin_memory=True).numpy().view(np.uint64)
-    host_cc = torch.empty(V, dtype=torch.int64, pin_memory=True).numpy().view(np.uint64)
-    e2e_steps = max(3, min(steps, 20))
+    host = {a: torch.empty(V, dtype=torch.int64, pin_memory=True).numpy().view(np.uint64) for a in APPS}
+    e2e_steps = max(3, min(steps, 10))
     dist.barrier()
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     for _ in range(e2e_steps):
-        gb.run(W.APP_BFS, p_bfs)
-        gb.read_results(host_bfs)
-        gc.run(W.APP_CC, p_cc)
-        gc.read_results(host_cc)
+        for a in APPS:
+            suite.run(a)
+            suite.g[a].read_results(host[a])
     e2e_wall = dist.max(time.perf_counter() - t0)
-    e2e_value = dist.world * e2e_steps * edges_step / e2e_wall / 1e9
-    params_bytes = 2 * ctypes.sizeof(W.Params)  # each query's wedge_params_t, carried to the device in kernel arguments
+    e2e_value = dist.world * e2e_steps * suite.step_edges() / e2e_wall / 1e9
+    params_bytes = len(APPS) * ctypes.sizeof(W.Params)  # each query's wedge_params_t, in kernel arguments
 
-    # ---- roofline of the dominant kernel (the edge pull), per launch, timed with CUDA events
-    rec_b = _timed_records(W, gb, W.APP_BFS, p_bfs)
-    rec_c = _timed_records(W, gc, W.APP_CC, p_cc)
+    # ---- roofline of the dominant kernel (the PageRank pull) and of every application's pulls
     peak, peak_kind = measured_peaks()
-    Vne_b = Vne_c = V  # visited-bitmap term bounded by |V|/8
-    pull_ms = sum(r["pull_ms"] for r in rec_b + rec_c)
-    pull_bytes_tot = sum(pull_bytes("bfs", r, V, Vne_b) for r in rec_b) + \
-        sum(pull_bytes("cc", r, V, Vne_c) for r in rec_c)
-    n_launch = len(rec_b) + len(rec_c)
-    achieved = pull_bytes_tot / (pull_ms / 1e3) / 1e9 if pull_ms > 0 else 0.0
-    dense = [r for r in rec_b + rec_c if not r["used_wedge"]]
-    dense_ms = sum(r["pull_ms"] for r in dense)
-    dense_bytes = sum(pull_bytes("bfs", r, V, Vne_b) for r in rec_b if not r["used_wedge"]) + \
-        sum(pull_bytes("cc", r, V, Vne_c) for r in rec_c if not r["used_wedge"])
-    traffic = _ncu_traffic()
-
+    roof = _roofline(W, suite, peak)
+    pr_roof = roof["pr"]
     line = {
-        "metric": "GTEPS per app at 1 GB300 (BFS + CC, plain fixed-threshold schedule)",
+        "metric": "GTEPS per app at 1 GB300 (BFS + CC + SSSP + 30-iteration PageRank, plain fixed-threshold "
+                  "schedule; learned-scheduled beside it)",
         "value": round(value, 4),
         "unit": "GTEPS",
         "n_gpus": dist.world,
@@ -277,134 +392,206 @@ def run_ours(args, dist: Dist):
         "higher_is_better": True,
         "scaling": "weak",
         "vs_baseline": None,
-        "dtype": "u32",
+        "dtype": "u32/u64 (BFS, CC, SSSP), fp32 compensated (PageRank)",
         "data": "synthetic (device R-MAT, counter-based generator; no dataset)",
         "config": {"workload": workload_name(scale, ef), "scale": scale, "edge_factor": ef, "seed": WORKLOAD["seed"],
-                   "vertices": V, "edges_bfs": E_bfs, "edges_cc": E_cc, "bfs_root": WORKLOAD["bfs_root"],
-                   "threshold_pct": WORKLOAD["threshold_pct"], "loop": args.mode,
-                   "l2": "inputs larger than L2 (sources 1 GiB / 2 GiB vs 126 MB L2); no flush",
+                   "vertices": V, "edges": suite.E["bfs"], "edges_sym": suite.E["cc"], "root": WORKLOAD["root"],
+                   "threshold_pct": WORKLOAD["threshold_pct"], "pr_iterations": WORKLOAD["pr_iterations"],
+                   "damping": WORKLOAD["damping"], "loop": args.mode,
+                   "l2": f"inputs larger than L2 (in-edge sources {4 * suite.E['bfs'] / 2**30:.1f} GiB / "
+                         f"{4 * suite.E['cc'] / 2**30:.1f} GiB vs 126 MB L2); no flush",
                    "parallelism": "replicas" if dist.world > 1 else "single GPU"},
-        "per_app": {
-            "bfs": {"iterations": counts.get("iters_bfs"), "wedge_iterations": counts.get("wedge_bfs")},
-            "cc": {"iterations": counts.get("iters_cc"), "wedge_iterations": counts.get("wedge_cc")},
-        },
+        "per_app": per_app,
         "e2e": {"value": round(e2e_value, 4), "unit": "GTEPS", "h2d_bytes_per_step": params_bytes,
-                "d2h_bytes_per_step": 2 * 8 * V, "steps": e2e_steps,
-                "what": "wedge_cuda_run + wedge_cuda_read_results per app into pinned host memory; "
-                        "graph resident (loaded once, as the reference excludes load from Running Time)"},
-        "roofline": {"bound": "hbm", "kernel": "edge pull: dst_kernel + pull_kernel (BFS + CC, all iterations)",
-                     "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
-                     "frac": round(achieved / peak, 4), "peak_source": peak_kind,
-                     "traffic": traffic,
-                     "traffic_scope": "achieved, algorithmic_bytes and traffic are per step: all pull launches of "
-                                      "one BFS + one CC traversal (traffic: ncu DRAM bytes, profiles/)",
-                     "pull_iterations": n_launch,
-                     "algorithmic_bytes": int(pull_bytes_tot), "pull_ms": round(pull_ms, 4),
-                     "dense_only": {"achieved": round(dense_bytes / (dense_ms / 1e3) / 1e9, 1) if dense_ms else None,
-                                    "frac": round(dense_bytes / (dense_ms / 1e3) / 1e9 / peak, 4) if dense_ms else None,
-                                    "pull_iterations": len(dense)}},
+                "d2h_bytes_per_step": len(APPS) * 8 * V, "steps": e2e_steps,
+                "what": "wedge_cuda_run + wedge_cuda_read_results per application into pinned host memory; graphs "
+                        "resident (loaded once, as the reference excludes load from Running Time)"},
+        "roofline": {"bound": "hbm", "kernel": pr_roof["kernel"], "achieved": pr_roof["achieved"], "peak": peak,
+                     "unit": "GB/s", "frac": pr_roof["frac"], "peak_source": peak_kind,
+                     "traffic": _ncu_traffic(default_workload),
+                     "traffic_scope": "per launch (one PageRank iteration's pull): ncu DRAM bytes of the scale-22 "
+                                      "capture in profiles/ scaled by edges to scale 26",
+                     "algorithmic_bytes_per_launch": int(pr_roof["algorithmic_bytes"] / max(1, pr_roof["iterations"])),
+                     "launch_ms": round(pr_roof["pull_ms"] / max(1, pr_roof["iterations"]), 4),
+                     "per_app": roof},
         "learned": learned,
         "clocks": clocks,
-        "gpu_launches": int(counts["launches"]),
+        "gpu_launches": int(launches),
         "wall_s_timed": round(wall, 4),
     }
+    suite.close()
+    if not args.no_sub and dist.world == 1:
+        line["sub"] = sub_records(W, S, blob, args, peak)
     if dist.rank == 0 and dist.world == 1 and not args.no_cpu_baseline:
-        line["cpu_baseline"] = cpu_baseline(scale, ef)
-    gb.close()
-    gc.close()
+        line["cpu_baseline"] = cpu_baseline(scale, ef, pr32=host["pr"].view(np.float64))
     if dist.rank == 0:
         print(json.dumps(line), flush=True)
     dist.done()
 
 
-def _learned_arm(W, gb, gc, p_bfs, p_cc, steps, warmup, s_bfs, s_cc, edges_step, dist, plain_value):
-    """GTEPS of the same workload with WEDGE_SCHED_LEARNED and the committed network"""
-    import torch
-    from wedge_gb300 import scheduler as S
+# ---------------------------------------------------------------- sub-records (other configurations)
+def _event_ms(g, fn, reps):
+    """median of the runs' own device times (Running Time, CUDA events)"""
+    import numpy as np
 
-    try:
-        blob = S.load()
-    except Exception as e:  # no trained network: report it, do not guess
-        return {"unavailable": f"no scheduler network: {e}"}
-    gb.set_scheduler(blob)
-    gc.set_scheduler(blob)
-    lb = W.Params(root=p_bfs.root, threshold_pct=p_bfs.threshold_pct, flags=p_bfs.flags, sched=W.SCHED_LEARNED)
-    lc = W.Params(threshold_pct=p_cc.threshold_pct, flags=p_cc.flags, sched=W.SCHED_LEARNED)
-    for _ in range(warmup):
-        gb.run(W.APP_BFS, lb)
-        gc.run(W.APP_CC, lc)
-    dist.barrier()
-    torch.cuda.synchronize()
-    e0 = torch.cuda.Event(enable_timing=True)
-    e1 = torch.cuda.Event(enable_timing=True)
-    e0.record(s_bfs)
-    for _ in range(steps):
-        gb.run(W.APP_BFS, lb)
-        gc.run(W.APP_CC, lc)
-    e1.record(s_cc)
-    e1.synchronize()
-    t = dist.max(e0.elapsed_time(e1) / 1e3)
-    # which iterations the network changed (one timed-free run per app)
-    changed = {}
-    for name, g, app, p in (("bfs", gb, W.APP_BFS, lb), ("cc", gc, W.APP_CC, lc)):
-        g.run(app, p)
+    fn()
+    ts = [fn()["running_ms"] for _ in range(reps)]
+    return float(np.median(ts))
+
+
+def sub_records(W, S, blob, args, peak):
+    import numpy as np
+
+    out = {}
+    reps = 5
+    # C2: BFS + CC on R-MAT scale 24 (seed 2), plain and learned
+    gb = W.Graph.rmat(24, 16, 2)
+    gc = W.Graph.rmat(24, 16, 2, symmetrise=True)
+    rec = {"workload": "rmat24_bfs_cc", "vertices": gb.V, "edges_bfs": gb.E, "edges_cc": gc.E}
+    for name, sched in (("plain", W.SCHED_PLAIN), ("learned", W.SCHED_LEARNED)):
+        if sched == W.SCHED_LEARNED:
+            if blob is None:
+                continue
+            gb.set_scheduler(blob)
+            gc.set_scheduler(blob)
+        tb = _event_ms(gb, lambda: gb.run(W.APP_BFS, W.Params(root=0, sched=sched, flags=W.FLAG_GRAPH)), reps)
+        tc = _event_ms(gc, lambda: gc.run(W.APP_CC, W.Params(sched=sched, flags=W.FLAG_GRAPH)), reps)
+        rec[name] = {"gteps": round((gb.E + gc.E) / ((tb + tc) / 1e3) / 1e9, 2), "bfs_ms": round(tb, 4),
+                     "cc_ms": round(tc, 4)}
+    if "learned" in rec:
+        rec["learned"]["ratio_vs_plain"] = round(rec["learned"]["gteps"] / rec["plain"]["gteps"], 4)
+    gb.close()
+    gc.close()
+    out["C2"] = rec
+    # C1: PageRank FP64, R-MAT scale 16 (seed 1), 16 iterations, damping 0.85
+    g = W.Graph.rmat(16, 16, 1)
+    t = _event_ms(g, lambda: g.run(W.APP_PR, W.Params(num_iterations=16, damping=0.85, flags=W.FLAG_GRAPH)), reps)
+    out["C1"] = {"workload": "rmat16_pr_fp64", "vertices": g.V, "edges": g.E, "iterations": 16, "ms": round(t, 4),
+                 "gteps": round(16 * g.E / (t / 1e3) / 1e9, 2),
+                 "note": "the 4 MB graph stays in L2; launch-bound"}
+    g.close()
+    # C3: SSSP from vertex 0 on the 4096^2 grid with 1% long-range edges (seed 3), uint64 and FP64 weights
+    for kind, wk in (("u64", W.WEIGHTS_U64), ("f64", W.WEIGHTS_F64)):
+        g = W.Graph.grid(4096, 0.01, 3, wk)
+        t = _event_ms(g, lambda: g.run(W.APP_SSSP, W.Params(root=0, flags=W.FLAG_GRAPH)), 3)
+        st = g.run(W.APP_SSSP, W.Params(root=0, flags=W.FLAG_TIMING))
         log = g.iteration_log()
-        changed[name] = {"iterations": len(log), "chosen_by_network": sum(r["learned"] for r in log),
-                         "modes": [r["mode"] for r in log]}
-    value = dist.world * steps * edges_step / t / 1e9
-    return {"value": round(value, 4), "unit": "GTEPS", "ms_per_step": round(t * 1e3 / steps, 4),
-            "ratio_vs_plain": round(value / plain_value, 4), "network": "wedge_gb300/data/sched_net.f32",
-            "per_app": changed}
+        ms = sum(r["pull_ms"] for r in log)
+        byts = sum(pull_bytes("sssp", r, g.V, 1 if kind == "u64" else 8) for r in log)
+        out[f"C3_{kind}"] = {"workload": f"grid4096_sssp_{kind}", "vertices": g.V, "edges": g.E, "ms": round(t, 4),
+                             "gteps": round(g.E / (t / 1e3) / 1e9, 2), "iterations": st["iterations"],
+                             "wedge_iterations": st["wedge_iterations"],
+                             "roofline": {"pull_ms": round(ms, 4), "algorithmic_bytes": int(byts),
+                                          "frac": round(byts / (ms / 1e3) / 1e9 / peak, 4) if ms > 0 else None}}
+        g.close()
+    # C4: 256 BFS + 256 SSSP over 64 graphs in one persistent kernel, against one query at a time
+    out["C4"] = _batch_record(W)
+    return out
 
 
-def _timed_records(W, g, app, p):
-    q = W.Params(root=p.root, threshold_pct=p.threshold_pct, flags=W.FLAG_TIMING)
-    g.run(app, q)
-    return g.iteration_log()
+def _batch_record(W):
+    import json as _json
 
+    import numpy as np
+    from wedge_gb300 import batch as B
 
-def _ncu_traffic():
-    """DRAM bytes of one step's pull launches (ncu, full-size workload, one pass), if the
-    committed profile summary holds them"""
-    path = os.path.join(ROOT, "profiles", "pull_kernel_traffic.json")
+    params = B.graph_params()
+    queries = B.queries(params)
+    graphs = B.load_graphs(params)
+    tuning = None
     try:
-        with open(path) as f:
-            return json.load(f).get("traffic_bytes_per_step")
+        with open(os.path.join(ROOT, "wedge_gb300", "data", "batch_tuning.json")) as f:
+            best = _json.load(f)["best"]
+        tuning = W.BatchTuning(best["threshold_pct"], best["grab"], best["blocks_per_sm"], best["split"])
     except Exception:
-        return None
+        pass
+    with W.Batch(graphs, queries) as b:
+        b.run(tuning, W.FLAG_GRAPH)
+        ts = [b.run(tuning, W.FLAG_GRAPH)["running_ms"] for _ in range(3)]
+        t0 = time.perf_counter()
+        b.run(tuning, W.FLAG_GRAPH)
+        bwall = (time.perf_counter() - t0) * 1e3
+    # one query at a time through wedge_cuda_run's graph loop (BFS queries of a graph, then its SSSP queries)
+    seq_dev = 0.0
+    t0 = time.perf_counter()
+    for gi, g in enumerate(graphs):
+        for app in (W.APP_BFS, W.APP_SSSP):
+            for (qg, qa, root) in queries:
+                if qg == gi and qa == app:
+                    seq_dev += g.run(app, W.Params(root=root, flags=W.FLAG_GRAPH))["running_ms"]
+    seq_wall = (time.perf_counter() - t0) * 1e3
+    edges = sum(g.E for g in graphs)
+    qedges = sum(graphs[qg].E for (qg, _a, _r) in queries)
+    for g in graphs:
+        g.close()
+    dev = float(np.median(ts))
+    return {"workload": "batch64_bfs256_sssp256", "graphs": len(graphs), "queries": len(queries),
+            "edges_resident": edges, "batch_ms": round(dev, 3), "batch_wall_ms": round(bwall, 3),
+            "sequential_ms": round(seq_dev, 3), "sequential_wall_ms": round(seq_wall, 3),
+            "speedup_device": round(seq_dev / dev, 3), "speedup_wall": round(seq_wall / bwall, 3),
+            "gteps": round(qedges / (dev / 1e3) / 1e9, 2)}
 
 
 # ---------------------------------------------------------------- CPU legs (oracle)
-def _cpu_graphs(scale, ef, threads):
+def _cpu_suite(scale, ef, threads):
+    """the oracle's graphs for the four applications (the same generator as the device's)"""
     from oracle import oracle as O
 
     V, s, d = O.rmat(scale, ef, WORKLOAD["seed"], threads=threads)
-    sb, db = O.sort_edges(V, s, d, threads=threads)
+    sd, dd = O.sort_edges(V, s, d, threads=threads)
     ss, ds = O.sort_edges(V, *O.symmetrise(s, d), threads=threads)
     del s, d
-    gb = O.Graph.from_edges(V, sb, db, O.BFS)
-    E_b = len(sb)
-    del sb, db
-    gc = O.Graph.from_edges(V, ss, ds, O.CC)
-    E_c = len(ss)
-    return O, gb, gc, V, E_b, E_c
+    w = O.weights(sd, dd)
+    g = {"bfs": O.Graph.from_edges(V, sd, dd, O.BFS, threads=threads),
+         "sssp": O.Graph.from_edges(V, sd, dd, O.SSSP, w, threads=threads),
+         "pr": O.Graph.from_edges(V, sd, dd, O.PR, threads=threads)}
+    E = {"bfs": len(sd), "sssp": len(sd), "pr": len(sd)}
+    del sd, dd, w
+    g["cc"] = O.Graph.from_edges(V, ss, ds, O.CC, threads=threads)
+    E["cc"] = len(ss)
+    return O, g, V, E
 
 
-def cpu_baseline(scale, ef):
-    """the oracle's restatement of the reference on this host's cores: one BFS + one CC"""
+def _cpu_run(g, a, threads, pr_iterations):
+    if a == "bfs":
+        return g.run(root=WORKLOAD["root"], threshold_pct=WORKLOAD["threshold_pct"], threads=threads)
+    if a == "cc":
+        return g.run(threshold_pct=WORKLOAD["threshold_pct"], threads=threads)
+    if a == "sssp":
+        return g.run(root=WORKLOAD["root"], threshold_pct=WORKLOAD["threshold_pct"], threads=threads)
+    return g.run(iterations=pr_iterations, damping=WORKLOAD["damping"], threads=threads)
+
+
+def cpu_baseline(scale, ef, pr32=None):
+    """the oracle's restatement of the reference on this host's cores: one run of
+    each application on the same graphs (PageRank all 30 iterations); the FP64
+    PageRank ranks also give the error of the GPU's compensated-FP32 ranks"""
+    import numpy as np
     from oracle import oracle as O
 
     O.build()
     threads = O.lib().orc_online_cores()
-    O, gb, gc, V, E_b, E_c = _cpu_graphs(scale, ef, threads)
-    _, _, sb = gb.run(root=WORKLOAD["bfs_root"], threshold_pct=WORKLOAD["threshold_pct"], threads=threads)
-    _, _, sc = gc.run(threshold_pct=WORKLOAD["threshold_pct"], threads=threads)
-    secs = (sb["running_ms"] + sc["running_ms"]) / 1e3
-    return {"value": round((E_b + E_c) / secs / 1e9, 4), "unit": "GTEPS", "cores": threads, "kind": "port",
-            "sample": f"one BFS (root 0) + one CC traversal of the same R-MAT scale-{scale} graphs; "
-                      f"timed as the reference's Running Time (pull + Wedge phases, load excluded)",
-            "bfs_ms": round(sb["running_ms"], 3), "cc_ms": round(sc["running_ms"], 3),
-            "bfs_iterations": sb["iterations"], "cc_iterations": sc["iterations"]}
+    O, g, V, E = _cpu_suite(scale, ef, threads)
+    ms = {}
+    pr_err = None
+    for a in APPS:
+        props, _, st = _cpu_run(g[a], a, threads, WORKLOAD["pr_iterations"])
+        ms[a] = st["running_ms"]
+        if a == "pr" and pr32 is not None and len(pr32) == V:
+            ref = props.view(np.float64)
+            pr_err = {"rel_l1": float(np.abs(pr32 - ref).sum() / np.abs(ref).sum()),
+                      "max_rel": float(np.max(np.abs(pr32 - ref) / np.abs(ref))),
+                      "what": "GPU compensated-FP32 ranks (the e2e arm's last read) against the oracle's FP64 ranks"}
+        g[a].close()
+    edges = sum(E[a] * (WORKLOAD["pr_iterations"] if a == "pr" else 1) for a in APPS)
+    secs = sum(ms.values()) / 1e3
+    return {"value": round(edges / secs / 1e9, 4), "unit": "GTEPS", "cores": threads, "kind": "port",
+            "sample": f"one run of each application on the same R-MAT scale-{scale} graphs (PageRank 30 iterations, "
+                      f"FP64); timed as the reference's Running Time (pull, vertex and Wedge phases, load excluded)",
+            "ms": {a: round(ms[a], 3) for a in APPS},
+            "per_app_gteps": {a: round(E[a] * (WORKLOAD["pr_iterations"] if a == "pr" else 1) / (ms[a] / 1e3) / 1e9, 4)
+                              for a in APPS},
+            "pr_error_vs_fp64_oracle": pr_err}
 
 
 def run_reference(args, dist: Dist):
@@ -415,35 +602,53 @@ def run_reference(args, dist: Dist):
     O.build()
     threads = O.lib().orc_online_cores()
     scale, ef = args.scale, args.edge_factor
-    O, gb, gc, V, E_b, E_c = _cpu_graphs(scale, ef, threads)
+    O, g, V, E = _cpu_suite(scale, ef, threads)
     warmup = max(3, args.warmup)
     steps = args.steps
-    # each step is one BFS + one CC traversal; the step count is capped so the run stays within minutes
-    steps = min(steps, 10)
-    warmup = min(warmup, 3)
+    # Each step is one BFS, CC and SSSP traversal and a bounded sample of the
+    # PageRank run: PR_SAMPLE of its 30 iterations, whose time is scaled to 30
+    # (every iteration is the same dense pull and vertex phase).
+    pr_sample = 2
+    scale_pr = WORKLOAD["pr_iterations"] / pr_sample
 
     def step():
-        _, _, sb = gb.run(root=WORKLOAD["bfs_root"], threshold_pct=WORKLOAD["threshold_pct"], threads=threads)
-        _, _, sc = gc.run(threshold_pct=WORKLOAD["threshold_pct"], threads=threads)
-        return (sb["running_ms"] + sc["running_ms"]) / 1e3
+        t = {}
+        for a in APPS:
+            _, _, st = _cpu_run(g[a], a, threads, pr_sample)
+            t[a] = st["running_ms"] / 1e3 * (scale_pr if a == "pr" else 1.0)
+        return t
 
     for _ in range(warmup):
         step()
-    t = sum(step() for _ in range(steps))
-    value = steps * (E_b + E_c) / t / 1e9
+    tot = {a: 0.0 for a in APPS}
+    for _ in range(steps):
+        for a, x in step().items():
+            tot[a] += x
+    t = sum(tot.values())
+    edges = sum(E[a] * (WORKLOAD["pr_iterations"] if a == "pr" else 1) for a in APPS)
+    value = steps * edges / t / 1e9
     line = {
         "impl": "reference",
-        "metric": "GTEPS per app at 1 GB300 (BFS + CC, plain fixed-threshold schedule)",
+        "metric": "GTEPS per app at 1 GB300 (BFS + CC + SSSP + 30-iteration PageRank, plain fixed-threshold "
+                  "schedule; learned-scheduled beside it)",
         "value": round(value, 4), "unit": "GTEPS", "n_gpus": args.gpus, "steps": steps, "warmup": warmup,
         "ms_per_step": round(t * 1e3 / steps, 3), "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": "u32", "data": "synthetic (CPU R-MAT, same generator as the GPU arm)",
+        "vs_baseline": None, "dtype": "u64 (BFS, SSSP), fp64 (CC labels, PageRank)",
+        "data": "synthetic (CPU R-MAT, same generator as the GPU arm)",
         "config": {"workload": workload_name(scale, ef), "scale": scale, "edge_factor": ef, "seed": WORKLOAD["seed"],
-                   "vertices": V, "edges_bfs": E_b, "edges_cc": E_c, "threads": threads},
+                   "vertices": V, "edges": E["bfs"], "edges_sym": E["cc"], "root": WORKLOAD["root"],
+                   "threshold_pct": WORKLOAD["threshold_pct"], "pr_iterations": WORKLOAD["pr_iterations"],
+                   "damping": WORKLOAD["damping"], "threads": threads},
+        "per_app": {a: {"gteps": round(steps * E[a] * (WORKLOAD["pr_iterations"] if a == "pr" else 1) / tot[a] / 1e9, 4),
+                        "ms_per_run": round(tot[a] * 1e3 / steps, 3)} for a in APPS},
         "cpu_baseline": {"value": round(value, 4), "unit": "GTEPS", "cores": threads, "kind": "port",
-                         "sample": f"{steps} steps of one BFS + one CC on the full scale-{scale} graphs "
-                                   f"(the AVX2 reference does not compile on this Arm host)"},
+                         "sample": f"{steps} steps of one BFS, CC and SSSP traversal and {pr_sample} PageRank "
+                                   f"iterations (time scaled to 30) on the full scale-{scale} graphs (the AVX2 "
+                                   f"reference does not compile on this Arm host)"},
         "e2e": {"value": round(value, 4), "unit": "GTEPS", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
+    for x in g.values():
+        x.close()
     print(json.dumps(line), flush=True)
 
 

@@ -47,7 +47,8 @@ def build(quiet: bool = True) -> None:
 
 def build_ref(quiet: bool = True) -> bool:
     """Compile the reference from its own sources (x86-64 + AVX2 hosts only)."""
-    ref = os.environ.get("WEDGE_REFERENCE_DIR", "/root/reference")
+    # WEDGE_REFERENCE_DIR, else the reference checkout beside this repository
+    ref = os.environ.get("WEDGE_REFERENCE_DIR", os.path.join(os.path.dirname(os.path.dirname(HERE)), "reference"))
     if not os.path.isdir(os.path.join(ref, "source")):
         return False
     r = subprocess.run(["make", "-C", HERE, "ref", f"REF={ref}"],

@@ -3,7 +3,7 @@ against the oracle on the same seeded inputs):
 
 - PageRank, R-MAT scale 16 (65,536 vertices, 1,048,576 edges, seed 1),
   16 iterations, damping 0.85: FP64 within 1e-12 relative L1 of the oracle;
-  compensated FP32 within 1e-6 of FP64.
+  compensated FP32 within 1e-6 relative L1 of the FP64 oracle.
 - BFS from vertex 0 and CC, R-MAT scale 24 (16,777,216 vertices, 268,435,456
   edges, seed 2; CC symmetrised): CC labels bit-exact, BFS levels exact and
   every parent an in-neighbour one level up.
@@ -11,7 +11,8 @@ against the oracle on the same seeded inputs):
   3): uint64 weights bit-exact, FP64 weights 0 ULP.
 - R-MAT scale 26 (67,108,864 vertices, 1,073,741,824 edges, seed 5): BFS,
   CC, SSSP bit-exact under the plain and the learned schedule, 30-iteration
-  compensated FP32 PageRank within 1e-6 relative L1 of FP64.
+  compensated FP32 PageRank (damping 0.85) within 1e-6 relative L1 of the
+  FP64 oracle, every vertex within 2e-5 relative of it.
 
 The GPU side generates each graph on the device; the device generators are
 bit-identical to the oracle's (test_gpu_parity.py checks them edge for edge).
@@ -26,7 +27,8 @@ from helpers import check_bfs_sorted, levels_from_parents, rel_l1
 pytestmark = pytest.mark.gpu
 THREADS = os.cpu_count() or 8
 PR_TOL = 1e-12
-PR32_TOL = 1e-6
+PR32_TOL = 1e-6      # relative L1 of compensated FP32 against the FP64 oracle
+PR32_MAXREL = 2e-5   # largest per-vertex relative difference
 
 
 @pytest.fixture(scope="module")
@@ -58,7 +60,13 @@ def test_pagerank_rmat16(W, O):
         got32 = g.read_results().view(np.float64)
     assert rel_l1(got, ref.view(np.float64)) < PR_TOL
     assert abs(st["pr_sum"] - 1.0) < 1e-9
-    assert rel_l1(got32, got) < PR32_TOL
+    _pr32_close(got32, ref.view(np.float64))
+
+
+def _pr32_close(got32, ref64):
+    err = rel_l1(got32, ref64)
+    maxrel = float(np.max(np.abs(got32 - ref64) / np.abs(ref64)))
+    assert err < PR32_TOL and maxrel < PR32_MAXREL, (err, maxrel)
 
 
 def test_bfs_cc_rmat24(W, O):
@@ -112,12 +120,12 @@ def test_rmat26_all_apps(W, O):
             assert np.array_equal(g.read_results(), sssp_ref)
             g.run(W.APP_BFS, W.Params(root=0, sched=sched, flags=W.FLAG_GRAPH))
             check_bfs_sorted(g.read_results(), V, s, d, 0, levels)
-        g.run(W.APP_PR, W.Params(num_iterations=30))
-        pr64 = g.read_results().view(np.float64).copy()
-        g.run(W.APP_PR, W.Params(num_iterations=30, precision=W.PREC_FP32C))
+        g.run(W.APP_PR, W.Params(num_iterations=30, damping=0.85, precision=W.PREC_FP32C, flags=W.FLAG_GRAPH))
         pr32 = g.read_results().view(np.float64).copy()
-    assert rel_l1(pr32, pr64) < PR32_TOL
-    del s, d, sssp_ref
+    del sssp_ref
+    pr_ref, _, _ = O.Graph.from_edges(V, s, d, O.PR, threads=THREADS).run(iterations=30, damping=0.85, threads=THREADS)
+    _pr32_close(pr32, pr_ref.view(np.float64))
+    del s, d, pr_ref
     Vs, ss, ds = _rmat_cpu(O, 26, 16, 5, symmetric=True)
     cc_ref, _, _ = O.Graph.from_edges(Vs, ss, ds, O.CC, threads=THREADS).run(threads=THREADS)
     del ss, ds

@@ -5,7 +5,8 @@ ABI of ``include/wedge_cuda.h``); this package is its ctypes front end.
 Build with ``wedge_gb300.build.build_all()``.
 """
 from .engine import (APP_BFS, APP_CC, APP_PR, APP_SSSP, FLAG_GRAPH, FLAG_TIMING, MODE_DENSE,  # noqa: F401
-                     MODE_FILTERED, MODE_WEDGE, PREC_FP32C, PREC_FP64, SCHED_BLOB, SCHED_DENSE, SCHED_FEATURES,
+                     MODE_FILTERED, MODE_WEDGE, PHASE_ADVANCE, PHASE_INIT, PHASE_PULL_DENSE, PHASE_PULL_WEDGE,
+                     PHASE_VERTEX_PR, PHASE_WEDGE_BUILD, PREC_FP32C, PREC_FP64, SCHED_BLOB, SCHED_DENSE, SCHED_FEATURES,
                      SCHED_FILTERED, SCHED_LEARNED, SCHED_PARAMS, SCHED_PLAIN, SCHED_PROBE, SCHED_WEDGE, WEIGHTS_F64,
                      WEIGHTS_NONE, WEIGHTS_U64, Batch, BatchTuning, Graph, Params, Query, WedgeError, application_select, lib, mlp_forward,
                      mlp_loss_grad, mlp_train, prop_string, status_string)

@@ -220,12 +220,12 @@ __global__ void dst_start_kernel(const unsigned long long* dst_off, uint32_t num
 // the longer ones from the back (count[1]; entry cap-1-j).  Every split holds a
 // distinct tile boundary, so the two ends never meet in lists of T entries.
 constexpr uint32_t SPLIT_SERIAL = 8;
-__global__ void split_kernel(const unsigned long long* dst_off, uint32_t Vne, uint32_t cap, uint32_t* split_k,
+__global__ void split_kernel(const unsigned long long* dst_off, uint32_t Vne, uint32_t cap, uint32_t tile, uint32_t* split_k,
                              uint32_t* split_t0, uint32_t* split_t1, unsigned int* count)
 {
     for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < Vne; k += gridDim.x * blockDim.x) {
-        const uint32_t t0 = (uint32_t)(dst_off[k] / TILE);
-        const uint32_t t1 = (uint32_t)((dst_off[k + 1] - 1) / TILE);
+        const uint32_t t0 = (uint32_t)(dst_off[k] / tile);
+        const uint32_t t1 = (uint32_t)((dst_off[k + 1] - 1) / tile);
         if (t0 != t1) {
             const unsigned int i = t1 - t0 <= SPLIT_SERIAL ? atomicAdd(&count[0], 1u) : cap - 1u - atomicAdd(&count[1], 1u);
             split_k[i] = k;
@@ -271,6 +271,26 @@ __global__ void sym_check_kernel(const uint32_t* src, const uint32_t* dst, uint6
             return;
         }
     }
+}
+
+// largest weight word (uint64 weights; the byte-wide copy applies below 256)
+__global__ void max_weight_kernel(const unsigned long long* w, uint64_t E, unsigned long long* out)
+{
+    unsigned long long m = 0;
+    for (uint64_t e = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; e < E; e += (uint64_t)gridDim.x * blockDim.x)
+        m = w[e] > m ? w[e] : m;
+    for (int d = 16; d > 0; d >>= 1) {
+        const unsigned long long y = __shfl_xor_sync(FULL, m, d);
+        m = y > m ? y : m;
+    }
+    if ((threadIdx.x & 31) == 0 && m)
+        atomicMax(out, m);
+}
+
+__global__ void narrow_weights_kernel(const unsigned long long* w, uint64_t Epad, uint8_t* w8)
+{
+    for (uint64_t e = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; e < Epad; e += (uint64_t)gridDim.x * blockDim.x)
+        w8[e] = (uint8_t)w[e];
 }
 
 __global__ void pad_kernel(uint32_t* src, unsigned long long* w, uint64_t E, uint64_t Epad)
@@ -518,7 +538,7 @@ int build_from_device_edges(wedge_graph* h, uint64_t V, uint64_t E, uint32_t* d_
     WEDGE_CHECK(cudaMallocAsync((void**)&d_cnt, 2 * sizeof(unsigned int), st));
     WEDGE_CHECK(cudaMemsetAsync(d_cnt, 0, 2 * sizeof(unsigned int), st));
     if (Vne)
-        split_kernel<<<grid_for(Vne, AUX_THREADS, cap), AUX_THREADS, 0, st>>>(dst_off, Vne, g.T, split_k, split_t0,
+        split_kernel<<<grid_for(Vne, AUX_THREADS, cap), AUX_THREADS, 0, st>>>(dst_off, Vne, g.T, TILE, split_k, split_t0,
                                                                              split_t1, d_cnt);
     unsigned int nsplit[2] = {0, 0};
     WEDGE_CHECK(cudaMemcpyAsync(nsplit, d_cnt, 2 * sizeof(unsigned int), cudaMemcpyDeviceToHost, st));
@@ -534,6 +554,27 @@ int build_from_device_edges(wedge_graph* h, uint64_t V, uint64_t E, uint32_t* d_
     WEDGE_CHECK(cudaGetLastError());
     g.nsplit = nsplit[0];
     g.nwide = nsplit[1];
+    // SSSP weights in one byte each where every uint64 weight is below 256: the
+    // pulls stream 1 byte per in-edge instead of 8 (same arithmetic, 64-bit sums)
+    g.w8 = nullptr;
+    if (d_w && weight_kind == WEDGE_WEIGHTS_U64 && E) {
+        unsigned long long* d_max = nullptr;
+        unsigned long long wmax = 0;
+        WEDGE_CHECK(cudaMallocAsync((void**)&d_max, sizeof(unsigned long long), st));
+        WEDGE_CHECK(cudaMemsetAsync(d_max, 0, sizeof(unsigned long long), st));
+        max_weight_kernel<<<grid_for(E, AUX_THREADS, cap), AUX_THREADS, 0, st>>>(d_w, E, d_max);
+        WEDGE_CHECK(cudaMemcpyAsync(&wmax, d_max, sizeof(wmax), cudaMemcpyDeviceToHost, st));
+        WEDGE_CHECK(cudaStreamSynchronize(st));
+        cudaFreeAsync(d_max, st);
+        if (wmax < 256ull) {
+            uint8_t* w8 = nullptr;
+            if ((rc = dalloc(h, &w8, g.Epad)))
+                return rc;
+            narrow_weights_kernel<<<grid_for(g.Epad, AUX_THREADS, cap), AUX_THREADS, 0, st>>>(d_w, g.Epad, w8);
+            WEDGE_CHECK(cudaGetLastError());
+            g.w8 = w8;
+        }
+    }
     g.dst_ident = (Vne && last_dst == Vne - 1) ? 1u : 0u;
     g.sym = h_asym ? 0u : 1u;
     g.dst_id = dst_id;
@@ -771,6 +812,112 @@ __host__ __device__ constexpr uint32_t dst_launches_of(int app)
     return app == WEDGE_APP_BFS ? 1u : app == WEDGE_APP_CC ? 2u : 0u;
 }
 
+// compressed destination owning in-edge position pos: the owner of the
+// 128-edge index tile's first edge plus the destination starts after it
+__device__ __forceinline__ uint32_t dst_of_pos(const DevGraph& g, uint32_t pos)
+{
+    const uint32_t t = pos >> 7, w0 = t << 2, wp = pos >> 5;
+    uint32_t n = 0;
+    for (uint32_t w = w0; w < wp; ++w)
+        n += __popc(g.dst_start[w]);
+    n += __popc(g.dst_start[wp] & ((pos & 31u) == 31u ? FULL : ((2u << (pos & 31u)) - 1u)));
+    return g.tile_dst0[t] + n - (g.dst_start[w0] & 1u); /* a start at the index tile's first edge is the owner's */
+}
+
+// The Wedge pull of SSSP over in-edge positions: every vertex the last pull
+// activated relaxes exactly the in-edges its out-edges are (the CSRI holds
+// their positions), where the chunk form pulls the whole 32-edge chunks
+// holding them (phase_edge_pull_sssp.c:171-306 over the chunks
+// wedge_generate_frontier marks).  Both reach the same fixed point, the least
+// dist[d] = min over in-edges of dist[s] + w, by monotone relaxations; only
+// the iteration counts may differ.  Vertices with at most BIG_LIST out-edges
+// take a thread each; expand_kernel split the longer lists into PIECE-entry
+// items, which take a warp each.  block_cnt as pull_kernel's.
+__device__ __forceinline__ void sssp_push_pull(const DevGraph& g, const DevState& s, const Ctrl* c,
+                                               unsigned long long* block_cnt)
+{
+    constexpr int WARPS = PULL_THREADS / 32;
+    __shared__ unsigned long long sh_pc[WARPS][3];
+    __shared__ unsigned int sh_pdeg[3];
+    const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+    uint32_t* nxt = next_front(s, c->parity);
+    const bool f64 = g.weight_kind == WEDGE_WEIGHTS_F64;
+    unsigned long long mass = 0, edges = 0, act = 0;
+    if (threadIdx.x < 3)
+        sh_pdeg[threadIdx.x] = 0u;
+    __syncthreads();
+    auto relax = [&](unsigned long long du, uint32_t pos) {
+        const unsigned long long wv = g.w8 ? (unsigned long long)g.w8[pos] : g.w[pos];
+        const unsigned long long nd =
+            f64 ? (unsigned long long)__double_as_longlong(__dadd_rn(__longlong_as_double((long long)du),
+                                                                     __longlong_as_double((long long)wv)))
+                : du + wv; /* phase_edge_pull_sssp.c:136-137; an activated source is reached */
+        const uint32_t k = dst_of_pos(g, pos);
+        const uint32_t vtx = g.dst_ident ? k : g.dst_id[k];
+        if (nd < s.prop64[vtx] && nd < atomicMin(&s.prop64[vtx], nd)) {
+            const uint32_t b = 1u << (vtx & 31u);
+            if (!(atomicOr(&nxt[vtx >> 5], b) & b)) {
+                const uint32_t od = g.outdeg[vtx];
+                mass += od;
+                ++act;
+                const uint32_t bk = degree_bucket(od);
+                if (bk < 3u)
+                    atomicAdd(&sh_pdeg[bk], 1u);
+            }
+        }
+    };
+    const uint32_t tid = blockIdx.x * blockDim.x + threadIdx.x;
+    const uint32_t nthr = gridDim.x * blockDim.x;
+    const uint32_t n = c->alist_n;
+    for (uint32_t i = tid; i < n; i += nthr) {
+        const uint32_t u = s.alist[i];
+        const unsigned long long lo = g.csri_off[u], len = g.csri_off[u + 1u] - lo;
+        if (len > BIG_LIST)
+            continue; /* an item of expand_kernel's */
+        const unsigned long long du = s.prop64[u];
+        uint32_t pos[BIG_LIST];
+#pragma unroll
+        for (uint32_t j = 0; j < BIG_LIST; ++j)
+            pos[j] = (j < len) ? g.csri[lo + j] : 0u;
+#pragma unroll
+        for (uint32_t j = 0; j < BIG_LIST; ++j)
+            if (j < len)
+                relax(du, pos[j]);
+        edges += len;
+    }
+    const uint32_t ni = c->items;
+    for (uint32_t i = tid >> 5; i < ni; i += nthr >> 5) {
+        const uint2 it = s.items[i];
+        const unsigned long long lo = g.csri_off[it.x] + (unsigned long long)it.y * PIECE;
+        const unsigned long long end = g.csri_off[it.x + 1u];
+        const unsigned long long hi = (lo + PIECE < end) ? lo + PIECE : end;
+        const unsigned long long du = s.prop64[it.x];
+        for (unsigned long long j = lo + (unsigned long long)lane; j < hi; j += 32u) {
+            relax(du, g.csri[j]);
+            ++edges;
+        }
+    }
+    mass = warp_sum_u64(mass);
+    edges = warp_sum_u64(edges);
+    act = warp_sum_u64(act);
+    if (lane == 0) {
+        sh_pc[wib][0] = mass;
+        sh_pc[wib][1] = edges;
+        sh_pc[wib][2] = act;
+    }
+    __syncthreads();
+    if (threadIdx.x < NCNT) {
+        unsigned long long a = 0;
+        const int col = threadIdx.x == CNT_MASS ? 0 : threadIdx.x == CNT_EDGES ? 1 : threadIdx.x == CNT_ACT ? 2 : -1;
+        if (col >= 0)
+            for (int w = 0; w < WARPS; ++w)
+                a += sh_pc[w][col];
+        if (threadIdx.x >= CNT_DEG0)
+            a = sh_pdeg[threadIdx.x - CNT_DEG0];
+        block_cnt[NCNT * blockIdx.x + threadIdx.x] = a;
+    }
+}
+
 // BFS/CC probe: in-edges of an unfinished destination read before the tile pull
 constexpr uint32_t PROBE_EDGES = 16;
 
@@ -805,6 +952,10 @@ __global__ void __launch_bounds__(PULL_THREADS, 1)
             block_cnt[NCNT * blockIdx.x + threadIdx.x] = 0ull;
         return;
     }
+    if (APP == WEDGE_APP_SSSP && mode == MODE_WEDGE && s.push) {
+        sssp_push_pull(g, s, c, block_cnt);
+        return;
+    }
     const int lane = threadIdx.x & 31;
     const int wib = threadIdx.x >> 5;
     const uint32_t gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
@@ -835,12 +986,11 @@ __global__ void __launch_bounds__(PULL_THREADS, 1)
     auto vid = [&](uint32_t k, uint32_t slot) -> uint32_t { return slot < TAB ? my_id[slot] : g.dst_id[k]; };
 
     // ---- hub cache
-    const bool wide = (APP == WEDGE_APP_SSSP) || (APP == WEDGE_APP_PR && s.precision != WEDGE_PREC_FP32C);
+    const bool wide = (APP == WEDGE_APP_SSSP) || (APP == WEDGE_APP_PR); /* FP32C PageRank: pr32_pull_kernel */
     const void* hub_src = (APP == WEDGE_APP_BFS)    ? (const void*)cur
                           : (APP == WEDGE_APP_CC)   ? (const void*)s.prop32
                           : (APP == WEDGE_APP_SSSP) ? (const void*)s.prop64
-                          : wide                    ? (const void*)s.rank
-                                                    : (const void*)s.rank32;
+                                                    : (const void*)s.rank;
     const uint64_t hub_have = ((APP == WEDGE_APP_BFS) ? (g.V + 31) / 32 : g.V) * (wide ? 8u : 4u);
     const uint64_t hub_fit = hub_have & ~15ull;
     const uint32_t hub_bytes = (uint64_t)s.hub_bytes < hub_fit ? s.hub_bytes : (uint32_t)hub_fit; /* within smem and the array */
@@ -1019,15 +1169,25 @@ __global__ void __launch_bounds__(PULL_THREADS, 1)
         } else if (APP == WEDGE_APP_SSSP) {
             unsigned long long wv[EPL];
             const bool on = (in.cmask >> (((uint32_t)lane * EPL) >> 5)) & 1u;
-            const unsigned long long* wp = g.w + base + (uint64_t)lane * EPL;
+            if (g.w8) { /* byte-wide weights: EPL bytes per lane (SSSP's EPL is a multiple of 8) */
 #pragma unroll
-            for (int q = 0; q < EPL / 4; ++q) {
-                unsigned long long x[4] = {0ull, 0ull, 0ull, 0ull};
-                if (on)
-                    ld_stream_v4u64(wp + 4 * q, x);
+                for (int q = 0; q < EPL / 8; ++q) {
+                    const unsigned long long x = on ? ld_stream_u64(g.w8 + base + (uint64_t)lane * EPL + 8 * q) : 0ull;
 #pragma unroll
-                for (int j = 0; j < 4; ++j)
-                    wv[4 * q + j] = x[j];
+                    for (int j = 0; j < 8; ++j)
+                        wv[8 * q + j] = (x >> (8 * j)) & 0xFFull;
+                }
+            } else {
+                const unsigned long long* wp = g.w + base + (uint64_t)lane * EPL;
+#pragma unroll
+                for (int q = 0; q < EPL / 4; ++q) {
+                    unsigned long long x[4] = {0ull, 0ull, 0ull, 0ull};
+                    if (on)
+                        ld_stream_v4u64(wp + 4 * q, x);
+#pragma unroll
+                    for (int j = 0; j < 4; ++j)
+                        wv[4 * q + j] = x[j];
+                }
             }
             unsigned long long v[EPL];
 #pragma unroll
@@ -1071,52 +1231,26 @@ __global__ void __launch_bounds__(PULL_THREADS, 1)
                 }
             });
         } else if (APP == WEDGE_APP_PR) {
-            if (s.precision == WEDGE_PREC_FP32C) {
-                F2 v[EPL];
+            double v[EPL];
 #pragma unroll
-                for (int q = 0; q < EPL; ++q)
-                    v[q] = F2{(sa[q] < hub_lim)    ? reinterpret_cast<const float*>(hub_smem)[sa[q]]
-                              : (sa[q] != NONE32) ? ld_ro_f32(s.rank32 + sa[q])
-                                                  : 0.0f,
-                              0.0f};
-                TileGeo<EPL> tg;
-                tile_geometry_bits<EPL>(g, base, last_tile, in.k0, in.kend, lane, tg);
-                dsts += tg.ndst;
-                for (uint32_t slot = (uint32_t)lane; slot < min(tg.ndst, TAB); slot += 32u)
-                    my_id[slot] = g.dst_ident ? tg.k0 + slot : g.dst_id[tg.k0 + slot];
-                __syncwarp();
-                const AddF2 add;
-                seg_reduce<EPL>(v, tg, lane, add, [&](uint32_t k, F2 val, int kind) {
-                    if (kind == EMIT_COMPLETE) {
-                        s.acc[vid(k, k - tg.k0)] = __dadd_rn((double)val.s, (double)val.c);
-                    } else {
-                        float* p = (kind == EMIT_HEAD) ? s.head_part32 : s.tail_part32;
-                        p[2u * t] = val.s;
-                        p[2u * t + 1u] = val.c;
-                    }
-                });
-            } else {
-                double v[EPL];
-#pragma unroll
-                for (int q = 0; q < EPL; ++q)
-                    v[q] = (sa[q] < hub_lim)    ? reinterpret_cast<const double*>(hub_smem)[sa[q]]
-                           : (sa[q] != NONE32) ? ld_ro_f64(s.rank + sa[q])
-                                               : 0.0;
-                TileGeo<EPL> tg;
-                tile_geometry_bits<EPL>(g, base, last_tile, in.k0, in.kend, lane, tg);
-                dsts += tg.ndst;
-                for (uint32_t slot = (uint32_t)lane; slot < min(tg.ndst, TAB); slot += 32u)
-                    my_id[slot] = g.dst_ident ? tg.k0 + slot : g.dst_id[tg.k0 + slot];
-                __syncwarp();
-                seg_reduce<EPL>(v, tg, lane, AddF64(), [&](uint32_t k, double val, int kind) {
-                    if (kind == EMIT_COMPLETE)
-                        s.acc[vid(k, k - tg.k0)] = val;
-                    else if (kind == EMIT_HEAD)
-                        s.head_part[t] = val;
-                    else
-                        s.tail_part[t] = val;
-                });
-            }
+            for (int q = 0; q < EPL; ++q)
+                v[q] = (sa[q] < hub_lim)    ? reinterpret_cast<const double*>(hub_smem)[sa[q]]
+                       : (sa[q] != NONE32) ? ld_ro_f64(s.rank + sa[q])
+                                           : 0.0;
+            TileGeo<EPL> tg;
+            tile_geometry_bits<EPL>(g, base, last_tile, in.k0, in.kend, lane, tg);
+            dsts += tg.ndst;
+            for (uint32_t slot = (uint32_t)lane; slot < min(tg.ndst, TAB); slot += 32u)
+                my_id[slot] = g.dst_ident ? tg.k0 + slot : g.dst_id[tg.k0 + slot];
+            __syncwarp();
+            seg_reduce<EPL>(v, tg, lane, AddF64(), [&](uint32_t k, double val, int kind) {
+                if (kind == EMIT_COMPLETE)
+                    s.acc[vid(k, k - tg.k0)] = val;
+                else if (kind == EMIT_HEAD)
+                    s.head_part[t] = val;
+                else
+                    s.tail_part[t] = val;
+            });
         }
         __syncwarp(); /* the table is rewritten by the next tile */
     }
@@ -1781,17 +1915,6 @@ __device__ __forceinline__ uint32_t chunk_tile_shift(uint32_t app)
     return 31u - (uint32_t)__clz(epl);
 }
 
-// compressed destination owning in-edge position pos: the owner of the
-// 128-edge index tile's first edge plus the destination starts after it
-__device__ __forceinline__ uint32_t dst_of_pos(const DevGraph& g, uint32_t pos)
-{
-    const uint32_t t = pos >> 7, w0 = t << 2, wp = pos >> 5;
-    uint32_t n = 0;
-    for (uint32_t w = w0; w < wp; ++w)
-        n += __popc(g.dst_start[w]);
-    n += __popc(g.dst_start[wp] & ((pos & 31u) == 31u ? FULL : ((2u << (pos & 31u)) - 1u)));
-    return g.tile_dst0[t] + n - (g.dst_start[w0] & 1u); /* a start at the index tile's first edge is the owner's */
-}
 
 // Wedge build over in-edge positions (BFS, CC): the destination of in-edge
 // pos, if unfinished (BFS unvisited, CC label not 0), becomes a candidate of
@@ -1941,6 +2064,8 @@ __global__ void expand_kernel(DevGraph g, DevState s)
                 np = (uint32_t)((len + PIECE - 1) / PIECE);
                 len = 0;
             }
+            if (s.push)
+                len = 0; /* SSSP over in-edge positions: the pull relaxes the short lists itself */
         }
         // a short list's entries are loaded together, then marked
         uint32_t ch[BIG_LIST];
@@ -1978,7 +2103,7 @@ __global__ void expand_kernel(DevGraph g, DevState s)
 __global__ void wedge_build_kernel(DevGraph g, DevState s)
 {
     Ctrl* c = s.ctrl;
-    if (c->done || c->mode != MODE_WEDGE)
+    if (c->done || c->mode != MODE_WEDGE || s.push) /* SSSP over in-edge positions: the pull takes the items */
         return;
     const int lane = threadIdx.x & 31;
     const uint32_t gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
@@ -2013,7 +2138,7 @@ __global__ void compact_kernel(DevGraph g, DevState s)
     constexpr uint32_t TPW = 32 / EPL;
     constexpr uint32_t MASK = (EPL >= 32) ? FULL : ((1u << EPL) - 1u);
     Ctrl* c = s.ctrl;
-    if (c->done || c->mode != MODE_WEDGE || s.cand) /* over in-edge positions: a candidate list, no tiles */
+    if (c->done || c->mode != MODE_WEDGE || s.cand || s.push) /* over in-edge positions: no tiles */
         return;
     const int lane = threadIdx.x & 31;
     const uint32_t gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
@@ -2263,12 +2388,8 @@ __global__ void pr_init_kernel(DevGraph g, DevState s, uint32_t max_iter)
 {
     const double invN = __ddiv_rn(1.0, (double)g.V);
     for (uint64_t v = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; v < g.V; v += (uint64_t)gridDim.x * blockDim.x) {
-        const double r = __dmul_rn(invN, s.inv_od[v]);
         s.acc[v] = 0.0;
-        if (s.precision == WEDGE_PREC_FP32C)
-            s.rank32[v] = (float)r;
-        else
-            s.rank[v] = r;
+        s.rank[v] = __dmul_rn(invN, s.inv_od[v]);
     }
     if (blockIdx.x == 0 && threadIdx.x == 0) {
         Ctrl* c = s.ctrl;
@@ -2286,6 +2407,7 @@ __global__ void pr_init_kernel(DevGraph g, DevState s, uint32_t max_iter)
         c->need_n = 0;
         c->error = 0;
         c->pr_total = 0.0;
+        c->pr_prev = 0.0;
         c->pr_sum = 0.0;
         c->max_iter = max_iter;
     }
@@ -2348,17 +2470,8 @@ __global__ void pr_finish_kernel(DevGraph g, DevState s, uint32_t nblocks, const
             log_iteration(s, c, cnt);
         }
     }
-    if (s.precision == WEDGE_PREC_FP32C) {
-        const float2* tp = (const float2*)s.tail_part32; /* (value, compensation) */
-        const float2* hp = (const float2*)s.head_part32;
-        merge_splits(
-            g, s.acc, g.split_k, g.split_t0, g.split_t1, g.nsplit, g.nwide, g.T,
-            [&](uint32_t t) { const float2 v = tp[t]; return __dadd_rn((double)v.x, (double)v.y); },
-            [&](uint32_t t) { const float2 v = hp[t]; return __dadd_rn((double)v.x, (double)v.y); });
-    } else {
-        merge_splits(g, s.acc, g.split_k, g.split_t0, g.split_t1, g.nsplit, g.nwide, g.T, [&](uint32_t t) { return s.tail_part[t]; },
-                     [&](uint32_t t) { return s.head_part[t]; });
-    }
+    merge_splits(g, s.acc, g.split_k, g.split_t0, g.split_t1, g.nsplit, g.nwide, g.T, [&](uint32_t t) { return s.tail_part[t]; },
+                 [&](uint32_t t) { return s.head_part[t]; });
 }
 
 // perform_vertex_phase_pr (phase_vertex_pr.c:26-77):
@@ -2371,20 +2484,14 @@ __global__ void pr_vertex_kernel(DevGraph g, DevState s)
     const double d = s.damping;
     const double omd = __ddiv_rn(__dsub_rn(1.0, d), N);
     const double corr = __ddiv_rn(__dsub_rn(1.0, s.ctrl->pr_total), N);
-    const bool c32 = s.precision == WEDGE_PREC_FP32C;
     for (uint64_t v = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; v < g.V; v += (uint64_t)gridDim.x * blockDim.x) {
         const double x = __dadd_rn(__dmul_rn(__dadd_rn(s.acc[v], corr), d), omd);
-        double r;
         if (s.inv_od) {
-            r = __dmul_rn(x, s.inv_od[v]);
+            s.rank[v] = __dmul_rn(x, s.inv_od[v]);
         } else {
             const uint32_t od = g.outdeg[v];
-            r = __ddiv_rn(x, od ? (double)od : N);
+            s.rank[v] = __ddiv_rn(x, od ? (double)od : N);
         }
-        if (c32)
-            s.rank32[v] = (float)r;
-        else
-            s.rank[v] = r;
     }
 }
 
@@ -2437,6 +2544,399 @@ __global__ void pr_total_kernel(const double* acc, uint64_t V, double* part, Ctr
     }
 }
 
+/* -------------------------------------------- compensated-FP32 PageRank */
+//
+// WEDGE_PREC_FP32C: ranks, gathers, per-destination sums and the vertex phase
+// in FP32; FP64 only for the total rank S, whose (1 - S)/N term renormalises
+// the dangling mass (phase_vertex_pr.c:57-72).  The reference computes S as
+// the sum of all accumulators after the edge phase (phases.c:37-46).  Since
+//     S(i) = sum_v acc_v(i) = sum_{s : outdeg_s > 0} rank_s(i-1),
+// the total an iteration needs is known when its pull starts: the previous
+// iteration sums its new non-dangling ranks.  So the vertex phase runs inside
+// the pull, once per destination, as soon as the destination's sum is
+// complete, and nothing per vertex is written twice:
+//   pr32_pull_kernel    tiles of PR32_TILE in-edges; a destination inside one
+//                       tile gets its new rank there (staged per warp in shared
+//                       memory, then written by the warp's lanes together)
+//   pr32_finish_kernel  destinations spanning tiles (two-sum of the per-tile
+//                       partials in tile order) and vertices with out-edges but
+//                       no in-edges (all take the same rank)
+//   pr32_total_kernel   S of the next iteration from the per-block FP64 sums
+// Ranks are double-buffered by iteration parity; vertices with neither in- nor
+// out-edges are written once, after the last iteration (pr32_iso_kernel).
+constexpr int PR32_EPL = 16;
+constexpr uint32_t PR32_TILE = 32u * PR32_EPL;
+
+__device__ __forceinline__ const float* pr32_cur(const DevState& s)
+{
+    return s.rank32 + ((s.ctrl->iter & 1u) ? s.rstride : 0ull);
+}
+
+// FP32 constants of one iteration's vertex phase: rank' = (acc + corr)*d + omd
+struct Pr32K {
+    float corr, d, omd;
+};
+
+__device__ __forceinline__ Pr32K pr32_constants(const DevGraph& g, const DevState& s, double total)
+{
+    const double N = (double)g.V;
+    Pr32K k;
+    k.corr = __double2float_rn(__ddiv_rn(__dsub_rn(1.0, total), N));
+    k.d = __double2float_rn(s.damping);
+    k.omd = __double2float_rn(__ddiv_rn(__dsub_rn(1.0, s.damping), N));
+    return k;
+}
+
+// the vertex phase of one vertex (phase_vertex_pr.c:72) in FP32: its rank
+// (before the division by outdegree') from its in-edge sum
+__device__ __forceinline__ float pr32_rank(const Pr32K& k, float sum)
+{
+    return __fmaf_rn(__fadd_rn(sum, k.corr), k.d, k.omd);
+}
+
+__device__ __forceinline__ F2 f2_add(F2 a, float x) { return AddF2()(a, F2{x, 0.0f}); }
+
+// FP64 sum of a block's per-thread (sum, compensation) pairs, in a fixed
+// order; returned on thread 0.  blockDim.x is a multiple of 32, at most 1024.
+__device__ __forceinline__ double block_sum_f2(F2 x)
+{
+    __shared__ double sh[32];
+    double v = warp_sum_f64(__dadd_rn((double)x.s, (double)x.c));
+    if ((threadIdx.x & 31) == 0)
+        sh[threadIdx.x >> 5] = v;
+    __syncthreads();
+    double t = 0.0;
+    if (threadIdx.x == 0)
+        for (uint32_t w = 0; w < blockDim.x / 32u; ++w)
+            t = __dadd_rn(t, sh[w]);
+    return t;
+}
+
+// 1/outdegree' in FP32 (the reference divides by outdegree, or by N for a
+// dangling vertex: execution_pr.c:384-390); negative marks a dangling vertex
+__global__ void pr32_inv_kernel(DevGraph g, float* inv32)
+{
+    const double N = (double)g.V;
+    for (uint64_t v = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; v < g.V; v += (uint64_t)gridDim.x * blockDim.x) {
+        const uint32_t od = g.outdeg[v];
+        inv32[v] = od ? __double2float_rn(__ddiv_rn(1.0, (double)od)) : -__double2float_rn(__ddiv_rn(1.0, N));
+    }
+}
+
+// flags of the vertices without in-edges: 1 with out-edges (zlist), 2 without (ilist)
+__global__ void pr32_noin_flags_kernel(DevGraph g, const uint32_t* has_in, uint32_t* fz, uint32_t* fi)
+{
+    for (uint64_t v = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; v < g.V; v += (uint64_t)gridDim.x * blockDim.x) {
+        const bool noin = !((has_in[v >> 5] >> (v & 31u)) & 1u);
+        fz[v] = (noin && g.outdeg[v] != 0u) ? 1u : 0u;
+        fi[v] = (noin && g.outdeg[v] == 0u) ? 1u : 0u;
+    }
+}
+
+__global__ void mark_has_in_kernel(DevGraph g, uint32_t* has_in)
+{
+    for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < g.Vne; k += gridDim.x * blockDim.x) {
+        const uint32_t v = g.dst_ident ? k : g.dst_id[k];
+        atomicOr(&has_in[v >> 5], 1u << (v & 31u));
+    }
+}
+
+// stream compaction by an exclusive scan of 0/1 flags: list in ascending id order
+__global__ void compact_flags_kernel(const uint32_t* flag, const uint32_t* pos, uint64_t n, uint32_t* list)
+{
+    for (uint64_t v = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; v < n; v += (uint64_t)gridDim.x * blockDim.x)
+        if (flag[v])
+            list[pos[v]] = (uint32_t)v;
+}
+
+// execution_initialize_pr (execution_pr.c:380-392) in FP32: rank = 1/N, stored
+// divided by outdegree'; the per-block sums of the non-dangling ranks give the
+// total of iteration 0 (pr32_total_kernel)
+__global__ void pr32_init_kernel(DevGraph g, DevState s, uint32_t max_iter)
+{
+    const float r = __double2float_rn(__ddiv_rn(1.0, (double)g.V));
+    F2 m{0.0f, 0.0f};
+    for (uint64_t v = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; v < g.V; v += (uint64_t)gridDim.x * blockDim.x) {
+        const float inv = s.inv32[v];
+        s.rank32[v] = __fmul_rn(r, fabsf(inv));
+        if (inv > 0.0f)
+            m = f2_add(m, r);
+    }
+    const double t = block_sum_f2(m);
+    if (threadIdx.x == 0)
+        s.pmass[blockIdx.x] = t;
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        Ctrl* c = s.ctrl;
+        c->iter = 0;
+        c->wedge_iters = 0;
+        c->edges_scanned = 0;
+        c->tiles_scanned = 0;
+        c->dsts_scanned = 0;
+        c->activated = 0;
+        c->pull_launches = 0;
+        c->last_mass = 0;
+        c->done = 0;
+        c->mode = MODE_DENSE;
+        c->parity = 0;
+        c->need_n = 0;
+        c->error = 0;
+        c->pr_total = 0.0;
+        c->pr_prev = 0.0;
+        c->pr_sum = 0.0;
+        c->max_iter = max_iter;
+    }
+}
+
+// The edge pull and, for every destination whose in-edges lie in one tile, the
+// vertex phase (perform_edge_pull_phase_pr, phase_edge_pull_pr.c:28-116, and
+// perform_vertex_phase_pr, phase_vertex_pr.c:26-77).  One 1024-thread block per
+// SM; a warp takes tiles of PR32_TILE in-edges in a static stride: 16 sources
+// per lane in two 256-bit loads, their ranks gathered from the hub cache (the
+// low-id end of the rank array, bulk-copied into shared memory at launch) or
+// global memory, folded per destination by the segmented two-sum reduction.
+// The sums of the tile's complete destinations are staged in the warp's slice
+// of shared memory and finished by the warp's lanes together: consecutive
+// destinations, so their outdegree' and rank writes coalesce.  Destinations
+// spanning tiles leave (sum, compensation) partials for pr32_finish_kernel.
+// Dynamic shared memory: hub cache (hub_bytes) | staged sums [32 warps][PR32_TILE].
+// block_cnt[NCNT*b + CNT_*] as pull_kernel's; s.pmass[b] = the block's sum of
+// the new non-dangling ranks.
+__global__ void __launch_bounds__(PULL_THREADS, 1) pr32_pull_kernel(DevGraph g, DevState s, unsigned long long* block_cnt)
+{
+    constexpr int EPL = PR32_EPL;
+    constexpr int WARPS = PULL_THREADS / 32;
+    constexpr uint32_t Q = PR32_TILE / TILE; /* 128-edge index entries per tile */
+    __shared__ unsigned long long sh_cnt[WARPS][3];
+    __shared__ unsigned long long hub_bar;
+    extern __shared__ __align__(16) unsigned char pr32_smem[];
+    const Ctrl* c = s.ctrl;
+    const uint32_t par = c->iter & 1u;
+    const float* cur = s.rank32 + (par ? s.rstride : 0ull);
+    float* nxt = s.rank32 + (par ? 0ull : s.rstride);
+    const Pr32K K = pr32_constants(g, s, c->pr_total);
+    const int lane = threadIdx.x & 31;
+    const int wib = threadIdx.x >> 5;
+    const uint32_t gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const uint32_t nw = (gridDim.x * blockDim.x) >> 5;
+    const uint32_t T = (uint32_t)((g.E + PR32_TILE - 1) / PR32_TILE); /* tiles holding real in-edges */
+    const uint32_t hub_bytes = s.hub_bytes;
+    const float* hub = reinterpret_cast<const float*>(pr32_smem);
+    float* my_sum = reinterpret_cast<float*>(pr32_smem + hub_bytes) + (uint32_t)wib * PR32_TILE;
+
+    // ---- hub cache: ranks [0, hub_n) of the current buffer
+    const bool use_hub = hub_bytes != 0u && (s.rstride & 3ull) == 0ull;
+    if (use_hub) {
+        if (threadIdx.x == 0) {
+            mbar_init(&hub_bar, 1u);
+            mbar_arrive_expect_tx(&hub_bar, hub_bytes);
+            for (uint32_t off = 0; off < hub_bytes; off += 32768u)
+                bulk_g2s(pr32_smem + off, reinterpret_cast<const unsigned char*>(cur) + off, min(32768u, hub_bytes - off),
+                         &hub_bar);
+        }
+        __syncthreads();
+    }
+    uint32_t hub_lim = 0; /* cache entries this warp reads: 0 until the copy completed */
+
+    unsigned long long edges = 0, tiles = 0, dsts = 0;
+    F2 mass{0.0f, 0.0f};
+    uint32_t t = gw;
+    uint32_t k0n = 0, kendn = 0;
+    if (t < T) {
+        k0n = g.tile_dst0[(uint64_t)t * Q];
+        kendn = g.tile_dst0[((uint64_t)t + 1u) * Q];
+    }
+    for (; t < T; t += nw) {
+        const uint32_t k0 = k0n, kend = kendn;
+        if (t + nw < T) { /* the next tile's bounds, one tile ahead */
+            k0n = g.tile_dst0[(uint64_t)(t + nw) * Q];
+            kendn = g.tile_dst0[((uint64_t)(t + nw) + 1u) * Q];
+        }
+        if (use_hub && hub_lim == 0u) {
+            uint32_t ready = 0u;
+            if (lane == 0)
+                ready = mbar_test_wait(&hub_bar, 0u) ? 1u : 0u;
+            if (__shfl_sync(FULL, ready, 0))
+                hub_lim = hub_bytes / 4u;
+        }
+        ++tiles;
+        const uint64_t base = (uint64_t)t * PR32_TILE;
+        uint32_t sa[EPL];
+        {
+            const uint32_t* p = g.src + base + (uint64_t)lane * EPL;
+            uint32_t x[8];
+            ld_stream_v8(p, x);
+#pragma unroll
+            for (int j = 0; j < 8; ++j)
+                sa[j] = x[j];
+            ld_stream_v8(p + 8, x);
+#pragma unroll
+            for (int j = 0; j < 8; ++j)
+                sa[8 + j] = x[j];
+        }
+        F2 v[EPL];
+#pragma unroll
+        for (int q = 0; q < EPL; ++q) {
+            const uint32_t x = sa[q];
+            v[q] = F2{(x < hub_lim) ? hub[x] : (x != NONE32) ? ld_ro_f32(cur + x) : 0.0f, 0.0f};
+            edges += (x != NONE32) ? 1u : 0u;
+        }
+        TileGeo<EPL> tg;
+        tile_geometry_bits<EPL>(g, base, t + 1u >= T, k0, kend, lane, tg);
+        dsts += tg.ndst;
+        seg_reduce<EPL>(v, tg, lane, AddF2(), [&](uint32_t k, F2 val, int kind) {
+            if (kind == EMIT_COMPLETE)
+                my_sum[k - tg.k0] = __fadd_rn(val.s, val.c);
+            else
+                (kind == EMIT_HEAD ? s.phead : s.ptail)[t] = make_float2(val.s, val.c);
+        });
+        __syncwarp();
+        // the vertex phase of the tile's complete destinations, lanes over consecutive ones
+        const uint32_t nd = tg.ndst;
+        const uint32_t jlo = tg.k0_fresh ? 0u : 1u;              /* slot 0 began in an earlier tile */
+        const uint32_t jhi = tg.tail_cont ? nd - 1u : nd;         /* the last slot continues */
+        for (uint32_t j = jlo + (uint32_t)lane; j < jhi; j += 32u) {
+            const uint32_t k = tg.k0 + j;
+            const uint32_t vtx = g.dst_ident ? k : g.dst_id[k];
+            const float inv = s.inv32[vtx];
+            const float r = pr32_rank(K, my_sum[j]);
+            nxt[vtx] = __fmul_rn(r, fabsf(inv));
+            if (inv > 0.0f)
+                mass = f2_add(mass, r);
+        }
+        __syncwarp(); /* my_sum is rewritten by the next tile */
+    }
+    // the block may not retire with its bulk copy in flight
+    if (use_hub && threadIdx.x == 0 && !mbar_wait_bounded(&hub_bar, 0u, HUB_WAIT_TRIES)) {
+        atomicOr(&s.ctrl->error, ERR_HUB_TIMEOUT);
+        mbar_wait_bounded(&hub_bar, 0u, HUB_WAIT_TRIES);
+    }
+    edges = warp_sum_u64(edges);
+    if (lane == 0) {
+        sh_cnt[wib][0] = edges;
+        sh_cnt[wib][1] = tiles; /* warp-uniform */
+        sh_cnt[wib][2] = dsts;  /* warp-uniform */
+    }
+    const double bm = block_sum_f2(mass); /* contains __syncthreads */
+    if (threadIdx.x == 0)
+        s.pmass[blockIdx.x] = bm;
+    if (threadIdx.x < NCNT) {
+        unsigned long long a = 0;
+        if (threadIdx.x == CNT_EDGES || threadIdx.x == CNT_TILES || threadIdx.x == CNT_DSTS) {
+            const int col = threadIdx.x == CNT_EDGES ? 0 : threadIdx.x == CNT_TILES ? 1 : 2;
+            for (int w = 0; w < WARPS; ++w)
+                a += sh_cnt[w][col];
+        }
+        block_cnt[NCNT * blockIdx.x + threadIdx.x] = a;
+    }
+}
+
+// Destinations whose in-edges span tiles: the (sum, compensation) partials of
+// the tiles they continue through, then of the tile they end in, combined by
+// two-sum in tile order (the counterpart of the ordered merge of
+// phases.c:71-114), then their vertex phase; and the vertices with out-edges
+// but no in-edges, whose sum is 0.  Short splits take a thread each, long ones
+// (hubs) a warp each.  s.pmass[part0 + b] = the block's sum of new non-dangling ranks.
+__global__ void pr32_finish_kernel(DevGraph g, DevState s, uint32_t part0)
+{
+    const Ctrl* c = s.ctrl;
+    float* nxt = s.rank32 + ((c->iter & 1u) ? 0ull : s.rstride);
+    const Pr32K K = pr32_constants(g, s, c->pr_total);
+    const uint32_t tid = blockIdx.x * blockDim.x + threadIdx.x;
+    const uint32_t nthr = gridDim.x * blockDim.x;
+    const int lane = threadIdx.x & 31;
+    F2 mass{0.0f, 0.0f};
+    auto finish = [&](uint32_t k, F2 sum) {
+        const uint32_t vtx = g.dst_ident ? k : g.dst_id[k];
+        const float inv = s.inv32[vtx];
+        const float r = pr32_rank(K, __fadd_rn(sum.s, sum.c));
+        nxt[vtx] = __fmul_rn(r, fabsf(inv));
+        if (inv > 0.0f)
+            mass = f2_add(mass, r);
+    };
+    const AddF2 add;
+    for (uint32_t i = tid; i < s.pnsplit; i += nthr) {
+        const uint32_t t0 = s.psplit_t0[i], t1 = s.psplit_t1[i];
+        F2 x{0.0f, 0.0f};
+        for (uint32_t tt = t0; tt < t1; ++tt) {
+            const float2 p = s.ptail[tt];
+            x = add(x, F2{p.x, p.y});
+        }
+        const float2 h = s.phead[t1];
+        finish(s.psplit_k[i], add(x, F2{h.x, h.y}));
+    }
+    for (uint32_t j = tid >> 5; j < s.pnwide; j += nthr >> 5) {
+        const uint32_t i = s.pT - 1u - j;
+        const uint32_t a = s.psplit_t0[i], b = s.psplit_t1[i];
+        F2 x{0.0f, 0.0f};
+        for (uint32_t tt = a + (uint32_t)lane; tt < b; tt += 32u) {
+            const float2 p = s.ptail[tt];
+            x = add(x, F2{p.x, p.y});
+        }
+#pragma unroll
+        for (int d = 16; d > 0; d >>= 1) /* butterfly: the same fixed order on every run */
+            x = add(x, F2{__shfl_xor_sync(FULL, x.s, d), __shfl_xor_sync(FULL, x.c, d)});
+        if (lane == 0) {
+            const float2 h = s.phead[b];
+            finish(s.psplit_k[i], add(x, F2{h.x, h.y}));
+        }
+    }
+    const float r0 = pr32_rank(K, 0.0f);
+    for (uint32_t i = tid; i < s.nz; i += nthr) {
+        const uint32_t v = s.zlist[i];
+        nxt[v] = __fmul_rn(r0, s.inv32[v]); /* out-edges: inv32 > 0 */
+        mass = f2_add(mass, r0);
+    }
+    const double bm = block_sum_f2(mass);
+    if (threadIdx.x == 0)
+        s.pmass[part0 + blockIdx.x] = bm;
+}
+
+// The total rank the next iteration uses: the per-block FP64 sums in block
+// order (one block of AUX_THREADS).  With nblocks > 0 the iteration is also
+// counted and logged from the pull's block counters.
+__global__ void pr32_total_kernel(DevState s, uint32_t nparts, const unsigned long long* block_cnt, uint32_t nblocks)
+{
+    __shared__ double sh[AUX_THREADS / 32];
+    Ctrl* c = s.ctrl;
+    double x = 0.0;
+    for (uint32_t i = threadIdx.x; i < nparts; i += blockDim.x)
+        x = __dadd_rn(x, s.pmass[i]);
+    x = warp_sum_f64(x);
+    if ((threadIdx.x & 31) == 0)
+        sh[threadIdx.x >> 5] = x;
+    __syncthreads();
+    unsigned long long cnt[NCNT];
+    if (nblocks)
+        reduce_counters(block_cnt, nblocks, cnt); /* uniform branch; contains __syncthreads */
+    if (threadIdx.x == 0) {
+        double S = 0.0;
+        for (int w = 0; w < AUX_THREADS / 32; ++w)
+            S = __dadd_rn(S, sh[w]);
+        c->pr_prev = c->pr_total;
+        c->pr_total = S;
+        if (nblocks) {
+            c->last_mass = 0;
+            log_iteration(s, c, cnt);
+        }
+    }
+}
+
+// After the last iteration: the vertices with neither in- nor out-edges, whose
+// rank is the same constant and which no pull gathers, in the last buffer
+// written (nothing before the first iteration: the initial ranks stand)
+__global__ void pr32_iso_kernel(DevGraph g, DevState s)
+{
+    const Ctrl* c = s.ctrl;
+    if (c->iter == 0u)
+        return;
+    float* last = s.rank32 + ((c->iter & 1u) ? s.rstride : 0ull);
+    const float r0 = pr32_rank(pr32_constants(g, s, c->pr_prev), 0.0f);
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < s.ni; i += gridDim.x * blockDim.x) {
+        const uint32_t v = s.ilist[i];
+        last[v] = __fmul_rn(r0, fabsf(s.inv32[v]));
+    }
+}
+
 // condition of the captured PageRank iteration loop
 __global__ void pr_loop_cond_kernel(DevState s, cudaGraphConditionalHandle handle)
 {
@@ -2449,10 +2949,11 @@ __global__ void pr_sum_kernel(DevGraph g, DevState s, double* block_out)
     __shared__ double sh[AUX_THREADS / 32];
     const double N = (double)g.V;
     const bool c32 = s.precision == WEDGE_PREC_FP32C;
+    const float* r32 = c32 ? pr32_cur(s) : nullptr;
     double x = 0.0;
     for (uint64_t v = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; v < g.V; v += (uint64_t)gridDim.x * blockDim.x) {
         const uint32_t od = g.outdeg[v];
-        const double r = c32 ? (double)s.rank32[v] : s.rank[v];
+        const double r = c32 ? (double)r32[v] : s.rank[v];
         x = __dadd_rn(x, __dmul_rn(r, od ? (double)od : N));
     }
     x = warp_sum_f64(x);
@@ -2494,7 +2995,7 @@ __global__ void export_kernel(DevGraph g, DevState s, uint32_t app, unsigned lon
         } else if (app == WEDGE_APP_SSSP) {
             x = s.prop64[v];
         } else {
-            x = (unsigned long long)__double_as_longlong(s.precision == WEDGE_PREC_FP32C ? (double)s.rank32[v] : s.rank[v]);
+            x = (unsigned long long)__double_as_longlong(s.precision == WEDGE_PREC_FP32C ? (double)pr32_cur(s)[v] : s.rank[v]);
         }
         out[o] = x;
     }
@@ -2688,6 +3189,112 @@ static int setup_hub(wedge_graph* h, int app, int precision)
     return WEDGE_OK;
 }
 
+// dynamic shared memory of pr32_pull_kernel beyond its hub cache: the staged sums
+constexpr uint32_t PR32_STAGE_BYTES = (PULL_THREADS / 32) * PR32_TILE * sizeof(float);
+
+// hub cache of the compensated-FP32 pull: HUB_BYTES_DEFAULT (or WEDGE_HUB_BYTES)
+// of the rank array, within what the block can opt into beside the staged sums
+static int pr32_setup_hub(wedge_graph* h)
+{
+    cudaFuncAttributes fa;
+    WEDGE_CHECK(cudaFuncGetAttributes(&fa, pr32_pull_kernel));
+    int optin = 0;
+    WEDGE_CHECK(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, h->device));
+    const uint64_t fixed = fa.sharedSizeBytes + PR32_STAGE_BYTES + 64u;
+    if ((uint64_t)optin < fixed)
+        return WEDGE_ERR_UNSUPPORTED;
+    uint64_t avail = (uint64_t)optin - fixed;
+    const char* cap = getenv("WEDGE_HUB_BYTES");
+    const uint64_t want = cap ? strtoull(cap, nullptr, 10) : HUB_BYTES_DEFAULT;
+    if (want < avail)
+        avail = want;
+    uint64_t n = avail / 4u;
+    if (n > h->g.V)
+        n = h->g.V;
+    n &= ~3ull; /* whole 16-byte lines */
+    h->s.hub_n = (uint32_t)n;
+    h->s.hub_bytes = (uint32_t)(n * 4u);
+    h->hub_bytes = h->s.hub_bytes;
+    WEDGE_CHECK(cudaFuncSetAttribute(pr32_pull_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     (int)(h->hub_bytes + PR32_STAGE_BYTES)));
+    return WEDGE_OK;
+}
+
+// State of the compensated-FP32 PageRank: the double-buffered FP32 ranks,
+// FP32 1/outdegree', the split lists of its PR32_TILE-edge tiles, the lists of
+// vertices without in-edges, and the per-block sums of the total rank.
+static int pr32_state(wedge_graph* h)
+{
+    DevGraph& g = h->g;
+    DevState& s = h->s;
+    cudaStream_t st = h->stream;
+    const uint64_t V = g.V;
+    const uint32_t cap = (uint32_t)h->num_sms * 8u;
+    int rc;
+    s.rstride = (V + 31) & ~31ull;
+    s.pT = (uint32_t)(g.Epad / PR32_TILE);
+    if ((rc = dalloc(h, &s.rank32, 2 * s.rstride, true)) || (rc = dalloc(h, &s.inv32, V, true)) ||
+        (rc = dalloc(h, &s.pmass, (uint64_t)h->pull_grid + cap + 8, true)) ||
+        (rc = dalloc(h, &s.psplit_k, (uint64_t)s.pT + 1, true)) || (rc = dalloc(h, &s.psplit_t0, (uint64_t)s.pT + 1, true)) ||
+        (rc = dalloc(h, &s.psplit_t1, (uint64_t)s.pT + 1, true)) || (rc = dalloc(h, &s.phead, (uint64_t)s.pT + 1, true)) ||
+        (rc = dalloc(h, &s.ptail, (uint64_t)s.pT + 1, true)))
+        return rc;
+    pr32_inv_kernel<<<grid_for(V, AUX_THREADS, cap), AUX_THREADS, 0, st>>>(g, s.inv32);
+    // destinations spanning the pull's tiles
+    unsigned int* d_cnt = nullptr;
+    WEDGE_CHECK(cudaMallocAsync((void**)&d_cnt, 2 * sizeof(unsigned int), st));
+    WEDGE_CHECK(cudaMemsetAsync(d_cnt, 0, 2 * sizeof(unsigned int), st));
+    if (g.Vne)
+        split_kernel<<<grid_for(g.Vne, AUX_THREADS, cap), AUX_THREADS, 0, st>>>(g.dst_off, g.Vne, s.pT, PR32_TILE, s.psplit_k,
+                                                                               s.psplit_t0, s.psplit_t1, d_cnt);
+    unsigned int nsplit[2] = {0, 0};
+    WEDGE_CHECK(cudaMemcpyAsync(nsplit, d_cnt, sizeof(nsplit), cudaMemcpyDeviceToHost, st));
+    // vertices without in-edges, in id order: with out-edges (gathered, so written every
+    // iteration) and without (written once at the end)
+    if (V == 0) {
+        s.pnsplit = s.pnwide = s.nz = s.ni = 0;
+        WEDGE_CHECK(cudaStreamSynchronize(st));
+        cudaFree(d_cnt);
+        return WEDGE_OK;
+    }
+    const uint64_t words = (V + 31) / 32;
+    uint32_t *has_in = nullptr, *fz = nullptr, *fi = nullptr, *pz = nullptr, *pi = nullptr;
+    WEDGE_CHECK(cudaMallocAsync((void**)&has_in, words * sizeof(uint32_t), st));
+    WEDGE_CHECK(cudaMallocAsync((void**)&fz, V * sizeof(uint32_t), st));
+    WEDGE_CHECK(cudaMallocAsync((void**)&fi, V * sizeof(uint32_t), st));
+    WEDGE_CHECK(cudaMallocAsync((void**)&pz, V * sizeof(uint32_t), st));
+    WEDGE_CHECK(cudaMallocAsync((void**)&pi, V * sizeof(uint32_t), st));
+    WEDGE_CHECK(cudaMemsetAsync(has_in, 0, words * sizeof(uint32_t), st));
+    if (g.Vne)
+        mark_has_in_kernel<<<grid_for(g.Vne, AUX_THREADS, cap), AUX_THREADS, 0, st>>>(g, has_in);
+    pr32_noin_flags_kernel<<<grid_for(V, AUX_THREADS, cap), AUX_THREADS, 0, st>>>(g, has_in, fz, fi);
+    if ((rc = device_scan(h, fz, pz, V, false)) || (rc = device_scan(h, fi, pi, V, false)))
+        return rc;
+    uint32_t tail[4] = {0, 0, 0, 0}; /* last flag and position of each list */
+    WEDGE_CHECK(cudaMemcpyAsync(&tail[0], fz + (V - 1), 4, cudaMemcpyDeviceToHost, st));
+    WEDGE_CHECK(cudaMemcpyAsync(&tail[1], pz + (V - 1), 4, cudaMemcpyDeviceToHost, st));
+    WEDGE_CHECK(cudaMemcpyAsync(&tail[2], fi + (V - 1), 4, cudaMemcpyDeviceToHost, st));
+    WEDGE_CHECK(cudaMemcpyAsync(&tail[3], pi + (V - 1), 4, cudaMemcpyDeviceToHost, st));
+    WEDGE_CHECK(cudaStreamSynchronize(st));
+    s.pnsplit = nsplit[0];
+    s.pnwide = nsplit[1];
+    s.nz = tail[0] + tail[1];
+    s.ni = tail[2] + tail[3];
+    if ((rc = dalloc(h, &s.zlist, (uint64_t)s.nz + 1, true)) || (rc = dalloc(h, &s.ilist, (uint64_t)s.ni + 1, true)))
+        return rc;
+    compact_flags_kernel<<<grid_for(V, AUX_THREADS, cap), AUX_THREADS, 0, st>>>(fz, pz, V, s.zlist);
+    compact_flags_kernel<<<grid_for(V, AUX_THREADS, cap), AUX_THREADS, 0, st>>>(fi, pi, V, s.ilist);
+    cudaFreeAsync(d_cnt, st);
+    cudaFreeAsync(has_in, st);
+    cudaFreeAsync(fz, st);
+    cudaFreeAsync(fi, st);
+    cudaFreeAsync(pz, st);
+    cudaFreeAsync(pi, st);
+    WEDGE_CHECK(cudaStreamSynchronize(st));
+    WEDGE_CHECK(cudaGetLastError());
+    return WEDGE_OK;
+}
+
 // state arrays of one application (allocated on first use, reused by later runs)
 static int ensure_state(wedge_graph* h, int app, int precision)
 {
@@ -2713,20 +3320,18 @@ static int ensure_state(wedge_graph* h, int app, int precision)
     s.block_part = bp; /* [grid] doubles, then the counters */
     WEDGE_CHECK(cudaMemset(bp, 0, sizeof(double) * (grid + slots * NCNT)));
     s.app = (uint32_t)app;
-    if (app == WEDGE_APP_PR) {
+    s.push = (app == WEDGE_APP_SSSP && g.csri_pos) ? 1u : 0u;
+    if (app == WEDGE_APP_PR && precision == WEDGE_PREC_FP32C) {
+        if ((rc = pr32_state(h)))
+            return rc;
+    } else if (app == WEDGE_APP_PR) {
         if ((rc = dalloc(h, &s.acc, V, true)) || (rc = dalloc(h, &s.inv_od, V, true)))
             return rc;
         pr_inv_outdeg_kernel<<<grid_for(V, AUX_THREADS, (uint32_t)h->num_sms * 8u), AUX_THREADS, 0, h->stream>>>(g, s.inv_od);
         WEDGE_CHECK(cudaGetLastError());
-        if (precision == WEDGE_PREC_FP32C) {
-            if ((rc = dalloc(h, &s.rank32, V, true)) || (rc = dalloc(h, &s.head_part32, 2ull * g.T + 2, true)) ||
-                (rc = dalloc(h, &s.tail_part32, 2ull * g.T + 2, true)))
-                return rc;
-        } else {
-            if ((rc = dalloc(h, &s.rank, V, true)) || (rc = dalloc(h, &s.head_part, (uint64_t)g.T + 1, true)) ||
-                (rc = dalloc(h, &s.tail_part, (uint64_t)g.T + 1, true)))
-                return rc;
-        }
+        if ((rc = dalloc(h, &s.rank, V, true)) || (rc = dalloc(h, &s.head_part, (uint64_t)g.T + 1, true)) ||
+            (rc = dalloc(h, &s.tail_part, (uint64_t)g.T + 1, true)))
+            return rc;
     } else {
         if (app == WEDGE_APP_SSSP) {
             if ((rc = dalloc(h, &s.prop64, V, true)))
@@ -2762,7 +3367,7 @@ static int ensure_state(wedge_graph* h, int app, int precision)
                 return rc;
         }
     }
-    if ((rc = setup_hub(h, app, precision)))
+    if ((rc = (app == WEDGE_APP_PR && precision == WEDGE_PREC_FP32C) ? pr32_setup_hub(h) : setup_hub(h, app, precision)))
         return rc;
     h->built_app = app;
     h->last_precision = precision;
@@ -2823,9 +3428,16 @@ static void launch_pull(wedge_graph* h, int app)
 }
 
 // kernels one iteration launches: the pull(s) and the five of the tail
+// the Wedge build's launches: collect, expand, build (not for SSSP over
+// in-edge positions), compact (chunk frontiers only)
+static uint64_t build_launches(const wedge_graph* h)
+{
+    return 2ull + (h->s.push ? 0ull : 1ull) + ((h->s.cand || h->s.push) ? 0ull : 1ull);
+}
+
 static uint64_t iteration_launches(const wedge_graph* h, int app)
 {
-    return (h->s.cand ? 4ull : 5ull) + pull_launches_of(app); /* no compact_kernel for candidate lists */
+    return 1ull + build_launches(h) + pull_launches_of(app); /* decide, the build, the pull */
 }
 
 static uint32_t aux_grid(wedge_graph* h, uint64_t work)
@@ -2865,8 +3477,9 @@ static void launch_wedge_build(wedge_graph* h, const DevGraph& g, int app)
 {
     collect_kernel<<<aux_grid(h, (g.V + 31) / 32), AUX_THREADS, 0, h->stream>>>(g, h->s, (uint32_t)app);
     expand_kernel<<<h->build_grid, AUX_THREADS, 0, h->stream>>>(g, h->s);
-    wedge_build_kernel<<<h->build_grid, AUX_THREADS, 0, h->stream>>>(g, h->s);
-    if (!h->s.cand) /* over in-edge positions the build lists candidates, not tiles */
+    if (!h->s.push) /* SSSP over in-edge positions: the pull takes expand_kernel's items */
+        wedge_build_kernel<<<h->build_grid, AUX_THREADS, 0, h->stream>>>(g, h->s);
+    if (!h->s.cand && !h->s.push) /* over in-edge positions the build lists candidates or items, not tiles */
         launch_compact(h, app);
 }
 
@@ -2980,7 +3593,7 @@ static int run_traversal(wedge_graph* h, int app, const wedge_params_t* p, wedge
     }
     WEDGE_CHECK(cudaEventRecord(h->ev[0], h->stream));
     launch_init(h, app, root, (uint32_t)p->sched, thr, (uint32_t)cap, p->probe_iter, (uint32_t)p->probe_mode);
-    launches += h->s.cand ? 5 : 6; /* init, root, the Wedge build */
+    launches += 2ull + build_launches(h); /* init, root, the Wedge build */
     Ctrl c;
     if (use_graph) {
         WEDGE_CHECK(cudaGraphLaunch(h->graph_exec, h->stream));
@@ -3063,6 +3676,42 @@ static int run_traversal(wedge_graph* h, int app, const wedge_params_t* p, wedge
     return WEDGE_OK;
 }
 
+// compensated-FP32 PageRank: the grid of pr32_finish_kernel (a thread per short
+// split and per vertex without in-edges, a warp per long split)
+static uint32_t pr32_finish_grid(wedge_graph* h)
+{
+    const DevState& s = h->s;
+    uint64_t work = (uint64_t)s.pnwide * 32u;
+    if (s.pnsplit > work)
+        work = s.pnsplit;
+    if (s.nz > work)
+        work = s.nz;
+    return aux_grid(h, work + 1);
+}
+
+// one compensated-FP32 PageRank iteration: pull (with the vertex phase of the
+// destinations inside one tile), split destinations, total rank
+static void launch_pr32_iteration(wedge_graph* h)
+{
+    const uint32_t fgrid = pr32_finish_grid(h);
+    pr32_pull_kernel<<<h->pull_grid, PULL_THREADS, h->hub_bytes + PR32_STAGE_BYTES, h->stream>>>(h->g, h->s, counters(h));
+    pr32_finish_kernel<<<fgrid, AUX_THREADS, 0, h->stream>>>(h->g, h->s, h->pull_grid);
+    pr32_total_kernel<<<1, AUX_THREADS, 0, h->stream>>>(h->s, h->pull_grid + fgrid, counters(h), h->pull_grid);
+}
+
+// execution_initialize_pr for the compensated-FP32 form: ranks 1/N and the total of iteration 0
+static void launch_pr32_init(wedge_graph* h, uint32_t max_iter)
+{
+    const uint32_t vgrid = aux_grid(h, h->g.V);
+    pr32_init_kernel<<<vgrid, AUX_THREADS, 0, h->stream>>>(h->g, h->s, max_iter);
+    pr32_total_kernel<<<1, AUX_THREADS, 0, h->stream>>>(h->s, vgrid, nullptr, 0);
+}
+
+static void launch_pr32_iso(wedge_graph* h)
+{
+    pr32_iso_kernel<<<aux_grid(h, h->s.ni), AUX_THREADS, 0, h->stream>>>(h->g, h->s);
+}
+
 // Captures one PageRank iteration (pull, ordered merge, vertex phase) as the
 // body of a device-side while loop on Ctrl::iter < Ctrl::max_iter.  The
 // kernels hold the state by value, so the capture is keyed on the damping
@@ -3091,10 +3740,14 @@ static int build_pr_graph(wedge_graph* h)
     WEDGE_CHECK(cudaGraphAddNode(&cnode, graph, nullptr, nullptr, 0, &cparams));
     cudaGraph_t body = cparams.conditional.phGraph_out[0];
     WEDGE_CHECK(cudaStreamBeginCaptureToGraph(h->stream, body, nullptr, nullptr, 0, cudaStreamCaptureModeRelaxed));
-    launch_pull(h, WEDGE_APP_PR);
-    pr_finish_kernel<<<finish_grid(h, g), AUX_THREADS, 0, h->stream>>>(g, h->s, h->pull_grid, counters(h));
-    launch_pr_total(h);
-    pr_vertex_kernel<<<aux_grid(h, g.V), AUX_THREADS, 0, h->stream>>>(g, h->s);
+    if (h->s.precision == WEDGE_PREC_FP32C) {
+        launch_pr32_iteration(h);
+    } else {
+        launch_pull(h, WEDGE_APP_PR);
+        pr_finish_kernel<<<finish_grid(h, g), AUX_THREADS, 0, h->stream>>>(g, h->s, h->pull_grid, counters(h));
+        launch_pr_total(h);
+        pr_vertex_kernel<<<aux_grid(h, g.V), AUX_THREADS, 0, h->stream>>>(g, h->s);
+    }
     pr_loop_cond_kernel<<<1, 1, 0, h->stream>>>(h->s, handle);
     cudaGraph_t captured;
     WEDGE_CHECK(cudaStreamEndCapture(h->stream, &captured));
@@ -3118,20 +3771,34 @@ static int run_pr(wedge_graph* h, const wedge_params_t* p, wedge_stats_t* st)
         if (rc)
             return rc;
     }
+    const bool c32 = h->s.precision == WEDGE_PREC_FP32C;
     double t_pull = 0, t_vertex = 0;
     WEDGE_CHECK(cudaEventRecord(h->ev[0], h->stream));
-    pr_init_kernel<<<vgrid, AUX_THREADS, 0, h->stream>>>(g, h->s, p->num_iterations);
+    if (c32)
+        launch_pr32_init(h, p->num_iterations);
+    else
+        pr_init_kernel<<<vgrid, AUX_THREADS, 0, h->stream>>>(g, h->s, p->num_iterations);
     if (use_graph)
         WEDGE_CHECK(cudaGraphLaunch(h->pr_exec, h->stream));
     for (uint32_t it = 0; !use_graph && it < p->num_iterations; ++it) {
         if (timing)
             WEDGE_CHECK(cudaEventRecord(h->ev[2], h->stream));
-        launch_pull(h, WEDGE_APP_PR);
+        if (c32)
+            pr32_pull_kernel<<<h->pull_grid, PULL_THREADS, h->hub_bytes + PR32_STAGE_BYTES, h->stream>>>(g, h->s,
+                                                                                                    counters(h));
+        else
+            launch_pull(h, WEDGE_APP_PR);
         if (timing)
             WEDGE_CHECK(cudaEventRecord(h->ev[3], h->stream));
-        pr_finish_kernel<<<fgrid, AUX_THREADS, 0, h->stream>>>(g, h->s, h->pull_grid, counters(h));
-        launch_pr_total(h);
-        pr_vertex_kernel<<<vgrid, AUX_THREADS, 0, h->stream>>>(g, h->s);
+        if (c32) {
+            const uint32_t g32 = pr32_finish_grid(h);
+            pr32_finish_kernel<<<g32, AUX_THREADS, 0, h->stream>>>(g, h->s, h->pull_grid);
+            pr32_total_kernel<<<1, AUX_THREADS, 0, h->stream>>>(h->s, h->pull_grid + g32, counters(h), h->pull_grid);
+        } else {
+            pr_finish_kernel<<<fgrid, AUX_THREADS, 0, h->stream>>>(g, h->s, h->pull_grid, counters(h));
+            launch_pr_total(h);
+            pr_vertex_kernel<<<vgrid, AUX_THREADS, 0, h->stream>>>(g, h->s);
+        }
         if (timing) {
             WEDGE_CHECK(cudaEventRecord(h->ev[4], h->stream));
             WEDGE_CHECK(cudaEventSynchronize(h->ev[4]));
@@ -3146,6 +3813,8 @@ static int run_pr(wedge_graph* h, const wedge_params_t* p, wedge_stats_t* st)
             }
         }
     }
+    if (c32)
+        launch_pr32_iso(h); /* vertices with neither in- nor out-edges, once */
     WEDGE_CHECK(cudaEventRecord(h->ev[1], h->stream));
     double* sums = pr_sums(h);
     pr_sum_kernel<<<vgrid, AUX_THREADS, 0, h->stream>>>(g, h->s, sums);
@@ -3169,7 +3838,9 @@ static int run_pr(wedge_graph* h, const wedge_params_t* p, wedge_stats_t* st)
         st->edges_scanned = c.edges_scanned;
         st->tiles_scanned = c.tiles_scanned;
         st->pull_launches = c.pull_launches;
-        st->kernel_launches = 3ull + (use_graph ? 5ull : 4ull) * p->num_iterations; /* + the loop condition */
+        /* init (+ total), the iterations (+ the loop condition), the sums (+ isolated vertices) */
+        st->kernel_launches = c32 ? 5ull + (use_graph ? 4ull : 3ull) * p->num_iterations
+                                  : 3ull + (use_graph ? 5ull : 4ull) * p->num_iterations;
         st->pr_sum = c.pr_sum;
     }
     if (c.error)
@@ -3252,7 +3923,9 @@ int wedge_cuda_run_phase(wedge_graph_t* g, int app, int phase, const wedge_param
     Ctrl c;
     switch (phase) {
     case WEDGE_PHASE_INIT:
-        if (app == WEDGE_APP_PR) {
+        if (app == WEDGE_APP_PR && g->s.precision == WEDGE_PREC_FP32C) {
+            launch_pr32_init(g, 0u);
+        } else if (app == WEDGE_APP_PR) {
             pr_init_kernel<<<vgrid, AUX_THREADS, 0, g->stream>>>(dg, g->s, 0u);
         } else {
             const uint64_t root = params->root < dg.V ? params->root : 0;
@@ -3280,12 +3953,15 @@ int wedge_cuda_run_phase(wedge_graph_t* g, int app, int phase, const wedge_param
         } else if (phase == WEDGE_PHASE_PULL_WEDGE) {
             return WEDGE_ERR_UNSUPPORTED; /* PageRank has no Wedge pull (application.c:154) */
         }
-        launch_pull(g, app);
-        if (app == WEDGE_APP_PR) {
+        if (app == WEDGE_APP_PR && g->s.precision == WEDGE_PREC_FP32C) {
+            launch_pr32_iteration(g); /* the vertex phase of vertices with in-edges included */
+        } else if (app == WEDGE_APP_PR) {
+            launch_pull(g, app);
             pr_finish_kernel<<<finish_grid(g, dg), AUX_THREADS, 0, g->stream>>>(
                 dg, g->s, g->pull_grid, counters(g));
             launch_pr_total(g);
         } else {
+            launch_pull(g, app);
             decide_kernel<<<1, AUX_THREADS, 0, g->stream>>>(dg, g->s, counters(g), pull_slots(g, app), (uint32_t)app);
         }
         break;
@@ -3293,7 +3969,10 @@ int wedge_cuda_run_phase(wedge_graph_t* g, int app, int phase, const wedge_param
     case WEDGE_PHASE_VERTEX_PR:
         if (app != WEDGE_APP_PR)
             return WEDGE_ERR_ARG;
-        pr_vertex_kernel<<<vgrid, AUX_THREADS, 0, g->stream>>>(dg, g->s);
+        if (g->s.precision == WEDGE_PREC_FP32C)
+            launch_pr32_iso(g); /* the pull finished every other vertex */
+        else
+            pr_vertex_kernel<<<vgrid, AUX_THREADS, 0, g->stream>>>(dg, g->s);
         break;
     case WEDGE_PHASE_WEDGE_BUILD:
         if (app == WEDGE_APP_PR)
@@ -3696,7 +4375,7 @@ extern "C" int wedge_cuda_pr_iteration_noalloc(uint64_t num_vertices, uint64_t n
                                                                                           sc->dst_start);
     if (num_dsts)
         split_kernel<<<grid_for(num_dsts, AUX_THREADS, grid * 2u), AUX_THREADS, 0, st>>>(
-            g.dst_off, g.Vne, T, sc->split_k, sc->split_t0, sc->split_t1, sc->nsplit);
+            g.dst_off, g.Vne, T, TILE, sc->split_k, sc->split_t0, sc->split_t1, sc->nsplit);
     WEDGE_CHECK(cudaMemsetAsync(rank_out, 0, num_vertices * sizeof(double), st));
     DevState sp = s;
     sp.rank = (double*)rank_in; /* gathered by the pull */

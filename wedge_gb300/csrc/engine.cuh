@@ -99,7 +99,9 @@ struct Ctrl {
     unsigned int learned_iters;        // iterations whose mode the scheduler network chose
     unsigned int alist_n;              // vertices in the Wedge-build vertex list
     unsigned int pr_ticket;            // blocks of pr_total_kernel done (the last one resets it)
-    double pr_total;                   // sum of all accumulators (phase_vertex_pr.c:161)
+    double pr_total;                   // sum of all accumulators (phase_vertex_pr.c:161); compensated FP32:
+                                       // the total the next iteration uses
+    double pr_prev;                    // compensated FP32: the total the last iteration used
     double pr_sum;                     // PageRank Sum statistic
 };
 
@@ -113,6 +115,7 @@ struct DevGraph {
     uint32_t csri_pos;         // csri holds in-edge positions (Epad < 2^32), else chunk ids
     const uint32_t* src;
     const unsigned long long* w;
+    const uint8_t* w8;         // the same weights in one byte each, when every weight is a uint64 below 256
     const uint32_t* dst_id;
     const unsigned long long* dst_off;
     const uint32_t* tile_dst0;
@@ -133,13 +136,24 @@ struct DevState {
     uint32_t* prop32;              // BFS parent / CC label
     unsigned long long* prop64;    // SSSP distance (uint64 or double bits)
     double* rank;                  // PageRank FP64: rank / outdegree'
-    float* rank32;                 // PageRank FP32C: rank / outdegree'
     double* acc;                   // PageRank accumulators (graph_vertex_accumulators)
     double* inv_od;                // PageRank 1 / outdegree' (outdegree, or N for dangling vertices)
     double* head_part;             // [T] partial sum of a split destination ending in tile t
     double* tail_part;             // [T] partial sum of a split destination continuing past tile t
-    float* head_part32;            // FP32C partial sums (value, compensation) interleaved
-    float* tail_part32;
+    // compensated-FP32 PageRank (WEDGE_PREC_FP32C): see pr32_pull_kernel
+    float* rank32;                 // [2][rstride] rank / outdegree', double-buffered by iteration parity
+    float* inv32;                  // [V] 1 / outdegree' in FP32, negative for a dangling vertex (-1/N)
+    uint64_t rstride;              // floats between the two rank buffers (V rounded up to 32)
+    uint32_t* zlist;               // vertices without in-edges and with out-edges (their rank is the same constant)
+    uint32_t* ilist;               // vertices without in-edges or out-edges (written once, after the last iteration)
+    uint32_t nz, ni;
+    uint32_t* psplit_k;            // destinations spanning pull tiles (PR32_TILE in-edges): short ones from the
+    uint32_t* psplit_t0;           // front (pnsplit), long ones from the back (pnwide; entry pT-1-j)
+    uint32_t* psplit_t1;
+    uint32_t pnsplit, pnwide, pT;
+    float2* phead;                 // [pT] (sum, compensation) of a split destination ending in tile t
+    float2* ptail;                 // [pT] (sum, compensation) of a split destination continuing past tile t
+    double* pmass;                 // per-block partial sums of the non-dangling ranks (the next total rank)
     double* block_part;            // [grid] per-block sums of tile sums
     uint32_t* front0;              // V-bit frontier bitmaps (active / snapshot)
     uint32_t* front1;
@@ -166,6 +180,7 @@ struct DevState {
     uint32_t hub_tile;             // CC/SSSP: first tile whose destinations all have ids >= hub_n
     uint32_t hub_k;                // CC/SSSP: compressed destinations with ids < hub_n
     const float* net;              // scheduler network blob (WEDGE_SCHED_LEARNED), or null
+    uint32_t push;                 // SSSP over in-edge positions: Wedge pulls relax the activated sources' out-edges
 };
 
 }  // namespace wedge

@@ -34,6 +34,13 @@ __device__ __forceinline__ void ld_stream_v4u64(const unsigned long long* p, uns
                  : "l"(p));
 }
 
+__device__ __forceinline__ unsigned long long ld_stream_u64(const void* p)
+{
+    unsigned long long r;
+    asm volatile("ld.global.nc.L1::no_allocate.u64 %0, [%1];" : "=l"(r) : "l"(p));
+    return r;
+}
+
 /* ---- hub cache: a bulk (TMA) copy of the low-id end of the gathered array
  * into shared memory, completed on an mbarrier.  Vertices are relabelled by
  * descending out-degree, so ids [0, hub_n) are the sources most in-edges
