@@ -329,7 +329,9 @@ void wedge_cuda_batch_free(wedge_batch_t* b);
  * for the default stream) and the call returns without waiting.  The first call
  * on a device looks up the scratch array's device address (make that first call
  * before any stream capture).  All calls share the one array: calls that
- * overlap on the GPU race and must be ordered by the caller. */
+ * overlap on the GPU race and must be ordered by the caller.  The address is
+ * kept for the life of the process: calls from a context other than the
+ * device's primary context, or after a cudaDeviceReset, are not supported. */
 #define WEDGE_NOALLOC_MAX_EDGES (1ull << 24)
 int wedge_cuda_pr_iteration_noalloc(uint64_t num_vertices, uint64_t num_dsts, uint64_t num_edges,
                                     const uint64_t* dst_off, const uint32_t* dst_id, const uint32_t* src,

@@ -75,6 +75,41 @@ def test_noalloc_iteration_matches_engine(engine_lib, oracle_lib, scale, edge_fa
     assert _rel_l1(got1, want1) < PR_TOL
     got2 = call(r1, r2)  # second call in a row: the shared scratch is reused
     assert _rel_l1(got2, want2) < PR_TOL
+    # and against the oracle's restatement of the reference
+    ref, _, _ = O.Graph.from_edges(V, s, d, O.PR).run(iterations=2, threads=4)
+    assert _rel_l1(got2, ref.view(np.float64)) < PR_TOL
+
+
+def test_noalloc_reuse_across_graphs_on_a_stream(engine_lib, oracle_lib):
+    """One caller-created stream; a graph at the scratch's limit (R-MAT scale 20,
+    edge factor 16: exactly 2^24 in-edges) and then a smaller one reuse the shared
+    scratch, which must hold nothing over from the larger call."""
+    torch = pytest.importorskip("torch")
+    W, O = engine_lib, oracle_lib
+    L = W.lib()
+    stream = torch.cuda.Stream()
+    for scale, edge_factor, seed in ((20, 16, 21), (12, 8, 22)):
+        V, s, d, dst_id, dst_off, src, outdeg = _csc(O, scale, edge_factor, seed)
+        E = len(s)
+        assert E <= 1 << 24
+        with W.Graph.from_edges(V, s, d) as g:
+            g.run(W.APP_PR, W.Params(num_iterations=1, damping=0.85))
+            want = g.read_results().view(np.float64).copy()
+        ref, _, _ = O.Graph.from_edges(V, s, d, O.PR).run(iterations=1, damping=0.85, threads=4)
+        od = np.where(outdeg == 0, V, outdeg).astype(np.float64)
+        with torch.cuda.stream(stream):
+            t_off, t_id, t_src, t_od = (_dev(torch, x) for x in (dst_off, dst_id, src, outdeg))
+            r0 = _dev(torch, (1.0 / V) / od)
+            r1 = torch.empty(V, dtype=torch.float64, device="cuda")
+        stream.synchronize()
+        rc = L.wedge_cuda_pr_iteration_noalloc(V, len(dst_id), E, t_off.data_ptr(), t_id.data_ptr(), t_src.data_ptr(),
+                                                t_od.data_ptr(), r0.data_ptr(), r1.data_ptr(), 0.85,
+                                                C.c_void_p(stream.cuda_stream))
+        assert rc == 0, W.status_string(rc)
+        stream.synchronize()
+        got = r1.cpu().numpy()
+        assert _rel_l1(got, want) < PR_TOL, scale
+        assert _rel_l1(got, ref.view(np.float64)) < PR_TOL, scale
 
 
 def test_noalloc_rejects_sizes_beyond_its_scratch(engine_lib):

@@ -1284,6 +1284,206 @@ __global__ void __launch_bounds__(PULL_THREADS, 1)
     }
 }
 
+// SSSP dense and source-filtered pulls over 512-edge tiles, for graphs with
+// byte-wide weights and in-edge positions in the CSRI (Wedge pulls relax the
+// activated sources' in-edges, sssp_push_pull).  Lane l loads its 16 sources
+// (two 256-bit loads) and 16 weight bytes (one 128-bit load), gathers the
+// sources' distances (hub cache or global memory) and adds the weights; the
+// warp takes the per-destination minimum with the segmented reduction.  The
+// minima of the tile's complete destinations (SSSP_SLOTS at most) are staged
+// in the warp's slice of shared memory and compared, written and activated by
+// the warp's lanes together over consecutive destinations; spanning
+// destinations take atomicMin.  Two launches as pull_kernel's (hub
+// destinations' tiles first).  Dynamic shared memory: hub cache | staged minima.
+constexpr int SSSP_EPL = 16;
+constexpr uint32_t SSSP_TILE = 32u * SSSP_EPL;
+constexpr uint32_t SSSP_SLOTS = 128;
+constexpr uint32_t SSSP_STAGE_BYTES = (PULL_THREADS / 32) * SSSP_SLOTS * 8u;
+
+__global__ void __launch_bounds__(PULL_THREADS, 1)
+    sssp_pull_kernel(DevGraph g, DevState s, unsigned long long* block_cnt, uint32_t phase)
+{
+    constexpr int EPL = SSSP_EPL;
+    constexpr int WARPS = PULL_THREADS / 32;
+    constexpr uint32_t Q = SSSP_TILE / TILE;
+    __shared__ unsigned long long sh_cnt[WARPS][NCNT];
+    __shared__ unsigned long long hub_bar;
+    __shared__ unsigned int sh_deg[3];
+    extern __shared__ __align__(16) unsigned char sssp_smem[];
+    Ctrl* c = s.ctrl;
+    if (c->done)
+        return;
+    const uint32_t mode = c->mode;
+    if (mode == MODE_WEDGE) {
+        if (phase == PHASE_HUBS)
+            sssp_push_pull(g, s, c, block_cnt);
+        else if (threadIdx.x < NCNT)
+            block_cnt[NCNT * blockIdx.x + threadIdx.x] = 0ull; /* a Wedge pull runs whole in the first launch */
+        return;
+    }
+    const int lane = threadIdx.x & 31;
+    const int wib = threadIdx.x >> 5;
+    const uint32_t gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const uint32_t nw = (gridDim.x * blockDim.x) >> 5;
+    const uint32_t T = (uint32_t)((g.E + SSSP_TILE - 1) / SSSP_TILE);
+    const uint32_t split = min(s.hub_tile, T);
+    const uint32_t t_begin = phase == PHASE_HUBS ? 0u : split, t_end = phase == PHASE_HUBS ? split : T;
+    const uint32_t* cur = cur_front(s, c->parity);
+    uint32_t* nxt = next_front(s, c->parity);
+    const bool filtered = mode == MODE_FILTERED;
+    const uint32_t hub_bytes = s.hub_bytes;
+    unsigned long long* hub64 = reinterpret_cast<unsigned long long*>(sssp_smem);
+    unsigned long long* my_min = reinterpret_cast<unsigned long long*>(sssp_smem + hub_bytes) + (uint32_t)wib * SSSP_SLOTS;
+    unsigned long long mass = 0, edges = 0, tiles = 0, dsts = 0, act = 0;
+    if (threadIdx.x < 3)
+        sh_deg[threadIdx.x] = 0u;
+    const bool use_hub = hub_bytes != 0u && ((uintptr_t)s.prop64 & 15u) == 0u;
+    __syncthreads();
+    if (use_hub) {
+        if (threadIdx.x == 0) {
+            mbar_init(&hub_bar, 1u);
+            mbar_arrive_expect_tx(&hub_bar, hub_bytes);
+            for (uint32_t off = 0; off < hub_bytes; off += 32768u)
+                bulk_g2s(sssp_smem + off, reinterpret_cast<const unsigned char*>(s.prop64) + off,
+                         min(32768u, hub_bytes - off), &hub_bar);
+        }
+        __syncthreads();
+    }
+    uint32_t hub_lim = 0;
+    // a changed destination: its bit in the next frontier and, the first time, its out-edge mass
+    auto activate = [&](uint32_t vtx) {
+        const uint32_t b = 1u << (vtx & 31u);
+        if (!(atomicOr(&nxt[vtx >> 5], b) & b)) {
+            const uint32_t od = g.outdeg[vtx];
+            mass += od;
+            ++act;
+            const uint32_t bk = degree_bucket(od);
+            if (bk < 3u)
+                atomicAdd(&sh_deg[bk], 1u);
+        }
+    };
+    uint32_t t = t_begin + gw;
+    uint32_t k0n = 0, kendn = 0;
+    if (t < t_end) {
+        k0n = g.tile_dst0[(uint64_t)t * Q];
+        kendn = g.tile_dst0[((uint64_t)t + 1u) * Q];
+    }
+    for (; t < t_end; t += nw) {
+        const uint32_t k0 = k0n, kend = kendn;
+        if (t + nw < t_end) {
+            k0n = g.tile_dst0[(uint64_t)(t + nw) * Q];
+            kendn = g.tile_dst0[((uint64_t)(t + nw) + 1u) * Q];
+        }
+        if (use_hub && hub_lim == 0u) {
+            uint32_t ready = 0u;
+            if (lane == 0)
+                ready = mbar_test_wait(&hub_bar, 0u) ? 1u : 0u;
+            if (__shfl_sync(FULL, ready, 0))
+                hub_lim = hub_bytes / 8u;
+        }
+        ++tiles;
+        const uint64_t base = (uint64_t)t * SSSP_TILE;
+        uint32_t sa[EPL];
+        {
+            const uint32_t* p = g.src + base + (uint64_t)lane * EPL;
+            uint32_t x[8];
+            ld_stream_v8(p, x);
+#pragma unroll
+            for (int j = 0; j < 8; ++j)
+                sa[j] = x[j];
+            ld_stream_v8(p + 8, x);
+#pragma unroll
+            for (int j = 0; j < 8; ++j)
+                sa[8 + j] = x[j];
+        }
+        const uint4 wq = __ldg(reinterpret_cast<const uint4*>(g.w8 + base + (uint64_t)lane * EPL));
+        const uint32_t wword[4] = {wq.x, wq.y, wq.z, wq.w};
+        unsigned long long v[EPL];
+#pragma unroll
+        for (int q = 0; q < EPL; ++q) {
+            const uint32_t x = sa[q];
+            bool on = x != NONE32;
+            if (filtered && on)
+                on = (ld_ro_u32(cur + (x >> 5)) >> (x & 31u)) & 1u; /* changed by the previous pull */
+            const unsigned long long d = !on ? NONE64 : (x < hub_lim) ? hub64[x] : s.prop64[x];
+            const unsigned long long w = (wword[q >> 2] >> (8 * (q & 3))) & 0xFFu;
+            v[q] = (d == NONE64) ? NONE64 : d + w; /* phase_edge_pull_sssp.c:136-137 */
+            edges += (x != NONE32) ? 1u : 0u;
+        }
+        TileGeo<EPL> tg;
+        tile_geometry_bits<EPL>(g, base, t + 1u >= T, k0, kend, lane, tg);
+        dsts += tg.ndst;
+        // the reduction stages the minima of the tile's first SSSP_SLOTS complete
+        // destinations, which the lanes then compare and write over consecutive
+        // destinations; the others (tiles of many low in-degree destinations)
+        // and the spanning ones are applied where the reduction ends them
+        seg_reduce<EPL>(v, tg, lane, MinU64(), [&](uint32_t k, unsigned long long val, int kind) {
+            const uint32_t slot = k - tg.k0;
+            if (kind == EMIT_COMPLETE && slot < SSSP_SLOTS) {
+                my_min[slot] = val;
+                return;
+            }
+            if (val == NONE64)
+                return;
+            const uint32_t vtx = g.dst_ident ? k : g.dst_id[k];
+            if (kind == EMIT_COMPLETE) { /* the destination's only writer in this launch */
+                if (val < s.prop64[vtx]) {
+                    s.prop64[vtx] = val;
+                    if (vtx < hub_lim)
+                        atomicMin(&hub64[vtx], val);
+                    activate(vtx);
+                }
+            } else if (val < s.prop64[vtx] && val < atomicMin(&s.prop64[vtx], val)) {
+                if (vtx < hub_lim)
+                    atomicMin(&hub64[vtx], val);
+                activate(vtx);
+            }
+        });
+        __syncwarp();
+        const uint32_t nd = tg.ndst;
+        const uint32_t jlo = tg.k0_fresh ? 0u : 1u;
+        const uint32_t jhi = min(tg.tail_cont ? nd - 1u : nd, SSSP_SLOTS);
+        for (uint32_t j = jlo + (uint32_t)lane; j < jhi; j += 32u) {
+            const unsigned long long val = my_min[j];
+            if (val == NONE64)
+                continue;
+            const uint32_t k = tg.k0 + j;
+            const uint32_t vtx = g.dst_ident ? k : g.dst_id[k];
+            if (val < s.prop64[vtx]) { /* the destination's only writer in this launch */
+                s.prop64[vtx] = val;
+                if (vtx < hub_lim)
+                    atomicMin(&hub64[vtx], val);
+                activate(vtx);
+            }
+        }
+        __syncwarp(); /* my_min is rewritten by the next tile */
+    }
+    if (use_hub && threadIdx.x == 0 && !mbar_wait_bounded(&hub_bar, 0u, HUB_WAIT_TRIES)) {
+        atomicOr(&c->error, ERR_HUB_TIMEOUT);
+        mbar_wait_bounded(&hub_bar, 0u, HUB_WAIT_TRIES);
+    }
+    mass = warp_sum_u64(mass);
+    edges = warp_sum_u64(edges);
+    act = warp_sum_u64(act);
+    if (lane == 0) {
+        sh_cnt[wib][CNT_MASS] = mass;
+        sh_cnt[wib][CNT_EDGES] = edges;
+        sh_cnt[wib][CNT_TILES] = tiles;
+        sh_cnt[wib][CNT_DSTS] = dsts;
+        sh_cnt[wib][CNT_ACT] = act;
+    }
+    __syncthreads();
+    if (threadIdx.x < NCNT) {
+        unsigned long long a = 0;
+        if (threadIdx.x >= CNT_DEG0)
+            a = sh_deg[threadIdx.x - CNT_DEG0];
+        else
+            for (int w = 0; w < WARPS; ++w)
+                a += sh_cnt[w][threadIdx.x];
+        block_cnt[NCNT * blockIdx.x + threadIdx.x] = a;
+    }
+}
+
 // The per-destination work of a dense pull, one destination per lane, launched
 // before the tile pull (pull_kernel): the BFS probe; the CC probe; CC's first
 // pull over engine-id labels (launch A: the hub destinations, launch B: the
@@ -2566,6 +2766,11 @@ __global__ void pr_total_kernel(const double* acc, uint64_t V, double* part, Ctr
 // out-edges are written once, after the last iteration (pr32_iso_kernel).
 constexpr int PR32_EPL = 16;
 constexpr uint32_t PR32_TILE = 32u * PR32_EPL;
+// staged destination sums per warp: 128 cover every destination of 97% of the
+// 512-edge tiles of an R-MAT graph; the shared memory they take comes out of
+// the L1 the gathers depend on (a stage of a whole tile's 512 ran 0.5 ms per
+// iteration slower at R-MAT scale 26)
+constexpr uint32_t PR32_SLOTS = 128;
 
 __device__ __forceinline__ const float* pr32_cur(const DevState& s)
 {
@@ -2641,6 +2846,34 @@ __global__ void mark_has_in_kernel(DevGraph g, uint32_t* has_in)
     }
 }
 
+// complete destinations past the first PR32_SLOTS of their PR32_TILE-edge
+// tile (they are finished from ovf_sum): their count per tile (fill == null)
+// or, at the tile's offset from a scan of the counts, the list itself in tile
+// order.  The tile geometry is the pull's (the destination-start bitmap).
+__global__ void pr32_overflow_kernel(DevGraph g, uint32_t T, uint32_t* count, const uint32_t* off, uint32_t* fill)
+{
+    constexpr uint32_t W = PR32_TILE / 32, Q = PR32_TILE / TILE;
+    for (uint32_t t = blockIdx.x * blockDim.x + threadIdx.x; t < T; t += gridDim.x * blockDim.x) {
+        const uint64_t w0 = (uint64_t)t * W;
+        uint32_t starts = 0;
+        for (uint32_t i = 0; i < W; ++i)
+            starts += __popc(g.dst_start[w0 + i]);
+        const bool fresh = g.dst_start[w0] & 1u;
+        const uint32_t nd = starts - (fresh ? 1u : 0u) + 1u;
+        const uint32_t k0 = g.tile_dst0[(uint64_t)t * Q], kend = g.tile_dst0[((uint64_t)t + 1u) * Q];
+        const bool tail_cont = t + 1u < T && kend == k0 + nd - 1u;
+        const uint32_t jlo = max(fresh ? 0u : 1u, PR32_SLOTS);
+        const uint32_t jhi = tail_cont ? nd - 1u : nd;
+        const uint32_t n = jhi > jlo ? jhi - jlo : 0u;
+        if (!fill) {
+            count[t] = n;
+        } else {
+            for (uint32_t j = 0; j < n; ++j)
+                fill[off[t] + j] = k0 + jlo + j;
+        }
+    }
+}
+
 // stream compaction by an exclusive scan of 0/1 flags: list in ascending id order
 __global__ void compact_flags_kernel(const uint32_t* flag, const uint32_t* pos, uint64_t n, uint32_t* list)
 {
@@ -2698,7 +2931,7 @@ __global__ void pr32_init_kernel(DevGraph g, DevState s, uint32_t max_iter)
 // of shared memory and finished by the warp's lanes together: consecutive
 // destinations, so their outdegree' and rank writes coalesce.  Destinations
 // spanning tiles leave (sum, compensation) partials for pr32_finish_kernel.
-// Dynamic shared memory: hub cache (hub_bytes) | staged sums [32 warps][PR32_TILE].
+// Dynamic shared memory: hub cache (hub_bytes) | staged sums [32 warps][PR32_SLOTS].
 // block_cnt[NCNT*b + CNT_*] as pull_kernel's; s.pmass[b] = the block's sum of
 // the new non-dangling ranks.
 __global__ void __launch_bounds__(PULL_THREADS, 1) pr32_pull_kernel(DevGraph g, DevState s, unsigned long long* block_cnt)
@@ -2721,7 +2954,7 @@ __global__ void __launch_bounds__(PULL_THREADS, 1) pr32_pull_kernel(DevGraph g, 
     const uint32_t T = (uint32_t)((g.E + PR32_TILE - 1) / PR32_TILE); /* tiles holding real in-edges */
     const uint32_t hub_bytes = s.hub_bytes;
     const float* hub = reinterpret_cast<const float*>(pr32_smem);
-    float* my_sum = reinterpret_cast<float*>(pr32_smem + hub_bytes) + (uint32_t)wib * PR32_TILE;
+    float* my_sum = reinterpret_cast<float*>(pr32_smem + hub_bytes) + (uint32_t)wib * PR32_SLOTS;
 
     // ---- hub cache: ranks [0, hub_n) of the current buffer
     const bool use_hub = hub_bytes != 0u && (s.rstride & 3ull) == 0ull;
@@ -2739,6 +2972,9 @@ __global__ void __launch_bounds__(PULL_THREADS, 1) pr32_pull_kernel(DevGraph g, 
 
     unsigned long long edges = 0, tiles = 0, dsts = 0;
     F2 mass{0.0f, 0.0f};
+#ifdef WEDGE_STREAM_EVICT_FIRST
+    const unsigned long long pol = l2_evict_first_policy();
+#endif
     uint32_t t = gw;
     uint32_t k0n = 0, kendn = 0;
     if (t < T) {
@@ -2764,11 +3000,19 @@ __global__ void __launch_bounds__(PULL_THREADS, 1) pr32_pull_kernel(DevGraph g, 
         {
             const uint32_t* p = g.src + base + (uint64_t)lane * EPL;
             uint32_t x[8];
+#ifdef WEDGE_STREAM_EVICT_FIRST
+            ld_stream_v8_ef(p, x, pol);
+#else
             ld_stream_v8(p, x);
+#endif
 #pragma unroll
             for (int j = 0; j < 8; ++j)
                 sa[j] = x[j];
+#ifdef WEDGE_STREAM_EVICT_FIRST
+            ld_stream_v8_ef(p + 8, x, pol);
+#else
             ld_stream_v8(p + 8, x);
+#endif
 #pragma unroll
             for (int j = 0; j < 8; ++j)
                 sa[8 + j] = x[j];
@@ -2783,17 +3027,26 @@ __global__ void __launch_bounds__(PULL_THREADS, 1) pr32_pull_kernel(DevGraph g, 
         TileGeo<EPL> tg;
         tile_geometry_bits<EPL>(g, base, t + 1u >= T, k0, kend, lane, tg);
         dsts += tg.ndst;
+        // The reduction stages the sums of the tile's first PR32_SLOTS complete
+        // destinations; the vertex phase then runs for them with the lanes over
+        // consecutive destinations.  A tile of more destinations (many low
+        // in-degree ones) leaves the others' sums in ovf_sum, finished by
+        // pr32_finish_kernel from the graph's fixed list of such destinations.
         seg_reduce<EPL>(v, tg, lane, AddF2(), [&](uint32_t k, F2 val, int kind) {
-            if (kind == EMIT_COMPLETE)
-                my_sum[k - tg.k0] = __fadd_rn(val.s, val.c);
-            else
+            if (kind == EMIT_COMPLETE) {
+                const uint32_t slot = k - tg.k0;
+                if (slot < PR32_SLOTS)
+                    my_sum[slot] = __fadd_rn(val.s, val.c);
+                else
+                    s.ovf_sum[k] = __fadd_rn(val.s, val.c);
+            } else {
                 (kind == EMIT_HEAD ? s.phead : s.ptail)[t] = make_float2(val.s, val.c);
+            }
         });
         __syncwarp();
-        // the vertex phase of the tile's complete destinations, lanes over consecutive ones
         const uint32_t nd = tg.ndst;
-        const uint32_t jlo = tg.k0_fresh ? 0u : 1u;              /* slot 0 began in an earlier tile */
-        const uint32_t jhi = tg.tail_cont ? nd - 1u : nd;         /* the last slot continues */
+        const uint32_t jlo = tg.k0_fresh ? 0u : 1u;                        /* slot 0 began in an earlier tile */
+        const uint32_t jhi = min(tg.tail_cont ? nd - 1u : nd, PR32_SLOTS); /* the last slot may continue */
         for (uint32_t j = jlo + (uint32_t)lane; j < jhi; j += 32u) {
             const uint32_t k = tg.k0 + j;
             const uint32_t vtx = g.dst_ident ? k : g.dst_id[k];
@@ -2879,6 +3132,10 @@ __global__ void pr32_finish_kernel(DevGraph g, DevState s, uint32_t part0)
             const float2 h = s.phead[b];
             finish(s.psplit_k[i], add(x, F2{h.x, h.y}));
         }
+    }
+    for (uint32_t i = tid; i < s.novf; i += nthr) { /* complete destinations past a tile's staged slots */
+        const uint32_t k = s.ovf_list[i];
+        finish(k, F2{s.ovf_sum[k], 0.0f});
     }
     const float r0 = pr32_rank(K, 0.0f);
     for (uint32_t i = tid; i < s.nz; i += nthr) {
@@ -3116,8 +3373,18 @@ int compute_grids(wedge_graph* h)
 // launches + two tile launches)
 static uint64_t counter_slots(const wedge_graph* h) { return 2ull * h->dst_grid + 2ull * h->pull_grid; }
 
-static const void* pull_fn(int app)
+// SSSP runs sssp_pull_kernel where the graph has byte-wide weights and the
+// Wedge pulls relax over in-edge positions, else pull_kernel
+static bool sssp_tiles512(const wedge_graph* h)
 {
+    const char* e = getenv("WEDGE_SSSP_TILES512");
+    return h->s.push && h->g.w8 && !(e && e[0] == '0');
+}
+
+static const void* pull_fn(const wedge_graph* h, int app)
+{
+    if (app == WEDGE_APP_SSSP && sssp_tiles512(h))
+        return (const void*)sssp_pull_kernel;
     switch (app) {
     case WEDGE_APP_BFS:
         return (const void*)pull_kernel<WEDGE_APP_BFS, PullEpl<WEDGE_APP_BFS>::value>;
@@ -3130,8 +3397,10 @@ static const void* pull_fn(int app)
     }
 }
 
-static uint32_t pull_tile_e(int app)
+static uint32_t pull_tile_e(const wedge_graph* h, int app)
 {
+    if (app == WEDGE_APP_SSSP && sssp_tiles512(h))
+        return SSSP_TILE;
     switch (app) {
     case WEDGE_APP_BFS:
         return 32u * PullEpl<WEDGE_APP_BFS>::value;
@@ -3154,13 +3423,14 @@ constexpr uint64_t HUB_BYTES_DEFAULT = 65536;
 
 static int setup_hub(wedge_graph* h, int app, int precision)
 {
-    const void* fn = pull_fn(app);
+    const void* fn = pull_fn(h, app);
     cudaFuncAttributes fa;
     WEDGE_CHECK(cudaFuncGetAttributes(&fa, fn));
     int optin = 0;
     WEDGE_CHECK(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, h->device));
     const uint64_t elem = (app == WEDGE_APP_SSSP || (app == WEDGE_APP_PR && precision != WEDGE_PREC_FP32C)) ? 8 : 4;
-    uint64_t avail = (uint64_t)optin > fa.sharedSizeBytes + 64u ? (uint64_t)optin - fa.sharedSizeBytes - 64u : 0u;
+    const uint64_t stage = (app == WEDGE_APP_SSSP && sssp_tiles512(h)) ? SSSP_STAGE_BYTES : 0u; /* after the cache */
+    uint64_t avail = (uint64_t)optin > fa.sharedSizeBytes + stage + 64u ? (uint64_t)optin - fa.sharedSizeBytes - stage - 64u : 0u;
     const char* cap = getenv("WEDGE_HUB_BYTES");
     const uint64_t want = cap ? strtoull(cap, nullptr, 10) : HUB_BYTES_DEFAULT;
     if (want < avail)
@@ -3175,10 +3445,11 @@ static int setup_hub(wedge_graph* h, int app, int precision)
     h->s.hub_k = 0;
     h->hub_bytes = (uint32_t)(n * elem);
     h->s.hub_bytes = h->hub_bytes;
-    WEDGE_CHECK(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)h->hub_bytes));
+    h->pull_smem = h->hub_bytes + (uint32_t)stage;
+    WEDGE_CHECK(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)h->pull_smem));
     if (two_phase_app(app) && n) {
         uint32_t* d = (uint32_t*)(h->s.block_part + h->pull_grid); /* counters: scratch until the first pull */
-        hub_split_kernel<<<1, 1, 0, h->stream>>>(h->g, (uint32_t)n, pull_tile_e(app), d);
+        hub_split_kernel<<<1, 1, 0, h->stream>>>(h->g, (uint32_t)n, pull_tile_e(h, app), d);
         WEDGE_CHECK(cudaGetLastError());
         uint32_t t[2] = {0, 0};
         WEDGE_CHECK(cudaMemcpyAsync(t, d, sizeof(t), cudaMemcpyDeviceToHost, h->stream));
@@ -3190,7 +3461,7 @@ static int setup_hub(wedge_graph* h, int app, int precision)
 }
 
 // dynamic shared memory of pr32_pull_kernel beyond its hub cache: the staged sums
-constexpr uint32_t PR32_STAGE_BYTES = (PULL_THREADS / 32) * PR32_TILE * sizeof(float);
+constexpr uint32_t PR32_STAGE_BYTES = (PULL_THREADS / 32) * PR32_SLOTS * sizeof(float);
 
 // hub cache of the compensated-FP32 pull: HUB_BYTES_DEFAULT (or WEDGE_HUB_BYTES)
 // of the rank array, within what the block can opt into beside the staged sums
@@ -3249,6 +3520,29 @@ static int pr32_state(wedge_graph* h)
                                                                                s.psplit_t0, s.psplit_t1, d_cnt);
     unsigned int nsplit[2] = {0, 0};
     WEDGE_CHECK(cudaMemcpyAsync(nsplit, d_cnt, sizeof(nsplit), cudaMemcpyDeviceToHost, st));
+    // complete destinations past a tile's staged slots, in tile order
+    const uint32_t T = (uint32_t)((g.E + PR32_TILE - 1) / PR32_TILE);
+    s.novf = 0;
+    if ((rc = dalloc(h, &s.ovf_sum, (uint64_t)g.Vne + 1, true)))
+        return rc;
+    if (T) {
+        uint32_t *cnt = nullptr, *off = nullptr;
+        WEDGE_CHECK(cudaMallocAsync((void**)&cnt, T * sizeof(uint32_t), st));
+        WEDGE_CHECK(cudaMallocAsync((void**)&off, T * sizeof(uint32_t), st));
+        pr32_overflow_kernel<<<grid_for(T, AUX_THREADS, cap), AUX_THREADS, 0, st>>>(g, T, cnt, nullptr, nullptr);
+        if ((rc = device_scan(h, cnt, off, T, false)))
+            return rc;
+        uint32_t last[2] = {0, 0};
+        WEDGE_CHECK(cudaMemcpyAsync(&last[0], cnt + (T - 1), 4, cudaMemcpyDeviceToHost, st));
+        WEDGE_CHECK(cudaMemcpyAsync(&last[1], off + (T - 1), 4, cudaMemcpyDeviceToHost, st));
+        WEDGE_CHECK(cudaStreamSynchronize(st));
+        s.novf = last[0] + last[1];
+        if ((rc = dalloc(h, &s.ovf_list, (uint64_t)s.novf + 1, true)))
+            return rc;
+        pr32_overflow_kernel<<<grid_for(T, AUX_THREADS, cap), AUX_THREADS, 0, st>>>(g, T, cnt, off, s.ovf_list);
+        cudaFreeAsync(cnt, st);
+        cudaFreeAsync(off, st);
+    }
     // vertices without in-edges, in id order: with out-edges (gathered, so written every
     // iteration) and without (written once at the end)
     if (V == 0) {
@@ -3400,7 +3694,10 @@ static void launch_pull_app(wedge_graph* h)
             cnt += (uint64_t)NCNT * dgrid;
         }
     }
-    if (two_phase_app(APP)) {
+    if (APP == WEDGE_APP_SSSP && sssp_tiles512(h)) {
+        sssp_pull_kernel<<<grid, PULL_THREADS, h->pull_smem, h->stream>>>(h->g, h->s, cnt, PHASE_HUBS);
+        sssp_pull_kernel<<<grid, PULL_THREADS, h->pull_smem, h->stream>>>(h->g, h->s, cnt + NCNT * grid, PHASE_REST);
+    } else if (two_phase_app(APP)) {
         pull_kernel<APP, EPL><<<grid, PULL_THREADS, h->hub_bytes, h->stream>>>(h->g, h->s, cnt, PHASE_HUBS);
         pull_kernel<APP, EPL><<<grid, PULL_THREADS, h->hub_bytes, h->stream>>>(h->g, h->s, cnt + NCNT * grid,
                                                                                PHASE_REST);
@@ -3494,7 +3791,7 @@ static void launch_init(wedge_graph* h, int app, uint64_t root, uint32_t sched, 
                         uint32_t probe_iter = 0xFFFFFFFFu, uint32_t probe_mode = MODE_DENSE)
 {
     const uint64_t work = h->g.V > h->g.T ? h->g.V : h->g.T;
-    const uint32_t tile_e = pull_tile_e(app);
+    const uint32_t tile_e = pull_tile_e(h, app);
     const uint32_t topen = (uint32_t)((h->g.E + tile_e - 1) / tile_e); /* pull tiles holding in-edges */
     init_kernel<<<aux_grid(h, work), AUX_THREADS, 0, h->stream>>>(h->g, h->s, (uint32_t)app, topen);
     init_root_kernel<<<1, 32, 0, h->stream>>>(h->g, h->s, (uint32_t)app, root, sched, thr,
@@ -3686,6 +3983,8 @@ static uint32_t pr32_finish_grid(wedge_graph* h)
         work = s.pnsplit;
     if (s.nz > work)
         work = s.nz;
+    if (s.novf > work)
+        work = s.novf;
     return aux_grid(h, work + 1);
 }
 

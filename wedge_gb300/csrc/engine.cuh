@@ -154,6 +154,9 @@ struct DevState {
     float2* phead;                 // [pT] (sum, compensation) of a split destination ending in tile t
     float2* ptail;                 // [pT] (sum, compensation) of a split destination continuing past tile t
     double* pmass;                 // per-block partial sums of the non-dangling ranks (the next total rank)
+    float* ovf_sum;                // [Vne] sums of the destinations in ovf_list, by compressed destination
+    uint32_t* ovf_list;            // complete destinations past the staged slots of their tile (tile order)
+    uint32_t novf;
     double* block_part;            // [grid] per-block sums of tile sums
     uint32_t* front0;              // V-bit frontier bitmaps (active / snapshot)
     uint32_t* front1;
@@ -199,7 +202,8 @@ struct wedge_graph {
     uint32_t pull_grid;                // persistent grid of the pull kernels (one 1024-thread block per SM)
     uint32_t build_grid;
     uint32_t dst_grid;                 // dst_kernel grid (two 1024-thread blocks per SM)
-    uint32_t hub_bytes;                // dynamic shared memory of the pull kernels (the hub cache)
+    uint32_t hub_bytes;                // the hub cache's bytes
+    uint32_t pull_smem;                // dynamic shared memory of the tile pulls (hub cache + staged minima)
     float* net;                        // device copy of the scheduler network (wedge_cuda_set_scheduler)
     // allocations owned by the handle
     void* allocs[32];

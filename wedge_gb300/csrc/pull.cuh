@@ -27,6 +27,22 @@ __device__ __forceinline__ void ld_stream_v8(const uint32_t* p, uint32_t (&r)[8]
                  : "l"(p));
 }
 
+// the same with an L2 evict-first policy: the in-edge stream is read once per
+// pull and should not push the gathered property array out of L2
+__device__ __forceinline__ unsigned long long l2_evict_first_policy()
+{
+    unsigned long long pol;
+    asm volatile("createpolicy.fractional.L2::evict_first.b64 %0, 1.0;" : "=l"(pol));
+    return pol;
+}
+
+__device__ __forceinline__ void ld_stream_v8_ef(const uint32_t* p, uint32_t (&r)[8], unsigned long long pol)
+{
+    asm volatile("ld.global.nc.L1::no_allocate.L2::cache_hint.v8.u32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8], %9;"
+                 : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7])
+                 : "l"(p), "l"(pol));
+}
+
 __device__ __forceinline__ void ld_stream_v4u64(const unsigned long long* p, unsigned long long (&r)[4])
 {
     asm volatile("ld.global.nc.L1::no_allocate.v4.u64 {%0,%1,%2,%3}, [%4];"
@@ -115,7 +131,11 @@ __device__ __forceinline__ double ld_ro_f64(const double* p)
 __device__ __forceinline__ float ld_ro_f32(const float* p)
 {
     float r;
+#ifdef WEDGE_GATHER_NOALLOC
+    asm volatile("ld.global.nc.L1::no_allocate.f32 %0, [%1];" : "=f"(r) : "l"(p));
+#else
     asm volatile("ld.global.nc.f32 %0, [%1];" : "=f"(r) : "l"(p));
+#endif
     return r;
 }
 
