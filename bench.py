@@ -362,18 +362,40 @@ def run_ours(args, dist: Dist):
         learned = {"unavailable": f"no scheduler network: {blob_err}"}
 
     # ---- end to end through the C ABI with host buffers: query parameters in,
-    # full property arrays (8 bytes per vertex, graph_vertex_props) out, every step
+    # full property arrays (8 bytes per vertex, graph_vertex_props) out, every
+    # step.  The four handles share one stream, so their traversals run one
+    # after another as in the device-timed region; each export to page-locked
+    # host memory runs on its handle's second stream, under the next traversal.
     host = {a: torch.empty(V, dtype=torch.int64, pin_memory=True).numpy().view(np.uint64) for a in APPS}
+    shared = torch.cuda.Stream()
+    for a in APPS:
+        suite.g[a].set_stream(shared.cuda_stream)
     e2e_steps = max(3, min(steps, 10))
+
+    def e2e_step():
+        for a in APPS:
+            suite.g[a].run_async(suite.app[a], suite.params["plain"][a])
+            suite.g[a].read_results_async(host[a])
+        for a in APPS:
+            suite.g[a].wait()
+
+    e2e_step()
     dist.barrier()
     torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        e2e_step()
+    e2e_wall = dist.max(time.perf_counter() - t0)
+    e2e_value = dist.world * e2e_steps * suite.step_edges() / e2e_wall / 1e9
+    # the same with the blocking calls (run, then read into the same page-locked memory)
+    for a in APPS:
+        suite.g[a].set_stream(None)
     t0 = time.perf_counter()
     for _ in range(e2e_steps):
         for a in APPS:
             suite.run(a)
             suite.g[a].read_results(host[a])
-    e2e_wall = dist.max(time.perf_counter() - t0)
-    e2e_value = dist.world * e2e_steps * suite.step_edges() / e2e_wall / 1e9
+    e2e_sync = dist.world * e2e_steps * suite.step_edges() / dist.max(time.perf_counter() - t0) / 1e9
     params_bytes = len(APPS) * ctypes.sizeof(W.Params)  # each query's wedge_params_t, in kernel arguments
 
     # ---- roofline of the dominant kernel (the PageRank pull) and of every application's pulls
@@ -404,8 +426,12 @@ def run_ours(args, dist: Dist):
         "per_app": per_app,
         "e2e": {"value": round(e2e_value, 4), "unit": "GTEPS", "h2d_bytes_per_step": params_bytes,
                 "d2h_bytes_per_step": len(APPS) * 8 * V, "steps": e2e_steps,
-                "what": "wedge_cuda_run + wedge_cuda_read_results per application into pinned host memory; graphs "
-                        "resident (loaded once, as the reference excludes load from Running Time)"},
+                "what": "per application wedge_cuda_run_async + wedge_cuda_read_results_async into page-locked host "
+                        "memory, then wedge_cuda_wait; the four handles share one stream (traversals in sequence, "
+                        "each export under the next traversal); graphs resident (loaded once, as the reference "
+                        "excludes load from Running Time)",
+                "blocking_calls": {"value": round(e2e_sync, 4),
+                                   "what": "wedge_cuda_run + wedge_cuda_read_results, one after another"}},
         "roofline": {"bound": "hbm", "kernel": pr_roof["kernel"], "achieved": pr_roof["achieved"], "peak": peak,
                      "unit": "GB/s", "frac": pr_roof["frac"], "peak_source": peak_kind,
                      "traffic": _ncu_traffic(default_workload),

@@ -219,6 +219,58 @@ int wedge_cuda_run(wedge_graph_t* g, int app, const wedge_params_t* params, wedg
 int wedge_cuda_run_phase(wedge_graph_t* g, int app, int phase, const wedge_params_t* params,
                          uint64_t* active_mass);
 
+/* Asynchronous forms (no counterpart in the reference, whose driver returns
+ * when the traversal is done).  wedge_cuda_run_async queues the whole
+ * traversal -- the iteration loop runs on the device as with WEDGE_FLAG_GRAPH;
+ * WEDGE_FLAG_TIMING is rejected -- and returns without waiting.
+ * wedge_cuda_read_results_async queues the export of the last run's results
+ * into page-locked host memory (cudaHostAlloc / cudaHostRegister; other memory
+ * is rejected with WEDGE_ERR_ARG) on a second stream of the handle -- a kernel
+ * writes them to a device staging buffer of 8 bytes per vertex (allocated on
+ * the first call) and the copy engine moves them to the host -- so work
+ * queued next on the handle's stream -- the next query, or other handles'
+ * queries sharing that stream -- overlaps the transfer; a later run of the
+ * same handle waits for the export before it overwrites the properties.
+ * wedge_cuda_wait waits for both and returns the queued run's status and
+ * statistics (stats may be NULL).  The host memory holds the results once
+ * wedge_cuda_wait returns. */
+int wedge_cuda_run_async(wedge_graph_t* g, int app, const wedge_params_t* params);
+int wedge_cuda_read_results_async(wedge_graph_t* g, void* host_props, uint64_t bytes);
+int wedge_cuda_wait(wedge_graph_t* g, wedge_stats_t* stats);
+
+/* Queues the handle's work on a caller's stream (a cudaStream_t; NULL restores
+ * the handle's own), after the work already queued on the previous one has
+ * finished.  Handles sharing a stream run in the order their work was queued;
+ * the traversal loops are still captured on the handle's own stream. */
+int wedge_cuda_set_stream(wedge_graph_t* g, void* stream);
+
+/* ---------------------------------------------------------------- shards */
+
+/* Destination-range shards: the reference's NUMA split (graphdata.c:1050-1065:
+ * edge vectors divided evenly; graphdata.c:656-689: each part's vertex range
+ * ends at its last destination, rounded up to a 512-vertex boundary), one
+ * shard per GPU.  A shard holds the in-edges of its destination range only
+ * (grouped by ascending dst, as wedge_cuda_load_edges), over all vertices as
+ * sources; global_outdeg[num_vertices] are the whole graph's out-degrees and
+ * global_edges its edge count, so every shard numbers vertices alike and
+ * takes the dense/Wedge decision on the whole graph's terms.  BFS, CC and
+ * SSSP run phase by phase (wedge_cuda_run_phase): after each pull the host
+ * combines the shards' properties (element-wise minimum) and pulled frontier
+ * bitmaps (bitwise or; the shards' destinations are disjoint), imports them
+ * into every shard, and hands every shard the summed changed mass. */
+enum wedge_shard_state {
+    WEDGE_SHARD_PROPS = 0,    /* one word per vertex in the engine's numbering: uint32 (BFS parent, CC label)
+                                 or uint64 (SSSP distance) */
+    WEDGE_SHARD_FRONTIER = 1  /* the bitmap of vertices the last pull changed, (V + 31) / 32 uint32 words */
+};
+int wedge_cuda_load_shard(uint64_t num_vertices, uint64_t num_edges, const uint32_t* src, const uint32_t* dst,
+                          const uint64_t* weights, int weight_kind, const uint64_t* global_outdeg,
+                          uint64_t global_edges, wedge_graph_t** out);
+/* copies a shard's state (enum wedge_shard_state) to host memory (import 0) or back from it (import 1) */
+int wedge_cuda_shard_state(wedge_graph_t* g, int which, void* host, uint64_t bytes, int import);
+/* after a pull and the import: the iteration's decision from the changed mass of all shards */
+int wedge_cuda_shard_decide(wedge_graph_t* g, uint64_t global_mass, uint64_t threshold_pct);
+
 /* ---------------------------------------------------------------- results */
 
 /* per-iteration records of the last run (at most 4096 kept); *count receives the number

@@ -50,6 +50,10 @@ def test_null_handles_are_rejected(engine_lib):
 
     assert L.wedge_cuda_run(None, 0, C.byref(Params()), C.byref(Stats())) == -6
     assert L.wedge_cuda_read_results(None, None, 0) == -6
+    assert L.wedge_cuda_run_async(None, 0, C.byref(Params())) == -6
+    assert L.wedge_cuda_read_results_async(None, None, 0) == -6
+    assert L.wedge_cuda_wait(None, None) == -6
+    assert L.wedge_cuda_set_stream(None, None) == -6
     assert L.wedge_cuda_num_vertices(None) == 0
     L.wedge_cuda_free(None)
 

@@ -212,6 +212,44 @@ def test_pagerank_fp32_phase_api(W, O):
     assert np.array_equal(a, b)
 
 
+def test_async_runs_and_reads_match_sync(W, O):
+    """wedge_cuda_run_async + wedge_cuda_read_results_async into page-locked memory
+    give wedge_cuda_run's results; handles sharing a caller's stream run in
+    order; a later run of a handle waits for its queued export"""
+    torch = pytest.importorskip("torch")
+    V, s, d = graph_edges(O, "rmat", dict(scale=13, edge_factor=16, seed=31))
+    w = O.weights(s, d)
+    p_pr = dict(num_iterations=5, damping=0.85, precision=W.PREC_FP32C)
+    with W.Graph.from_edges(V, s, d, w, W.WEIGHTS_U64) as g1, W.Graph.from_edges(V, s, d) as g2:
+        g1.run(W.APP_SSSP, W.Params(root=0))
+        want0 = g1.read_results()
+        g1.run(W.APP_SSSP, W.Params(root=3))
+        want3 = g1.read_results()
+        g2.run(W.APP_PR, W.Params(**p_pr))
+        want_pr = g2.read_results()
+        stream = torch.cuda.Stream()
+        g1.set_stream(stream.cuda_stream)
+        g2.set_stream(stream.cuda_stream)
+        host = [torch.empty(V, dtype=torch.int64, pin_memory=True).numpy().view(np.uint64) for _ in range(3)]
+        g1.run_async(W.APP_SSSP, W.Params(root=0))
+        g1.read_results_async(host[0])
+        g2.run_async(W.APP_PR, W.Params(**p_pr))
+        g2.read_results_async(host[1])
+        g1.run_async(W.APP_SSSP, W.Params(root=3))  # overwrites the distances once host[0] is written
+        g1.read_results_async(host[2])
+        st1, st2 = g1.wait(), g2.wait()
+        assert np.array_equal(host[0], want0)
+        assert np.array_equal(host[1], want_pr)
+        assert np.array_equal(host[2], want3)
+        assert st1["iterations"] > 0 and st2["iterations"] == 5
+        assert abs(st2["pr_sum"] - 1.0) < 1e-5
+        g1.set_stream(None)
+        with pytest.raises(W.WedgeError):  # asynchronous reads need page-locked memory
+            g1.read_results_async(np.empty(V, np.uint64))
+        with pytest.raises(W.WedgeError):  # per-iteration timing needs the host between iterations
+            g1.run_async(W.APP_SSSP, W.Params(root=0, flags=W.FLAG_TIMING))
+
+
 def test_grid_sssp_and_bfs(W, O):
     V, s, d = graph_edges(O, "grid", dict(side=64, frac=0.01, seed=3))
     w = O.weights(s, d)

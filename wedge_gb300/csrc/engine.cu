@@ -47,11 +47,15 @@ int new_handle(wedge_graph** out)
     h->built_app = -1;
     h->last_app = -1;
     h->graph_app = -1;
+    h->pend_app = -1;
     WEDGE_CHECK(cudaGetDevice(&h->device));
     WEDGE_CHECK(cudaDeviceGetAttribute(&h->num_sms, cudaDevAttrMultiProcessorCount, h->device));
-    WEDGE_CHECK(cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking));
+    WEDGE_CHECK(cudaStreamCreateWithFlags(&h->own_stream, cudaStreamNonBlocking));
+    h->stream = h->own_stream;
     for (int i = 0; i < 8; ++i)
         WEDGE_CHECK(cudaEventCreate(&h->ev[i]));
+    WEDGE_CHECK(cudaEventCreateWithFlags(&h->ev_run, cudaEventDisableTiming));
+    WEDGE_CHECK(cudaEventCreateWithFlags(&h->ev_x, cudaEventDisableTiming));
     WEDGE_CHECK(cudaMallocHost((void**)&h->h_ctrl, sizeof(Ctrl)));
     h->iter_pull_ms = (double*)calloc(LOG_CAP, sizeof(double));
     h->iter_wedge_ms = (double*)calloc(LOG_CAP, sizeof(double));
@@ -103,6 +107,8 @@ void free_handle(wedge_graph* h)
         return;
     if (h->stream)
         cudaStreamSynchronize(h->stream);
+    if (h->xstream)
+        cudaStreamSynchronize(h->xstream);
     free_state(h);
     for (int i = 0; i < h->nallocs; ++i)
         cudaFree(h->allocs[i]);
@@ -115,8 +121,16 @@ void free_handle(wedge_graph* h)
         cudaFree(h->net);
     free(h->iter_pull_ms);
     free(h->iter_wedge_ms);
-    if (h->stream)
-        cudaStreamDestroy(h->stream);
+    if (h->ev_run)
+        cudaEventDestroy(h->ev_run);
+    if (h->ev_x)
+        cudaEventDestroy(h->ev_x);
+    if (h->xstream)
+        cudaStreamDestroy(h->xstream);
+    if (h->xbuf)
+        cudaFree(h->xbuf);
+    if (h->own_stream)
+        cudaStreamDestroy(h->own_stream); /* a caller's stream stays the caller's */
     free(h);
 }
 
@@ -355,7 +369,8 @@ __global__ void unpack_edges_kernel(const unsigned long long* key, uint64_t E, u
 // lines; edges are renumbered and re-sorted by (destination, source).  The
 // permutations stay on the device: roots are mapped in, results mapped back.
 static int relabel_by_degree(wedge_graph* h, uint64_t V, uint64_t E, uint32_t* d_src, uint32_t* d_dst,
-                             unsigned long long* d_w, uint32_t** new2old, uint32_t** old2new)
+                             unsigned long long* d_w, uint32_t** new2old, uint32_t** old2new,
+                             const uint32_t* global_outdeg)
 {
     cudaStream_t st = h->stream;
     const uint32_t cap = (uint32_t)h->num_sms * 16u;
@@ -367,9 +382,13 @@ static int relabel_by_degree(wedge_graph* h, uint64_t V, uint64_t E, uint32_t* d
     WEDGE_CHECK(cudaMallocAsync((void**)&deg, V * sizeof(uint32_t), st));
     WEDGE_CHECK(cudaMallocAsync((void**)&vk, V * sizeof(unsigned long long), st));
     WEDGE_CHECK(cudaMallocAsync((void**)&vk2, V * sizeof(unsigned long long), st));
-    WEDGE_CHECK(cudaMemsetAsync(deg, 0, V * sizeof(uint32_t), st));
-    if (E)
-        outdeg_kernel<<<grid_for(E, AUX_THREADS, cap), AUX_THREADS, 0, st>>>(d_src, E, deg);
+    if (global_outdeg) { /* a shard: the whole graph's degrees, so every shard numbers vertices alike */
+        WEDGE_CHECK(cudaMemcpyAsync(deg, global_outdeg, V * sizeof(uint32_t), cudaMemcpyDeviceToDevice, st));
+    } else {
+        WEDGE_CHECK(cudaMemsetAsync(deg, 0, V * sizeof(uint32_t), st));
+        if (E)
+            outdeg_kernel<<<grid_for(E, AUX_THREADS, cap), AUX_THREADS, 0, st>>>(d_src, E, deg);
+    }
     degree_key_kernel<<<grid_for(V, AUX_THREADS, cap), AUX_THREADS, 0, st>>>(deg, V, vk);
     {
         cub::DoubleBuffer<unsigned long long> db(vk, vk2);
@@ -422,13 +441,24 @@ static int relabel_by_degree(wedge_graph* h, uint64_t V, uint64_t E, uint32_t* d
 // Builds the device CSC from destination-sorted device edge arrays.  d_src and
 // d_w (if any) must hold roundup(E, TILE) entries and become owned by the
 // handle; d_dst is consumed and freed.
+__global__ void permute_degrees_kernel(const uint32_t* global_outdeg, const uint32_t* new2old, uint64_t V, uint32_t* outdeg)
+{
+    for (uint64_t v = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; v < V; v += (uint64_t)gridDim.x * blockDim.x)
+        outdeg[v] = global_outdeg[new2old[v]];
+}
+
+// Builds the device CSC.  A shard (d_global_outdeg given: the whole graph's
+// out-degrees, caller numbering) numbers vertices by those degrees, so all
+// shards share one numbering, and keeps them as its out-degrees (the changed
+// mass and PageRank's divisor), while its CSRI indexes its own in-edges.
 int build_from_device_edges(wedge_graph* h, uint64_t V, uint64_t E, uint32_t* d_src, uint32_t* d_dst,
-                            unsigned long long* d_w, int weight_kind)
+                            unsigned long long* d_w, int weight_kind, const uint32_t* d_global_outdeg)
 {
     cudaStream_t st = h->stream;
     DevGraph& g = h->g;
     g.V = V;
     g.E = E;
+    g.E_thr = E;
     g.Epad = (E + MAX_TILE_E - 1) / MAX_TILE_E * MAX_TILE_E;
     g.T = (uint32_t)(g.Epad / TILE);
     g.weight_kind = (uint32_t)weight_kind;
@@ -452,7 +482,7 @@ int build_from_device_edges(wedge_graph* h, uint64_t V, uint64_t E, uint32_t* d_
     }
     {
         uint32_t *n2o = nullptr, *o2n = nullptr;
-        int rc = relabel_by_degree(h, V, E, d_src, d_dst, d_w, &n2o, &o2n);
+        int rc = relabel_by_degree(h, V, E, d_src, d_dst, d_w, &n2o, &o2n, d_global_outdeg);
         if (rc)
             return rc;
         g.new2old = n2o;
@@ -520,6 +550,8 @@ int build_from_device_edges(wedge_graph* h, uint64_t V, uint64_t E, uint32_t* d_
     if (E)
         csri_fill_kernel<<<grid_for(E, AUX_THREADS, cap), AUX_THREADS, 0, st>>>(d_src, E, wide, csri, csri_pos);
     cudaFreeAsync(wide, st);
+    if (d_global_outdeg) /* the shard's own counts built the CSRI; the graph's degrees from here on */
+        permute_degrees_kernel<<<grid_for(V, AUX_THREADS, cap), AUX_THREADS, 0, st>>>(d_global_outdeg, g.new2old, V, outdeg);
 
     // destination starts, one bit per in-edge (the pulls' tile geometry)
     uint32_t* dst_start = nullptr;
@@ -2972,9 +3004,7 @@ __global__ void __launch_bounds__(PULL_THREADS, 1) pr32_pull_kernel(DevGraph g, 
 
     unsigned long long edges = 0, tiles = 0, dsts = 0;
     F2 mass{0.0f, 0.0f};
-#ifdef WEDGE_STREAM_EVICT_FIRST
     const unsigned long long pol = l2_evict_first_policy();
-#endif
     uint32_t t = gw;
     uint32_t k0n = 0, kendn = 0;
     if (t < T) {
@@ -3000,19 +3030,11 @@ __global__ void __launch_bounds__(PULL_THREADS, 1) pr32_pull_kernel(DevGraph g, 
         {
             const uint32_t* p = g.src + base + (uint64_t)lane * EPL;
             uint32_t x[8];
-#ifdef WEDGE_STREAM_EVICT_FIRST
-            ld_stream_v8_ef(p, x, pol);
-#else
-            ld_stream_v8(p, x);
-#endif
+            ld_stream_v8_ef(p, x, pol); /* read once: evict first, the ranks stay in L2 */
 #pragma unroll
             for (int j = 0; j < 8; ++j)
                 sa[j] = x[j];
-#ifdef WEDGE_STREAM_EVICT_FIRST
             ld_stream_v8_ef(p + 8, x, pol);
-#else
-            ld_stream_v8(p + 8, x);
-#endif
 #pragma unroll
             for (int j = 0; j < 8; ++j)
                 sa[8 + j] = x[j];
@@ -3377,8 +3399,9 @@ static uint64_t counter_slots(const wedge_graph* h) { return 2ull * h->dst_grid 
 // Wedge pulls relax over in-edge positions, else pull_kernel
 static bool sssp_tiles512(const wedge_graph* h)
 {
+    // measured slower at R-MAT scale 26 (20.6 -> 23.2 ms per SSSP): off unless WEDGE_SSSP_TILES512=1
     const char* e = getenv("WEDGE_SSSP_TILES512");
-    return h->s.push && h->g.w8 && !(e && e[0] == '0');
+    return h->s.push && h->g.w8 && e && e[0] == '1';
 }
 
 static const void* pull_fn(const wedge_graph* h, int app)
@@ -3859,23 +3882,66 @@ static int build_graph(wedge_graph* h, int app)
     cudaGraphNode_t cnode;
     WEDGE_CHECK(cudaGraphAddNode(&cnode, graph, nullptr, nullptr, 0, &cparams));
     cudaGraph_t body = cparams.conditional.phGraph_out[0];
+    // captured on the handle's own stream (a caller's stream may carry other work)
+    const cudaStream_t run_stream = h->stream;
+    h->stream = h->own_stream;
     WEDGE_CHECK(cudaStreamBeginCaptureToGraph(h->stream, body, nullptr, nullptr, 0, cudaStreamCaptureModeRelaxed));
     launch_pull(h, app);
     launch_tail(h, app);
     loop_cond_kernel<<<1, 1, 0, h->stream>>>(h->s, handle);
     cudaGraph_t captured;
-    WEDGE_CHECK(cudaStreamEndCapture(h->stream, &captured));
+    const cudaError_t ce = cudaStreamEndCapture(h->stream, &captured);
+    h->stream = run_stream;
+    WEDGE_CHECK(ce);
     WEDGE_CHECK(cudaGraphInstantiate(&h->graph_exec, graph, 0));
     cudaGraphDestroy(graph);
     h->graph_app = app;
     return WEDGE_OK;
 }
 
-static int run_traversal(wedge_graph* h, int app, const wedge_params_t* p, wedge_stats_t* st)
+// The statistics of the traversal that just ran on h->stream (waits for it).
+// launches: the kernels launched from the host; a graph loop adds its
+// iterations' launches and the loop condition's.
+static int traversal_stats(wedge_graph* h, int app, uint64_t launches, bool use_graph, bool timing, double t_pull_dense,
+                           double t_pull_wedge, double t_wedge, wedge_stats_t* st)
+{
+    Ctrl c;
+    int rc = read_ctrl(h, &c);
+    if (rc)
+        return rc;
+    float total = 0;
+    cudaEventElapsedTime(&total, h->ev[0], h->ev[1]);
+    h->last_app = app;
+    h->last_timing = timing;
+    if (st) {
+        memset(st, 0, sizeof(*st));
+        st->dsts_scanned = c.dsts_scanned;
+        st->vertices_activated = c.activated;
+        st->iterations = c.iter;
+        st->wedge_iterations = c.wedge_iters;
+        st->running_ms = total;
+        st->pull_ms_dense = t_pull_dense;
+        st->pull_ms_wedge = t_pull_wedge;
+        st->wedge_ms = t_wedge;
+        st->edges_scanned = c.edges_scanned;
+        st->tiles_scanned = c.tiles_scanned;
+        st->pull_launches = c.pull_launches;
+        st->kernel_launches = use_graph ? launches + (iteration_launches(h, app) + 1ull) * c.iter : launches;
+    }
+    if (c.error)
+        return WEDGE_ERR_CUDA;
+    if (c.not_converged)
+        return WEDGE_ERR_NOT_CONVERGED;
+    return WEDGE_OK;
+}
+
+// One traversal.  With wait false (graph loop only) the work is queued and the
+// statistics are left to traversal_stats, through wedge_cuda_wait.
+static int run_traversal(wedge_graph* h, int app, const wedge_params_t* p, wedge_stats_t* st, bool wait = true)
 {
     const DevGraph& g = h->g;
     const uint64_t root = p->root < g.V ? p->root : 0; /* main.c:81-85 */
-    const unsigned long long thr = (unsigned long long)((g.E * (unsigned long long)p->threshold_pct) / 100ull);
+    const unsigned long long thr = (unsigned long long)((g.E_thr * (unsigned long long)p->threshold_pct) / 100ull);
     uint64_t cap = p->max_iterations ? p->max_iterations : g.V + 1;
     if (cap > 0x7fffffffull)
         cap = 0x7fffffffull;
@@ -3943,34 +4009,13 @@ static int run_traversal(wedge_graph* h, int app, const wedge_params_t* p, wedge
     }
     WEDGE_CHECK(cudaEventRecord(h->ev[1], h->stream));
     WEDGE_CHECK(cudaGetLastError());
-    int rc = read_ctrl(h, &c);
-    if (rc)
-        return rc;
-    float total = 0;
-    cudaEventElapsedTime(&total, h->ev[0], h->ev[1]);
     h->last_app = app;
-    h->last_timing = timing;
-    if (st) {
-        memset(st, 0, sizeof(*st));
-        st->dsts_scanned = c.dsts_scanned;
-        st->vertices_activated = c.activated;
-        st->iterations = c.iter;
-        st->wedge_iterations = c.wedge_iters;
-        st->running_ms = total;
-        st->pull_ms_dense = t_pull_dense;
-        st->pull_ms_wedge = t_pull_wedge;
-        st->wedge_ms = t_wedge;
-        st->edges_scanned = c.edges_scanned;
-        st->tiles_scanned = c.tiles_scanned;
-        st->pull_launches = c.pull_launches;
-        // graph loop: `launches` holds the init (and the CC label conversion); + the loop condition per iteration
-        st->kernel_launches = use_graph ? launches + (iteration_launches(h, app) + 1ull) * c.iter : launches;
+    if (!wait && use_graph) {
+        h->pend_app = app;
+        h->pend_launches = launches;
+        return WEDGE_OK;
     }
-    if (c.error)
-        return WEDGE_ERR_CUDA;
-    if (c.not_converged)
-        return WEDGE_ERR_NOT_CONVERGED;
-    return WEDGE_OK;
+    return traversal_stats(h, app, launches, use_graph, timing, t_pull_dense, t_pull_wedge, t_wedge, st);
 }
 
 // compensated-FP32 PageRank: the grid of pr32_finish_kernel (a thread per short
@@ -4038,6 +4083,8 @@ static int build_pr_graph(wedge_graph* h)
     cudaGraphNode_t cnode;
     WEDGE_CHECK(cudaGraphAddNode(&cnode, graph, nullptr, nullptr, 0, &cparams));
     cudaGraph_t body = cparams.conditional.phGraph_out[0];
+    const cudaStream_t run_stream = h->stream; /* captured on the handle's own stream */
+    h->stream = h->own_stream;
     WEDGE_CHECK(cudaStreamBeginCaptureToGraph(h->stream, body, nullptr, nullptr, 0, cudaStreamCaptureModeRelaxed));
     if (h->s.precision == WEDGE_PREC_FP32C) {
         launch_pr32_iteration(h);
@@ -4049,14 +4096,48 @@ static int build_pr_graph(wedge_graph* h)
     }
     pr_loop_cond_kernel<<<1, 1, 0, h->stream>>>(h->s, handle);
     cudaGraph_t captured;
-    WEDGE_CHECK(cudaStreamEndCapture(h->stream, &captured));
+    const cudaError_t ce = cudaStreamEndCapture(h->stream, &captured);
+    h->stream = run_stream;
+    WEDGE_CHECK(ce);
     WEDGE_CHECK(cudaGraphInstantiate(&h->pr_exec, graph, 0));
     cudaGraphDestroy(graph);
     h->pr_key = key;
     return WEDGE_OK;
 }
 
-static int run_pr(wedge_graph* h, const wedge_params_t* p, wedge_stats_t* st)
+// The statistics of the PageRank run that just ran on h->stream (waits for it)
+static int pr_stats(wedge_graph* h, uint32_t iters, bool use_graph, bool timing, double t_pull, double t_vertex,
+                    wedge_stats_t* st)
+{
+    Ctrl c;
+    int rc = read_ctrl(h, &c);
+    if (rc)
+        return rc;
+    float total = 0;
+    cudaEventElapsedTime(&total, h->ev[0], h->ev[1]);
+    h->last_app = WEDGE_APP_PR;
+    h->last_timing = timing;
+    const bool c32 = h->s.precision == WEDGE_PREC_FP32C;
+    if (st) {
+        memset(st, 0, sizeof(*st));
+        st->dsts_scanned = c.dsts_scanned;
+        st->iterations = iters;
+        st->running_ms = total;
+        st->pull_ms_dense = t_pull;
+        st->vertex_ms = t_vertex;
+        st->edges_scanned = c.edges_scanned;
+        st->tiles_scanned = c.tiles_scanned;
+        st->pull_launches = c.pull_launches;
+        /* init (+ total), the iterations (+ the loop condition), the sums (+ isolated vertices) */
+        st->kernel_launches = c32 ? 5ull + (use_graph ? 4ull : 3ull) * iters : 3ull + (use_graph ? 5ull : 4ull) * iters;
+        st->pr_sum = c.pr_sum;
+    }
+    if (c.error)
+        return WEDGE_ERR_CUDA;
+    return WEDGE_OK;
+}
+
+static int run_pr(wedge_graph* h, const wedge_params_t* p, wedge_stats_t* st, bool wait = true)
 {
     const DevGraph& g = h->g;
     const bool timing = (p->flags & WEDGE_FLAG_TIMING) != 0;
@@ -4119,32 +4200,14 @@ static int run_pr(wedge_graph* h, const wedge_params_t* p, wedge_stats_t* st)
     pr_sum_kernel<<<vgrid, AUX_THREADS, 0, h->stream>>>(g, h->s, sums);
     pr_sum_final_kernel<<<1, 32, 0, h->stream>>>(h->s, sums, vgrid);
     WEDGE_CHECK(cudaGetLastError());
-    Ctrl c;
-    int rc = read_ctrl(h, &c);
-    if (rc)
-        return rc;
-    float total = 0;
-    cudaEventElapsedTime(&total, h->ev[0], h->ev[1]);
     h->last_app = WEDGE_APP_PR;
-    h->last_timing = timing;
-    if (st) {
-        memset(st, 0, sizeof(*st));
-        st->dsts_scanned = c.dsts_scanned;
-        st->iterations = p->num_iterations;
-        st->running_ms = total;
-        st->pull_ms_dense = t_pull;
-        st->vertex_ms = t_vertex;
-        st->edges_scanned = c.edges_scanned;
-        st->tiles_scanned = c.tiles_scanned;
-        st->pull_launches = c.pull_launches;
-        /* init (+ total), the iterations (+ the loop condition), the sums (+ isolated vertices) */
-        st->kernel_launches = c32 ? 5ull + (use_graph ? 4ull : 3ull) * p->num_iterations
-                                  : 3ull + (use_graph ? 5ull : 4ull) * p->num_iterations;
-        st->pr_sum = c.pr_sum;
+    if (!wait && !timing) {
+        h->pend_app = WEDGE_APP_PR;
+        h->pend_iters = p->num_iterations;
+        h->pend_launches = use_graph ? 1u : 0u; /* the launch count formula's graph term */
+        return WEDGE_OK;
     }
-    if (c.error)
-        return WEDGE_ERR_CUDA;
-    return WEDGE_OK;
+    return pr_stats(h, p->num_iterations, use_graph, timing, t_pull, t_vertex, st);
 }
 
 }  // namespace wedge
@@ -4194,17 +4257,186 @@ static int check_params(const wedge_graph_t* g, int app, const wedge_params_t* p
     return WEDGE_OK;
 }
 
+// work on the handle's stream that overwrites state waits for queued asynchronous exports
+static int after_exports(wedge_graph_t* g)
+{
+    if (g->x_pending)
+        WEDGE_CHECK(cudaStreamWaitEvent(g->stream, g->ev_x, 0));
+    return WEDGE_OK;
+}
+
 int wedge_cuda_run(wedge_graph_t* g, int app, const wedge_params_t* params, wedge_stats_t* stats)
 {
     int rc = check_params(g, app, params);
     if (rc)
         return rc;
     WEDGE_CHECK(cudaSetDevice(g->device));
+    if ((rc = after_exports(g)))
+        return rc;
     if ((rc = ensure_state(g, app, params->precision)))
         return rc;
+    g->pend_app = -1;
     if (app == WEDGE_APP_PR)
         return run_pr(g, params, stats);
     return run_traversal(g, app, params, stats);
+}
+
+int wedge_cuda_run_async(wedge_graph_t* g, int app, const wedge_params_t* params)
+{
+    int rc = check_params(g, app, params);
+    if (rc)
+        return rc;
+    if (params->flags & WEDGE_FLAG_TIMING)
+        return WEDGE_ERR_ARG; /* per-iteration events need the host between iterations */
+    WEDGE_CHECK(cudaSetDevice(g->device));
+    if ((rc = after_exports(g)))
+        return rc;
+    if ((rc = ensure_state(g, app, params->precision)))
+        return rc;
+    wedge_params_t p = *params;
+    p.flags |= WEDGE_FLAG_GRAPH; /* the iteration loop runs on the device */
+    g->pend_app = -1;
+    return app == WEDGE_APP_PR ? run_pr(g, &p, nullptr, false) : run_traversal(g, app, &p, nullptr, false);
+}
+
+int wedge_cuda_read_results_async(wedge_graph_t* g, void* host_props, uint64_t bytes)
+{
+    if (!g || !host_props || bytes < 8ull * g->g.V || g->last_app < 0)
+        return WEDGE_ERR_ARG;
+    WEDGE_CHECK(cudaSetDevice(g->device));
+    cudaPointerAttributes pa;
+    if (cudaPointerGetAttributes(&pa, host_props) != cudaSuccess || pa.type != cudaMemoryTypeHost || !pa.devicePointer ||
+        ((uintptr_t)pa.devicePointer & 7u) != 0u) {
+        cudaGetLastError();
+        return WEDGE_ERR_ARG; /* asynchronous reads need page-locked host memory */
+    }
+    if (!g->xstream)
+        WEDGE_CHECK(cudaStreamCreateWithFlags(&g->xstream, cudaStreamNonBlocking));
+    if (!g->xbuf) { /* the words are staged in device memory and copied by the copy engine, off the SMs */
+        void* p = nullptr;
+        WEDGE_CHECK(cudaMalloc(&p, 8ull * (g->g.V ? g->g.V : 1)));
+        g->xbuf = (unsigned long long*)p;
+    }
+    DevState rs;
+    int rc = result_state(g, &rs);
+    if (rc)
+        return rc;
+    WEDGE_CHECK(cudaEventRecord(g->ev_run, g->stream));
+    WEDGE_CHECK(cudaStreamWaitEvent(g->xstream, g->ev_run, 0));
+    export_kernel<<<aux_grid(g, g->g.V), AUX_THREADS, 0, g->xstream>>>(g->g, rs, (uint32_t)g->last_app, g->xbuf);
+    WEDGE_CHECK(cudaGetLastError());
+    WEDGE_CHECK(cudaMemcpyAsync(host_props, g->xbuf, 8ull * g->g.V, cudaMemcpyDeviceToHost, g->xstream));
+    WEDGE_CHECK(cudaEventRecord(g->ev_x, g->xstream));
+    g->x_pending = 1;
+    return WEDGE_OK;
+}
+
+int wedge_cuda_wait(wedge_graph_t* g, wedge_stats_t* stats)
+{
+    if (!g)
+        return WEDGE_ERR_ARG;
+    WEDGE_CHECK(cudaSetDevice(g->device));
+    WEDGE_CHECK(cudaStreamSynchronize(g->stream));
+    if (g->x_pending) {
+        WEDGE_CHECK(cudaStreamSynchronize(g->xstream));
+        g->x_pending = 0;
+    }
+    int rc = WEDGE_OK;
+    if (g->pend_app == WEDGE_APP_PR)
+        rc = pr_stats(g, g->pend_iters, g->pend_launches != 0, false, 0.0, 0.0, stats);
+    else if (g->pend_app >= 0)
+        rc = traversal_stats(g, g->pend_app, g->pend_launches, true, false, 0.0, 0.0, 0.0, stats);
+    else if (stats)
+        memset(stats, 0, sizeof(*stats));
+    g->pend_app = -1;
+    return rc;
+}
+
+int wedge_cuda_set_stream(wedge_graph_t* g, void* stream)
+{
+    if (!g)
+        return WEDGE_ERR_ARG;
+    WEDGE_CHECK(cudaSetDevice(g->device));
+    WEDGE_CHECK(cudaStreamSynchronize(g->stream)); /* the handle's queued work finishes on its old stream */
+    g->stream = stream ? (cudaStream_t)stream : g->own_stream;
+    return WEDGE_OK;
+}
+
+/* ------------------------------------------------------------ shards */
+
+}  // extern "C"
+
+namespace wedge {
+// the whole graph's iteration decision on a shard (after its own pull's
+// decide_kernel): the changed mass of all shards, the dense/Wedge rule against
+// the whole graph's threshold (execution_bfs.c:132,141), convergence
+// (execution_bfs.c:239-251)
+__global__ void shard_decide_kernel(DevState s, unsigned long long mass, unsigned long long thr)
+{
+    Ctrl* c = s.ctrl;
+    c->mass = mass;
+    c->last_mass = mass;
+    c->threshold = thr;
+    if (mass == 0ull) {
+        c->done = 1u;
+        c->loop = 0u;
+        c->not_converged = 0u;
+    } else if (c->iter >= c->max_iter) {
+        c->done = 1u;
+        c->loop = 0u;
+        c->not_converged = 1u;
+    } else {
+        c->done = 0u;
+        c->loop = 1u;
+        c->not_converged = 0u;
+        c->mode = mass > thr ? MODE_DENSE : MODE_WEDGE;
+    }
+}
+}  // namespace wedge
+
+extern "C" {
+
+int wedge_cuda_shard_state(wedge_graph_t* g, int which, void* host, uint64_t bytes, int import)
+{
+    if (!g || !host || g->built_app < 0 || (which != WEDGE_SHARD_PROPS && which != WEDGE_SHARD_FRONTIER))
+        return WEDGE_ERR_ARG;
+    const int app = g->built_app;
+    if (app == WEDGE_APP_PR)
+        return WEDGE_ERR_UNSUPPORTED;
+    WEDGE_CHECK(cudaSetDevice(g->device));
+    void* dev = nullptr;
+    uint64_t need = 0;
+    if (which == WEDGE_SHARD_PROPS) {
+        dev = app == WEDGE_APP_SSSP ? (void*)g->s.prop64 : (void*)g->s.prop32;
+        need = g->g.V * (app == WEDGE_APP_SSSP ? 8ull : 4ull);
+    } else {
+        Ctrl c;
+        int rc = read_ctrl(g, &c);
+        if (rc)
+            return rc;
+        dev = (void*)(c.parity ? g->s.front1 : g->s.front0); /* the bitmap the last pull wrote */
+        need = (g->g.V + 31) / 32 * 4ull;
+    }
+    if (bytes < need)
+        return WEDGE_ERR_ARG;
+    if (import)
+        WEDGE_CHECK(cudaMemcpyAsync(dev, host, need, cudaMemcpyHostToDevice, g->stream));
+    else
+        WEDGE_CHECK(cudaMemcpyAsync(host, dev, need, cudaMemcpyDeviceToHost, g->stream));
+    WEDGE_CHECK(cudaStreamSynchronize(g->stream));
+    return WEDGE_OK;
+}
+
+int wedge_cuda_shard_decide(wedge_graph_t* g, uint64_t global_mass, uint64_t threshold_pct)
+{
+    if (!g || g->built_app < 0 || g->built_app == WEDGE_APP_PR || threshold_pct > 100)
+        return WEDGE_ERR_ARG;
+    WEDGE_CHECK(cudaSetDevice(g->device));
+    const unsigned long long thr = (unsigned long long)((g->g.E_thr * threshold_pct) / 100ull);
+    shard_decide_kernel<<<1, 1, 0, g->stream>>>(g->s, global_mass, thr);
+    WEDGE_CHECK(cudaGetLastError());
+    WEDGE_CHECK(cudaStreamSynchronize(g->stream));
+    return WEDGE_OK;
 }
 
 int wedge_cuda_run_phase(wedge_graph_t* g, int app, int phase, const wedge_params_t* params, uint64_t* active_mass)
@@ -4213,6 +4445,9 @@ int wedge_cuda_run_phase(wedge_graph_t* g, int app, int phase, const wedge_param
     if (rc)
         return rc;
     WEDGE_CHECK(cudaSetDevice(g->device));
+    if ((rc = after_exports(g)))
+        return rc;
+    g->pend_app = -1;
     if ((rc = ensure_state(g, app, params->precision)))
         return rc;
     const DevGraph& dg = g->g;
@@ -4229,7 +4464,7 @@ int wedge_cuda_run_phase(wedge_graph_t* g, int app, int phase, const wedge_param
         } else {
             const uint64_t root = params->root < dg.V ? params->root : 0;
             const unsigned long long thr =
-                (unsigned long long)((dg.E * (unsigned long long)params->threshold_pct) / 100ull);
+                (unsigned long long)((dg.E_thr * (unsigned long long)params->threshold_pct) / 100ull);
             uint64_t cap = params->max_iterations ? params->max_iterations : dg.V + 1;
             launch_init(g, app, root, (uint32_t)params->sched, thr, (uint32_t)(cap > 0x7fffffffull ? 0x7fffffffull : cap));
         }

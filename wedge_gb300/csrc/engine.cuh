@@ -108,6 +108,7 @@ struct Ctrl {
 // Immutable graph, passed to kernels by value.
 struct DevGraph {
     uint64_t V, E, Epad;
+    uint64_t E_thr;            // edges the dense/Wedge threshold is a share of: E, or the whole graph's for a shard
     uint32_t Vne, T, nsplit, weight_kind;
     uint32_t dst_ident;        // dst_id[k] == k for every k (the vertices with in-edges are [0, Vne))
     uint32_t nwide;            // destinations spanning more than SPLIT_SERIAL tile boundaries (back of the split lists)
@@ -192,7 +193,16 @@ struct DevState {
 struct wedge_graph {
     wedge::DevGraph g;
     wedge::DevState s;
-    cudaStream_t stream;
+    cudaStream_t stream;               // the stream the handle's work is queued on (own_stream or a caller's)
+    cudaStream_t own_stream;
+    cudaStream_t xstream;              // result exports of wedge_cuda_read_results_async (created on first use)
+    cudaEvent_t ev_run;                // recorded after a run, before an asynchronous export
+    cudaEvent_t ev_x;                  // recorded after an asynchronous export: later runs wait for it
+    int x_pending;                     // an asynchronous export is queued (until wedge_cuda_wait)
+    unsigned long long* xbuf;          // device staging of asynchronous exports (8 bytes per vertex, on first use)
+    int pend_app;                      // run queued by wedge_cuda_run_async, reported by wedge_cuda_wait (-1 none)
+    uint64_t pend_launches;
+    uint32_t pend_iters;
     int device;
     int num_sms;
     int weight_kind;
@@ -226,7 +236,7 @@ struct wedge_graph {
 namespace wedge {
 // implemented in engine.cu, used by loaders in graph.cu
 int build_from_device_edges(wedge_graph* h, uint64_t V, uint64_t E, uint32_t* d_src, uint32_t* d_dst,
-                            unsigned long long* d_w, int weight_kind);
+                            unsigned long long* d_w, int weight_kind, const uint32_t* d_global_outdeg = nullptr);
 int new_handle(wedge_graph** out);
 void free_handle(wedge_graph* h);
 int track(wedge_graph* h, void* p);

@@ -367,6 +367,68 @@ int wedge_cuda_load_graph_image(const void* image, uint64_t bytes, int app, int 
     return WEDGE_OK;
 }
 
+int wedge_cuda_load_shard(uint64_t num_vertices, uint64_t num_edges, const uint32_t* src, const uint32_t* dst,
+                          const uint64_t* weights, int weight_kind, const uint64_t* global_outdeg,
+                          uint64_t global_edges, wedge_graph_t** out)
+{
+    if (!out || (num_edges && (!src || !dst)) || !global_outdeg || num_vertices == 0 || num_vertices > MAX_VERTICES ||
+        global_edges < num_edges)
+        return WEDGE_ERR_ARG;
+    if (weights && weight_kind == WEDGE_WEIGHTS_NONE)
+        return WEDGE_ERR_ARG;
+    *out = nullptr;
+    uint32_t* deg32 = (uint32_t*)malloc(num_vertices * sizeof(uint32_t));
+    if (!deg32)
+        return WEDGE_ERR_OOM;
+    for (uint64_t v = 0; v < num_vertices; ++v) {
+        if (global_outdeg[v] > 0xFFFFFFFFull) {
+            free(deg32);
+            return WEDGE_ERR_FORMAT;
+        }
+        deg32[v] = (uint32_t)global_outdeg[v];
+    }
+    wedge_graph* h = nullptr;
+    int rc = new_handle(&h);
+    if (rc) {
+        free(deg32);
+        return rc;
+    }
+    uint32_t *d_src, *d_dst, *d_deg = nullptr;
+    unsigned long long* d_w;
+    const uint64_t E = num_edges;
+    if ((rc = alloc_edges(E, weights != nullptr, &d_src, &d_dst, &d_w)) || (rc = track(h, d_src)) ||
+        (d_w && (rc = track(h, d_w)))) {
+        free(deg32);
+        free_handle(h);
+        return rc;
+    }
+    cudaError_t e0 = cudaMalloc((void**)&d_deg, num_vertices * sizeof(uint32_t));
+    cudaError_t e1 = cudaMemcpyAsync(d_src, src, E * 4, cudaMemcpyHostToDevice, h->stream);
+    cudaError_t e2 = cudaMemcpyAsync(d_dst, dst, E * 4, cudaMemcpyHostToDevice, h->stream);
+    cudaError_t e3 = weights ? cudaMemcpyAsync(d_w, weights, E * 8, cudaMemcpyHostToDevice, h->stream) : cudaSuccess;
+    cudaError_t e4 = e0 == cudaSuccess ? cudaMemcpyAsync(d_deg, deg32, num_vertices * 4, cudaMemcpyHostToDevice, h->stream)
+                                       : e0;
+    cudaError_t e5 = cudaStreamSynchronize(h->stream);
+    free(deg32);
+    if (e0 != cudaSuccess || e1 != cudaSuccess || e2 != cudaSuccess || e3 != cudaSuccess || e4 != cudaSuccess ||
+        e5 != cudaSuccess) {
+        cudaFree(d_deg);
+        cudaFree(d_dst);
+        free_handle(h);
+        return e0 == cudaErrorMemoryAllocation ? WEDGE_ERR_OOM : WEDGE_ERR_CUDA;
+    }
+    rc = build_from_device_edges(h, num_vertices, E, d_src, d_dst, d_w, weights ? weight_kind : WEDGE_WEIGHTS_NONE, d_deg);
+    cudaStreamSynchronize(h->stream);
+    cudaFree(d_deg);
+    if (rc) {
+        free_handle(h);
+        return rc;
+    }
+    h->g.E_thr = global_edges;
+    *out = h;
+    return WEDGE_OK;
+}
+
 int wedge_cuda_load_edges(uint64_t num_vertices, uint64_t num_edges, const uint32_t* src, const uint32_t* dst,
                           const uint64_t* weights, int weight_kind, wedge_graph_t** out)
 {

@@ -32,6 +32,7 @@ SCHED_PARAMS = 64 * 16 + 64 + 64 * 64 + 64 + 3 * 64 + 3
 SCHED_BLOB = SCHED_PARAM_OFFSET + SCHED_PARAMS + 1
 PHASE_INIT, PHASE_PULL_DENSE, PHASE_PULL_WEDGE, PHASE_VERTEX_PR, PHASE_WEDGE_BUILD, PHASE_ADVANCE = range(6)
 FLAG_GRAPH, FLAG_TIMING = 1, 2
+SHARD_PROPS, SHARD_FRONTIER = 0, 1
 
 OK = 0
 ERR_IO, ERR_FORMAT, ERR_OOM, ERR_CUDA, ERR_NOT_CONVERGED, ERR_ARG, ERR_UNSUPPORTED = -1, -2, -3, -4, -5, -6, -7
@@ -132,6 +133,14 @@ _SIGNATURES = {
     "wedge_cuda_run": (C.c_int, [C.c_void_p, C.c_int, C.POINTER(Params), C.POINTER(Stats)]),
     "wedge_cuda_run_phase": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.POINTER(Params), C.POINTER(C.c_uint64)]),
     "wedge_cuda_read_results": (C.c_int, [C.c_void_p, C.c_void_p, C.c_uint64]),
+    "wedge_cuda_run_async": (C.c_int, [C.c_void_p, C.c_int, C.POINTER(Params)]),
+    "wedge_cuda_read_results_async": (C.c_int, [C.c_void_p, C.c_void_p, C.c_uint64]),
+    "wedge_cuda_wait": (C.c_int, [C.c_void_p, C.POINTER(Stats)]),
+    "wedge_cuda_set_stream": (C.c_int, [C.c_void_p, C.c_void_p]),
+    "wedge_cuda_load_shard": (C.c_int, [C.c_uint64, C.c_uint64, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int,
+                                        C.c_void_p, C.c_uint64, C.POINTER(C.c_void_p)]),
+    "wedge_cuda_shard_state": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_uint64, C.c_int]),
+    "wedge_cuda_shard_decide": (C.c_int, [C.c_void_p, C.c_uint64, C.c_uint64]),
     "wedge_cuda_iteration_log": (C.c_int, [C.c_void_p, C.c_void_p, C.c_uint64, C.POINTER(C.c_uint64)]),
     "wedge_cuda_read_outdegrees": (C.c_int, [C.c_void_p, C.c_void_p, C.c_uint64]),
     "wedge_cuda_set_scheduler": (C.c_int, [C.c_void_p, C.c_void_p, C.c_uint64]),
@@ -226,6 +235,20 @@ class Graph:
         return cls(h, weight_kind if w is not None else WEIGHTS_NONE)
 
     @classmethod
+    def shard(cls, V: int, src, dst, global_outdeg, global_edges: int, weights=None,
+              weight_kind: int = WEIGHTS_U64) -> "Graph":
+        """one destination-range shard: the in-edges of its destinations, the whole graph's out-degrees"""
+        s = np.ascontiguousarray(src, np.uint32)
+        d = np.ascontiguousarray(dst, np.uint32)
+        od = np.ascontiguousarray(global_outdeg, np.uint64)
+        w = None if weights is None else np.ascontiguousarray(weights, np.uint64)
+        h = C.c_void_p()
+        _check(lib().wedge_cuda_load_shard(V, len(s), _ptr(s), _ptr(d), None if w is None else _ptr(w),
+                                           weight_kind if w is not None else WEIGHTS_NONE, _ptr(od), global_edges,
+                                           C.byref(h)), "wedge_cuda_load_shard")
+        return cls(h, weight_kind if w is not None else WEIGHTS_NONE)
+
+    @classmethod
     def from_edge_vectors(cls, V: int, vectors: np.ndarray, weighted: bool, weight_kind: int = WEIGHTS_U64) -> "Graph":
         v = np.ascontiguousarray(vectors, np.uint64)
         words = 8 if weighted else 4
@@ -272,6 +295,39 @@ class Graph:
         d = st.as_dict()
         d["status"] = rc
         return d
+
+    def run_async(self, app: int, params: Params | None = None):
+        """queue the whole traversal (device-side loop) without waiting; see wait()"""
+        self._async_params = params or Params()  # kept alive until the call returns
+        _check(lib().wedge_cuda_run_async(self._h, app, C.byref(self._async_params)), "wedge_cuda_run_async")
+        self.last_app = app
+
+    def read_results_async(self, out: np.ndarray):
+        """queue the export of the last run's results into page-locked host memory (out)"""
+        _check(lib().wedge_cuda_read_results_async(self._h, _ptr(out), out.nbytes), "wedge_cuda_read_results_async")
+
+    def wait(self, allow_not_converged: bool = False) -> dict:
+        """wait for the queued run and reads; the queued run's statistics"""
+        st = Stats()
+        rc = lib().wedge_cuda_wait(self._h, C.byref(st))
+        if not (rc == OK or (allow_not_converged and rc == ERR_NOT_CONVERGED)):
+            raise WedgeError(rc, "wedge_cuda_wait")
+        d = st.as_dict()
+        d["status"] = rc
+        return d
+
+    def set_stream(self, stream: int | None):
+        """queue this handle's work on a caller's CUDA stream (its handle as an int; None: its own)"""
+        _check(lib().wedge_cuda_set_stream(self._h, C.c_void_p(stream) if stream else None), "wedge_cuda_set_stream")
+
+    def shard_state(self, which: int, out: np.ndarray, import_: bool = False):
+        """a shard's properties or pulled frontier, to (import_ False) or from host memory"""
+        _check(lib().wedge_cuda_shard_state(self._h, which, _ptr(out), out.nbytes, int(import_)),
+               "wedge_cuda_shard_state")
+        return out
+
+    def shard_decide(self, global_mass: int, threshold_pct: int = 20):
+        _check(lib().wedge_cuda_shard_decide(self._h, global_mass, threshold_pct), "wedge_cuda_shard_decide")
 
     def run_phase(self, app: int, phase: int, params: Params | None = None) -> int:
         p = params or Params()
