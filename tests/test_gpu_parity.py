@@ -112,6 +112,51 @@ def test_sssp_fp64_weights_bit_exact(W, O, scale, ef, seed):
     assert np.array_equal(got, ref)  # 0 ULP
 
 
+def dijkstra_u64(V, s, d, w, root):
+    """exact shortest distances (float64 holds these integer sums exactly) of the
+    parallel-edge multigraph; UINT64_MAX where unreachable"""
+    sp = pytest.importorskip("scipy.sparse")
+    csgraph = pytest.importorskip("scipy.sparse.csgraph")
+    order = np.lexsort((w, d, s))
+    s, d, w = s[order], d[order], w[order]
+    first = np.ones(len(s), bool)
+    first[1:] = (s[1:] != s[:-1]) | (d[1:] != d[:-1])  # the least weight of each (s, d)
+    m = sp.csr_matrix((w[first].astype(np.float64), (s[first], d[first])), shape=(V, V))
+    dist = csgraph.dijkstra(m, directed=True, indices=root)
+    out = np.full(V, np.iinfo(np.uint64).max, np.uint64)
+    fin = np.isfinite(dist)
+    out[fin] = dist[fin].astype(np.uint64)
+    return out
+
+
+@pytest.mark.parametrize("sched", SCHEDS)
+@pytest.mark.parametrize("shift", [0, 25, 30])
+def test_sssp_distances_beyond_32_bits(W, O, sched, shift):
+    """the pulls gather a 32-bit copy of the distances while they fit: weights
+    scaled by 2^shift push a fifth of the distances past 2^32 (shift 25) or
+    nearly all (30), and the engine switches to the 64-bit distances; the results are
+    exact shortest distances (the reference's 32-bit minimum, _mm_min_epu32,
+    is not a 64-bit minimum there, so the check is Dijkstra's)"""
+    V, s, d = graph_edges(O, "rmat", dict(scale=11, edge_factor=16, seed=12))
+    w = O.weights(s, d).astype(np.uint64) << np.uint64(shift)
+    for root in (0, 5):
+        got, _, _ = run_engine(W, V, s, d, W.APP_SSSP, w, root=root, sched=sched_id(W, sched))
+        ref = dijkstra_u64(V, s, d, w, root)
+        assert np.array_equal(got, ref)
+        if shift:
+            assert got[got != np.iinfo(np.uint64).max].max() >= 2**32
+
+
+def test_sssp_narrow_copy_off_matches(W, O, monkeypatch):
+    """WEDGE_SSSP_NARROW=0 (64-bit gathers) gives the same distances"""
+    V, s, d = graph_edges(O, "rmat", dict(scale=13, edge_factor=8, seed=13))
+    w = O.weights(s, d)
+    on, _, _ = run_engine(W, V, s, d, W.APP_SSSP, w, root=0)
+    monkeypatch.setenv("WEDGE_SSSP_NARROW", "0")
+    off, _, _ = run_engine(W, V, s, d, W.APP_SSSP, w, root=0)
+    assert np.array_equal(on, off)
+
+
 @pytest.mark.parametrize("scale,ef,seed", SIZES)
 @pytest.mark.parametrize("sched", SCHEDS)
 def test_bfs_levels_exact_parents_valid(W, O, scale, ef, seed, sched):

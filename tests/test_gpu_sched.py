@@ -169,8 +169,9 @@ def test_trained_network_against_the_fixed_rule(W):
     """Held-out graphs (seeds not in the training set): every strategy's cost is
     measured per iteration, and the total cost of the network's choices is
     compared with the fixed rule's (gain = plain / learned) and with the
-    per-iteration best.  The network must not lose more than measurement noise
-    (5%) against the rule it falls back to; the measured gain is printed."""
+    per-iteration best (bound = plain / best, the most any choice could gain).
+    Both are scored on the same measured cost table, so the comparison carries
+    no run-to-run noise: the network must recover at least half of the bound."""
     from wedge_gb300 import scheduler as S
 
     if not os.path.exists(S.DEFAULT_NET):
@@ -182,7 +183,8 @@ def test_trained_network_against_the_fixed_rule(W):
         with W.Graph.rmat(20, 16, 91, symmetrise=sym, weight_kind=wk) as g:
             samples += S.probe_costs(g, app, reps=3, tag="heldout")
     r = S.evaluate(blob, samples)
-    print("held-out R-MAT scale 20:", r)
+    b = S.bound(samples)
+    print("held-out R-MAT scale 20:", r, "bound", b)
     assert r["iterations"] > 5
-    assert r["learned_us"] <= 1.05 * r["plain_us"]
+    assert r["gain"] - 1.0 >= 0.5 * (b - 1.0)
     assert r["learned_us"] >= r["best_us"] - 1e-9

@@ -5,7 +5,11 @@
 //   build   Wedge frontier of the queries whose next pull is sparse: the
 //           out-edge chunks of the vertices the last pull activated are
 //           marked (wedge.c:63-155), and newly marked chunks are appended to
-//           the query's chunk list; the previous frontier bitmaps are cleared
+//           the query's chunk list -- or, on graphs whose CSRI holds in-edge
+//           positions, every activated vertex's out-list becomes PIECE-entry
+//           items whose in-edges the pull relaxes one by one (as the single-
+//           query engine's SSSP Wedge pulls); the previous frontier bitmaps
+//           are cleared
 //   prefix  (block 0) per-query chunk counts -> one offset table: the work
 //           queue of the pull
 //   pull    warps take chunks of 32 in-edges from the queue, across all
@@ -38,6 +42,9 @@ struct BGraph {
     const uint32_t* dst_id;
     const unsigned long long* dst_off;
     const uint32_t* chunk_dst0;  // [nchunks+1] compressed destination owning edge 32*c (Vne past the end)
+    const uint32_t* dst_start;   // destination-start bitmap and 128-edge tile index of the graph handle
+    const uint32_t* tile_dst0;
+    const uint8_t* w8;           // byte-wide weights, or null
     const uint32_t* outdeg;
     const unsigned long long* csri_off;
     const uint32_t* csri;
@@ -45,7 +52,8 @@ struct BGraph {
     const uint32_t* new2old;
     const uint32_t* old2new;
     uint64_t V, E;
-    uint32_t Vne, nchunks, weight_kind, pad;
+    uint32_t Vne, nchunks, weight_kind;
+    uint32_t push;               // sparse pulls relax in-edge positions (CSRI of positions)
 };
 
 struct BQuery {
@@ -55,6 +63,7 @@ struct BQuery {
     uint32_t* list[2];        // [V] the same vertices as lists
     uint32_t* chunk_bits;     // [nchunks/32+1] Wedge frontier
     uint32_t* chunk_list;     // [nchunks] its marked chunks
+    uint2* vitems;            // [V + E/PIECE + 1] (vertex, piece) items of a sparse pull over in-edge positions
 };
 
 struct BCtl {
@@ -166,6 +175,16 @@ __device__ void phase_build(const BArgs& a)
             start = G.csri_off[v];
             len = G.csri_off[v + 1] - start;
         }
+        // sparse pulls over in-edge positions: PIECE-entry items of each out-list
+        if (valid && a.graphs[a.q[q].graph].push) {
+            const uint32_t np = (uint32_t)((len + PIECE - 1) / PIECE);
+            if (np) {
+                const uint32_t pos = atomicAdd(&a.ctl[q].items, np);
+                for (uint32_t j = 0; j < np; ++j)
+                    a.q[q].vitems[pos + j] = make_uint2(v, j);
+            }
+            len = 0; /* nothing to mark */
+        }
         // short lists: one lane each
         if (valid && len <= a.split) {
             const BGraph& G = a.graphs[a.q[q].graph];
@@ -173,7 +192,7 @@ __device__ void phase_build(const BArgs& a)
                 mark_batch_chunk(a.q[q], a.ctl[q], G.csri[start + j] >> G.csri_shift);
         }
         // long lists: the whole warp, one list at a time
-        uint32_t longs = __ballot_sync(FULL, valid && len > a.split);
+        uint32_t longs = __ballot_sync(FULL, valid && len > a.split && !a.graphs[a.q[q].graph].push);
         while (longs) {
             const int l = __ffs(longs) - 1;
             longs &= longs - 1u;
@@ -294,6 +313,48 @@ __device__ void pull_chunk(const BArgs& a, uint32_t q, uint32_t ch, uint32_t* he
     }
 }
 
+// A sparse pull over in-edge positions: the in-edges of one PIECE of an
+// activated vertex's out-list are relaxed by the warp's lanes (BFS: an
+// unvisited destination takes the vertex as its parent; SSSP: min-plus)
+__device__ void push_piece(const BArgs& a, uint32_t q, uint2 it, unsigned long long& mass)
+{
+    const int lane = threadIdx.x & 31;
+    const BQuery& qq = a.q[q];
+    BCtl& c = a.ctl[q];
+    const BGraph& G = a.graphs[qq.graph];
+    uint32_t* nxt = qq.front[c.parity ^ 1u];
+    uint32_t* nlist = qq.list[c.parity ^ 1u];
+    auto activate = [&](uint32_t vtx) {
+        const uint32_t b = 1u << (vtx & 31u);
+        if (!(atomicOr(&nxt[vtx >> 5], b) & b)) {
+            const uint32_t pos = atomicAdd(&c.nlist[c.parity ^ 1u], 1u);
+            nlist[pos] = vtx;
+            mass += G.outdeg[vtx];
+        }
+    };
+    const unsigned long long lo = G.csri_off[it.x] + (unsigned long long)it.y * PIECE;
+    const unsigned long long end = G.csri_off[it.x + 1u];
+    const unsigned long long hi = (lo + PIECE < end) ? lo + PIECE : end;
+    const unsigned long long du = qq.prop[it.x];
+    const bool f64 = G.weight_kind == WEDGE_WEIGHTS_F64;
+    for (unsigned long long j = lo + (unsigned long long)lane; j < hi; j += 32u) {
+        const uint32_t p = G.csri[j];
+        const uint32_t vtx = G.dst_id[dst_of_pos(G.dst_start, G.tile_dst0, p)];
+        if (qq.app == WEDGE_APP_BFS) {
+            if (qq.prop[vtx] == NONE64 && atomicCAS(&qq.prop[vtx], NONE64, (unsigned long long)it.x) == NONE64)
+                activate(vtx);
+        } else {
+            const unsigned long long wt = G.w8 ? (unsigned long long)G.w8[p] : G.w[p];
+            const unsigned long long nd =
+                f64 ? (unsigned long long)__double_as_longlong(
+                          __dadd_rn(__longlong_as_double((long long)du), __longlong_as_double((long long)wt)))
+                    : du + wt; /* phase_edge_pull_sssp.c:136-137; an activated source is reached */
+            if (nd < qq.prop[vtx] && nd < atomicMin(&qq.prop[vtx], nd))
+                activate(vtx);
+        }
+    }
+}
+
 __device__ void phase_pull(const BArgs& a)
 {
     __shared__ uint32_t heads_all[BT / 32];
@@ -316,16 +377,20 @@ __device__ void phase_pull(const BArgs& a)
             const unsigned long long local = i - a.pull_off[q];
             const BCtl& c = a.ctl[q];
             const bool sparse = c.mode == MODE_WEDGE;
-            const uint32_t ch = sparse ? a.q[q].chunk_list[local] : (uint32_t)local;
+            const bool push = sparse && a.graphs[a.q[q].graph].push;
+            const uint32_t ch = (sparse && !push) ? a.q[q].chunk_list[local] : (uint32_t)local;
             unsigned long long mass = 0;
-            pull_chunk(a, q, ch, heads, mass);
+            if (push)
+                push_piece(a, q, a.q[q].vitems[local], mass);
+            else
+                pull_chunk(a, q, ch, heads, mass);
 #pragma unroll
             for (int d = 16; d > 0; d >>= 1)
                 mass += __shfl_xor_sync(FULL, mass, d);
             if (lane == 0) {
                 if (mass)
                     atomicAdd(&a.ctl[q].mass, mass);
-                if (sparse)
+                if (sparse && !push)
                     atomicAnd(&a.q[q].chunk_bits[ch >> 5], ~(1u << (ch & 31u))); /* consumed */
             }
             ++pulled;
@@ -577,7 +642,7 @@ extern "C" int wedge_cuda_batch_create(wedge_graph_t* const* graphs, uint32_t nu
     b->device = dev;
     b->Q = num_queries;
     b->G = num_graphs;
-    b->qallocs = (void**)calloc((size_t)num_queries * 7 + num_graphs + 1, sizeof(void*)); /* 7 arrays per query */
+    b->qallocs = (void**)calloc((size_t)num_queries * 8 + num_graphs + 1, sizeof(void*)); /* 8 arrays per query */
     b->h_graphs = (BGraph*)calloc(num_graphs, sizeof(BGraph));
     b->h_queries = (BQuery*)calloc(num_queries, sizeof(BQuery));
     int rc = WEDGE_OK;
@@ -602,6 +667,10 @@ extern "C" int wedge_cuda_batch_create(wedge_graph_t* const* graphs, uint32_t nu
         G.csri_off = g.csri_off;
         G.csri = g.csri;
         G.csri_shift = g.csri_pos ? 5u : 0u;
+        G.push = g.csri_pos ? 1u : 0u;
+        G.dst_start = g.dst_start;
+        G.tile_dst0 = g.tile_dst0;
+        G.w8 = g.w8;
         G.new2old = g.new2old;
         G.old2new = g.old2new;
         G.V = g.V;
@@ -625,7 +694,8 @@ extern "C" int wedge_cuda_batch_create(wedge_graph_t* const* graphs, uint32_t nu
         if ((rc = balloc(b, &q.prop, G.V, true)) || (rc = balloc(b, &q.front[0], words, true)) ||
             (rc = balloc(b, &q.front[1], words, true)) || (rc = balloc(b, &q.list[0], G.V, true)) ||
             (rc = balloc(b, &q.list[1], G.V, true)) || (rc = balloc(b, &q.chunk_bits, (uint64_t)G.nchunks / 32 + 1, true)) ||
-            (rc = balloc(b, &q.chunk_list, (uint64_t)G.nchunks, true)))
+            (rc = balloc(b, &q.chunk_list, (uint64_t)G.nchunks, true)) ||
+            (rc = balloc(b, &q.vitems, G.push ? G.V + G.E / PIECE + 1 : 1, true)))
             return fail(rc);
     }
     if ((rc = balloc(b, &b->d_graphs, num_graphs, false)) || (rc = balloc(b, &b->d_queries, num_queries, false)) ||

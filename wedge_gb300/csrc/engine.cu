@@ -844,16 +844,24 @@ __host__ __device__ constexpr uint32_t dst_launches_of(int app)
     return app == WEDGE_APP_BFS ? 1u : app == WEDGE_APP_CC ? 2u : 0u;
 }
 
-// compressed destination owning in-edge position pos: the owner of the
-// 128-edge index tile's first edge plus the destination starts after it
-__device__ __forceinline__ uint32_t dst_of_pos(const DevGraph& g, uint32_t pos)
+// SSSP narrow distances: a distance write, recorded in the 32-bit copy the
+// pulls gather (4 bytes per gather instead of 8).  Distances only decrease, so
+// a copy saturated at NONE32 is never below the distance; a finite distance
+// that does not fit sets Ctrl::narrow_ovf, after which the pulls gather the
+// 64-bit distances from their next launch on (a source a pull skipped as
+// unreached meanwhile changed in this iteration: the next pull relaxes it).
+__device__ __forceinline__ void dist32_put(const DevState& s, uint32_t v, unsigned long long d, bool sole)
 {
-    const uint32_t t = pos >> 7, w0 = t << 2, wp = pos >> 5;
-    uint32_t n = 0;
-    for (uint32_t w = w0; w < wp; ++w)
-        n += __popc(g.dst_start[w]);
-    n += __popc(g.dst_start[wp] & ((pos & 31u) == 31u ? FULL : ((2u << (pos & 31u)) - 1u)));
-    return g.tile_dst0[t] + n - (g.dst_start[w0] & 1u); /* a start at the index tile's first edge is the owner's */
+    if (!s.dist32)
+        return;
+    if (d >= (unsigned long long)NONE32) {
+        atomicOr(&s.ctrl->narrow_ovf, 1u);
+        return;
+    }
+    if (sole)
+        s.dist32[v] = (uint32_t)d;
+    else
+        atomicMin(&s.dist32[v], (uint32_t)d);
 }
 
 // The Wedge pull of SSSP over in-edge positions: every vertex the last pull
@@ -869,12 +877,12 @@ __device__ __forceinline__ void sssp_push_pull(const DevGraph& g, const DevState
                                                unsigned long long* block_cnt)
 {
     constexpr int WARPS = PULL_THREADS / 32;
-    __shared__ unsigned long long sh_pc[WARPS][3];
+    __shared__ unsigned long long sh_pc[WARPS][4];
     __shared__ unsigned int sh_pdeg[3];
     const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
     uint32_t* nxt = next_front(s, c->parity);
     const bool f64 = g.weight_kind == WEDGE_WEIGHTS_F64;
-    unsigned long long mass = 0, edges = 0, act = 0;
+    unsigned long long mass = 0, edges = 0, act = 0, occ = 0;
     if (threadIdx.x < 3)
         sh_pdeg[threadIdx.x] = 0u;
     __syncthreads();
@@ -887,8 +895,11 @@ __device__ __forceinline__ void sssp_push_pull(const DevGraph& g, const DevState
         const uint32_t k = dst_of_pos(g, pos);
         const uint32_t vtx = g.dst_ident ? k : g.dst_id[k];
         if (nd < s.prop64[vtx] && nd < atomicMin(&s.prop64[vtx], nd)) {
+            dist32_put(s, vtx, nd, false);
             const uint32_t b = 1u << (vtx & 31u);
-            if (!(atomicOr(&nxt[vtx >> 5], b) & b)) {
+            const uint32_t o = atomicOr(&nxt[vtx >> 5], b);
+            occ += o == 0u ? 1u : 0u;
+            if (!(o & b)) {
                 const uint32_t od = g.outdeg[vtx];
                 mass += od;
                 ++act;
@@ -932,25 +943,29 @@ __device__ __forceinline__ void sssp_push_pull(const DevGraph& g, const DevState
     mass = warp_sum_u64(mass);
     edges = warp_sum_u64(edges);
     act = warp_sum_u64(act);
+    occ = warp_sum_u64(occ);
     if (lane == 0) {
         sh_pc[wib][0] = mass;
         sh_pc[wib][1] = edges;
         sh_pc[wib][2] = act;
+        sh_pc[wib][3] = occ;
     }
     __syncthreads();
     if (threadIdx.x < NCNT) {
         unsigned long long a = 0;
-        const int col = threadIdx.x == CNT_MASS ? 0 : threadIdx.x == CNT_EDGES ? 1 : threadIdx.x == CNT_ACT ? 2 : -1;
+        const int col = threadIdx.x == CNT_MASS ? 0 : threadIdx.x == CNT_EDGES ? 1 : threadIdx.x == CNT_ACT ? 2
+                      : threadIdx.x == CNT_OCC ? 3 : -1;
         if (col >= 0)
             for (int w = 0; w < WARPS; ++w)
                 a += sh_pc[w][col];
-        if (threadIdx.x >= CNT_DEG0)
+        if (threadIdx.x >= CNT_DEG0 && threadIdx.x <= CNT_DEG2)
             a = sh_pdeg[threadIdx.x - CNT_DEG0];
         block_cnt[NCNT * blockIdx.x + threadIdx.x] = a;
     }
 }
 
 // BFS/CC probe: in-edges of an unfinished destination read before the tile pull
+// (the default of Ctrl::probe_edges; WEDGE_PROBE_EDGES overrides it)
 constexpr uint32_t PROBE_EDGES = 16;
 
 // Edge pull over all tiles (dense) or over the tiles of the Wedge frontier.
@@ -1007,7 +1022,7 @@ __global__ void __launch_bounds__(PULL_THREADS, 1)
     uint32_t* nxt = next_front(s, parity);
     uint32_t* my_id = tab_id[wib];
     cur_t* my_cur = tab_cur[wib];
-    unsigned long long mass = 0, edges = 0, tiles = 0, dsts = 0, act = 0;
+    unsigned long long mass = 0, edges = 0, tiles = 0, dsts = 0, act = 0, occ = 0;
     auto count_act = [&](uint32_t d) {
         mass += d;
         ++act;
@@ -1018,10 +1033,12 @@ __global__ void __launch_bounds__(PULL_THREADS, 1)
     auto vid = [&](uint32_t k, uint32_t slot) -> uint32_t { return slot < TAB ? my_id[slot] : g.dst_id[k]; };
 
     // ---- hub cache
-    const bool wide = (APP == WEDGE_APP_SSSP) || (APP == WEDGE_APP_PR); /* FP32C PageRank: pr32_pull_kernel */
+    // SSSP gathers the 32-bit copy of the distances while every distance fits
+    const bool narrow = APP == WEDGE_APP_SSSP && s.dist32 && !c->narrow_ovf;
+    const bool wide = (APP == WEDGE_APP_SSSP && !narrow) || (APP == WEDGE_APP_PR); /* FP32C PageRank: pr32_pull_kernel */
     const void* hub_src = (APP == WEDGE_APP_BFS)    ? (const void*)cur
                           : (APP == WEDGE_APP_CC)   ? (const void*)s.prop32
-                          : (APP == WEDGE_APP_SSSP) ? (const void*)s.prop64
+                          : (APP == WEDGE_APP_SSSP) ? (narrow ? (const void*)s.dist32 : (const void*)s.prop64)
                                                     : (const void*)s.rank;
     const uint64_t hub_have = ((APP == WEDGE_APP_BFS) ? (g.V + 31) / 32 : g.V) * (wide ? 8u : 4u);
     const uint64_t hub_fit = hub_have & ~15ull;
@@ -1031,6 +1048,8 @@ __global__ void __launch_bounds__(PULL_THREADS, 1)
         use_hub = use_hub && (mode != MODE_WEDGE || c->tiles >= T / 16u);
     else if (two_phase_app(APP))
         use_hub = use_hub && mode != MODE_WEDGE;
+    if (APP == WEDGE_APP_SSSP && s.dist32 && !narrow)
+        use_hub = false; /* the cache is sized and split for the 32-bit copy */
     uint32_t* hub32 = reinterpret_cast<uint32_t*>(hub_smem);
     unsigned long long* hub64 = reinterpret_cast<unsigned long long*>(hub_smem);
     if (threadIdx.x < 3)
@@ -1129,7 +1148,7 @@ __global__ void __launch_bounds__(PULL_THREADS, 1)
                 const uint32_t old = (kind == EMIT_COMPLETE) ? (s.prop32[vtx] = val, NONE32) : atomicMin(&s.prop32[vtx], val);
                 if (old == NONE32) {
                     atomicOr(&s.vis_c[k >> 5], 1u << (k & 31u));
-                    atomicOr(&nxt[vtx >> 5], 1u << (vtx & 31u));
+                    occ += atomicOr(&nxt[vtx >> 5], 1u << (vtx & 31u)) == 0u ? 1u : 0u;
                     count_act(g.outdeg[vtx]);
                 }
             });
@@ -1189,12 +1208,15 @@ __global__ void __launch_bounds__(PULL_THREADS, 1)
                         // sole writer of vtx in this launch: cv is current; the
                         // probe may have set its changed bit already
                         s.prop32[vtx] = val;
-                        if (!(atomicOr(&nxt[vtx >> 5], b) & b))
+                        const uint32_t o = atomicOr(&nxt[vtx >> 5], b);
+                        occ += o == 0u ? 1u : 0u;
+                        if (!(o & b))
                             count_act(g.outdeg[vtx]);
                     } else if (val < atomicMin(&s.prop32[vtx], val)) {
-                        if (!(atomicOr(&nxt[vtx >> 5], b) & b)) {
+                        const uint32_t o = atomicOr(&nxt[vtx >> 5], b);
+                        occ += o == 0u ? 1u : 0u;
+                        if (!(o & b))
                             count_act(g.outdeg[vtx]);
-                        }
                     }
                 }
             });
@@ -1226,7 +1248,13 @@ __global__ void __launch_bounds__(PULL_THREADS, 1)
             for (int q = 0; q < EPL; ++q) {
                 v[q] = NONE64;
                 if (sa[q] != NONE32 && (!filtered || ((ld_ro_u32(cur + (sa[q] >> 5)) >> (sa[q] & 31u)) & 1u))) {
-                    const unsigned long long d = (sa[q] < hub_lim) ? hub64[sa[q]] : s.prop64[sa[q]];
+                    unsigned long long d;
+                    if (narrow) {
+                        const uint32_t x = (sa[q] < hub_lim) ? hub32[sa[q]] : s.dist32[sa[q]];
+                        d = (x == NONE32) ? NONE64 : (unsigned long long)x;
+                    } else {
+                        d = (sa[q] < hub_lim) ? hub64[sa[q]] : s.prop64[sa[q]];
+                    }
                     if (g.weight_kind == WEDGE_WEIGHTS_F64)
                         v[q] = (unsigned long long)__double_as_longlong(
                             __dadd_rn(__longlong_as_double((long long)d), __longlong_as_double((long long)wv[q])));
@@ -1248,17 +1276,24 @@ __global__ void __launch_bounds__(PULL_THREADS, 1)
                 const uint32_t vtx = vid(k, slot);
                 const unsigned long long cv = slot < TAB ? (unsigned long long)my_cur[slot] : s.prop64[vtx];
                 if (val < cv) {
-                    if (vtx < hub_lim)
-                        atomicMin(&hub64[vtx], val);
+                    if (vtx < hub_lim) {
+                        if (narrow)
+                            atomicMin(&hub32[vtx], val < (unsigned long long)NONE32 ? (uint32_t)val : NONE32);
+                        else
+                            atomicMin(&hub64[vtx], val);
+                    }
                     const uint32_t b = 1u << (vtx & 31u);
                     if (kind == EMIT_COMPLETE) {
                         s.prop64[vtx] = val; /* sole writer, as for CC */
-                        atomicOr(&nxt[vtx >> 5], b);
+                        dist32_put(s, vtx, val, true);
+                        occ += atomicOr(&nxt[vtx >> 5], b) == 0u ? 1u : 0u;
                         count_act(g.outdeg[vtx]);
                     } else if (val < atomicMin(&s.prop64[vtx], val)) {
-                        if (!(atomicOr(&nxt[vtx >> 5], b) & b)) {
+                        dist32_put(s, vtx, val, false);
+                        const uint32_t o = atomicOr(&nxt[vtx >> 5], b);
+                        occ += o == 0u ? 1u : 0u;
+                        if (!(o & b))
                             count_act(g.outdeg[vtx]);
-                        }
                     }
                 }
             });
@@ -1295,6 +1330,7 @@ __global__ void __launch_bounds__(PULL_THREADS, 1)
     mass = warp_sum_u64(mass);
     edges = warp_sum_u64(edges);
     act = warp_sum_u64(act);
+    occ = warp_sum_u64(occ);
     if (lane == 0) {
         sh_cnt[wib][CNT_MASS] = mass;
         sh_cnt[wib][CNT_EDGES] = edges;
@@ -1304,13 +1340,14 @@ __global__ void __launch_bounds__(PULL_THREADS, 1)
         sh_cnt[wib][CNT_DEG0] = 0ull;
         sh_cnt[wib][CNT_DEG1] = 0ull;
         sh_cnt[wib][CNT_DEG2] = 0ull;
+        sh_cnt[wib][CNT_OCC] = occ;
     }
     __syncthreads();
     if (threadIdx.x < NCNT) {
         unsigned long long a = 0;
         for (int w = 0; w < WARPS; ++w)
             a += sh_cnt[w][threadIdx.x];
-        if (threadIdx.x >= CNT_DEG0)
+        if (threadIdx.x >= CNT_DEG0 && threadIdx.x <= CNT_DEG2)
             a = sh_deg[threadIdx.x - CNT_DEG0];
         block_cnt[NCNT * blockIdx.x + threadIdx.x] = a;
     }
@@ -1364,28 +1401,42 @@ __global__ void __launch_bounds__(PULL_THREADS, 1)
     uint32_t* nxt = next_front(s, c->parity);
     const bool filtered = mode == MODE_FILTERED;
     const uint32_t hub_bytes = s.hub_bytes;
+    const bool narrow = s.dist32 && !c->narrow_ovf; /* gathers from the 32-bit copy */
+    const unsigned char* hub_src = narrow ? reinterpret_cast<const unsigned char*>(s.dist32)
+                                          : reinterpret_cast<const unsigned char*>(s.prop64);
+    uint32_t* hub32 = reinterpret_cast<uint32_t*>(sssp_smem);
     unsigned long long* hub64 = reinterpret_cast<unsigned long long*>(sssp_smem);
     unsigned long long* my_min = reinterpret_cast<unsigned long long*>(sssp_smem + hub_bytes) + (uint32_t)wib * SSSP_SLOTS;
-    unsigned long long mass = 0, edges = 0, tiles = 0, dsts = 0, act = 0;
+    unsigned long long mass = 0, edges = 0, tiles = 0, dsts = 0, act = 0, occ = 0;
     if (threadIdx.x < 3)
         sh_deg[threadIdx.x] = 0u;
-    const bool use_hub = hub_bytes != 0u && ((uintptr_t)s.prop64 & 15u) == 0u;
+    /* the cache is sized and split for the 32-bit copy where there is one */
+    const bool use_hub = hub_bytes != 0u && ((uintptr_t)hub_src & 15u) == 0u && (narrow || !s.dist32);
     __syncthreads();
     if (use_hub) {
         if (threadIdx.x == 0) {
             mbar_init(&hub_bar, 1u);
             mbar_arrive_expect_tx(&hub_bar, hub_bytes);
             for (uint32_t off = 0; off < hub_bytes; off += 32768u)
-                bulk_g2s(sssp_smem + off, reinterpret_cast<const unsigned char*>(s.prop64) + off,
-                         min(32768u, hub_bytes - off), &hub_bar);
+                bulk_g2s(sssp_smem + off, hub_src + off, min(32768u, hub_bytes - off), &hub_bar);
         }
         __syncthreads();
     }
     uint32_t hub_lim = 0;
+    auto hub_min = [&](uint32_t vtx, unsigned long long val) {
+        if (vtx >= hub_lim)
+            return;
+        if (narrow)
+            atomicMin(&hub32[vtx], val < (unsigned long long)NONE32 ? (uint32_t)val : NONE32);
+        else
+            atomicMin(&hub64[vtx], val);
+    };
     // a changed destination: its bit in the next frontier and, the first time, its out-edge mass
     auto activate = [&](uint32_t vtx) {
         const uint32_t b = 1u << (vtx & 31u);
-        if (!(atomicOr(&nxt[vtx >> 5], b) & b)) {
+        const uint32_t o = atomicOr(&nxt[vtx >> 5], b);
+        occ += o == 0u ? 1u : 0u;
+        if (!(o & b)) {
             const uint32_t od = g.outdeg[vtx];
             mass += od;
             ++act;
@@ -1411,7 +1462,7 @@ __global__ void __launch_bounds__(PULL_THREADS, 1)
             if (lane == 0)
                 ready = mbar_test_wait(&hub_bar, 0u) ? 1u : 0u;
             if (__shfl_sync(FULL, ready, 0))
-                hub_lim = hub_bytes / 8u;
+                hub_lim = hub_bytes / (narrow ? 4u : 8u);
         }
         ++tiles;
         const uint64_t base = (uint64_t)t * SSSP_TILE;
@@ -1437,7 +1488,13 @@ __global__ void __launch_bounds__(PULL_THREADS, 1)
             bool on = x != NONE32;
             if (filtered && on)
                 on = (ld_ro_u32(cur + (x >> 5)) >> (x & 31u)) & 1u; /* changed by the previous pull */
-            const unsigned long long d = !on ? NONE64 : (x < hub_lim) ? hub64[x] : s.prop64[x];
+            unsigned long long d = NONE64;
+            if (on && narrow) {
+                const uint32_t y = (x < hub_lim) ? hub32[x] : s.dist32[x];
+                d = (y == NONE32) ? NONE64 : (unsigned long long)y;
+            } else if (on) {
+                d = (x < hub_lim) ? hub64[x] : s.prop64[x];
+            }
             const unsigned long long w = (wword[q >> 2] >> (8 * (q & 3))) & 0xFFu;
             v[q] = (d == NONE64) ? NONE64 : d + w; /* phase_edge_pull_sssp.c:136-137 */
             edges += (x != NONE32) ? 1u : 0u;
@@ -1461,13 +1518,13 @@ __global__ void __launch_bounds__(PULL_THREADS, 1)
             if (kind == EMIT_COMPLETE) { /* the destination's only writer in this launch */
                 if (val < s.prop64[vtx]) {
                     s.prop64[vtx] = val;
-                    if (vtx < hub_lim)
-                        atomicMin(&hub64[vtx], val);
+                    dist32_put(s, vtx, val, true);
+                    hub_min(vtx, val);
                     activate(vtx);
                 }
             } else if (val < s.prop64[vtx] && val < atomicMin(&s.prop64[vtx], val)) {
-                if (vtx < hub_lim)
-                    atomicMin(&hub64[vtx], val);
+                dist32_put(s, vtx, val, false);
+                hub_min(vtx, val);
                 activate(vtx);
             }
         });
@@ -1483,8 +1540,8 @@ __global__ void __launch_bounds__(PULL_THREADS, 1)
             const uint32_t vtx = g.dst_ident ? k : g.dst_id[k];
             if (val < s.prop64[vtx]) { /* the destination's only writer in this launch */
                 s.prop64[vtx] = val;
-                if (vtx < hub_lim)
-                    atomicMin(&hub64[vtx], val);
+                dist32_put(s, vtx, val, true);
+                hub_min(vtx, val);
                 activate(vtx);
             }
         }
@@ -1497,17 +1554,19 @@ __global__ void __launch_bounds__(PULL_THREADS, 1)
     mass = warp_sum_u64(mass);
     edges = warp_sum_u64(edges);
     act = warp_sum_u64(act);
+    occ = warp_sum_u64(occ);
     if (lane == 0) {
         sh_cnt[wib][CNT_MASS] = mass;
         sh_cnt[wib][CNT_EDGES] = edges;
         sh_cnt[wib][CNT_TILES] = tiles;
         sh_cnt[wib][CNT_DSTS] = dsts;
         sh_cnt[wib][CNT_ACT] = act;
+        sh_cnt[wib][CNT_OCC] = occ;
     }
     __syncthreads();
     if (threadIdx.x < NCNT) {
         unsigned long long a = 0;
-        if (threadIdx.x >= CNT_DEG0)
+        if (threadIdx.x >= CNT_DEG0 && threadIdx.x <= CNT_DEG2)
             a = sh_deg[threadIdx.x - CNT_DEG0];
         else
             for (int w = 0; w < WARPS; ++w)
@@ -1549,10 +1608,24 @@ __global__ void __launch_bounds__(PULL_THREADS, 2)
     const uint32_t gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const uint32_t* cur = cur_front(s, c->parity);
     uint32_t* nxt = next_front(s, c->parity);
-    unsigned long long mass = 0, edges = 0, dsts = 0, act = 0;
+    const unsigned long long pwin = c->probe_edges; /* probe window of this pull */
+    unsigned long long mass = 0, edges = 0, dsts = 0, act = 0, occ = 0;
     if (threadIdx.x < 3)
         sh_deg[threadIdx.x] = 0u;
     __syncthreads();
+    // Bits into the pull's output bitmap, and the count of its words they
+    // occupy (no atomic returns: a word only this warp writes in the launch
+    // counts once; lanes' scattered bits count once per distinct word of the
+    // warp's group, count_words after the group)
+    auto set_word = [&](uint32_t w, uint32_t bits) {
+        atomicOr(&nxt[w], bits);
+        ++occ;
+    };
+    auto count_words = [&](uint32_t dw) {
+        const uint32_t same = __match_any_sync(FULL, dw);
+        if (dw != NONE32 && (uint32_t)(__ffs(same) - 1) == (uint32_t)lane)
+            ++occ;
+    };
 
     // bitmap marks of tiles [ta, tb] (one lane)
     auto mark_tiles = [](uint32_t* bm, uint32_t ta, uint32_t tb) {
@@ -1670,9 +1743,9 @@ __global__ void __launch_bounds__(PULL_THREADS, 2)
                 const uint32_t z1 = __reduce_or_sync(FULL, (zero && !in0) ? bit : 0u);
                 if (lane == 0) {
                     if (c0)
-                        atomicOr(&nxt[w0], c0);
+                        set_word(w0, c0);
                     if (c1)
-                        atomicOr(&nxt[w0 + 1u], c1);
+                        set_word(w0 + 1u, c1);
                     if (z0)
                         atomicOr(&s.vis_c[w0], z0); /* label 0 is final */
                     if (z1)
@@ -1683,6 +1756,7 @@ __global__ void __launch_bounds__(PULL_THREADS, 2)
                     atomicOr(&nxt[d >> 5], 1u << (d & 31u));
                 if (zero)
                     atomicOr(&s.vis_c[k >> 5], 1u << (k & 31u));
+                count_words(chg ? d >> 5 : NONE32);
             }
         }
     }
@@ -1696,13 +1770,13 @@ __global__ void __launch_bounds__(PULL_THREADS, 2)
         for (uint32_t base = gw * 32u; base < n; base += nthr) {
             const uint32_t i = base + (uint32_t)lane;
             bool hit = false;
-            uint32_t od = 0u;
+            uint32_t od = 0u, dw = NONE32;
             if (i < n) {
                 const uint32_t k = s.cand_list[i];
                 s.cand[k >> 5] = 0u;
                 const uint32_t d = g.dst_ident ? k : g.dst_id[k];
                 const unsigned long long lo = g.dst_off[k], hi = g.dst_off[k + 1u];
-                const unsigned long long lim = hi - lo > PROBE_EDGES ? lo + PROBE_EDGES : hi;
+                const unsigned long long lim = hi - lo > pwin ? lo + pwin : hi;
                 unsigned long long e = lo;
                 uint32_t par = NONE32;
                 while (e < lim) {
@@ -1720,11 +1794,13 @@ __global__ void __launch_bounds__(PULL_THREADS, 2)
                     s.prop32[d] = par; /* the destination's only writer in this launch */
                     atomicOr(&s.vis_c[k >> 5], 1u << (k & 31u));
                     atomicOr(&nxt[d >> 5], 1u << (d & 31u));
+                    dw = d >> 5;
                     od = g.outdeg[d];
                     mass += od;
                     ++act;
                 }
             }
+            count_words(dw);
             dsts += (uint64_t)__popc(__ballot_sync(FULL, i < n));
 #pragma unroll
             for (uint32_t b = 0; b < 3u; ++b) {
@@ -1763,11 +1839,11 @@ __global__ void __launch_bounds__(PULL_THREADS, 2)
             prefetch(base + nthr);
             const bool todo = k < g.Vne && !((vw >> lane) & 1u);
             bool hit = false;
-            uint32_t od = 0u;
+            uint32_t od = 0u, dw = NONE32;
             uint32_t ta = 1u, tb = 0u; /* tiles of a destination left unvisited (none: ta > tb) */
             if (todo) {
                 const uint32_t d = g.dst_ident ? k : g.dst_id[k];
-                const unsigned long long lim = hi - lo > PROBE_EDGES ? lo + PROBE_EDGES : hi;
+                const unsigned long long lim = hi - lo > pwin ? lo + pwin : hi;
                 unsigned long long e = lo;
                 uint32_t par = NONE32;
                 while (e < lim) {
@@ -1791,11 +1867,14 @@ __global__ void __launch_bounds__(PULL_THREADS, 2)
                     od = g.outdeg[d];
                     mass += od;
                     ++act;
-                    if (!g.dst_ident)
+                    if (!g.dst_ident) {
                         atomicOr(&nxt[d >> 5], 1u << (d & 31u));
+                        dw = d >> 5;
+                    }
                 }
             }
             mark_open(ta, tb);
+            count_words(dw);
             dsts += (uint64_t)__popc(__ballot_sync(FULL, todo));
 #pragma unroll
             for (uint32_t b = 0; b < 3u; ++b) {
@@ -1807,7 +1886,7 @@ __global__ void __launch_bounds__(PULL_THREADS, 2)
             if (lane == 0 && hits) {
                 atomicOr(&s.vis_c[base >> 5], hits);
                 if (g.dst_ident)
-                    atomicOr(&nxt[base >> 5], hits); /* d = k */
+                    set_word(base >> 5, hits); /* d = k */
             }
         }
     }
@@ -1821,13 +1900,13 @@ __global__ void __launch_bounds__(PULL_THREADS, 2)
         for (uint32_t base = gw * 32u; base < n; base += nthr) {
             const uint32_t i = base + (uint32_t)lane;
             bool chg = false;
-            uint32_t od = 0u;
+            uint32_t od = 0u, dw = NONE32;
             if (i < n) {
                 const uint32_t k = s.cand_list[i];
                 s.cand[k >> 5] = 0u;
                 const uint32_t d = g.dst_ident ? k : g.dst_id[k];
                 const unsigned long long lo = g.dst_off[k], hi = g.dst_off[k + 1u];
-                const unsigned long long lim = hi - lo > PROBE_EDGES ? lo + PROBE_EDGES : hi;
+                const unsigned long long lim = hi - lo > pwin ? lo + pwin : hi;
                 const uint32_t cv = s.prop32[d];
                 uint32_t m = cv;
                 unsigned long long e = lo;
@@ -1845,6 +1924,7 @@ __global__ void __launch_bounds__(PULL_THREADS, 2)
                     if (m == 0u)
                         atomicOr(&s.vis_c[k >> 5], 1u << (k & 31u)); /* label 0 is final */
                     atomicOr(&nxt[d >> 5], 1u << (d & 31u));
+                    dw = d >> 5;
                     od = g.outdeg[d];
                     mass += od;
                     ++act;
@@ -1852,6 +1932,7 @@ __global__ void __launch_bounds__(PULL_THREADS, 2)
                 if (!whole)
                     need_tiles((uint32_t)(lo / TILE_E), (uint32_t)((hi - 1u) / TILE_E));
             }
+            count_words(dw);
             dsts += (uint64_t)__popc(__ballot_sync(FULL, i < n));
 #pragma unroll
             for (uint32_t b = 0; b < 3u; ++b) {
@@ -1890,11 +1971,12 @@ __global__ void __launch_bounds__(PULL_THREADS, 2)
             prefetch(base + nthr);
             const bool todo = k < g.Vne && !((vw >> lane) & 1u);
             bool chg = false, zero = false;
+            uint32_t dw = NONE32;
             uint32_t d = 0u, od = 0u;
             uint32_t ta = 1u, tb = 0u;
             if (todo) {
                 d = g.dst_ident ? k : g.dst_id[k];
-                const unsigned long long lim = hi - lo > PROBE_EDGES ? lo + PROBE_EDGES : hi;
+                const unsigned long long lim = hi - lo > pwin ? lo + pwin : hi;
                 const uint32_t cv = s.prop32[d];
                 uint32_t m = cv;
                 unsigned long long e = lo;
@@ -1913,8 +1995,10 @@ __global__ void __launch_bounds__(PULL_THREADS, 2)
                     od = g.outdeg[d];
                     mass += od;
                     ++act;
-                    if (!g.dst_ident)
+                    if (!g.dst_ident) {
                         atomicOr(&nxt[d >> 5], 1u << (d & 31u));
+                        dw = d >> 5;
+                    }
                 }
                 if (!whole)
                     need_tiles((uint32_t)(lo / TILE_E), (uint32_t)((hi - 1u) / TILE_E));
@@ -1924,6 +2008,7 @@ __global__ void __launch_bounds__(PULL_THREADS, 2)
                 }
             }
             mark_open(ta, tb);
+            count_words(dw);
             dsts += (uint64_t)__popc(__ballot_sync(FULL, todo));
 #pragma unroll
             for (uint32_t b = 0; b < 3u; ++b) {
@@ -1936,13 +2021,14 @@ __global__ void __launch_bounds__(PULL_THREADS, 2)
                 if (zeros)
                     atomicOr(&s.vis_c[base >> 5], zeros); /* label 0 is final */
                 if (chgs && g.dst_ident)
-                    atomicOr(&nxt[base >> 5], chgs); /* d = k */
+                    set_word(base >> 5, chgs); /* d = k */
             }
         }
     }
     mass = warp_sum_u64(mass);
     edges = warp_sum_u64(edges);
     act = warp_sum_u64(act);
+    occ = warp_sum_u64(occ);
     if (lane == 0) {
         sh_cnt[wib][CNT_MASS] = mass;
         sh_cnt[wib][CNT_EDGES] = edges;
@@ -1952,13 +2038,14 @@ __global__ void __launch_bounds__(PULL_THREADS, 2)
         sh_cnt[wib][CNT_DEG0] = 0ull;
         sh_cnt[wib][CNT_DEG1] = 0ull;
         sh_cnt[wib][CNT_DEG2] = 0ull;
+        sh_cnt[wib][CNT_OCC] = occ;
     }
     __syncthreads();
     if (threadIdx.x < NCNT) {
         unsigned long long a = 0;
         for (int w = 0; w < WARPS; ++w)
             a += sh_cnt[w][threadIdx.x];
-        if (threadIdx.x >= CNT_DEG0)
+        if (threadIdx.x >= CNT_DEG0 && threadIdx.x <= CNT_DEG2)
             a = sh_deg[threadIdx.x - CNT_DEG0];
         block_cnt[NCNT * blockIdx.x + threadIdx.x] = a;
     }
@@ -1986,17 +2073,17 @@ __device__ void sched_features(const DevGraph& g, const Ctrl* c, uint32_t app, c
 {
     const float V = (float)(g.V ? g.V : 1), E = (float)(g.E ? g.E : 1);
     const float m = (float)cnt[CNT_MASS], act = (float)cnt[CNT_ACT];
-    const uint32_t tile_e = (app == WEDGE_APP_CC) ? 32u * PullEpl<WEDGE_APP_CC>::value
-                            : (app == WEDGE_APP_BFS) ? 32u * PullEpl<WEDGE_APP_BFS>::value
-                                                    : 32u * PullEpl<WEDGE_APP_SSSP>::value;
-    const float T = (float)((g.E + tile_e - 1) / tile_e) + 1.0f;
     const float a = act > 0.0f ? act : 1.0f;
     const float b0 = (float)cnt[CNT_DEG0], b1 = (float)cnt[CNT_DEG1], b2 = (float)cnt[CNT_DEG2];
     f[0] = log2f(1.0f + m) / 32.0f;         // out-edge mass of the activated vertices
     f[1] = m / E;
     f[2] = log2f(1.0f + act) / 32.0f;       // activated vertices
     f[3] = act / V;                         // frontier bitmap density
-    f[4] = (float)cnt[CNT_TILES] / T;       // tiles the last pull visited
+    // clustering of the changed bitmap: writes of distinct 32-vertex words
+    // (per warp group) against activated vertices; 1/2 when every activated
+    // vertex sits in a word of its own, near 0 when they fill whole words
+    const float occ = (float)cnt[CNT_OCC];
+    f[4] = occ > 0.0f ? occ / (occ + act) : 0.0f;
     f[5] = b0 / a;                          // out-degree histogram of the activated vertices
     f[6] = b1 / a;
     f[7] = b2 / a;
@@ -2445,8 +2532,11 @@ __global__ void init_kernel(DevGraph g, DevState s, uint32_t app, uint32_t topen
             if (s.cc_best)
                 s.cc_best[v] = NONE32;
         }
-        else
+        else {
             s.prop64[v] = (g.weight_kind == WEDGE_WEIGHTS_F64) ? 0x7FF0000000000000ull : NONE64; /* execution_sssp.c:78 */
+            if (s.dist32)
+                s.dist32[v] = NONE32;
+        }
     }
     const uint64_t nwords = (g.V + 31) / 32;
     for (uint64_t i = tid; i < nwords; i += stride) {
@@ -2535,12 +2625,17 @@ __global__ void init_root_kernel(DevGraph g, DevState s, uint32_t app, uint64_t 
         c->learned_iters = 0;
         c->pr_total = 0.0;
         c->pr_sum = 0.0;
+        c->probe_edges = s.probe_edges;
+        c->narrow_ovf = 0;
         if (app == WEDGE_APP_CC) {
             c->last_mass = g.E;
             c->mode = MODE_DENSE; /* first CC pull is always dense, execution_cc.c:103 */
         } else {
-            if (app == WEDGE_APP_SSSP)
+            if (app == WEDGE_APP_SSSP) {
                 s.prop64[root] = 0ull; /* 0.0 has the same bits */
+                if (s.dist32)
+                    s.dist32[root] = 0u;
+            }
             s.front0[root >> 5] |= 1u << (root & 31u);
             c->last_mass = g.outdeg[root];
             c->mode = choose_mode(sched, g.outdeg[root], thr);
@@ -3451,7 +3546,8 @@ static int setup_hub(wedge_graph* h, int app, int precision)
     WEDGE_CHECK(cudaFuncGetAttributes(&fa, fn));
     int optin = 0;
     WEDGE_CHECK(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, h->device));
-    const uint64_t elem = (app == WEDGE_APP_SSSP || (app == WEDGE_APP_PR && precision != WEDGE_PREC_FP32C)) ? 8 : 4;
+    const uint64_t elem = (app == WEDGE_APP_SSSP) ? (h->s.dist32 ? 4 : 8)
+                          : (app == WEDGE_APP_PR && precision != WEDGE_PREC_FP32C) ? 8 : 4;
     const uint64_t stage = (app == WEDGE_APP_SSSP && sssp_tiles512(h)) ? SSSP_STAGE_BYTES : 0u; /* after the cache */
     uint64_t avail = (uint64_t)optin > fa.sharedSizeBytes + stage + 64u ? (uint64_t)optin - fa.sharedSizeBytes - stage - 64u : 0u;
     const char* cap = getenv("WEDGE_HUB_BYTES");
@@ -3638,6 +3734,11 @@ static int ensure_state(wedge_graph* h, int app, int precision)
     WEDGE_CHECK(cudaMemset(bp, 0, sizeof(double) * (grid + slots * NCNT)));
     s.app = (uint32_t)app;
     s.push = (app == WEDGE_APP_SSSP && g.csri_pos) ? 1u : 0u;
+    {
+        const char* pe = getenv("WEDGE_PROBE_EDGES");
+        const unsigned long long w = pe ? strtoull(pe, nullptr, 10) : PROBE_EDGES;
+        s.probe_edges = (uint32_t)(w >= 1 && w <= 4096 ? w : PROBE_EDGES);
+    }
     if (app == WEDGE_APP_PR && precision == WEDGE_PREC_FP32C) {
         if ((rc = pr32_state(h)))
             return rc;
@@ -3652,6 +3753,11 @@ static int ensure_state(wedge_graph* h, int app, int precision)
     } else {
         if (app == WEDGE_APP_SSSP) {
             if ((rc = dalloc(h, &s.prop64, V, true)))
+                return rc;
+            // uint64 weights: the pulls gather a 32-bit copy of the distances
+            // (WEDGE_SSSP_NARROW=0: the 64-bit distances)
+            const char* nv = getenv("WEDGE_SSSP_NARROW");
+            if (g.weight_kind != WEDGE_WEIGHTS_F64 && !(nv && nv[0] == '0') && (rc = dalloc(h, &s.dist32, V, true)))
                 return rc;
         } else if ((rc = dalloc(h, &s.prop32, V, true))) {
             return rc;
@@ -4392,6 +4498,18 @@ __global__ void shard_decide_kernel(DevState s, unsigned long long mass, unsigne
         c->mode = mass > thr ? MODE_DENSE : MODE_WEDGE;
     }
 }
+
+// the 32-bit copy of SSSP distances a caller imported (dist32_put's rule)
+__global__ void narrow_copy_kernel(DevGraph g, DevState s)
+{
+    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+    for (uint64_t v = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; v < g.V; v += stride) {
+        const unsigned long long d = s.prop64[v];
+        s.dist32[v] = d < (unsigned long long)NONE32 ? (uint32_t)d : NONE32;
+        if (d >= (unsigned long long)NONE32 && d != NONE64)
+            atomicOr(&s.ctrl->narrow_ovf, 1u);
+    }
+}
 }  // namespace wedge
 
 extern "C" {
@@ -4419,9 +4537,14 @@ int wedge_cuda_shard_state(wedge_graph_t* g, int which, void* host, uint64_t byt
     }
     if (bytes < need)
         return WEDGE_ERR_ARG;
-    if (import)
+    if (import) {
         WEDGE_CHECK(cudaMemcpyAsync(dev, host, need, cudaMemcpyHostToDevice, g->stream));
-    else
+        if (which == WEDGE_SHARD_PROPS && g->s.dist32) {
+            narrow_copy_kernel<<<grid_for(g->g.V, AUX_THREADS, (uint32_t)g->num_sms * 8u), AUX_THREADS, 0, g->stream>>>(
+                g->g, g->s);
+            WEDGE_CHECK(cudaGetLastError());
+        }
+    } else
         WEDGE_CHECK(cudaMemcpyAsync(host, dev, need, cudaMemcpyDeviceToHost, g->stream));
     WEDGE_CHECK(cudaStreamSynchronize(g->stream));
     return WEDGE_OK;

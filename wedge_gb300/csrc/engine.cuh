@@ -46,9 +46,13 @@ constexpr uint32_t FULL = 0xFFFFFFFFu;
 enum : uint32_t { MODE_DENSE = 0, MODE_WEDGE = 1, MODE_FILTERED = 2 };
 
 // per-block counters written by the pulls (NCNT slots per block)
-constexpr uint32_t NCNT = 8;
+// CNT_OCC: writes of 32-vertex words of the pull's output bitmap, counted once
+// per distinct word of a warp's group (a word written by several warps counts
+// once per warp): how clustered the changed vertices are, the GPU form of the
+// reference's test of empty frontier groups (phase_edge_pull_bfs.c:244-246)
+constexpr uint32_t NCNT = 9;
 enum : uint32_t { CNT_MASS = 0, CNT_EDGES = 1, CNT_TILES = 2, CNT_DSTS = 3, CNT_ACT = 4, CNT_DEG0 = 5, CNT_DEG1 = 6,
-                  CNT_DEG2 = 7 };
+                  CNT_DEG2 = 7, CNT_OCC = 8 };
 // out-degree buckets of activated vertices (scheduler features): <= 4, <= 32, <= 256, more
 __host__ __device__ constexpr uint32_t degree_bucket(uint32_t d) { return d <= 4u ? 0u : d <= 32u ? 1u : d <= 256u ? 2u : 3u; }
 constexpr uint32_t LOG_CAP = 4096;  // iterations kept in the per-iteration log
@@ -99,6 +103,8 @@ struct Ctrl {
     unsigned int learned_iters;        // iterations whose mode the scheduler network chose
     unsigned int alist_n;              // vertices in the Wedge-build vertex list
     unsigned int pr_ticket;            // blocks of pr_total_kernel done (the last one resets it)
+    unsigned int probe_edges;          // BFS/CC probe window of the next pull (in-edges per destination)
+    unsigned int narrow_ovf;           // SSSP: a finite distance reached 2^32-1; pulls gather the 64-bit distances
     double pr_total;                   // sum of all accumulators (phase_vertex_pr.c:161); compensated FP32:
                                        // the total the next iteration uses
     double pr_prev;                    // compensated FP32: the total the last iteration used
@@ -136,6 +142,8 @@ struct DevGraph {
 struct DevState {
     uint32_t* prop32;              // BFS parent / CC label
     unsigned long long* prop64;    // SSSP distance (uint64 or double bits)
+    uint32_t* dist32;              // SSSP, uint64 weights: the distances narrowed to 32 bits (NONE32: unreached or
+                                   // >= 2^32-1), the array the pulls gather while Ctrl::narrow_ovf is 0; or null
     double* rank;                  // PageRank FP64: rank / outdegree'
     double* acc;                   // PageRank accumulators (graph_vertex_accumulators)
     double* inv_od;                // PageRank 1 / outdegree' (outdegree, or N for dangling vertices)
@@ -185,6 +193,7 @@ struct DevState {
     uint32_t hub_k;                // CC/SSSP: compressed destinations with ids < hub_n
     const float* net;              // scheduler network blob (WEDGE_SCHED_LEARNED), or null
     uint32_t push;                 // SSSP over in-edge positions: Wedge pulls relax the activated sources' out-edges
+    uint32_t probe_edges;          // default BFS/CC probe window
 };
 
 }  // namespace wedge

@@ -247,6 +247,24 @@ __device__ __forceinline__ uint32_t pos_dst(const TileGeo<EPL>& tg, int i)
     return tg.k0 + tg.before + __popc(tg.nib_inner & ((2u << i) - 1u));
 }
 
+// compressed destination owning in-edge position pos, from the destination-start
+// bitmap and the 128-edge tile index: the owner of the index tile's first edge
+// plus the destination starts after it
+__device__ __forceinline__ uint32_t dst_of_pos(const uint32_t* dst_start, const uint32_t* tile_dst0, uint32_t pos)
+{
+    const uint32_t t = pos >> 7, w0 = t << 2, wp = pos >> 5;
+    uint32_t n = 0;
+    for (uint32_t w = w0; w < wp; ++w)
+        n += __popc(dst_start[w]);
+    n += __popc(dst_start[wp] & ((pos & 31u) == 31u ? FULL : ((2u << (pos & 31u)) - 1u)));
+    return tile_dst0[t] + n - (dst_start[w0] & 1u); /* a start at the index tile's first edge is the owner's */
+}
+
+__device__ __forceinline__ uint32_t dst_of_pos(const DevGraph& g, uint32_t pos)
+{
+    return dst_of_pos(g.dst_start, g.tile_dst0, pos);
+}
+
 // (value, compensation) pair for the FP32 compensated PageRank sums
 struct F2 {
     float s, c;
