@@ -197,6 +197,10 @@ class Suite:
             "sssp": W.Graph.rmat(scale, ef, seed, weight_kind=W.WEIGHTS_U64),
             "pr": W.Graph.rmat(scale, ef, seed),
         }
+        # launch knobs from the engine autotuner's table where it was tuned on graphs of this size
+        from wedge_gb300 import autotune as A
+
+        self.knobs = {a: A.apply_engine_tuning(self.g[a], a, scale, ef) for a in APPS}
         self.V = self.g["bfs"].V
         self.E = {a: self.g[a].E for a in APPS}
         self.app = {"bfs": W.APP_BFS, "cc": W.APP_CC, "sssp": W.APP_SSSP, "pr": W.APP_PR}
@@ -382,22 +386,39 @@ def run_ours(args, dist: Dist):
     for a in APPS:
         suite.g[a].set_stream(shared.cuda_stream)
     e2e_steps = max(3, min(steps, 10))
+    checks = {a: 0 for a in APPS}
 
-    def e2e_step():
+    def consume(a):
+        checks[a] ^= int(host[a][V // 2])  # the host touches every step's results
+
+    def e2e_step(pipelined):
         for a in APPS:
+            if pipelined:
+                suite.g[a].wait_results()  # the previous step's results of a, while this step runs
+                consume(a)
             suite.g[a].run_async(suite.app[a], suite.params["plain"][a])
             suite.g[a].read_results_async(host[a])
-        for a in APPS:
-            suite.g[a].wait()
+        if not pipelined:
+            for a in APPS:
+                suite.g[a].wait()
+                consume(a)
 
-    e2e_step()
-    dist.barrier()
-    torch.cuda.synchronize()
-    t0 = time.perf_counter()
-    for _ in range(e2e_steps):
-        e2e_step()
-    e2e_wall = dist.max(time.perf_counter() - t0)
+    def e2e_run(pipelined):
+        e2e_step(False)
+        dist.barrier()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(e2e_steps):
+            e2e_step(pipelined)
+        if pipelined:
+            for a in APPS:
+                suite.g[a].wait()
+                consume(a)
+        return dist.max(time.perf_counter() - t0)
+
+    e2e_wall = e2e_run(True)
     e2e_value = dist.world * e2e_steps * suite.step_edges() / e2e_wall / 1e9
+    e2e_step_wait = dist.world * e2e_steps * suite.step_edges() / e2e_run(False) / 1e9
     # the same with the blocking calls (run, then read into the same page-locked memory)
     for a in APPS:
         suite.g[a].set_stream(None)
@@ -431,16 +452,23 @@ def run_ours(args, dist: Dist):
                    "vertices": V, "edges": suite.E["bfs"], "edges_sym": suite.E["cc"], "root": WORKLOAD["root"],
                    "threshold_pct": WORKLOAD["threshold_pct"], "pr_iterations": WORKLOAD["pr_iterations"],
                    "damping": WORKLOAD["damping"], "loop": args.mode,
+                   "knobs": {a: {k: suite.g[a].knob(k) for k in W.KNOB_NAMES} for a in APPS},
+                   "knobs_from": "wedge_gb300/data/engine_tuning.json" if any(suite.knobs.values()) else "defaults",
                    "l2": f"inputs larger than L2 (in-edge sources {4 * suite.E['bfs'] / 2**30:.1f} GiB / "
                          f"{4 * suite.E['cc'] / 2**30:.1f} GiB vs 126 MB L2); no flush",
                    "parallelism": "replicas" if dist.world > 1 else "single GPU"},
         "per_app": per_app,
         "e2e": {"value": round(e2e_value, 4), "unit": "GTEPS", "h2d_bytes_per_step": params_bytes,
                 "d2h_bytes_per_step": len(APPS) * 8 * V, "steps": e2e_steps,
-                "what": "per application wedge_cuda_run_async + wedge_cuda_read_results_async into page-locked host "
-                        "memory, then wedge_cuda_wait; the four handles share one stream (traversals in sequence, "
-                        "each export under the next traversal); graphs resident (loaded once, as the reference "
-                        "excludes load from Running Time)",
+                "what": "per application and step wedge_cuda_run_async + wedge_cuda_read_results_async into "
+                        "page-locked host memory; the four handles share one stream (traversals in sequence, each "
+                        "export under the next traversal); before queueing an application's next query the host "
+                        "waits for its previous results (wedge_cuda_wait_results) and reads them, so the last "
+                        "export of a step runs under the next step; every step's results reach the host inside "
+                        "the timed region (the last step's by wedge_cuda_wait); graphs resident (loaded once, as "
+                        "the reference excludes load from Running Time)",
+                "per_step_wait": {"value": round(e2e_step_wait, 4),
+                                  "what": "the same calls with wedge_cuda_wait on every handle at the end of each step"},
                 "blocking_calls": {"value": round(e2e_sync, 4),
                                    "what": "wedge_cuda_run + wedge_cuda_read_results, one after another"}},
         "roofline": {"bound": "hbm", "kernel": pr_roof["kernel"], "achieved": pr_roof["achieved"], "peak": peak,

@@ -237,12 +237,44 @@ int wedge_cuda_run_phase(wedge_graph_t* g, int app, int phase, const wedge_param
 int wedge_cuda_run_async(wedge_graph_t* g, int app, const wedge_params_t* params);
 int wedge_cuda_read_results_async(wedge_graph_t* g, void* host_props, uint64_t bytes);
 int wedge_cuda_wait(wedge_graph_t* g, wedge_stats_t* stats);
+/* Waits only for the last wedge_cuda_read_results_async of the handle: its
+ * host memory holds the results on return, while work queued after it (the
+ * next queries on a shared stream) keeps running.  A pipelined host waits here
+ * for query i's results after queueing query i+1.  Returns at once when no
+ * export is pending. */
+int wedge_cuda_wait_results(wedge_graph_t* g);
 
 /* Queues the handle's work on a caller's stream (a cudaStream_t; NULL restores
  * the handle's own), after the work already queued on the previous one has
  * finished.  Handles sharing a stream run in the order their work was queued;
  * the traversal loops are still captured on the handle's own stream. */
 int wedge_cuda_set_stream(wedge_graph_t* g, void* stream);
+
+/* ---------------------------------------------------------------- knobs */
+
+/* Launch parameters of the single-query engine, per handle (no counterpart in
+ * the reference, whose kernels have none).  wedge_gb300/autotune.py times
+ * them on a workload and stores the fastest per application; the Python layer
+ * applies that table.  A knob set to WEDGE_KNOB_DEFAULT takes its environment
+ * variable, else the built-in default.  Setting a knob releases the handle's
+ * traversal state (the next run rebuilds it); results of the last run are
+ * gone.  Out-of-range values return WEDGE_ERR_ARG. */
+enum wedge_knob {
+    WEDGE_KNOB_HUB_BYTES = 0,    /* shared-memory hub cache of the pulls, bytes: 0 (none) .. 196608, multiple
+                                    of 16 (WEDGE_HUB_BYTES; default 65536); the device's limit applies */
+    WEDGE_KNOB_PROBE_EDGES = 1,  /* BFS/CC per-destination probe window, in-edges: 1 .. 4096
+                                    (WEDGE_PROBE_EDGES; default 16) */
+    WEDGE_KNOB_SSSP_TILE = 2,    /* SSSP dense-pull tile, in-edges: 256 or 512 (WEDGE_SSSP_TILES512=1;
+                                    default 256); 512 needs byte-wide weights and in-edge positions */
+    WEDGE_KNOB_SSSP_NARROW = 3,  /* SSSP pulls gather a 32-bit copy of the distances: 1 or 0
+                                    (WEDGE_SSSP_NARROW; default 1) */
+    WEDGE_KNOBS = 4
+};
+#define WEDGE_KNOB_DEFAULT UINT64_MAX
+
+int wedge_cuda_set_knob(wedge_graph_t* g, int knob, uint64_t value);
+/* the value the next state build uses (after the environment and defaults) */
+int wedge_cuda_get_knob(wedge_graph_t* g, int knob, uint64_t* value);
 
 /* ---------------------------------------------------------------- shards */
 

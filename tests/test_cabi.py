@@ -54,6 +54,10 @@ def test_null_handles_are_rejected(engine_lib):
     assert L.wedge_cuda_read_results_async(None, None, 0) == -6
     assert L.wedge_cuda_wait(None, None) == -6
     assert L.wedge_cuda_set_stream(None, None) == -6
+    assert L.wedge_cuda_wait_results(None) == -6
+    assert L.wedge_cuda_set_knob(None, 0, 65536) == -6
+    v = C.c_uint64()
+    assert L.wedge_cuda_get_knob(None, 0, C.byref(v)) == -6
     assert L.wedge_cuda_num_vertices(None) == 0
     L.wedge_cuda_free(None)
 

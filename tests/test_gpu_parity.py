@@ -288,6 +288,19 @@ def test_async_runs_and_reads_match_sync(W, O):
         assert np.array_equal(host[2], want3)
         assert st1["iterations"] > 0 and st2["iterations"] == 5
         assert abs(st2["pr_sum"] - 1.0) < 1e-5
+        # pipelined: each query's results are waited for after the next query is queued
+        roots = [0, 3, 7, 0]
+        wants = {0: want0, 3: want3}
+        for i, r in enumerate(roots):
+            if i:
+                g1.wait_results()  # query i-1's results are in host[0]
+                if roots[i - 1] in wants:
+                    assert np.array_equal(host[0], wants[roots[i - 1]])
+            g1.run_async(W.APP_SSSP, W.Params(root=r))
+            g1.read_results_async(host[0])
+        g1.wait()
+        assert np.array_equal(host[0], want0)
+        g1.wait_results()  # nothing pending: returns at once
         g1.set_stream(None)
         with pytest.raises(W.WedgeError):  # asynchronous reads need page-locked memory
             g1.read_results_async(np.empty(V, np.uint64))
@@ -545,6 +558,51 @@ def test_wedge_pulls_over_chunk_ids(W, O, monkeypatch):
         assert st["wedge_iterations"] >= 1
         got, _, _ = run_engine(W, Vs, ss, ds, W.APP_CC, sched=sched)
         assert np.array_equal(got, cc_ref)
+
+
+KNOB_SETTINGS = [{"hub_bytes": 0}, {"hub_bytes": 98304}, {"probe_edges": 1}, {"probe_edges": 4096},
+                 {"sssp_tile": 512}, {"sssp_narrow": 0}, {"sssp_tile": 512, "sssp_narrow": 0, "hub_bytes": 16}]
+
+
+@pytest.mark.parametrize("knobs", KNOB_SETTINGS, ids=[",".join(f"{k}={v}" for k, v in x.items()) for x in KNOB_SETTINGS])
+def test_knobs_keep_results(W, O, knobs):
+    """every launch knob the autotuner may set gives the same results"""
+    V, s, d = graph_edges(O, "rmat", dict(scale=12, edge_factor=16, seed=12))
+    Vs, ss, ds = graph_edges(O, "rmat", dict(scale=12, edge_factor=16, seed=12), True)
+    w = O.weights(s, d)
+    sssp_ref, _, _ = O.Graph.from_edges(V, s, d, O.SSSP, w).run(root=0, threads=4)
+    cc_ref, _, _ = O.Graph.from_edges(Vs, ss, ds, O.CC).run(threads=4)
+    pr_ref, _, _ = O.Graph.from_edges(V, s, d, O.PR).run(iterations=8, damping=0.85, threads=4)
+    lv = bfs_levels(V, s, d, 0)
+    with W.Graph.from_edges(V, s, d, w, W.WEIGHTS_U64) as g, W.Graph.from_edges(Vs, ss, ds) as gs:
+        for k, v in knobs.items():
+            g.set_knob(k, v)
+            gs.set_knob(k, v)
+            assert g.knob(k) == v
+        for sched in (W.SCHED_PLAIN, W.SCHED_DENSE, W.SCHED_WEDGE):
+            g.run(W.APP_SSSP, W.Params(root=0, sched=sched))
+            assert np.array_equal(g.read_results(), sssp_ref)
+            g.run(W.APP_BFS, W.Params(root=0, sched=sched))
+            check_bfs(g.read_results(), V, s, d, 0, lv)
+            gs.run(W.APP_CC, W.Params(sched=sched))
+            assert np.array_equal(gs.read_results(), cc_ref)
+        g.run(W.APP_PR, W.Params(num_iterations=8, damping=0.85, precision=W.PREC_FP32C))
+        check_pr32(g.read_results(), pr_ref)
+
+
+def test_knob_values_are_checked(W, O):
+    V, s, d = graph_edges(O, "rmat", dict(scale=8, edge_factor=4, seed=11))
+    with W.Graph.from_edges(V, s, d) as g:
+        for k, v in (("hub_bytes", 17), ("hub_bytes", 1 << 20), ("probe_edges", 0), ("probe_edges", 4097),
+                     ("sssp_tile", 128), ("sssp_narrow", 2)):
+            with pytest.raises(W.WedgeError) as e:
+                g.set_knob(k, v)
+            assert e.value.status == W.ERR_ARG
+        assert g.knob("hub_bytes") == 65536 or os.environ.get("WEDGE_HUB_BYTES")
+        g.set_knob("probe_edges", 8)
+        assert g.knob("probe_edges") == 8
+        g.set_knob("probe_edges", None)
+        assert g.knob("probe_edges") == int(os.environ.get("WEDGE_PROBE_EDGES", "16"))
 
 
 def test_iteration_cap_reports_not_converged(W, O):

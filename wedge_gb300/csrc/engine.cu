@@ -45,6 +45,8 @@ int new_handle(wedge_graph** out)
     if (!h)
         return WEDGE_ERR_OOM;
     h->built_app = -1;
+    for (int k = 0; k < WEDGE_KNOBS; ++k)
+        h->knob[k] = WEDGE_KNOB_DEFAULT;
     h->last_app = -1;
     h->graph_app = -1;
     h->pend_app = -1;
@@ -723,7 +725,7 @@ __device__ __forceinline__ void tile_prefetch(const DevGraph& g, const DevState&
 // is requested once, with no reliance on L1 reuse.
 template <int EPL>
 __device__ __forceinline__ void load_sources(const DevGraph& g, uint64_t base, uint32_t cmask, int lane,
-                                             uint32_t (&sa)[EPL])
+                                             uint32_t (&sa)[EPL], unsigned long long pol)
 {
     const bool on = (cmask >> (((uint32_t)lane * EPL) >> 5)) & 1u;
     const uint32_t* p = g.src + base + (uint64_t)lane * EPL;
@@ -732,7 +734,7 @@ __device__ __forceinline__ void load_sources(const DevGraph& g, uint64_t base, u
         for (int q = 0; q < EPL / 8; ++q) {
             uint32_t x[8];
             if (on) {
-                ld_stream_v8(p + 8 * q, x);
+                ld_stream_v8_ef(p + 8 * q, x, pol);
             } else {
 #pragma unroll
                 for (int j = 0; j < 8; ++j)
@@ -965,7 +967,7 @@ __device__ __forceinline__ void sssp_push_pull(const DevGraph& g, const DevState
 }
 
 // BFS/CC probe: in-edges of an unfinished destination read before the tile pull
-// (the default of Ctrl::probe_edges; WEDGE_PROBE_EDGES overrides it)
+// (the default of Ctrl::probe_edges; the probe-window knob overrides it)
 constexpr uint32_t PROBE_EDGES = 16;
 
 // Edge pull over all tiles (dense) or over the tiles of the Wedge frontier.
@@ -1003,6 +1005,8 @@ __global__ void __launch_bounds__(PULL_THREADS, 1)
         sssp_push_pull(g, s, c, block_cnt);
         return;
     }
+    /* the in-edge stream is read once per pull: it should not push the gathered array out of L2 */
+    const unsigned long long pol = l2_evict_first_policy();
     const int lane = threadIdx.x & 31;
     const int wib = threadIdx.x >> 5;
     const uint32_t gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
@@ -1097,7 +1101,7 @@ __global__ void __launch_bounds__(PULL_THREADS, 1)
         const uint64_t base = (uint64_t)t * TILE_E;
         const bool last_tile = (t + 1u >= T);
         uint32_t sa[EPL];
-        load_sources<EPL>(g, base, in.cmask, lane, sa);
+        load_sources<EPL>(g, base, in.cmask, lane, sa, pol);
 #pragma unroll
         for (int q = 0; q < EPL; ++q)
             edges += (sa[q] != NONE32) ? 1u : 0u;
@@ -1226,7 +1230,8 @@ __global__ void __launch_bounds__(PULL_THREADS, 1)
             if (g.w8) { /* byte-wide weights: EPL bytes per lane (SSSP's EPL is a multiple of 8) */
 #pragma unroll
                 for (int q = 0; q < EPL / 8; ++q) {
-                    const unsigned long long x = on ? ld_stream_u64(g.w8 + base + (uint64_t)lane * EPL + 8 * q) : 0ull;
+                    const unsigned long long x =
+                        on ? ld_stream_u64_ef(g.w8 + base + (uint64_t)lane * EPL + 8 * q, pol) : 0ull;
 #pragma unroll
                     for (int j = 0; j < 8; ++j)
                         wv[8 * q + j] = (x >> (8 * j)) & 0xFFull;
@@ -1237,7 +1242,7 @@ __global__ void __launch_bounds__(PULL_THREADS, 1)
                 for (int q = 0; q < EPL / 4; ++q) {
                     unsigned long long x[4] = {0ull, 0ull, 0ull, 0ull};
                     if (on)
-                        ld_stream_v4u64(wp + 4 * q, x);
+                        ld_stream_v4u64_ef(wp + 4 * q, x, pol);
 #pragma unroll
                     for (int j = 0; j < 4; ++j)
                         wv[4 * q + j] = x[j];
@@ -1268,7 +1273,12 @@ __global__ void __launch_bounds__(PULL_THREADS, 1)
             for (uint32_t slot = (uint32_t)lane; slot < min(tg.ndst, TAB); slot += 32u) {
                 const uint32_t vtx = g.dst_ident ? tg.k0 + slot : g.dst_id[tg.k0 + slot];
                 my_id[slot] = vtx;
-                my_cur[slot] = s.prop64[vtx];
+                if (narrow) { /* exact while no distance reached 2^32-1 (dist32_put) */
+                    const uint32_t x = s.dist32[vtx];
+                    my_cur[slot] = (x == NONE32) ? NONE64 : (unsigned long long)x;
+                } else {
+                    my_cur[slot] = s.prop64[vtx];
+                }
             }
             __syncwarp();
             seg_reduce<EPL>(v, tg, lane, MinU64(), [&](uint32_t k, unsigned long long val, int kind) {
@@ -1402,6 +1412,7 @@ __global__ void __launch_bounds__(PULL_THREADS, 1)
     const bool filtered = mode == MODE_FILTERED;
     const uint32_t hub_bytes = s.hub_bytes;
     const bool narrow = s.dist32 && !c->narrow_ovf; /* gathers from the 32-bit copy */
+    const unsigned long long pol = l2_evict_first_policy(); /* for the in-edge and weight streams */
     const unsigned char* hub_src = narrow ? reinterpret_cast<const unsigned char*>(s.dist32)
                                           : reinterpret_cast<const unsigned char*>(s.prop64);
     uint32_t* hub32 = reinterpret_cast<uint32_t*>(sssp_smem);
@@ -1470,16 +1481,16 @@ __global__ void __launch_bounds__(PULL_THREADS, 1)
         {
             const uint32_t* p = g.src + base + (uint64_t)lane * EPL;
             uint32_t x[8];
-            ld_stream_v8(p, x);
+            ld_stream_v8_ef(p, x, pol);
 #pragma unroll
             for (int j = 0; j < 8; ++j)
                 sa[j] = x[j];
-            ld_stream_v8(p + 8, x);
+            ld_stream_v8_ef(p + 8, x, pol);
 #pragma unroll
             for (int j = 0; j < 8; ++j)
                 sa[8 + j] = x[j];
         }
-        const uint4 wq = __ldg(reinterpret_cast<const uint4*>(g.w8 + base + (uint64_t)lane * EPL));
+        const uint4 wq = ld_stream_v4u32_ef(g.w8 + base + (uint64_t)lane * EPL, pol);
         const uint32_t wword[4] = {wq.x, wq.y, wq.z, wq.w};
         unsigned long long v[EPL];
 #pragma unroll
@@ -3490,13 +3501,64 @@ int compute_grids(wedge_graph* h)
 // launches + two tile launches)
 static uint64_t counter_slots(const wedge_graph* h) { return 2ull * h->dst_grid + 2ull * h->pull_grid; }
 
-// SSSP runs sssp_pull_kernel where the graph has byte-wide weights and the
-// Wedge pulls relax over in-edge positions, else pull_kernel
+// Launch knobs: the value set on the handle, else its environment variable,
+// else the default.  Values outside a knob's range read as unset.
+static bool knob_ok(int k, uint64_t v)
+{
+    switch (k) {
+    case WEDGE_KNOB_HUB_BYTES:
+        return v <= 196608u && v % 16u == 0u;
+    case WEDGE_KNOB_PROBE_EDGES:
+        return v >= 1u && v <= 4096u;
+    case WEDGE_KNOB_SSSP_TILE:
+        return v == 256u || v == 512u;
+    case WEDGE_KNOB_SSSP_NARROW:
+        return v <= 1u;
+    default:
+        return false;
+    }
+}
+
+constexpr uint64_t HUB_BYTES_DEFAULT = 65536;
+
+static uint64_t knob_value(const wedge_graph* h, int k)
+{
+    static const uint64_t defaults[WEDGE_KNOBS] = {HUB_BYTES_DEFAULT, PROBE_EDGES, 256u, 1u};
+    if (h->knob[k] != WEDGE_KNOB_DEFAULT)
+        return h->knob[k];
+    const char* e = nullptr;
+    uint64_t v = 0;
+    switch (k) {
+    case WEDGE_KNOB_HUB_BYTES:
+        e = getenv("WEDGE_HUB_BYTES");
+        break;
+    case WEDGE_KNOB_PROBE_EDGES:
+        e = getenv("WEDGE_PROBE_EDGES");
+        break;
+    case WEDGE_KNOB_SSSP_TILE: {
+        const char* t = getenv("WEDGE_SSSP_TILES512");
+        return (t && t[0] == '1') ? 512u : defaults[k];
+    }
+    case WEDGE_KNOB_SSSP_NARROW:
+        e = getenv("WEDGE_SSSP_NARROW");
+        break;
+    default:
+        return 0;
+    }
+    if (!e || !*e)
+        return defaults[k];
+    char* end = nullptr;
+    v = strtoull(e, &end, 10);
+    return (end && *end == '\0' && knob_ok(k, v)) ? v : defaults[k];
+}
+
+// SSSP runs sssp_pull_kernel (512-edge tiles) where the knob asks for it and
+// the graph has byte-wide weights and in-edge positions, else pull_kernel
+// (256-edge tiles; 20.6 against 23.2 ms per SSSP at R-MAT scale 26 with
+// 64-bit distance gathers)
 static bool sssp_tiles512(const wedge_graph* h)
 {
-    // measured slower at R-MAT scale 26 (20.6 -> 23.2 ms per SSSP): off unless WEDGE_SSSP_TILES512=1
-    const char* e = getenv("WEDGE_SSSP_TILES512");
-    return h->s.push && h->g.w8 && e && e[0] == '1';
+    return h->s.push && h->g.w8 && knob_value(h, WEDGE_KNOB_SSSP_TILE) == 512u;
 }
 
 static const void* pull_fn(const wedge_graph* h, int app)
@@ -3533,11 +3595,10 @@ static uint32_t pull_tile_e(const wedge_graph* h, int app)
 
 // Size the hub cache of an application's pull, in whole 16-byte lines of the
 // gathered array (frontier words for BFS, one property per vertex otherwise):
-// HUB_BYTES_DEFAULT, or WEDGE_HUB_BYTES (0 turns the cache off), within the
-// shared memory a block can opt into beside the kernel's static tables.  The
-// cache comes out of the SM's L1: on R-MAT scale 24 a 64 KB cache beat both no
-// cache and the largest one, whose small L1 left too few gather misses in flight.
-constexpr uint64_t HUB_BYTES_DEFAULT = 65536;
+// the hub-cache knob (0 turns the cache off), within the shared memory a block
+// can opt into beside the kernel's static tables.  The cache comes out of the
+// SM's L1: on R-MAT scale 24 a 64 KB cache beat both no cache and the largest
+// one, whose small L1 left too few gather misses in flight.
 
 static int setup_hub(wedge_graph* h, int app, int precision)
 {
@@ -3550,8 +3611,7 @@ static int setup_hub(wedge_graph* h, int app, int precision)
                           : (app == WEDGE_APP_PR && precision != WEDGE_PREC_FP32C) ? 8 : 4;
     const uint64_t stage = (app == WEDGE_APP_SSSP && sssp_tiles512(h)) ? SSSP_STAGE_BYTES : 0u; /* after the cache */
     uint64_t avail = (uint64_t)optin > fa.sharedSizeBytes + stage + 64u ? (uint64_t)optin - fa.sharedSizeBytes - stage - 64u : 0u;
-    const char* cap = getenv("WEDGE_HUB_BYTES");
-    const uint64_t want = cap ? strtoull(cap, nullptr, 10) : HUB_BYTES_DEFAULT;
+    const uint64_t want = knob_value(h, WEDGE_KNOB_HUB_BYTES);
     if (want < avail)
         avail = want;
     const uint64_t have = (app == WEDGE_APP_BFS) ? (h->g.V + 31) / 32 : h->g.V;
@@ -3582,7 +3642,7 @@ static int setup_hub(wedge_graph* h, int app, int precision)
 // dynamic shared memory of pr32_pull_kernel beyond its hub cache: the staged sums
 constexpr uint32_t PR32_STAGE_BYTES = (PULL_THREADS / 32) * PR32_SLOTS * sizeof(float);
 
-// hub cache of the compensated-FP32 pull: HUB_BYTES_DEFAULT (or WEDGE_HUB_BYTES)
+// hub cache of the compensated-FP32 pull: the hub-cache knob's bytes
 // of the rank array, within what the block can opt into beside the staged sums
 static int pr32_setup_hub(wedge_graph* h)
 {
@@ -3594,8 +3654,7 @@ static int pr32_setup_hub(wedge_graph* h)
     if ((uint64_t)optin < fixed)
         return WEDGE_ERR_UNSUPPORTED;
     uint64_t avail = (uint64_t)optin - fixed;
-    const char* cap = getenv("WEDGE_HUB_BYTES");
-    const uint64_t want = cap ? strtoull(cap, nullptr, 10) : HUB_BYTES_DEFAULT;
+    const uint64_t want = knob_value(h, WEDGE_KNOB_HUB_BYTES);
     if (want < avail)
         avail = want;
     uint64_t n = avail / 4u;
@@ -3734,11 +3793,7 @@ static int ensure_state(wedge_graph* h, int app, int precision)
     WEDGE_CHECK(cudaMemset(bp, 0, sizeof(double) * (grid + slots * NCNT)));
     s.app = (uint32_t)app;
     s.push = (app == WEDGE_APP_SSSP && g.csri_pos) ? 1u : 0u;
-    {
-        const char* pe = getenv("WEDGE_PROBE_EDGES");
-        const unsigned long long w = pe ? strtoull(pe, nullptr, 10) : PROBE_EDGES;
-        s.probe_edges = (uint32_t)(w >= 1 && w <= 4096 ? w : PROBE_EDGES);
-    }
+    s.probe_edges = (uint32_t)knob_value(h, WEDGE_KNOB_PROBE_EDGES);
     if (app == WEDGE_APP_PR && precision == WEDGE_PREC_FP32C) {
         if ((rc = pr32_state(h)))
             return rc;
@@ -3755,9 +3810,9 @@ static int ensure_state(wedge_graph* h, int app, int precision)
             if ((rc = dalloc(h, &s.prop64, V, true)))
                 return rc;
             // uint64 weights: the pulls gather a 32-bit copy of the distances
-            // (WEDGE_SSSP_NARROW=0: the 64-bit distances)
-            const char* nv = getenv("WEDGE_SSSP_NARROW");
-            if (g.weight_kind != WEDGE_WEIGHTS_F64 && !(nv && nv[0] == '0') && (rc = dalloc(h, &s.dist32, V, true)))
+            // (knob WEDGE_KNOB_SSSP_NARROW = 0: the 64-bit distances)
+            if (g.weight_kind != WEDGE_WEIGHTS_F64 && knob_value(h, WEDGE_KNOB_SSSP_NARROW) &&
+                (rc = dalloc(h, &s.dist32, V, true)))
                 return rc;
         } else if ((rc = dalloc(h, &s.prop32, V, true))) {
             return rc;
@@ -4458,6 +4513,18 @@ int wedge_cuda_wait(wedge_graph_t* g, wedge_stats_t* stats)
     return rc;
 }
 
+int wedge_cuda_wait_results(wedge_graph_t* g)
+{
+    if (!g)
+        return WEDGE_ERR_ARG;
+    WEDGE_CHECK(cudaSetDevice(g->device));
+    if (g->x_pending) {
+        WEDGE_CHECK(cudaEventSynchronize(g->ev_x));
+        g->x_pending = 0;
+    }
+    return WEDGE_OK;
+}
+
 int wedge_cuda_set_stream(wedge_graph_t* g, void* stream)
 {
     if (!g)
@@ -4465,6 +4532,31 @@ int wedge_cuda_set_stream(wedge_graph_t* g, void* stream)
     WEDGE_CHECK(cudaSetDevice(g->device));
     WEDGE_CHECK(cudaStreamSynchronize(g->stream)); /* the handle's queued work finishes on its old stream */
     g->stream = stream ? (cudaStream_t)stream : g->own_stream;
+    return WEDGE_OK;
+}
+
+int wedge_cuda_set_knob(wedge_graph_t* g, int knob, uint64_t value)
+{
+    if (!g || knob < 0 || knob >= WEDGE_KNOBS || (value != WEDGE_KNOB_DEFAULT && !knob_ok(knob, value)))
+        return WEDGE_ERR_ARG;
+    WEDGE_CHECK(cudaSetDevice(g->device));
+    if (g->knob[knob] == value)
+        return WEDGE_OK;
+    WEDGE_CHECK(cudaStreamSynchronize(g->stream)); /* no queued work may use the state released here */
+    if (g->xstream)
+        WEDGE_CHECK(cudaStreamSynchronize(g->xstream));
+    g->x_pending = 0;
+    g->knob[knob] = value;
+    free_state(g);
+    g->last_app = -1;
+    return WEDGE_OK;
+}
+
+int wedge_cuda_get_knob(wedge_graph_t* g, int knob, uint64_t* value)
+{
+    if (!g || !value || knob < 0 || knob >= WEDGE_KNOBS)
+        return WEDGE_ERR_ARG;
+    *value = knob_value(g, knob);
     return WEDGE_OK;
 }
 

@@ -240,6 +240,7 @@ struct wedge_graph {
     int graph_app;
     int graph_key;
     int cc_pending;                    // CC labels are engine ids (symmetric graph, not yet converted)
+    uint64_t knob[WEDGE_KNOBS];        // wedge_cuda_set_knob values (WEDGE_KNOB_DEFAULT: environment, else default)
 };
 
 namespace wedge {

@@ -57,6 +57,31 @@ __device__ __forceinline__ unsigned long long ld_stream_u64(const void* p)
     return r;
 }
 
+// evict-first forms of the streaming loads (weights beside the in-edge sources)
+__device__ __forceinline__ unsigned long long ld_stream_u64_ef(const void* p, unsigned long long pol)
+{
+    unsigned long long r;
+    asm volatile("ld.global.nc.L1::no_allocate.L2::cache_hint.u64 %0, [%1], %2;" : "=l"(r) : "l"(p), "l"(pol));
+    return r;
+}
+
+__device__ __forceinline__ void ld_stream_v4u64_ef(const unsigned long long* p, unsigned long long (&r)[4],
+                                                   unsigned long long pol)
+{
+    asm volatile("ld.global.nc.L1::no_allocate.L2::cache_hint.v4.u64 {%0,%1,%2,%3}, [%4], %5;"
+                 : "=l"(r[0]), "=l"(r[1]), "=l"(r[2]), "=l"(r[3])
+                 : "l"(p), "l"(pol));
+}
+
+__device__ __forceinline__ uint4 ld_stream_v4u32_ef(const void* p, unsigned long long pol)
+{
+    uint4 r;
+    asm volatile("ld.global.nc.L1::no_allocate.L2::cache_hint.v4.u32 {%0,%1,%2,%3}, [%4], %5;"
+                 : "=r"(r.x), "=r"(r.y), "=r"(r.z), "=r"(r.w)
+                 : "l"(p), "l"(pol));
+    return r;
+}
+
 /* ---- hub cache: a bulk (TMA) copy of the low-id end of the gathered array
  * into shared memory, completed on an mbarrier.  Vertices are relabelled by
  * descending out-degree, so ids [0, hub_n) are the sources most in-edges

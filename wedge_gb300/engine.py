@@ -33,6 +33,11 @@ SCHED_BLOB = SCHED_PARAM_OFFSET + SCHED_PARAMS + 1
 PHASE_INIT, PHASE_PULL_DENSE, PHASE_PULL_WEDGE, PHASE_VERTEX_PR, PHASE_WEDGE_BUILD, PHASE_ADVANCE = range(6)
 FLAG_GRAPH, FLAG_TIMING = 1, 2
 SHARD_PROPS, SHARD_FRONTIER = 0, 1
+# launch knobs (enum wedge_knob); KNOB_DEFAULT: the environment variable, else the built-in default
+KNOB_HUB_BYTES, KNOB_PROBE_EDGES, KNOB_SSSP_TILE, KNOB_SSSP_NARROW = 0, 1, 2, 3
+KNOB_NAMES = {"hub_bytes": KNOB_HUB_BYTES, "probe_edges": KNOB_PROBE_EDGES, "sssp_tile": KNOB_SSSP_TILE,
+              "sssp_narrow": KNOB_SSSP_NARROW}
+KNOB_DEFAULT = (1 << 64) - 1
 
 OK = 0
 ERR_IO, ERR_FORMAT, ERR_OOM, ERR_CUDA, ERR_NOT_CONVERGED, ERR_ARG, ERR_UNSUPPORTED = -1, -2, -3, -4, -5, -6, -7
@@ -137,6 +142,9 @@ _SIGNATURES = {
     "wedge_cuda_read_results_async": (C.c_int, [C.c_void_p, C.c_void_p, C.c_uint64]),
     "wedge_cuda_wait": (C.c_int, [C.c_void_p, C.POINTER(Stats)]),
     "wedge_cuda_set_stream": (C.c_int, [C.c_void_p, C.c_void_p]),
+    "wedge_cuda_wait_results": (C.c_int, [C.c_void_p]),
+    "wedge_cuda_set_knob": (C.c_int, [C.c_void_p, C.c_int, C.c_uint64]),
+    "wedge_cuda_get_knob": (C.c_int, [C.c_void_p, C.c_int, C.POINTER(C.c_uint64)]),
     "wedge_cuda_load_shard": (C.c_int, [C.c_uint64, C.c_uint64, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int,
                                         C.c_void_p, C.c_uint64, C.POINTER(C.c_void_p)]),
     "wedge_cuda_shard_state": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_uint64, C.c_int]),
@@ -316,9 +324,27 @@ class Graph:
         d["status"] = rc
         return d
 
+    def wait_results(self):
+        """wait only for the last asynchronous read (work queued after it keeps running)"""
+        _check(lib().wedge_cuda_wait_results(self._h), "wedge_cuda_wait_results")
+
     def set_stream(self, stream: int | None):
         """queue this handle's work on a caller's CUDA stream (its handle as an int; None: its own)"""
         _check(lib().wedge_cuda_set_stream(self._h, C.c_void_p(stream) if stream else None), "wedge_cuda_set_stream")
+
+    def set_knob(self, knob: int | str, value: int | None):
+        """set a launch knob (KNOB_* or its name in KNOB_NAMES); None: back to the default.
+        The handle's traversal state is released and rebuilt by the next run."""
+        k = KNOB_NAMES[knob] if isinstance(knob, str) else knob
+        _check(lib().wedge_cuda_set_knob(self._h, k, KNOB_DEFAULT if value is None else int(value)),
+               "wedge_cuda_set_knob")
+
+    def knob(self, knob: int | str) -> int:
+        """the value of a launch knob the next state build uses"""
+        k = KNOB_NAMES[knob] if isinstance(knob, str) else knob
+        v = C.c_uint64()
+        _check(lib().wedge_cuda_get_knob(self._h, k, C.byref(v)), "wedge_cuda_get_knob")
+        return int(v.value)
 
     def shard_state(self, which: int, out: np.ndarray, import_: bool = False):
         """a shard's properties or pulled frontier, to (import_ False) or from host memory"""
