@@ -103,6 +103,7 @@ def test_sssp_grid4096(W, O, kind):
 
 
 def test_rmat26_all_apps(W, O):
+    from wedge_gb300 import autotune as A
     from wedge_gb300 import scheduler as S
 
     blob = S.load()
@@ -120,6 +121,14 @@ def test_rmat26_all_apps(W, O):
             assert np.array_equal(g.read_results(), sssp_ref)
             g.run(W.APP_BFS, W.Params(root=0, sched=sched, flags=W.FLAG_GRAPH))
             check_bfs_sorted(g.read_results(), V, s, d, 0, levels)
+        # the launch knobs the benchmark runs with (the engine autotuner's table)
+        assert A.apply_engine_tuning(g, "sssp", 26, 16)
+        g.run(W.APP_SSSP, W.Params(root=0, flags=W.FLAG_GRAPH))
+        assert np.array_equal(g.read_results(), sssp_ref)
+        A.apply_engine_tuning(g, "bfs", 26, 16)
+        g.run(W.APP_BFS, W.Params(root=0, flags=W.FLAG_GRAPH))
+        check_bfs_sorted(g.read_results(), V, s, d, 0, levels)
+        A.apply_engine_tuning(g, "pr", 26, 16)
         g.run(W.APP_PR, W.Params(num_iterations=30, damping=0.85, precision=W.PREC_FP32C, flags=W.FLAG_GRAPH))
         pr32 = g.read_results().view(np.float64).copy()
     del sssp_ref
@@ -134,3 +143,6 @@ def test_rmat26_all_apps(W, O):
         for sched in (W.SCHED_PLAIN, W.SCHED_LEARNED):
             g.run(W.APP_CC, W.Params(sched=sched, flags=W.FLAG_GRAPH))
             assert np.array_equal(g.read_results(), cc_ref)
+        A.apply_engine_tuning(g, "cc", 26, 16)
+        g.run(W.APP_CC, W.Params(flags=W.FLAG_GRAPH))
+        assert np.array_equal(g.read_results(), cc_ref)

@@ -597,7 +597,7 @@ def test_knob_values_are_checked(W, O):
                      ("sssp_tile", 128), ("sssp_narrow", 2)):
             with pytest.raises(W.WedgeError) as e:
                 g.set_knob(k, v)
-            assert e.value.status == W.ERR_ARG
+            assert e.value.status == -6  # WEDGE_ERR_ARG
         assert g.knob("hub_bytes") == 65536 or os.environ.get("WEDGE_HUB_BYTES")
         g.set_knob("probe_edges", 8)
         assert g.knob("probe_edges") == 8

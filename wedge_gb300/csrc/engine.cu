@@ -1434,6 +1434,15 @@ __global__ void __launch_bounds__(PULL_THREADS, 1)
         __syncthreads();
     }
     uint32_t hub_lim = 0;
+    // a destination's distance before this launch (the 32-bit copy is exact
+    // while no distance reached 2^32-1)
+    auto cur_dist = [&](uint32_t vtx) -> unsigned long long {
+        if (narrow) {
+            const uint32_t x = s.dist32[vtx];
+            return x == NONE32 ? NONE64 : (unsigned long long)x;
+        }
+        return s.prop64[vtx];
+    };
     auto hub_min = [&](uint32_t vtx, unsigned long long val) {
         if (vtx >= hub_lim)
             return;
@@ -1492,6 +1501,16 @@ __global__ void __launch_bounds__(PULL_THREADS, 1)
         }
         const uint4 wq = ld_stream_v4u32_ef(g.w8 + base + (uint64_t)lane * EPL, pol);
         const uint32_t wword[4] = {wq.x, wq.y, wq.z, wq.w};
+        // the tile's first 32 destinations: id, current distance and out-degree,
+        // loaded now so that their latency overlaps the gathers'
+        const uint32_t npre = min(min(kend, g.Vne - 1u) - k0 + 1u, 32u);
+        uint32_t pre_vtx = 0u, pre_od = 0u;
+        unsigned long long pre_cur = NONE64;
+        if ((uint32_t)lane < npre) {
+            pre_vtx = g.dst_ident ? k0 + (uint32_t)lane : g.dst_id[k0 + (uint32_t)lane];
+            pre_cur = cur_dist(pre_vtx);
+            pre_od = g.outdeg[pre_vtx];
+        }
         unsigned long long v[EPL];
 #pragma unroll
         for (int q = 0; q < EPL; ++q) {
@@ -1543,17 +1562,42 @@ __global__ void __launch_bounds__(PULL_THREADS, 1)
         const uint32_t nd = tg.ndst;
         const uint32_t jlo = tg.k0_fresh ? 0u : 1u;
         const uint32_t jhi = min(tg.tail_cont ? nd - 1u : nd, SSSP_SLOTS);
-        for (uint32_t j = jlo + (uint32_t)lane; j < jhi; j += 32u) {
-            const unsigned long long val = my_min[j];
-            if (val == NONE64)
-                continue;
-            const uint32_t k = tg.k0 + j;
-            const uint32_t vtx = g.dst_ident ? k : g.dst_id[k];
-            if (val < s.prop64[vtx]) { /* the destination's only writer in this launch */
-                s.prop64[vtx] = val;
-                dist32_put(s, vtx, val, true);
-                hub_min(vtx, val);
-                activate(vtx);
+        // the staged complete destinations, 32 consecutive ones per round; each
+        // is this launch's only writer of its vertex, so its frontier bit is
+        // new: the bits of a round go out as one atomicOr per distinct word
+        for (uint32_t j0 = 0; j0 < jhi; j0 += 32u) { /* warp-uniform rounds */
+            const uint32_t j = j0 + (uint32_t)lane;
+            const unsigned long long val = (j >= jlo && j < jhi) ? my_min[j] : NONE64;
+            bool chg = false;
+            uint32_t vtx = 0u, od = 0u;
+            if (val != NONE64) {
+                const bool pre = j0 == 0u && (uint32_t)lane < npre;
+                vtx = pre ? pre_vtx : (g.dst_ident ? tg.k0 + j : g.dst_id[tg.k0 + j]);
+                if (val < (pre ? pre_cur : cur_dist(vtx))) {
+                    chg = true;
+                    s.prop64[vtx] = val;
+                    dist32_put(s, vtx, val, true);
+                    hub_min(vtx, val);
+                    od = pre ? pre_od : g.outdeg[vtx];
+                }
+            }
+            const uint32_t word = chg ? vtx >> 5 : NONE32;
+            const uint32_t grp = __match_any_sync(FULL, word);
+            const uint32_t bits = __reduce_or_sync(grp, chg ? 1u << (vtx & 31u) : 0u);
+            if (chg && (uint32_t)lane == (uint32_t)(__ffs(grp) - 1)) {
+                atomicOr(&nxt[word], bits);
+                ++occ; /* a distinct word of this round */
+            }
+            if (chg) {
+                mass += od;
+                ++act;
+            }
+            const uint32_t bk = chg ? degree_bucket(od) : 3u;
+#pragma unroll
+            for (uint32_t b = 0; b < 3u; ++b) {
+                const uint32_t n = __popc(__ballot_sync(FULL, bk == b));
+                if (lane == 0 && n)
+                    atomicAdd(&sh_deg[b], n);
             }
         }
         __syncwarp(); /* my_min is rewritten by the next tile */
