@@ -266,7 +266,9 @@ enum wedge_knob {
                                     (WEDGE_PROBE_EDGES; default 16) */
     WEDGE_KNOB_SSSP_TILE = 2,    /* SSSP dense-pull tile, in-edges: 256 or 512 (WEDGE_SSSP_TILES512=1;
                                     default 256); 512 needs byte-wide weights and in-edge positions */
-    WEDGE_KNOB_SSSP_NARROW = 3,  /* SSSP pulls gather a 32-bit copy of the distances: 1 or 0
+    WEDGE_KNOB_SSSP_NARROW = 3,  /* SSSP pulls gather a 32-bit copy of the distances (uint64 weights): 1, or
+                                    0 (none), or a limit 2 .. 2^32-2 below which distances stay in 32 bits
+                                    (the default limit is 2^32-1; lower ones test the switch to 64 bits)
                                     (WEDGE_SSSP_NARROW; default 1) */
     WEDGE_KNOBS = 4
 };

@@ -560,8 +560,12 @@ def test_wedge_pulls_over_chunk_ids(W, O, monkeypatch):
         assert np.array_equal(got, cc_ref)
 
 
+# sssp_narrow above 1: a limit of the 32-bit distance copy low enough that the
+# traversals cross it, switching to 64-bit distances mid-way (the 512-edge pull
+# drops its 32-bit sums at the limit and redoes the pull in 64 bits)
 KNOB_SETTINGS = [{"hub_bytes": 0}, {"hub_bytes": 98304}, {"probe_edges": 1}, {"probe_edges": 4096},
-                 {"sssp_tile": 512}, {"sssp_narrow": 0}, {"sssp_tile": 512, "sssp_narrow": 0, "hub_bytes": 16}]
+                 {"sssp_tile": 512}, {"sssp_narrow": 0}, {"sssp_tile": 512, "sssp_narrow": 0, "hub_bytes": 16},
+                 {"sssp_narrow": 40}, {"sssp_tile": 512, "sssp_narrow": 40}, {"sssp_tile": 512, "sssp_narrow": 150}]
 
 
 @pytest.mark.parametrize("knobs", KNOB_SETTINGS, ids=[",".join(f"{k}={v}" for k, v in x.items()) for x in KNOB_SETTINGS])
@@ -594,7 +598,7 @@ def test_knob_values_are_checked(W, O):
     V, s, d = graph_edges(O, "rmat", dict(scale=8, edge_factor=4, seed=11))
     with W.Graph.from_edges(V, s, d) as g:
         for k, v in (("hub_bytes", 17), ("hub_bytes", 1 << 20), ("probe_edges", 0), ("probe_edges", 4097),
-                     ("sssp_tile", 128), ("sssp_narrow", 2)):
+                     ("sssp_tile", 128), ("sssp_narrow", 2**32 - 1)):
             with pytest.raises(W.WedgeError) as e:
                 g.set_knob(k, v)
             assert e.value.status == -6  # WEDGE_ERR_ARG

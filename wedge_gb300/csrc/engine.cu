@@ -847,16 +847,18 @@ __host__ __device__ constexpr uint32_t dst_launches_of(int app)
 }
 
 // SSSP narrow distances: a distance write, recorded in the 32-bit copy the
-// pulls gather (4 bytes per gather instead of 8).  Distances only decrease, so
-// a copy saturated at NONE32 is never below the distance; a finite distance
-// that does not fit sets Ctrl::narrow_ovf, after which the pulls gather the
-// 64-bit distances from their next launch on (a source a pull skipped as
-// unreached meanwhile changed in this iteration: the next pull relaxes it).
+// pulls gather (4 bytes per gather instead of 8).  The copy holds distances
+// below narrow_lim (2^32-1, or a smaller limit that tests set), NONE32 for the
+// others; distances only decrease, so the copy is never below the distance.
+// A finite distance at or above the limit sets Ctrl::narrow_ovf, after which
+// the pulls gather the 64-bit distances from their next launch on (a source a
+// pull skipped as unreached meanwhile changed in this iteration: the next pull
+// relaxes it).
 __device__ __forceinline__ void dist32_put(const DevState& s, uint32_t v, unsigned long long d, bool sole)
 {
     if (!s.dist32)
         return;
-    if (d >= (unsigned long long)NONE32) {
+    if (d >= (unsigned long long)s.narrow_lim) {
         atomicOr(&s.ctrl->narrow_ovf, 1u);
         return;
     }
@@ -1288,15 +1290,16 @@ __global__ void __launch_bounds__(PULL_THREADS, 1)
                 if (val < cv) {
                     if (vtx < hub_lim) {
                         if (narrow)
-                            atomicMin(&hub32[vtx], val < (unsigned long long)NONE32 ? (uint32_t)val : NONE32);
+                            atomicMin(&hub32[vtx], val < (unsigned long long)s.narrow_lim ? (uint32_t)val : NONE32);
                         else
                             atomicMin(&hub64[vtx], val);
                     }
                     const uint32_t b = 1u << (vtx & 31u);
                     if (kind == EMIT_COMPLETE) {
-                        s.prop64[vtx] = val; /* sole writer, as for CC */
+                        s.prop64[vtx] = val; /* sole writer, as for CC: the bit is new */
                         dist32_put(s, vtx, val, true);
-                        occ += atomicOr(&nxt[vtx >> 5], b) == 0u ? 1u : 0u;
+                        atomicOr(&nxt[vtx >> 5], b);
+                        ++occ;
                         count_act(g.outdeg[vtx]);
                     } else if (val < atomicMin(&s.prop64[vtx], val)) {
                         dist32_put(s, vtx, val, false);
@@ -1372,8 +1375,12 @@ __global__ void __launch_bounds__(PULL_THREADS, 1)
 // minima of the tile's complete destinations (SSSP_SLOTS at most) are staged
 // in the warp's slice of shared memory and compared, written and activated by
 // the warp's lanes together over consecutive destinations; spanning
-// destinations take atomicMin.  Two launches as pull_kernel's (hub
-// destinations' tiles first).  Dynamic shared memory: hub cache | staged minima.
+// destinations take atomicMin.  While the distances fit the 32-bit copy the
+// candidates are 32-bit sums (a sum at or above the copy's limit is dropped,
+// Ctrl::narrow_ovf and Ctrl::ovf_redo are set, and the next pull is a dense
+// 64-bit one, which relaxes every in-edge again).  Two launches as
+// pull_kernel's (hub destinations' tiles first).  Dynamic shared memory: hub
+// cache | staged minima.
 constexpr int SSSP_EPL = 16;
 constexpr uint32_t SSSP_TILE = 32u * SSSP_EPL;
 constexpr uint32_t SSSP_SLOTS = 128;
@@ -1412,6 +1419,9 @@ __global__ void __launch_bounds__(PULL_THREADS, 1)
     const bool filtered = mode == MODE_FILTERED;
     const uint32_t hub_bytes = s.hub_bytes;
     const bool narrow = s.dist32 && !c->narrow_ovf; /* gathers from the 32-bit copy */
+    const bool sums32 = narrow && s.narrow_sums;    /* and sums in 32 bits */
+    const uint32_t lim = s.narrow_lim;
+    bool dropped = false;                           /* a 32-bit sum reached the limit */
     const unsigned long long pol = l2_evict_first_policy(); /* for the in-edge and weight streams */
     const unsigned char* hub_src = narrow ? reinterpret_cast<const unsigned char*>(s.dist32)
                                           : reinterpret_cast<const unsigned char*>(s.prop64);
@@ -1447,7 +1457,7 @@ __global__ void __launch_bounds__(PULL_THREADS, 1)
         if (vtx >= hub_lim)
             return;
         if (narrow)
-            atomicMin(&hub32[vtx], val < (unsigned long long)NONE32 ? (uint32_t)val : NONE32);
+            atomicMin(&hub32[vtx], val < (unsigned long long)lim ? (uint32_t)val : NONE32);
         else
             atomicMin(&hub64[vtx], val);
     };
@@ -1464,6 +1474,17 @@ __global__ void __launch_bounds__(PULL_THREADS, 1)
             if (bk < 3u)
                 atomicAdd(&sh_deg[bk], 1u);
         }
+    };
+    // the same for a destination this launch writes once (its bit is new)
+    auto activate_new = [&](uint32_t vtx) {
+        atomicOr(&nxt[vtx >> 5], 1u << (vtx & 31u));
+        ++occ;
+        const uint32_t od = g.outdeg[vtx];
+        mass += od;
+        ++act;
+        const uint32_t bk = degree_bucket(od);
+        if (bk < 3u)
+            atomicAdd(&sh_deg[bk], 1u);
     };
     uint32_t t = t_begin + gw;
     uint32_t k0n = 0, kendn = 0;
@@ -1511,32 +1532,14 @@ __global__ void __launch_bounds__(PULL_THREADS, 1)
             pre_cur = cur_dist(pre_vtx);
             pre_od = g.outdeg[pre_vtx];
         }
-        unsigned long long v[EPL];
-#pragma unroll
-        for (int q = 0; q < EPL; ++q) {
-            const uint32_t x = sa[q];
-            bool on = x != NONE32;
-            if (filtered && on)
-                on = (ld_ro_u32(cur + (x >> 5)) >> (x & 31u)) & 1u; /* changed by the previous pull */
-            unsigned long long d = NONE64;
-            if (on && narrow) {
-                const uint32_t y = (x < hub_lim) ? hub32[x] : s.dist32[x];
-                d = (y == NONE32) ? NONE64 : (unsigned long long)y;
-            } else if (on) {
-                d = (x < hub_lim) ? hub64[x] : s.prop64[x];
-            }
-            const unsigned long long w = (wword[q >> 2] >> (8 * (q & 3))) & 0xFFu;
-            v[q] = (d == NONE64) ? NONE64 : d + w; /* phase_edge_pull_sssp.c:136-137 */
-            edges += (x != NONE32) ? 1u : 0u;
-        }
+        if (lane == 0) /* in-edges of the tile: all but the padding after the last one */
+            edges += (g.E - base < SSSP_TILE) ? g.E - base : SSSP_TILE;
+        // a tile minimum the reduction ends: staged (the tile's first SSSP_SLOTS
+        // complete destinations, which the lanes then compare and write over
+        // consecutive destinations), else applied here (tiles of many low
+        // in-degree destinations, and the spanning ones)
         TileGeo<EPL> tg;
-        tile_geometry_bits<EPL>(g, base, t + 1u >= T, k0, kend, lane, tg);
-        dsts += tg.ndst;
-        // the reduction stages the minima of the tile's first SSSP_SLOTS complete
-        // destinations, which the lanes then compare and write over consecutive
-        // destinations; the others (tiles of many low in-degree destinations)
-        // and the spanning ones are applied where the reduction ends them
-        seg_reduce<EPL>(v, tg, lane, MinU64(), [&](uint32_t k, unsigned long long val, int kind) {
+        auto apply = [&](uint32_t k, unsigned long long val, int kind) {
             const uint32_t slot = k - tg.k0;
             if (kind == EMIT_COMPLETE && slot < SSSP_SLOTS) {
                 my_min[slot] = val;
@@ -1546,18 +1549,61 @@ __global__ void __launch_bounds__(PULL_THREADS, 1)
                 return;
             const uint32_t vtx = g.dst_ident ? k : g.dst_id[k];
             if (kind == EMIT_COMPLETE) { /* the destination's only writer in this launch */
-                if (val < s.prop64[vtx]) {
+                if (val < cur_dist(vtx)) {
                     s.prop64[vtx] = val;
                     dist32_put(s, vtx, val, true);
                     hub_min(vtx, val);
-                    activate(vtx);
+                    activate_new(vtx);
                 }
             } else if (val < s.prop64[vtx] && val < atomicMin(&s.prop64[vtx], val)) {
                 dist32_put(s, vtx, val, false);
                 hub_min(vtx, val);
                 activate(vtx);
             }
-        });
+        };
+        if (sums32) {
+            uint32_t v[EPL];
+#pragma unroll
+            for (int q = 0; q < EPL; ++q) {
+                const uint32_t x = sa[q];
+                bool on = x != NONE32;
+                if (filtered && on)
+                    on = (ld_ro_u32(cur + (x >> 5)) >> (x & 31u)) & 1u; /* changed by the previous pull */
+                const uint32_t y = on ? ((x < hub_lim) ? hub32[x] : s.dist32[x]) : NONE32;
+                const uint32_t w = (wword[q >> 2] >> (8 * (q & 3))) & 0xFFu;
+                uint32_t sum = y + w; /* phase_edge_pull_sssp.c:136-137 */
+                if (y != NONE32 && (sum < y || sum >= lim)) {
+                    dropped = true;
+                    sum = NONE32;
+                }
+                v[q] = (y == NONE32) ? NONE32 : sum;
+            }
+            tile_geometry_bits<EPL>(g, base, t + 1u >= T, k0, kend, lane, tg);
+            seg_reduce<EPL>(v, tg, lane, MinU32(), [&](uint32_t k, uint32_t val, int kind) {
+                apply(k, val == NONE32 ? NONE64 : (unsigned long long)val, kind);
+            });
+        } else {
+            unsigned long long v[EPL];
+#pragma unroll
+            for (int q = 0; q < EPL; ++q) {
+                const uint32_t x = sa[q];
+                bool on = x != NONE32;
+                if (filtered && on)
+                    on = (ld_ro_u32(cur + (x >> 5)) >> (x & 31u)) & 1u; /* changed by the previous pull */
+                unsigned long long d = NONE64;
+                if (on && narrow) {
+                    const uint32_t y = (x < hub_lim) ? hub32[x] : s.dist32[x];
+                    d = (y == NONE32) ? NONE64 : (unsigned long long)y;
+                } else if (on) {
+                    d = (x < hub_lim) ? hub64[x] : s.prop64[x];
+                }
+                const unsigned long long w = (wword[q >> 2] >> (8 * (q & 3))) & 0xFFu;
+                v[q] = (d == NONE64) ? NONE64 : d + w; /* phase_edge_pull_sssp.c:136-137 */
+            }
+            tile_geometry_bits<EPL>(g, base, t + 1u >= T, k0, kend, lane, tg);
+            seg_reduce<EPL>(v, tg, lane, MinU64(), apply);
+        }
+        dsts += tg.ndst;
         __syncwarp();
         const uint32_t nd = tg.ndst;
         const uint32_t jlo = tg.k0_fresh ? 0u : 1u;
@@ -1605,6 +1651,10 @@ __global__ void __launch_bounds__(PULL_THREADS, 1)
     if (use_hub && threadIdx.x == 0 && !mbar_wait_bounded(&hub_bar, 0u, HUB_WAIT_TRIES)) {
         atomicOr(&c->error, ERR_HUB_TIMEOUT);
         mbar_wait_bounded(&hub_bar, 0u, HUB_WAIT_TRIES);
+    }
+    if (__any_sync(FULL, dropped) && lane == 0) {
+        atomicOr(&c->narrow_ovf, 1u);
+        atomicOr(&c->ovf_redo, 1u);
     }
     mass = warp_sum_u64(mass);
     edges = warp_sum_u64(edges);
@@ -2233,7 +2283,11 @@ __global__ void decide_kernel(DevGraph g, DevState s, const unsigned long long* 
         c->items = 0u;
         c->alist_n = 0u;
         go = 0u;
-        if (m == 0ull) {
+        // SSSP: a pull dropped 32-bit sums that reached the copy's limit; the
+        // next pull is dense and 64-bit, and relaxes every in-edge again
+        const bool redo = c->ovf_redo != 0u;
+        c->ovf_redo = 0u;
+        if (m == 0ull && !redo) {
             c->done = 1u;
             c->loop = 0u;
         } else if (c->iter >= c->max_iter) {
@@ -2251,6 +2305,10 @@ __global__ void decide_kernel(DevGraph g, DevState s, const unsigned long long* 
                 s.log[c->iter].learned = 0u;
             }
             go = (c->sched == WEDGE_SCHED_LEARNED && s.net) ? 1u : 0u;
+            if (redo) {
+                c->mode = MODE_DENSE;
+                go = 0u;
+            }
         }
     }
     __syncthreads();
@@ -2682,6 +2740,7 @@ __global__ void init_root_kernel(DevGraph g, DevState s, uint32_t app, uint64_t 
         c->pr_sum = 0.0;
         c->probe_edges = s.probe_edges;
         c->narrow_ovf = 0;
+        c->ovf_redo = 0;
         if (app == WEDGE_APP_CC) {
             c->last_mass = g.E;
             c->mode = MODE_DENSE; /* first CC pull is always dense, execution_cc.c:103 */
@@ -3194,8 +3253,9 @@ __global__ void __launch_bounds__(PULL_THREADS, 1) pr32_pull_kernel(DevGraph g, 
         for (int q = 0; q < EPL; ++q) {
             const uint32_t x = sa[q];
             v[q] = F2{(x < hub_lim) ? hub[x] : (x != NONE32) ? ld_ro_f32(cur + x) : 0.0f, 0.0f};
-            edges += (x != NONE32) ? 1u : 0u;
         }
+        if (lane == 0) /* in-edges of the tile: all but the padding after the last one */
+            edges += (g.E - base < PR32_TILE) ? g.E - base : PR32_TILE;
         TileGeo<EPL> tg;
         tile_geometry_bits<EPL>(g, base, t + 1u >= T, k0, kend, lane, tg);
         dsts += tg.ndst;
@@ -3557,7 +3617,7 @@ static bool knob_ok(int k, uint64_t v)
     case WEDGE_KNOB_SSSP_TILE:
         return v == 256u || v == 512u;
     case WEDGE_KNOB_SSSP_NARROW:
-        return v <= 1u;
+        return v <= 0xFFFFFFFEull;
     default:
         return false;
     }
@@ -3855,9 +3915,11 @@ static int ensure_state(wedge_graph* h, int app, int precision)
                 return rc;
             // uint64 weights: the pulls gather a 32-bit copy of the distances
             // (knob WEDGE_KNOB_SSSP_NARROW = 0: the 64-bit distances)
-            if (g.weight_kind != WEDGE_WEIGHTS_F64 && knob_value(h, WEDGE_KNOB_SSSP_NARROW) &&
-                (rc = dalloc(h, &s.dist32, V, true)))
+            const uint64_t nk = knob_value(h, WEDGE_KNOB_SSSP_NARROW);
+            if (g.weight_kind != WEDGE_WEIGHTS_F64 && nk && (rc = dalloc(h, &s.dist32, V, true)))
                 return rc;
+            s.narrow_lim = nk > 1u ? (uint32_t)nk : NONE32; /* a limit below 2^32-1 tests the switch to 64 bits */
+            s.narrow_sums = g.shard ? 0u : 1u;
         } else if ((rc = dalloc(h, &s.prop32, V, true))) {
             return rc;
         }
@@ -4641,8 +4703,8 @@ __global__ void narrow_copy_kernel(DevGraph g, DevState s)
     const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
     for (uint64_t v = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; v < g.V; v += stride) {
         const unsigned long long d = s.prop64[v];
-        s.dist32[v] = d < (unsigned long long)NONE32 ? (uint32_t)d : NONE32;
-        if (d >= (unsigned long long)NONE32 && d != NONE64)
+        s.dist32[v] = d < (unsigned long long)s.narrow_lim ? (uint32_t)d : NONE32;
+        if (d >= (unsigned long long)s.narrow_lim && d != NONE64)
             atomicOr(&s.ctrl->narrow_ovf, 1u);
     }
 }

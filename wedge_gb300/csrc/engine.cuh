@@ -104,7 +104,10 @@ struct Ctrl {
     unsigned int alist_n;              // vertices in the Wedge-build vertex list
     unsigned int pr_ticket;            // blocks of pr_total_kernel done (the last one resets it)
     unsigned int probe_edges;          // BFS/CC probe window of the next pull (in-edges per destination)
-    unsigned int narrow_ovf;           // SSSP: a finite distance reached 2^32-1; pulls gather the 64-bit distances
+    unsigned int narrow_ovf;           // SSSP: a finite distance reached the 32-bit copy's limit; pulls gather the
+                                       // 64-bit distances from then on
+    unsigned int ovf_redo;             // SSSP: a pull dropped sums its 32-bit arithmetic could not hold: the next
+                                       // pull is dense (64-bit) and the traversal does not stop before it
     double pr_total;                   // sum of all accumulators (phase_vertex_pr.c:161); compensated FP32:
                                        // the total the next iteration uses
     double pr_prev;                    // compensated FP32: the total the last iteration used
@@ -120,6 +123,7 @@ struct DevGraph {
     uint32_t nwide;            // destinations spanning more than SPLIT_SERIAL tile boundaries (back of the split lists)
     uint32_t sym;              // every edge's reverse is an edge too: CC propagates engine ids (see cc_best_kernel)
     uint32_t csri_pos;         // csri holds in-edge positions (Epad < 2^32), else chunk ids
+    uint32_t shard;            // a destination-range shard (wedge_cuda_load_shard)
     const uint32_t* src;
     const unsigned long long* w;
     const uint8_t* w8;         // the same weights in one byte each, when every weight is a uint64 below 256
@@ -142,8 +146,11 @@ struct DevGraph {
 struct DevState {
     uint32_t* prop32;              // BFS parent / CC label
     unsigned long long* prop64;    // SSSP distance (uint64 or double bits)
-    uint32_t* dist32;              // SSSP, uint64 weights: the distances narrowed to 32 bits (NONE32: unreached or
-                                   // >= 2^32-1), the array the pulls gather while Ctrl::narrow_ovf is 0; or null
+    uint32_t* dist32;              // SSSP, uint64 weights: the distances below narrow_lim in 32 bits (NONE32:
+                                   // unreached or not below the limit), the array the pulls gather while
+                                   // Ctrl::narrow_ovf is 0; or null
+    uint32_t narrow_lim;           // distances the 32-bit copy holds: below this (2^32-1, or a smaller test limit)
+    uint32_t narrow_sums;          // the 512-edge SSSP pull may sum in 32 bits (not on shards: see ovf_redo)
     double* rank;                  // PageRank FP64: rank / outdegree'
     double* acc;                   // PageRank accumulators (graph_vertex_accumulators)
     double* inv_od;                // PageRank 1 / outdegree' (outdegree, or N for dangling vertices)

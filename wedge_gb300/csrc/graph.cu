@@ -425,6 +425,7 @@ int wedge_cuda_load_shard(uint64_t num_vertices, uint64_t num_edges, const uint3
         return rc;
     }
     h->g.E_thr = global_edges;
+    h->g.shard = 1u;
     *out = h;
     return WEDGE_OK;
 }
