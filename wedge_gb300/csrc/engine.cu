@@ -1378,14 +1378,18 @@ __global__ void __launch_bounds__(PULL_THREADS, 1)
 // destinations take atomicMin.  While the distances fit the 32-bit copy the
 // candidates are 32-bit sums (a sum at or above the copy's limit is dropped,
 // Ctrl::narrow_ovf and Ctrl::ovf_redo are set, and the next pull is a dense
-// 64-bit one, which relaxes every in-edge again).  Two launches as
-// pull_kernel's (hub destinations' tiles first).  Dynamic shared memory: hub
-// cache | staged minima.
+// 64-bit one, which relaxes every in-edge again).  Two instantiations run
+// each launch, the 64-bit one first: SUMS32 for dense and filtered pulls while
+// the distances fit the copy, the other for the rest (and the Wedge pulls);
+// each returns at once where the other runs (the 32-bit one may set
+// Ctrl::narrow_ovf, so it runs second).  Two launches as pull_kernel's (hub
+// destinations' tiles first).  Dynamic shared memory: hub cache | staged minima.
 constexpr int SSSP_EPL = 16;
 constexpr uint32_t SSSP_TILE = 32u * SSSP_EPL;
 constexpr uint32_t SSSP_SLOTS = 128;
 constexpr uint32_t SSSP_STAGE_BYTES = (PULL_THREADS / 32) * SSSP_SLOTS * 8u;
 
+template <bool SUMS32>
 __global__ void __launch_bounds__(PULL_THREADS, 1)
     sssp_pull_kernel(DevGraph g, DevState s, unsigned long long* block_cnt, uint32_t phase)
 {
@@ -1400,6 +1404,8 @@ __global__ void __launch_bounds__(PULL_THREADS, 1)
     if (c->done)
         return;
     const uint32_t mode = c->mode;
+    if ((mode != MODE_WEDGE && s.dist32 && !c->narrow_ovf && s.narrow_sums) != SUMS32)
+        return; /* the other instantiation's launch */
     if (mode == MODE_WEDGE) {
         if (phase == PHASE_HUBS)
             sssp_push_pull(g, s, c, block_cnt);
@@ -1418,8 +1424,7 @@ __global__ void __launch_bounds__(PULL_THREADS, 1)
     uint32_t* nxt = next_front(s, c->parity);
     const bool filtered = mode == MODE_FILTERED;
     const uint32_t hub_bytes = s.hub_bytes;
-    const bool narrow = s.dist32 && !c->narrow_ovf; /* gathers from the 32-bit copy */
-    const bool sums32 = narrow && s.narrow_sums;    /* and sums in 32 bits */
+    const bool narrow = s.dist32 && !c->narrow_ovf; /* gathers from the 32-bit copy (and, SUMS32, sums) */
     const uint32_t lim = s.narrow_lim;
     bool dropped = false;                           /* a 32-bit sum reached the limit */
     const unsigned long long pol = l2_evict_first_policy(); /* for the in-edge and weight streams */
@@ -1561,7 +1566,7 @@ __global__ void __launch_bounds__(PULL_THREADS, 1)
                 activate(vtx);
             }
         };
-        if (sums32) {
+        if constexpr (SUMS32) {
             uint32_t v[EPL];
 #pragma unroll
             for (int q = 0; q < EPL; ++q) {
@@ -3668,7 +3673,7 @@ static bool sssp_tiles512(const wedge_graph* h)
 static const void* pull_fn(const wedge_graph* h, int app)
 {
     if (app == WEDGE_APP_SSSP && sssp_tiles512(h))
-        return (const void*)sssp_pull_kernel;
+        return (const void*)sssp_pull_kernel<false>;
     switch (app) {
     case WEDGE_APP_BFS:
         return (const void*)pull_kernel<WEDGE_APP_BFS, PullEpl<WEDGE_APP_BFS>::value>;
@@ -3707,8 +3712,15 @@ static uint32_t pull_tile_e(const wedge_graph* h, int app)
 static int setup_hub(wedge_graph* h, int app, int precision)
 {
     const void* fn = pull_fn(h, app);
+    /* the 512-edge SSSP pull runs as two instantiations with one shared-memory layout */
+    const void* fn2 = (app == WEDGE_APP_SSSP && sssp_tiles512(h)) ? (const void*)sssp_pull_kernel<true> : nullptr;
     cudaFuncAttributes fa;
     WEDGE_CHECK(cudaFuncGetAttributes(&fa, fn));
+    if (fn2) {
+        cudaFuncAttributes fb;
+        WEDGE_CHECK(cudaFuncGetAttributes(&fb, fn2));
+        fa.sharedSizeBytes = fa.sharedSizeBytes > fb.sharedSizeBytes ? fa.sharedSizeBytes : fb.sharedSizeBytes;
+    }
     int optin = 0;
     WEDGE_CHECK(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, h->device));
     const uint64_t elem = (app == WEDGE_APP_SSSP) ? (h->s.dist32 ? 4 : 8)
@@ -3730,6 +3742,8 @@ static int setup_hub(wedge_graph* h, int app, int precision)
     h->s.hub_bytes = h->hub_bytes;
     h->pull_smem = h->hub_bytes + (uint32_t)stage;
     WEDGE_CHECK(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)h->pull_smem));
+    if (fn2)
+        WEDGE_CHECK(cudaFuncSetAttribute(fn2, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)h->pull_smem));
     if (two_phase_app(app) && n) {
         uint32_t* d = (uint32_t*)(h->s.block_part + h->pull_grid); /* counters: scratch until the first pull */
         hub_split_kernel<<<1, 1, 0, h->stream>>>(h->g, (uint32_t)n, pull_tile_e(h, app), d);
@@ -3985,8 +3999,12 @@ static void launch_pull_app(wedge_graph* h)
         }
     }
     if (APP == WEDGE_APP_SSSP && sssp_tiles512(h)) {
-        sssp_pull_kernel<<<grid, PULL_THREADS, h->pull_smem, h->stream>>>(h->g, h->s, cnt, PHASE_HUBS);
-        sssp_pull_kernel<<<grid, PULL_THREADS, h->pull_smem, h->stream>>>(h->g, h->s, cnt + NCNT * grid, PHASE_REST);
+        sssp_pull_kernel<false><<<grid, PULL_THREADS, h->pull_smem, h->stream>>>(h->g, h->s, cnt, PHASE_HUBS);
+        sssp_pull_kernel<true><<<grid, PULL_THREADS, h->pull_smem, h->stream>>>(h->g, h->s, cnt, PHASE_HUBS);
+        sssp_pull_kernel<false><<<grid, PULL_THREADS, h->pull_smem, h->stream>>>(h->g, h->s, cnt + NCNT * grid,
+                                                                                 PHASE_REST);
+        sssp_pull_kernel<true><<<grid, PULL_THREADS, h->pull_smem, h->stream>>>(h->g, h->s, cnt + NCNT * grid,
+                                                                                PHASE_REST);
     } else if (two_phase_app(APP)) {
         pull_kernel<APP, EPL><<<grid, PULL_THREADS, h->hub_bytes, h->stream>>>(h->g, h->s, cnt, PHASE_HUBS);
         pull_kernel<APP, EPL><<<grid, PULL_THREADS, h->hub_bytes, h->stream>>>(h->g, h->s, cnt + NCNT * grid,
@@ -4024,7 +4042,9 @@ static uint64_t build_launches(const wedge_graph* h)
 
 static uint64_t iteration_launches(const wedge_graph* h, int app)
 {
-    return 1ull + build_launches(h) + pull_launches_of(app); /* decide, the build, the pull */
+    /* decide, the build, the pull (the 512-edge SSSP pull: two instantiations per launch) */
+    const uint64_t pulls = pull_launches_of(app) * ((app == WEDGE_APP_SSSP && sssp_tiles512(h)) ? 2ull : 1ull);
+    return 1ull + build_launches(h) + pulls;
 }
 
 static uint32_t aux_grid(wedge_graph* h, uint64_t work)
