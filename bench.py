@@ -298,8 +298,8 @@ def _roofline(W, suite, peak):
 
 
 def _ncu_traffic(default_workload: bool):
-    """DRAM bytes per launch of the PageRank pull at this workload, scaled from the
-    committed ncu capture of a smaller case (profiles/), or None elsewhere"""
+    """DRAM bytes per launch of the PageRank pull at this workload, from the committed
+    one-pass ncu capture of one launch (profiles/), or None elsewhere"""
     if not default_workload:
         return None
     try:
@@ -474,8 +474,8 @@ def run_ours(args, dist: Dist):
         "roofline": {"bound": "hbm", "kernel": pr_roof["kernel"], "achieved": pr_roof["achieved"], "peak": peak,
                      "unit": "GB/s", "frac": pr_roof["frac"], "peak_source": peak_kind,
                      "traffic": _ncu_traffic(default_workload),
-                     "traffic_scope": "per launch (one PageRank iteration's pull): ncu DRAM bytes of the scale-22 "
-                                      "capture in profiles/ scaled by edges to scale 26",
+                     "traffic_scope": "per launch (one PageRank iteration's pull): ncu DRAM read + write bytes of "
+                                      "one launch at this workload (profiles/pr32_pull_traffic.json)",
                      "algorithmic_bytes_per_launch": int(pr_roof["algorithmic_bytes"] / max(1, pr_roof["iterations"])),
                      "launch_ms": round(pr_roof["pull_ms"] / max(1, pr_roof["iterations"]), 4),
                      "per_app": roof},

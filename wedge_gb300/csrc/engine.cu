@@ -1466,6 +1466,13 @@ __global__ void __launch_bounds__(PULL_THREADS, 1)
         else
             atomicMin(&hub64[vtx], val);
     };
+    // activated vertices per out-degree bucket 0..2, packed 21 bits each per lane
+    unsigned long long degs = 0;
+    auto count_deg = [&](uint32_t od) {
+        const uint32_t bk = degree_bucket(od);
+        if (bk < 3u)
+            degs += 1ull << (21u * bk);
+    };
     // a changed destination: its bit in the next frontier and, the first time, its out-edge mass
     auto activate = [&](uint32_t vtx) {
         const uint32_t b = 1u << (vtx & 31u);
@@ -1475,9 +1482,7 @@ __global__ void __launch_bounds__(PULL_THREADS, 1)
             const uint32_t od = g.outdeg[vtx];
             mass += od;
             ++act;
-            const uint32_t bk = degree_bucket(od);
-            if (bk < 3u)
-                atomicAdd(&sh_deg[bk], 1u);
+            count_deg(od);
         }
     };
     // the same for a destination this launch writes once (its bit is new)
@@ -1487,9 +1492,7 @@ __global__ void __launch_bounds__(PULL_THREADS, 1)
         const uint32_t od = g.outdeg[vtx];
         mass += od;
         ++act;
-        const uint32_t bk = degree_bucket(od);
-        if (bk < 3u)
-            atomicAdd(&sh_deg[bk], 1u);
+        count_deg(od);
     };
     uint32_t t = t_begin + gw;
     uint32_t k0n = 0, kendn = 0;
@@ -1527,16 +1530,6 @@ __global__ void __launch_bounds__(PULL_THREADS, 1)
         }
         const uint4 wq = ld_stream_v4u32_ef(g.w8 + base + (uint64_t)lane * EPL, pol);
         const uint32_t wword[4] = {wq.x, wq.y, wq.z, wq.w};
-        // the tile's first 32 destinations: id, current distance and out-degree,
-        // loaded now so that their latency overlaps the gathers'
-        const uint32_t npre = min(min(kend, g.Vne - 1u) - k0 + 1u, 32u);
-        uint32_t pre_vtx = 0u, pre_od = 0u;
-        unsigned long long pre_cur = NONE64;
-        if ((uint32_t)lane < npre) {
-            pre_vtx = g.dst_ident ? k0 + (uint32_t)lane : g.dst_id[k0 + (uint32_t)lane];
-            pre_cur = cur_dist(pre_vtx);
-            pre_od = g.outdeg[pre_vtx];
-        }
         if (lane == 0) /* in-edges of the tile: all but the padding after the last one */
             edges += (g.E - base < SSSP_TILE) ? g.E - base : SSSP_TILE;
         // a tile minimum the reduction ends: staged (the tile's first SSSP_SLOTS
@@ -1622,14 +1615,13 @@ __global__ void __launch_bounds__(PULL_THREADS, 1)
             bool chg = false;
             uint32_t vtx = 0u, od = 0u;
             if (val != NONE64) {
-                const bool pre = j0 == 0u && (uint32_t)lane < npre;
-                vtx = pre ? pre_vtx : (g.dst_ident ? tg.k0 + j : g.dst_id[tg.k0 + j]);
-                if (val < (pre ? pre_cur : cur_dist(vtx))) {
+                vtx = g.dst_ident ? tg.k0 + j : g.dst_id[tg.k0 + j];
+                if (val < cur_dist(vtx)) {
                     chg = true;
                     s.prop64[vtx] = val;
                     dist32_put(s, vtx, val, true);
                     hub_min(vtx, val);
-                    od = pre ? pre_od : g.outdeg[vtx];
+                    od = g.outdeg[vtx];
                 }
             }
             const uint32_t word = chg ? vtx >> 5 : NONE32;
@@ -1642,13 +1634,7 @@ __global__ void __launch_bounds__(PULL_THREADS, 1)
             if (chg) {
                 mass += od;
                 ++act;
-            }
-            const uint32_t bk = chg ? degree_bucket(od) : 3u;
-#pragma unroll
-            for (uint32_t b = 0; b < 3u; ++b) {
-                const uint32_t n = __popc(__ballot_sync(FULL, bk == b));
-                if (lane == 0 && n)
-                    atomicAdd(&sh_deg[b], n);
+                count_deg(od);
             }
         }
         __syncwarp(); /* my_min is rewritten by the next tile */
@@ -1660,6 +1646,16 @@ __global__ void __launch_bounds__(PULL_THREADS, 1)
     if (__any_sync(FULL, dropped) && lane == 0) {
         atomicOr(&c->narrow_ovf, 1u);
         atomicOr(&c->ovf_redo, 1u);
+    }
+    {
+        const unsigned long long d0 = warp_sum_u64(degs & 0x1FFFFFull);
+        const unsigned long long d1 = warp_sum_u64((degs >> 21) & 0x1FFFFFull);
+        const unsigned long long d2 = warp_sum_u64(degs >> 42);
+        if (lane == 0) {
+            atomicAdd(&sh_deg[0], (unsigned int)d0);
+            atomicAdd(&sh_deg[1], (unsigned int)d1);
+            atomicAdd(&sh_deg[2], (unsigned int)d2);
+        }
     }
     mass = warp_sum_u64(mass);
     edges = warp_sum_u64(edges);

@@ -183,12 +183,18 @@ EVAL_GRID = [(768, 27)]
 
 
 def collect(rmat, grids, reps=3, log=print):
+    """per-iteration costs of every strategy; R-MAT graphs of a size the engine
+    autotuner's table covers run with its knobs, as the benchmark does"""
+    from . import autotune as A
+
     samples = []
+    names = {W.APP_BFS: "bfs", W.APP_CC: "cc", W.APP_SSSP: "sssp"}
     for scale, ef, seed in rmat:
         for app, sym, wk in ((W.APP_BFS, False, W.WEIGHTS_NONE), (W.APP_CC, True, W.WEIGHTS_NONE),
                              (W.APP_SSSP, False, W.WEIGHTS_U64)):
             t0 = time.time()
             with W.Graph.rmat(scale, ef, seed, symmetrise=sym, weight_kind=wk) as g:
+                A.apply_engine_tuning(g, names[app], scale, ef)
                 s = probe_costs(g, app, reps=reps, tag=f"rmat{scale}e{ef}s{seed}")
             samples += s
             log(f"rmat s{scale} ef{ef} seed{seed} app{app}: {len(s)} iterations probed in {time.time() - t0:.1f}s")
