@@ -1372,7 +1372,8 @@ __global__ void __launch_bounds__(PULL_THREADS, 1)
 // (two 256-bit loads) and 16 weight bytes (one 128-bit load), gathers the
 // sources' distances (hub cache or global memory) and adds the weights; the
 // warp takes the per-destination minimum with the segmented reduction.  The
-// minima of the tile's complete destinations (SSSP_SLOTS at most) are staged
+// minima of the tile's first complete destinations (256 with 32-bit sums, 128
+// with 64-bit ones) are staged
 // in the warp's slice of shared memory and compared, written and activated by
 // the warp's lanes together over consecutive destinations; spanning
 // destinations take atomicMin.  While the distances fit the 32-bit copy the
@@ -1386,8 +1387,11 @@ __global__ void __launch_bounds__(PULL_THREADS, 1)
 // destinations' tiles first).  Dynamic shared memory: hub cache | staged minima.
 constexpr int SSSP_EPL = 16;
 constexpr uint32_t SSSP_TILE = 32u * SSSP_EPL;
-constexpr uint32_t SSSP_SLOTS = 128;
-constexpr uint32_t SSSP_STAGE_BYTES = (PULL_THREADS / 32) * SSSP_SLOTS * 8u;
+constexpr uint32_t SSSP_SLOTS = 128;   /* staged 64-bit minima per warp (64-bit instantiation) */
+constexpr uint32_t SSSP_SLOTS32 = 256; /* staged 32-bit minima per warp: the tiles with more destinations
+                                          (R-MAT scale 22: 7% of the complete ones, 25% past 128 slots) */
+constexpr uint32_t SSSP_WARP_STAGE = SSSP_SLOTS * 8u > SSSP_SLOTS32 * 4u ? SSSP_SLOTS * 8u : SSSP_SLOTS32 * 4u;
+constexpr uint32_t SSSP_STAGE_BYTES = (PULL_THREADS / 32) * SSSP_WARP_STAGE;
 
 template <bool SUMS32>
 __global__ void __launch_bounds__(PULL_THREADS, 1)
@@ -1432,7 +1436,10 @@ __global__ void __launch_bounds__(PULL_THREADS, 1)
                                           : reinterpret_cast<const unsigned char*>(s.prop64);
     uint32_t* hub32 = reinterpret_cast<uint32_t*>(sssp_smem);
     unsigned long long* hub64 = reinterpret_cast<unsigned long long*>(sssp_smem);
-    unsigned long long* my_min = reinterpret_cast<unsigned long long*>(sssp_smem + hub_bytes) + (uint32_t)wib * SSSP_SLOTS;
+    constexpr uint32_t SLOTS = SUMS32 ? SSSP_SLOTS32 : SSSP_SLOTS;
+    unsigned char* stage = sssp_smem + hub_bytes + (uint32_t)wib * SSSP_WARP_STAGE;
+    uint32_t* my_min32 = reinterpret_cast<uint32_t*>(stage);
+    unsigned long long* my_min64 = reinterpret_cast<unsigned long long*>(stage);
     unsigned long long mass = 0, edges = 0, tiles = 0, dsts = 0, act = 0, occ = 0;
     if (threadIdx.x < 3)
         sh_deg[threadIdx.x] = 0u;
@@ -1532,15 +1539,22 @@ __global__ void __launch_bounds__(PULL_THREADS, 1)
         const uint32_t wword[4] = {wq.x, wq.y, wq.z, wq.w};
         if (lane == 0) /* in-edges of the tile: all but the padding after the last one */
             edges += (g.E - base < SSSP_TILE) ? g.E - base : SSSP_TILE;
-        // a tile minimum the reduction ends: staged (the tile's first SSSP_SLOTS
+        // a tile minimum the reduction ends: staged (the tile's first SLOTS
         // complete destinations, which the lanes then compare and write over
         // consecutive destinations), else applied here (tiles of many low
         // in-degree destinations, and the spanning ones)
         TileGeo<EPL> tg;
         auto apply = [&](uint32_t k, unsigned long long val, int kind) {
-            const uint32_t slot = k - tg.k0;
-            if (kind == EMIT_COMPLETE && slot < SSSP_SLOTS) {
-                my_min[slot] = val;
+            if (kind != EMIT_COMPLETE && s.shead) {
+                // a spanning destination: sssp_split_kernel writes and counts it
+                // after this launch; the 32-bit copy and the hub cache take the
+                // tile's minimum now, so that later tiles gather it
+                (kind == EMIT_HEAD ? s.shead : s.stail)[t] = val;
+                if (val != NONE64) {
+                    const uint32_t vtx = g.dst_ident ? k : g.dst_id[k];
+                    dist32_put(s, vtx, val, false);
+                    hub_min(vtx, val);
+                }
                 return;
             }
             if (val == NONE64)
@@ -1578,7 +1592,11 @@ __global__ void __launch_bounds__(PULL_THREADS, 1)
             }
             tile_geometry_bits<EPL>(g, base, t + 1u >= T, k0, kend, lane, tg);
             seg_reduce<EPL>(v, tg, lane, MinU32(), [&](uint32_t k, uint32_t val, int kind) {
-                apply(k, val == NONE32 ? NONE64 : (unsigned long long)val, kind);
+                const uint32_t slot = k - tg.k0;
+                if (kind == EMIT_COMPLETE && slot < SLOTS)
+                    my_min32[slot] = val;
+                else
+                    apply(k, val == NONE32 ? NONE64 : (unsigned long long)val, kind);
             });
         } else {
             unsigned long long v[EPL];
@@ -1599,19 +1617,33 @@ __global__ void __launch_bounds__(PULL_THREADS, 1)
                 v[q] = (d == NONE64) ? NONE64 : d + w; /* phase_edge_pull_sssp.c:136-137 */
             }
             tile_geometry_bits<EPL>(g, base, t + 1u >= T, k0, kend, lane, tg);
-            seg_reduce<EPL>(v, tg, lane, MinU64(), apply);
+            seg_reduce<EPL>(v, tg, lane, MinU64(), [&](uint32_t k, unsigned long long val, int kind) {
+                const uint32_t slot = k - tg.k0;
+                if (kind == EMIT_COMPLETE && slot < SLOTS)
+                    my_min64[slot] = val;
+                else
+                    apply(k, val, kind);
+            });
         }
         dsts += tg.ndst;
         __syncwarp();
         const uint32_t nd = tg.ndst;
         const uint32_t jlo = tg.k0_fresh ? 0u : 1u;
-        const uint32_t jhi = min(tg.tail_cont ? nd - 1u : nd, SSSP_SLOTS);
+        const uint32_t jhi = min(tg.tail_cont ? nd - 1u : nd, SLOTS);
         // the staged complete destinations, 32 consecutive ones per round; each
         // is this launch's only writer of its vertex, so its frontier bit is
         // new: the bits of a round go out as one atomicOr per distinct word
         for (uint32_t j0 = 0; j0 < jhi; j0 += 32u) { /* warp-uniform rounds */
             const uint32_t j = j0 + (uint32_t)lane;
-            const unsigned long long val = (j >= jlo && j < jhi) ? my_min[j] : NONE64;
+            unsigned long long val = NONE64;
+            if (j >= jlo && j < jhi) {
+                if constexpr (SUMS32) {
+                    const uint32_t x = my_min32[j];
+                    val = x == NONE32 ? NONE64 : (unsigned long long)x;
+                } else {
+                    val = my_min64[j];
+                }
+            }
             bool chg = false;
             uint32_t vtx = 0u, od = 0u;
             if (val != NONE64) {
@@ -1678,6 +1710,86 @@ __global__ void __launch_bounds__(PULL_THREADS, 1)
             for (int w = 0; w < WARPS; ++w)
                 a += sh_cnt[w][threadIdx.x];
         block_cnt[NCNT * blockIdx.x + threadIdx.x] = a;
+    }
+}
+
+// Destinations spanning the 512-edge SSSP pull's tiles: the minimum of their
+// tiles' partials (stail of every tile but the last, shead of the last),
+// compared with the 64-bit distance and written once -- this launch is their
+// only writer of it (the pull lowered only the 32-bit copy), so their
+// frontier bits are new.  Launched after each of the pull's two launches, for
+// the destinations whose last tile that launch covered, so that the hub
+// destinations' new distances reach the second launch's hub cache.  A thread
+// per destination of at most SPLIT_SERIAL+1 tiles, a warp per longer one.  Its
+// counters are added to the pull launch's block counters (nblk blocks).
+__global__ void sssp_split_kernel(DevGraph g, DevState s, unsigned long long* block_cnt, uint32_t nblk, uint32_t phase)
+{
+    Ctrl* c = s.ctrl;
+    if (c->done || c->mode == MODE_WEDGE)
+        return;
+    const uint32_t T = (uint32_t)((g.E + SSSP_TILE - 1) / SSSP_TILE);
+    const uint32_t split = min(s.hub_tile, T);
+    uint32_t* nxt = next_front(s, c->parity);
+    const uint32_t tid = blockIdx.x * blockDim.x + threadIdx.x;
+    const uint32_t nthr = gridDim.x * blockDim.x;
+    const int lane = threadIdx.x & 31;
+    unsigned long long mass = 0, act = 0, occ = 0, degs = 0;
+    auto mine = [&](uint32_t t1) { return (t1 < split) == (phase == PHASE_HUBS); };
+    auto apply = [&](uint32_t k, unsigned long long m) {
+        if (m == NONE64)
+            return;
+        const uint32_t vtx = g.dst_ident ? k : g.dst_id[k];
+        /* the 64-bit distance: the pull lowered the 32-bit copy already */
+        if (m < s.prop64[vtx]) {
+            s.prop64[vtx] = m;
+            dist32_put(s, vtx, m, true);
+            atomicOr(&nxt[vtx >> 5], 1u << (vtx & 31u));
+            ++occ;
+            const uint32_t od = g.outdeg[vtx];
+            mass += od;
+            ++act;
+            const uint32_t bk = degree_bucket(od);
+            if (bk < 3u)
+                degs += 1ull << (21u * bk);
+        }
+    };
+    for (uint32_t i = tid; i < s.pnsplit; i += nthr) {
+        const uint32_t t0 = s.psplit_t0[i], t1 = s.psplit_t1[i];
+        if (!mine(t1))
+            continue;
+        unsigned long long m = s.shead[t1];
+        for (uint32_t tt = t0; tt < t1; ++tt)
+            m = min(m, s.stail[tt]);
+        apply(s.psplit_k[i], m);
+    }
+    for (uint32_t j = tid >> 5; j < s.pnwide; j += nthr >> 5) {
+        const uint32_t i = s.pT - 1u - j;
+        const uint32_t a = s.psplit_t0[i], b = s.psplit_t1[i];
+        if (!mine(b))
+            continue; /* warp-uniform */
+        unsigned long long m = NONE64;
+        for (uint32_t tt = a + (uint32_t)lane; tt < b; tt += 32u)
+            m = min(m, s.stail[tt]);
+#pragma unroll
+        for (int d = 16; d > 0; d >>= 1)
+            m = min(m, __shfl_xor_sync(FULL, m, d));
+        if (lane == 0)
+            apply(s.psplit_k[i], min(m, s.shead[b]));
+    }
+    mass = warp_sum_u64(mass);
+    act = warp_sum_u64(act);
+    occ = warp_sum_u64(occ);
+    const unsigned long long d0 = warp_sum_u64(degs & 0x1FFFFFull);
+    const unsigned long long d1 = warp_sum_u64((degs >> 21) & 0x1FFFFFull);
+    const unsigned long long d2 = warp_sum_u64(degs >> 42);
+    if (lane == 0 && (mass | act | occ)) {
+        unsigned long long* bc = block_cnt + (uint64_t)NCNT * (((uint64_t)blockIdx.x * (AUX_THREADS / 32) + (threadIdx.x >> 5)) % nblk);
+        atomicAdd(&bc[CNT_MASS], mass);
+        atomicAdd(&bc[CNT_ACT], act);
+        atomicAdd(&bc[CNT_OCC], occ);
+        atomicAdd(&bc[CNT_DEG0], d0);
+        atomicAdd(&bc[CNT_DEG1], d1);
+        atomicAdd(&bc[CNT_DEG2], d2);
     }
 }
 
@@ -3665,6 +3777,7 @@ static bool sssp_tiles512(const wedge_graph* h)
 {
     return h->s.push && h->g.w8 && knob_value(h, WEDGE_KNOB_SSSP_TILE) == 512u;
 }
+static uint32_t sssp_split_grid(wedge_graph* h);
 
 static const void* pull_fn(const wedge_graph* h, int app)
 {
@@ -3882,6 +3995,37 @@ static int pr32_state(wedge_graph* h)
 }
 
 // state arrays of one application (allocated on first use, reused by later runs)
+// Split lists of the 512-edge SSSP pull's tiles (destinations spanning tiles:
+// short ones from the front, long ones from the back) and their per-tile
+// partial minima
+static int sssp_split_state(wedge_graph* h)
+{
+    DevGraph& g = h->g;
+    DevState& s = h->s;
+    cudaStream_t st = h->stream;
+    const uint32_t cap = (uint32_t)h->num_sms * 8u;
+    int rc;
+    s.pT = (uint32_t)(g.Epad / SSSP_TILE);
+    if ((rc = dalloc(h, &s.psplit_k, (uint64_t)s.pT + 1, true)) || (rc = dalloc(h, &s.psplit_t0, (uint64_t)s.pT + 1, true)) ||
+        (rc = dalloc(h, &s.psplit_t1, (uint64_t)s.pT + 1, true)) || (rc = dalloc(h, &s.shead, (uint64_t)s.pT + 1, true)) ||
+        (rc = dalloc(h, &s.stail, (uint64_t)s.pT + 1, true)))
+        return rc;
+    unsigned int* d_cnt = nullptr;
+    WEDGE_CHECK(cudaMallocAsync((void**)&d_cnt, 2 * sizeof(unsigned int), st));
+    WEDGE_CHECK(cudaMemsetAsync(d_cnt, 0, 2 * sizeof(unsigned int), st));
+    if (g.Vne)
+        split_kernel<<<grid_for(g.Vne, AUX_THREADS, cap), AUX_THREADS, 0, st>>>(g.dst_off, g.Vne, s.pT, SSSP_TILE, s.psplit_k,
+                                                                               s.psplit_t0, s.psplit_t1, d_cnt);
+    WEDGE_CHECK(cudaGetLastError());
+    unsigned int n[2] = {0, 0};
+    WEDGE_CHECK(cudaMemcpyAsync(n, d_cnt, sizeof(n), cudaMemcpyDeviceToHost, st));
+    WEDGE_CHECK(cudaStreamSynchronize(st));
+    cudaFreeAsync(d_cnt, st);
+    s.pnsplit = n[0];
+    s.pnwide = n[1];
+    return WEDGE_OK;
+}
+
 static int ensure_state(wedge_graph* h, int app, int precision)
 {
     if (h->built_app == app && (app != WEDGE_APP_PR || h->last_precision == precision))
@@ -3930,6 +4074,8 @@ static int ensure_state(wedge_graph* h, int app, int precision)
                 return rc;
             s.narrow_lim = nk > 1u ? (uint32_t)nk : NONE32; /* a limit below 2^32-1 tests the switch to 64 bits */
             s.narrow_sums = g.shard ? 0u : 1u;
+            if (sssp_tiles512(h) && (rc = sssp_split_state(h)))
+                return rc;
         } else if ((rc = dalloc(h, &s.prop32, V, true))) {
             return rc;
         }
@@ -3995,12 +4141,15 @@ static void launch_pull_app(wedge_graph* h)
         }
     }
     if (APP == WEDGE_APP_SSSP && sssp_tiles512(h)) {
+        const uint32_t sgrid = sssp_split_grid(h);
         sssp_pull_kernel<false><<<grid, PULL_THREADS, h->pull_smem, h->stream>>>(h->g, h->s, cnt, PHASE_HUBS);
         sssp_pull_kernel<true><<<grid, PULL_THREADS, h->pull_smem, h->stream>>>(h->g, h->s, cnt, PHASE_HUBS);
+        sssp_split_kernel<<<sgrid, AUX_THREADS, 0, h->stream>>>(h->g, h->s, cnt, grid, PHASE_HUBS);
         sssp_pull_kernel<false><<<grid, PULL_THREADS, h->pull_smem, h->stream>>>(h->g, h->s, cnt + NCNT * grid,
                                                                                  PHASE_REST);
         sssp_pull_kernel<true><<<grid, PULL_THREADS, h->pull_smem, h->stream>>>(h->g, h->s, cnt + NCNT * grid,
                                                                                 PHASE_REST);
+        sssp_split_kernel<<<sgrid, AUX_THREADS, 0, h->stream>>>(h->g, h->s, cnt + NCNT * grid, grid, PHASE_REST);
     } else if (two_phase_app(APP)) {
         pull_kernel<APP, EPL><<<grid, PULL_THREADS, h->hub_bytes, h->stream>>>(h->g, h->s, cnt, PHASE_HUBS);
         pull_kernel<APP, EPL><<<grid, PULL_THREADS, h->hub_bytes, h->stream>>>(h->g, h->s, cnt + NCNT * grid,
@@ -4038,9 +4187,17 @@ static uint64_t build_launches(const wedge_graph* h)
 
 static uint64_t iteration_launches(const wedge_graph* h, int app)
 {
-    /* decide, the build, the pull (the 512-edge SSSP pull: two instantiations per launch) */
-    const uint64_t pulls = pull_launches_of(app) * ((app == WEDGE_APP_SSSP && sssp_tiles512(h)) ? 2ull : 1ull);
+    /* decide, the build, the pull (the 512-edge SSSP pull: two instantiations per launch and a
+       split-destination finish after each) */
+    const uint64_t pulls = pull_launches_of(app) * ((app == WEDGE_APP_SSSP && sssp_tiles512(h)) ? 3ull : 1ull);
     return 1ull + build_launches(h) + pulls;
+}
+
+// sssp_split_kernel: a thread per short split, a warp per long one
+static uint32_t sssp_split_grid(wedge_graph* h)
+{
+    const uint64_t wide = (uint64_t)h->s.pnwide * 32u;
+    return grid_for((h->s.pnsplit > wide ? h->s.pnsplit : wide) + 1, AUX_THREADS, (uint32_t)h->num_sms * 8u);
 }
 
 static uint32_t aux_grid(wedge_graph* h, uint64_t work)

@@ -169,6 +169,9 @@ struct DevState {
     uint32_t pnsplit, pnwide, pT;
     float2* phead;                 // [pT] (sum, compensation) of a split destination ending in tile t
     float2* ptail;                 // [pT] (sum, compensation) of a split destination continuing past tile t
+    unsigned long long* shead;     // SSSP 512-edge pull: [pT] minimum of a split destination ending in tile t
+    unsigned long long* stail;     // [pT] minimum of a split destination continuing past tile t (the split lists
+                                   // psplit_* are those of the 512-edge tiles)
     double* pmass;                 // per-block partial sums of the non-dangling ranks (the next total rank)
     float* ovf_sum;                // [Vne] sums of the destinations in ovf_list, by compressed destination
     uint32_t* ovf_list;            // complete destinations past the staged slots of their tile (tile order)
