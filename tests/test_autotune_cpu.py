@@ -6,7 +6,7 @@ import numpy as np
 from wedge_gb300 import autotune as A
 from wedge_gb300 import engine as W
 
-DEFAULTS = {"hub_bytes": 65536, "probe_edges": 16, "sssp_tile": 256, "sssp_narrow": 1}
+DEFAULTS = {"hub_bytes": 65536, "probe_edges": 16, "sssp_tile": 512, "sssp_narrow": 1}
 
 
 class FakeGraph:
@@ -44,7 +44,7 @@ def test_tune_engine_keeps_the_defaults_on_a_tie():
     g = FakeGraph(lambda k: 5.0)
     default, best, _ = A.tune_engine(g, W.APP_SSSP, None, A.ENGINE_SPACE["sssp"], reps=2, log=lambda *_: None)
     assert best is default
-    assert {k: best[k] for k in ("hub_bytes", "sssp_tile", "sssp_narrow")} == {"hub_bytes": 65536, "sssp_tile": 256,
+    assert {k: best[k] for k in ("hub_bytes", "sssp_tile", "sssp_narrow")} == {"hub_bytes": 65536, "sssp_tile": 512,
                                                                               "sssp_narrow": 1}
 
 

@@ -564,8 +564,10 @@ def test_wedge_pulls_over_chunk_ids(W, O, monkeypatch):
 # traversals cross it, switching to 64-bit distances mid-way (the 512-edge pull
 # drops its 32-bit sums at the limit and redoes the pull in 64 bits)
 KNOB_SETTINGS = [{"hub_bytes": 0}, {"hub_bytes": 98304}, {"probe_edges": 1}, {"probe_edges": 4096},
-                 {"sssp_tile": 512}, {"sssp_narrow": 0}, {"sssp_tile": 512, "sssp_narrow": 0, "hub_bytes": 16},
-                 {"sssp_narrow": 40}, {"sssp_tile": 512, "sssp_narrow": 40}, {"sssp_tile": 512, "sssp_narrow": 150}]
+                 {"sssp_tile": 256}, {"sssp_narrow": 0}, {"sssp_tile": 256, "sssp_narrow": 0},
+                 {"sssp_tile": 512, "sssp_narrow": 0, "hub_bytes": 16},
+                 {"sssp_tile": 256, "sssp_narrow": 40}, {"sssp_tile": 512, "sssp_narrow": 40},
+                 {"sssp_tile": 512, "sssp_narrow": 150}]
 
 
 @pytest.mark.parametrize("knobs", KNOB_SETTINGS, ids=[",".join(f"{k}={v}" for k, v in x.items()) for x in KNOB_SETTINGS])

@@ -3740,7 +3740,7 @@ constexpr uint64_t HUB_BYTES_DEFAULT = 65536;
 
 static uint64_t knob_value(const wedge_graph* h, int k)
 {
-    static const uint64_t defaults[WEDGE_KNOBS] = {HUB_BYTES_DEFAULT, PROBE_EDGES, 256u, 1u};
+    static const uint64_t defaults[WEDGE_KNOBS] = {HUB_BYTES_DEFAULT, PROBE_EDGES, 512u, 1u};
     if (h->knob[k] != WEDGE_KNOB_DEFAULT)
         return h->knob[k];
     const char* e = nullptr;
@@ -3754,7 +3754,7 @@ static uint64_t knob_value(const wedge_graph* h, int k)
         break;
     case WEDGE_KNOB_SSSP_TILE: {
         const char* t = getenv("WEDGE_SSSP_TILES512");
-        return (t && t[0] == '1') ? 512u : defaults[k];
+        return (t && t[0] == '0') ? 256u : (t && t[0] == '1') ? 512u : defaults[k];
     }
     case WEDGE_KNOB_SSSP_NARROW:
         e = getenv("WEDGE_SSSP_NARROW");
