@@ -265,8 +265,8 @@ enum wedge_knob {
     WEDGE_KNOB_PROBE_EDGES = 1,  /* BFS/CC per-destination probe window, in-edges: 1 .. 4096
                                     (WEDGE_PROBE_EDGES; default 16) */
     WEDGE_KNOB_SSSP_TILE = 2,    /* SSSP dense-pull tile, in-edges: 512 or 256 (WEDGE_SSSP_TILES512=1/0;
-                                    default 512); 512 needs byte-wide weights and in-edge positions,
-                                    other graphs use 256 */
+                                    default 512 from 2^23 in-edges, else 256); 512 needs byte-wide weights
+                                    and in-edge positions, other graphs use 256 */
     WEDGE_KNOB_SSSP_NARROW = 3,  /* SSSP pulls gather a 32-bit copy of the distances (uint64 weights): 1, or
                                     0 (none), or a limit 2 .. 2^32-2 below which distances stay in 32 bits
                                     (the default limit is 2^32-1; lower ones test the switch to 64 bits)

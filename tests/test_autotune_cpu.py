@@ -6,7 +6,7 @@ import numpy as np
 from wedge_gb300 import autotune as A
 from wedge_gb300 import engine as W
 
-DEFAULTS = {"hub_bytes": 65536, "probe_edges": 16, "sssp_tile": 512, "sssp_narrow": 1}
+DEFAULTS = {"hub_bytes": 65536, "probe_edges": 16, "sssp_tile": 512, "sssp_narrow": 1}  # graphs of 2^23+ in-edges
 
 
 class FakeGraph:

@@ -39,9 +39,11 @@ def graph_edges(O, kind, p, symmetric=False):
     return V, s, d
 
 
-def run_engine(W, V, s, d, app, w=None, weight_kind=None, **params):
+def run_engine(W, V, s, d, app, w=None, weight_kind=None, knobs=None, **params):
     wk = weight_kind if weight_kind is not None else W.WEIGHTS_U64
     with W.Graph.from_edges(V, s, d, w, wk if w is not None else W.WEIGHTS_NONE) as g:
+        for k, v in (knobs or {}).items():
+            g.set_knob(k, v)
         st = g.run(app, W.Params(**params))
         props = g.read_results()
         od = g.read_outdegrees()
@@ -94,12 +96,13 @@ def test_cc_bit_exact(W, O, scale, ef, seed, sched):
 
 @pytest.mark.parametrize("scale,ef,seed", SIZES)
 @pytest.mark.parametrize("sched", SCHEDS)
-def test_sssp_bit_exact(W, O, scale, ef, seed, sched):
+@pytest.mark.parametrize("tile", [256, 512])
+def test_sssp_bit_exact(W, O, scale, ef, seed, sched, tile):
     V, s, d = graph_edges(O, "rmat", dict(scale=scale, edge_factor=ef, seed=seed))
     w = O.weights(s, d)
     for root in (0, 3):
         ref, _, _ = O.Graph.from_edges(V, s, d, O.SSSP, w).run(root=root, threads=4)
-        got, _, _ = run_engine(W, V, s, d, W.APP_SSSP, w, root=root, sched=sched_id(W, sched))
+        got, _, _ = run_engine(W, V, s, d, W.APP_SSSP, w, knobs={"sssp_tile": tile}, root=root, sched=sched_id(W, sched))
         assert np.array_equal(got, ref)
 
 
@@ -564,7 +567,7 @@ def test_wedge_pulls_over_chunk_ids(W, O, monkeypatch):
 # traversals cross it, switching to 64-bit distances mid-way (the 512-edge pull
 # drops its 32-bit sums at the limit and redoes the pull in 64 bits)
 KNOB_SETTINGS = [{"hub_bytes": 0}, {"hub_bytes": 98304}, {"probe_edges": 1}, {"probe_edges": 4096},
-                 {"sssp_tile": 256}, {"sssp_narrow": 0}, {"sssp_tile": 256, "sssp_narrow": 0},
+                 {"sssp_tile": 512}, {"sssp_narrow": 0}, {"sssp_tile": 256, "sssp_narrow": 0},
                  {"sssp_tile": 512, "sssp_narrow": 0, "hub_bytes": 16},
                  {"sssp_tile": 256, "sssp_narrow": 40}, {"sssp_tile": 512, "sssp_narrow": 40},
                  {"sssp_tile": 512, "sssp_narrow": 150}]

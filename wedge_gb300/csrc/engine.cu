@@ -3753,8 +3753,12 @@ static uint64_t knob_value(const wedge_graph* h, int k)
         e = getenv("WEDGE_PROBE_EDGES");
         break;
     case WEDGE_KNOB_SSSP_TILE: {
+        // default: 512-edge tiles from 2^23 in-edges; below, the extra launches of
+        // the 512-edge pull (two instantiations and a finish per launch) cost more
+        // than its faster tiles save (batched workload, scales 12-20: 181 against
+        // 156 ms one query at a time)
         const char* t = getenv("WEDGE_SSSP_TILES512");
-        return (t && t[0] == '0') ? 256u : (t && t[0] == '1') ? 512u : defaults[k];
+        return (t && t[0] == '0') ? 256u : (t && t[0] == '1') ? 512u : h->g.E >= (1ull << 23) ? 512u : 256u;
     }
     case WEDGE_KNOB_SSSP_NARROW:
         e = getenv("WEDGE_SSSP_NARROW");
