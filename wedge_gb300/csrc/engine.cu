@@ -3553,10 +3553,20 @@ __global__ void pr_sum_kernel(DevGraph g, DevState s, double* block_out)
     const bool c32 = s.precision == WEDGE_PREC_FP32C;
     const float* r32 = c32 ? pr32_cur(s) : nullptr;
     double x = 0.0;
-    for (uint64_t v = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; v < g.V; v += (uint64_t)gridDim.x * blockDim.x) {
-        const uint32_t od = g.outdeg[v];
-        const double r = c32 ? (double)r32[v] : s.rank[v];
-        x = __dadd_rn(x, __dmul_rn(r, od ? (double)od : N));
+    if (c32) {
+        // compensated FP32 per thread (this GPU's FP64 units are slow), FP64 across threads
+        const float Nf = (float)g.V;
+        F2 a{0.0f, 0.0f};
+        for (uint64_t v = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; v < g.V; v += (uint64_t)gridDim.x * blockDim.x) {
+            const uint32_t od = g.outdeg[v];
+            a = f2_add(a, __fmul_rn(r32[v], od ? (float)od : Nf));
+        }
+        x = __dadd_rn((double)a.s, (double)a.c);
+    } else {
+        for (uint64_t v = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; v < g.V; v += (uint64_t)gridDim.x * blockDim.x) {
+            const uint32_t od = g.outdeg[v];
+            x = __dadd_rn(x, __dmul_rn(s.rank[v], od ? (double)od : N));
+        }
     }
     x = warp_sum_f64(x);
     if ((threadIdx.x & 31) == 0)
