@@ -48,3 +48,36 @@ def queries(params, bfs_per_graph: int = 4, sssp_per_graph: int = 4):
 def load_graphs(params):
     """the graphs on the device (weighted, so BFS and SSSP queries share one handle)"""
     return [W.Graph.rmat(scale, ef, seed, weight_kind=W.WEIGHTS_U64) for scale, ef, seed, _h in params]
+
+
+def main():
+    """Run the batched workload (or its first N graphs) and print the device time
+    of each run: python -m wedge_gb300.batch [--graphs N] [--runs R] [--no-graph]"""
+    import argparse
+    import json
+    import os
+
+    from . import autotune as A
+
+    ap = argparse.ArgumentParser(description="the batched multi-query workload in one persistent kernel")
+    ap.add_argument("--graphs", type=int, default=64, help="the first N graphs of the workload (and their queries)")
+    ap.add_argument("--runs", type=int, default=3)
+    ap.add_argument("--no-graph", action="store_true", help="launch the kernel directly, not from a CUDA graph")
+    a = ap.parse_args()
+    params = graph_params()[:a.graphs]
+    qs = queries(params)
+    graphs = load_graphs(params)
+    tuning = A.load_tuning() if os.path.exists(A.DEFAULT_TUNING) else None
+    flags = 0 if a.no_graph else W.FLAG_GRAPH
+    try:
+        with W.Batch(graphs, qs) as b:
+            ms = [b.run(tuning, flags)["running_ms"] for _ in range(a.runs)]
+        print(json.dumps({"graphs": len(graphs), "queries": len(qs), "edges": sum(g.E for g in graphs),
+                          "running_ms": [round(x, 3) for x in ms]}))
+    finally:
+        for g in graphs:
+            g.close()
+
+
+if __name__ == "__main__":
+    main()
