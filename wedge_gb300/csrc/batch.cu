@@ -12,10 +12,11 @@
 //           are cleared
 //   prefix  (block 0) per-query chunk counts -> one offset table: the work
 //           queue of the pull
-//   pull    warps take chunks of 32 in-edges from the queue, across all
-//           queries, and pull them (phase_edge_pull_bfs.c / _sssp.c logic:
-//           gather, per-destination min, atomic min into the property,
-//           activation bit, activated-vertex list, changed out-edge mass)
+//   pull    warps take items from the queue, across all queries, and pull
+//           them (phase_edge_pull_bfs.c / _sssp.c logic: gather,
+//           per-destination min, the property, activation bit, activated-
+//           vertex list, changed out-edge mass): dense pulls in tiles of 256
+//           in-edges, sparse ones in marked 32-edge chunks or out-list pieces
 //   decide  (block 0) per query: done when no mass changed, else the plain
 //           rule (mass > t% of the query's edges: dense) picks the next pull
 // with a grid-wide barrier between the phases.  All blocks leave the loop
@@ -313,6 +314,96 @@ __device__ void pull_chunk(const BArgs& a, uint32_t q, uint32_t ch, uint32_t* he
     }
 }
 
+// A dense pull's item: a tile of BTILE_CH chunks (32*BEPL in-edges), lane l
+// holding BEPL consecutive ones, with the single-query engine's tile machinery
+// (destination-start bitmap geometry, segmented reduction).  BFS gathers the
+// frontier bits of the sources and claims an unvisited destination for the
+// least frontier source with one compare-and-swap; SSSP gathers distances,
+// adds the weights and lowers the destination with atomicMin.  Per
+// destination, not per in-edge: the visited test, the property write and the
+// activation.
+constexpr int BEPL = 8;
+constexpr uint32_t BTILE_CH = BEPL; /* 32-edge chunks per tile */
+
+__device__ void pull_tile(const BArgs& a, uint32_t q, uint32_t t, unsigned long long& mass)
+{
+    const int lane = threadIdx.x & 31;
+    const BQuery& qq = a.q[q];
+    BCtl& c = a.ctl[q];
+    const BGraph& G = a.graphs[qq.graph];
+    const uint64_t base = (uint64_t)t * (32u * BEPL);
+    const uint32_t ch0 = t * BTILE_CH;
+    const uint32_t k0 = G.chunk_dst0[ch0];
+    const uint32_t kend = G.chunk_dst0[min(ch0 + BTILE_CH, G.nchunks)];
+    const bool last = base + 32u * BEPL >= G.E;
+    uint32_t sa[BEPL];
+    {
+        const uint64_t p0 = base + (uint64_t)lane * BEPL;
+        uint32_t x[8];
+        ld_stream_v8(G.src + p0, x);
+#pragma unroll
+        for (int j = 0; j < BEPL; ++j)
+            sa[j] = (p0 + (uint64_t)j < G.E) ? x[j] : NONE32;
+    }
+    DevGraph dg;
+    dg.dst_start = G.dst_start;
+    TileGeo<BEPL> tg;
+    const uint32_t* cur = qq.front[c.parity];
+    uint32_t* nxt = qq.front[c.parity ^ 1u];
+    uint32_t* nlist = qq.list[c.parity ^ 1u];
+    auto activate = [&](uint32_t vtx) {
+        const uint32_t b = 1u << (vtx & 31u);
+        if (!(atomicOr(&nxt[vtx >> 5], b) & b)) {
+            const uint32_t pos = atomicAdd(&c.nlist[c.parity ^ 1u], 1u);
+            nlist[pos] = vtx;
+            mass += G.outdeg[vtx];
+        }
+    };
+    if (qq.app == WEDGE_APP_BFS) {
+        uint32_t v[BEPL];
+#pragma unroll
+        for (int j = 0; j < BEPL; ++j) {
+            const uint32_t x = sa[j];
+            v[j] = (x != NONE32 && ((cur[x >> 5] >> (x & 31u)) & 1u)) ? x : NONE32;
+        }
+        tile_geometry_bits<BEPL>(dg, base, last, k0, kend, lane, tg);
+        seg_reduce<BEPL>(v, tg, lane, MinU32(), [&](uint32_t k, uint32_t val, int) {
+            if (val == NONE32)
+                return;
+            const uint32_t vtx = G.dst_id[k];
+            /* the least frontier source of this tile claims an unvisited destination */
+            if (qq.prop[vtx] == NONE64 && atomicCAS(&qq.prop[vtx], NONE64, (unsigned long long)val) == NONE64)
+                activate(vtx);
+        });
+    } else {
+        const bool f64 = G.weight_kind == WEDGE_WEIGHTS_F64;
+        unsigned long long v[BEPL];
+        const uint64_t p0 = base + (uint64_t)lane * BEPL;
+#pragma unroll
+        for (int j = 0; j < BEPL; ++j) {
+            const uint32_t x = sa[j];
+            v[j] = NONE64;
+            if (x != NONE32) {
+                const unsigned long long d = qq.prop[x];
+                const unsigned long long wt = G.w8 ? (unsigned long long)G.w8[p0 + j] : G.w[p0 + j];
+                if (f64)
+                    v[j] = (unsigned long long)__double_as_longlong(
+                        __dadd_rn(__longlong_as_double((long long)d), __longlong_as_double((long long)wt)));
+                else
+                    v[j] = (d == NONE64) ? NONE64 : d + wt; /* phase_edge_pull_sssp.c:136-137 */
+            }
+        }
+        tile_geometry_bits<BEPL>(dg, base, last, k0, kend, lane, tg);
+        seg_reduce<BEPL>(v, tg, lane, MinU64(), [&](uint32_t k, unsigned long long val, int) {
+            if (val == NONE64)
+                return;
+            const uint32_t vtx = G.dst_id[k];
+            if (val < qq.prop[vtx] && val < atomicMin(&qq.prop[vtx], val))
+                activate(vtx);
+        });
+    }
+}
+
 // A sparse pull over in-edge positions: the in-edges of one PIECE of an
 // activated vertex's out-list are relaxed by the warp's lanes (BFS: an
 // unvisited destination takes the vertex as its parent; SSSP: min-plus)
@@ -382,8 +473,10 @@ __device__ void phase_pull(const BArgs& a)
             unsigned long long mass = 0;
             if (push)
                 push_piece(a, q, a.q[q].vitems[local], mass);
-            else
+            else if (sparse)
                 pull_chunk(a, q, ch, heads, mass);
+            else
+                pull_tile(a, q, (uint32_t)local, mass); /* dense: tiles of BTILE_CH chunks */
 #pragma unroll
             for (int d = 16; d > 0; d >>= 1)
                 mass += __shfl_xor_sync(FULL, mass, d);
@@ -418,7 +511,7 @@ __device__ void phase_decide(const BArgs& a)
         c.parity ^= 1u;
         const unsigned long long thr = (G.E * (unsigned long long)a.threshold_pct) / 100ull; /* execution_bfs.c:132 */
         c.mode = m > thr ? MODE_DENSE : MODE_WEDGE;                                         /* execution_bfs.c:141 */
-        c.items = c.mode == MODE_DENSE ? G.nchunks : 0u;
+        c.items = c.mode == MODE_DENSE ? (G.nchunks + BTILE_CH - 1u) / BTILE_CH : 0u;
     }
     __syncthreads();
     block_prefix(a.build_off, a.Q, [&](uint32_t q) -> unsigned long long {
@@ -521,7 +614,7 @@ __global__ void batch_seed_kernel(BArgs a)
         c.nlist[1] = 0u;
         const unsigned long long thr = (G.E * (unsigned long long)a.threshold_pct) / 100ull;
         c.mode = (unsigned long long)G.outdeg[r] > thr ? MODE_DENSE : MODE_WEDGE;
-        c.items = c.mode == MODE_DENSE ? G.nchunks : 0u;
+        c.items = c.mode == MODE_DENSE ? (G.nchunks + BTILE_CH - 1u) / BTILE_CH : 0u;
     }
     __syncthreads();
     block_prefix(a.build_off, a.Q, [&](uint32_t q) -> unsigned long long {
