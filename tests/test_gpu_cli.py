@@ -105,7 +105,12 @@ def test_cli_outputs_every_application(O, tmp_path):
     od = od.view(np.float64)  # PageRank keeps out-degrees as doubles (graph_vertex_outdegrees)
     got = _lines(o)
     want = ref.view(np.float64) * np.where(od == 0, V, od)
-    assert np.allclose([float(got[v]) for v in range(V)], want, rtol=1e-4)
+    # the reference's %.4le strings: the FP64 ranks agree with the oracle's to
+    # about 1e-12, so a line may differ only where a value lies that close to a
+    # rounding boundary of its fifth digit
+    differ = [v for v in range(V) if got[v] != "%.4e" % want[v]]
+    assert len(differ) <= 2, differ[:10]
+    assert all(abs(float(got[v]) - want[v]) <= 1e-4 * abs(want[v]) for v in differ)
 
 
 def test_gpu_formatting_equals_host_formatting(W, O, tmp_path):
