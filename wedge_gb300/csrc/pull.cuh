@@ -153,6 +153,15 @@ __device__ __forceinline__ double ld_ro_f64(const double* p)
     return r;
 }
 
+// a gathered 32-bit property that the launch itself may write (no .nc):
+// allocating in L1 with evict-last, so that the properties most gathered stay
+__device__ __forceinline__ uint32_t ld_gather_u32(const uint32_t* p)
+{
+    uint32_t r;
+    asm volatile("ld.global.L1::evict_last.u32 %0, [%1];" : "=r"(r) : "l"(p));
+    return r;
+}
+
 __device__ __forceinline__ float ld_ro_f32(const float* p)
 {
     float r;
