@@ -1667,7 +1667,7 @@ __global__ void __launch_bounds__(PULL_THREADS, 1)
             const uint32_t bits = __reduce_or_sync(grp, chg ? 1u << (vtx & 31u) : 0u);
             if (chg && (uint32_t)lane == (uint32_t)(__ffs(grp) - 1)) {
                 atomicOr(&nxt[word], bits);
-                ++occ; /* a distinct word of this round */
+                ++occ; /* a distinct word of these 32 destinations */
             }
             if (chg) {
                 mass += od;
