@@ -486,6 +486,33 @@ def test_phase_api_drives_the_reference_loop(W, O):
         check_bfs(g.read_results(), V, s, d, 0)
 
 
+@pytest.mark.parametrize("tile", [256, 512])
+def test_phase_api_drives_the_reference_sssp_loop(W, O, tile):
+    """execution_impl_sssp's loop over wedge_cuda_run_phase, with either dense-pull
+    tile (512: the 32-bit pull, its 64-bit twin and the spanning destinations'
+    finish run inside each pull phase); distances bit-exact"""
+    V, s, d = graph_edges(O, "rmat", dict(scale=12, edge_factor=16, seed=6))
+    w = O.weights(s, d)
+    E = len(s)
+    p = W.Params(root=0)
+    ref, _, _ = O.Graph.from_edges(V, s, d, O.SSSP, w).run(root=0, threads=4)
+    with W.Graph.from_edges(V, s, d, w, W.WEIGHTS_U64) as g:
+        g.set_knob("sssp_tile", tile)
+        g.run_phase(W.APP_SSSP, W.PHASE_INIT, p)
+        active = int(g.read_outdegrees()[0])
+        iters = 0
+        while True:
+            iters += 1
+            phase = W.PHASE_PULL_DENSE if active > E * 20 // 100 else W.PHASE_PULL_WEDGE
+            active = g.run_phase(W.APP_SSSP, phase, p)
+            if active == 0:
+                break
+            g.run_phase(W.APP_SSSP, W.PHASE_WEDGE_BUILD, p)
+            g.run_phase(W.APP_SSSP, W.PHASE_ADVANCE, p)
+            assert iters < 100
+        assert np.array_equal(g.read_results(), ref)
+
+
 def test_phase_api_cc_symmetric_reads_mid_traversal(W, O):
     """CC over wedge_cuda_run_phase on a symmetric graph (engine-id labels): results read
     between pulls are caller ids no lower than the final labels, and reading them does not
