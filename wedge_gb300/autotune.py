@@ -36,7 +36,7 @@ from . import engine as W
 
 DEFAULT_TUNING = os.path.join(os.path.dirname(os.path.abspath(__file__)), "data", "batch_tuning.json")
 DEFAULT_ENGINE_TUNING = os.path.join(os.path.dirname(os.path.abspath(__file__)), "data", "engine_tuning.json")
-HUB_CHOICES = (0, 32768, 65536, 98304)
+HUB_CHOICES = (0, 32768, 65536, 81920, 98304, 114688)
 ENGINE_SPACE = {
     "bfs": {"hub_bytes": HUB_CHOICES, "probe_edges": (8, 16, 32)},
     "cc": {"hub_bytes": HUB_CHOICES, "probe_edges": (8, 16, 32)},
